@@ -1,0 +1,273 @@
+/*
+ * hybridrt.h — C ABI of the GB300-native hybrid ray-tracing pass.
+ *
+ * The pass replaces the three GPU submissions that VkPinut's
+ * Renderer::rasterize_hybrid records after its G-buffer raster pass
+ * (src/renderer.cpp:559-580):
+ *
+ *   shadow trace   data/shaders/shadowRaygen.rgen + shadow.rmiss   -> hy_shadow_pass
+ *   denoise        data/shaders/blur.comp                          -> hy_accumulate_pass
+ *   hybrid trace   data/shaders/hybridRaygen.rgen + hybridHit.rchit
+ *                  + miss.rmiss                                    -> hy_shade_pass
+ *   all three, fused where the data flow allows                    -> hy_hybrid_forward
+ *
+ * and the driver-built acceleration structures (src/renderer.cpp:1696-1865)
+ * with a GPU LBVH collapsed to a compressed 8-wide BVH (hy_bvh_build).
+ *
+ * Conventions
+ *   - Every entry point returns HY_OK (0) or a negative HY_ERR_* code; no C++
+ *     exception crosses this boundary.
+ *   - Pointers named d_* are device pointers owned by the caller; pointers
+ *     named h_* (and the scene upload arrays) are host pointers.
+ *   - Work is stream-ordered on the context's stream.  Entry points that
+ *     return statistics or an error status read back a 4-byte status word and
+ *     so synchronise that stream.
+ *   - A context is used from one host thread at a time.
+ *   - Struct layouts that mirror a reference type keep its std140/std430
+ *     layout so a Vulkan-side buffer can be memcpy'd straight in.
+ */
+#ifndef HYBRIDRT_H
+#define HYBRIDRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HY_ABI_VERSION 1
+
+/* ---- error codes (the reference aborts through VK_CHECK, src/vk_engine.h:15-24) ---- */
+enum {
+    HY_OK                  = 0,
+    HY_ERR_INVALID_ARG     = -1,
+    HY_ERR_OOM             = -2,
+    HY_ERR_CUDA            = -3,
+    HY_ERR_TIMEOUT         = -4,  /* a bounded device loop ran out of its iteration budget */
+    HY_ERR_STACK_OVERFLOW  = -5,  /* traversal stack exceeded its depth */
+    HY_ERR_QUEUE_OVERFLOW  = -6,
+    HY_ERR_NAN_INPUT       = -7,
+    HY_ERR_NOT_READY       = -8,  /* scene or BVH missing */
+    HY_ERR_UNSUPPORTED     = -9
+};
+
+/* device status-word bits (HyStats.error_flags) */
+#define HY_STATUS_STACK_OVERFLOW 0x1u
+#define HY_STATUS_TIMEOUT        0x2u
+#define HY_STATUS_NAN_INPUT      0x4u
+#define HY_STATUS_QUEUE_OVERFLOW 0x8u
+#define HY_STATUS_BAD_INDEX      0x10u  /* a node/triangle index fell outside the structure */
+
+typedef struct HyCtx HyCtx;
+
+typedef struct HyCreateInfo {
+    int32_t  device;            /* CUDA device ordinal */
+    uint32_t flags;             /* reserved, 0 */
+    void*    stream;            /* cudaStream_t to run on; NULL: the context creates its own */
+    uint64_t max_device_bytes;  /* cap on context-owned device memory; 0 = no cap */
+} HyCreateInfo;
+
+/* == uboLight, src/vk_engine.h:76-80 (std140, 48 B).  pos.w = maxDistance, or -1
+ *    for a directional light (src/vk_engine.cpp:146-164); color.w = intensity. */
+typedef struct HyLight {
+    float pos[4];
+    float color[4];
+    float radius;
+    float _pad[3];
+} HyLight;
+
+/* == GPUMaterial, src/material.h:5-10, filled by Material::materialToShader
+ *    (src/material.cpp:19-26): diffuse = (rgb, ior); textures = (diffuse,
+ *    normal, emissive, metallicRoughness) texture ids or -1; smr =
+ *    (shadingModel, metallic, roughness, material index). */
+typedef struct HyMaterial {
+    float diffuse[4];
+    float textures[4];
+    float smr[4];
+} HyMaterial;
+
+/* == Vertex, src/vk_mesh.h:21-33 (44 B, tightly packed). */
+typedef struct HyVertex {
+    float pos[3];
+    float normal[3];
+    float color[3];
+    float uv[2];
+} HyVertex;
+
+/* One Primitive of a Node (src/vk_mesh.h:72-155).  first_index/index_count
+ * address the index array; index values are relative to vertex_offset (the
+ * start of the owning mesh's vertices).  material_id/transform_id are the
+ * .y/.z of the per-primitive id vec4 (src/vk_mesh.cpp:521-533). */
+typedef struct HyPrimitive {
+    uint32_t first_index;
+    uint32_t index_count;
+    uint32_t vertex_offset;
+    uint32_t material_id;
+    uint32_t transform_id;
+    uint32_t instance_id;
+} HyPrimitive;
+
+/* == RTCameraData, src/vk_engine.h:56-62 (column-major glm mat4s).
+ *    frame[0] seeds the per-pixel RNG: _denoise_frame with denoise on, else 0
+ *    (src/vk_engine.cpp:733). */
+typedef struct HyCamera {
+    float inv_view[16];
+    float inv_proj[16];
+    float frame[4];
+} HyCamera;
+
+/* G-buffer plane formats.  The reference's own attachments are
+ * RGBA16F, RGBA16F, RGBA8, RG16F, RGBA8, RGBA8 (src/renderer.cpp:255-260). */
+enum {
+    HY_FMT_RGBA32F = 0,
+    HY_FMT_RG32F   = 1,
+    HY_FMT_RGBA16F = 2,
+    HY_FMT_RG16F   = 3,
+    HY_FMT_RGBA8   = 4
+};
+
+/* Plane order and encoding of geometry_shader.frag:66-76:
+ *   0 (worldPos, materialIdx)  1 (N*0.5+0.5, 1)  2 albedo.rgb
+ *   3 motion*0.5+0.5           4 (0, roughness, metallic)  5 emissive.rgb
+ * Rows are tightly packed (pitch = width * texel size). */
+typedef struct HyGBuffer {
+    uint32_t    width;
+    uint32_t    height;
+    const void* plane[6];
+    uint32_t    format[6];
+} HyGBuffer;
+
+/* Per-light shadow images.  HY_ACCUM_U8 is the reference's R8_UNORM
+ * (src/renderer.cpp:1538); HY_ACCUM_F32 keeps full precision.  Light l's
+ * plane starts at l * width * height elements. */
+enum { HY_ACCUM_U8 = 0, HY_ACCUM_F32 = 1 };
+
+typedef struct HyAccum {
+    uint32_t format;
+    uint32_t num_lights;
+    void*    history;      /* device, caller-owned: the reference's _denoisedImages */
+} HyAccum;
+
+/* RNG modes.  REFERENCE reproduces sampleDisk's by-value seed
+ * (helpers.glsl:82-93): all samples of one pixel are the same ray, which is
+ * traced once.  DECORRELATED advances the TEA/LCG stream per sample. */
+enum { HY_RNG_REFERENCE = 0, HY_RNG_DECORRELATED = 1 };
+
+#define HY_FLAG_FULL_BLUR_DISPATCH 0x1u /* also accumulate the texels the W/16 x H/16 dispatch skips */
+#define HY_FLAG_NO_ACCUM           0x2u /* shade from the raw shadow images, no denoise pass */
+#define HY_FLAG_COUNT_TRAVERSAL    0x4u /* count BVH nodes visited / triangles tested into HyStats */
+#define HY_FLAG_NO_STATUS_SYNC     0x8u /* do not read back the status word (no host sync) */
+
+typedef struct HyPassConfig {
+    uint32_t shadow_spp;    /* samplesBuffer.samples (1..64, src/renderer.cpp:656) */
+    uint32_t max_bounces;   /* MAX_RECURSION (helpers.glsl:8): 8 */
+    uint32_t rng_mode;      /* HY_RNG_* */
+    int32_t  accum_frame;   /* frameCountBuffer = _denoise_frame (src/vk_engine.cpp:722) */
+    uint32_t flags;         /* HY_FLAG_* */
+    uint32_t block_size;    /* threads per block; 0 = default / autotuned */
+    uint32_t queue_chunk;   /* work items fetched per warp from the ray queue; 0 = default */
+    uint32_t stack_depth;   /* traversal stack entries; 0 = default (max 64) */
+} HyPassConfig;
+
+typedef struct HyStats {
+    uint64_t shadow_rays;       /* rays traced by the shadow pass */
+    uint64_t reflection_rays;   /* closest-hit bounce rays of mirror/glass pixels */
+    uint64_t hit_shadow_rays;   /* shadow rays cast from bounce hit points */
+    uint64_t nodes_visited;     /* with HY_FLAG_COUNT_TRAVERSAL */
+    uint64_t tris_tested;       /* with HY_FLAG_COUNT_TRAVERSAL */
+    uint32_t error_flags;       /* HY_STATUS_* */
+    uint32_t _pad;
+} HyStats;
+
+typedef struct HyBvhStats {
+    uint32_t num_tris;
+    uint32_t num_bvh2_nodes;    /* internal nodes of the binary LBVH */
+    uint32_t num_bvh8_nodes;
+    uint32_t depth;             /* BVH8 levels */
+    float    build_ms;          /* device time of the whole build */
+    float    scene_lo[3];
+    float    scene_hi[3];
+} HyBvhStats;
+
+/* Ray / hit records of hy_trace_rays: 32 B in, 16 B out.  tri_id is the
+ * triangle's global index (primitives in upload order, index_count/3 each);
+ * b1/b2 are the barycentrics of vertices 1/2 (Vulkan's hit attributes). */
+typedef struct HyRay { float org[3]; float tmin; float dir[3]; float tmax; } HyRay;
+typedef struct HyHit { float t; uint32_t tri_id; float b1; float b2; } HyHit;
+#define HY_NO_HIT 0xffffffffu
+
+/* ---- context ---- */
+int         hy_create(HyCtx** out, const HyCreateInfo* info);
+void        hy_destroy(HyCtx* ctx);
+const char* hy_error_string(int code);
+int         hy_get_abi_version(void);
+int         hy_synchronize(HyCtx* ctx);
+/* Allocation hook for fault-injection tests: the next `n`-th device
+ * allocation made by the context fails with HY_ERR_OOM (0 disables). */
+int         hy_debug_fail_alloc_after(HyCtx* ctx, uint32_t n);
+
+/* ---- scene upload (host arrays; replaces Renderer::load_data_to_gpu,
+ *      src/renderer.cpp:1477-1530, and the per-entity rtVertexAttribute /
+ *      index / id buffers of create_hybrid_descriptors, :3015-3048) ---- */
+int hy_scene_set_geometry(HyCtx* ctx,
+                          const HyVertex* verts, uint32_t num_verts,
+                          const uint32_t* indices, uint32_t num_indices,
+                          const HyPrimitive* prims, uint32_t num_prims,
+                          const float* transforms /* column-major mat4s */, uint32_t num_transforms);
+int hy_scene_set_materials(HyCtx* ctx, const HyMaterial* mats, uint32_t num_mats);
+int hy_scene_set_lights(HyCtx* ctx, const HyLight* lights, uint32_t num_lights);
+/* slot 0 = sky (miss.rmiss, skybox[0]), slot 1 = irradiance (environmentTexture[1]) */
+int hy_scene_set_env(HyCtx* ctx, int slot, const uint8_t* rgba8, uint32_t width, uint32_t height);
+
+/* ---- acceleration structure (replaces buildBlas/buildTlas) ---- */
+int hy_bvh_build(HyCtx* ctx, HyBvhStats* stats);
+/* Re-transforms the triangles with new transforms and refits every node box
+ * (topology kept): the per-frame TLAS update of src/vk_engine.cpp:172-187. */
+int hy_bvh_refit(HyCtx* ctx, const float* transforms, uint32_t num_transforms);
+/* Copies the built structure out for topology checks.  Any pointer may be
+ * NULL.  morton/order: num_tris each (sorted codes and triangle ids);
+ * bvh2: 10 words per internal node (left, right, first, last, lo[3], hi[3];
+ * a child with bit 31 set is leaf number child & 0x7fffffff); bvh8: 20 words
+ * per node; tris: 12 words per triangle. */
+int hy_bvh_download(HyCtx* ctx, uint32_t* morton, uint32_t* order, uint32_t* bvh2,
+                    uint32_t* bvh8, float* tris);
+
+/* ---- ray queries (any_hit: TerminateOnFirstHit semantics) ---- */
+int hy_trace_rays(HyCtx* ctx, const HyRay* d_rays, uint32_t num_rays, int any_hit,
+                  HyHit* d_hits, HyStats* stats);
+
+/* ---- G-buffer producer: primary rays (raygen.rgen:29-40 camera model)
+ *      writing the geometry_shader.frag encoding into RGBA32F/RG32F planes ---- */
+int hy_gbuffer_primary(HyCtx* ctx, const HyCamera* cam, uint32_t width, uint32_t height,
+                       float* d_planes[6]);
+
+/* ---- the pass ---- */
+/* shadowRaygen.rgen: writes one shadow image per light into d_shadow
+ * (format accum_format, num_lights planes). */
+int hy_shadow_pass(HyCtx* ctx, const HyGBuffer* gb, const HyCamera* cam,
+                   const HyPassConfig* cfg, uint32_t accum_format, void* d_shadow, HyStats* stats);
+/* blur.comp: folds the shadow images into the history (in place). */
+int hy_accumulate_pass(HyCtx* ctx, const HyGBuffer* gb, const HyPassConfig* cfg,
+                       const void* d_shadow, HyAccum* accum);
+/* hybridRaygen.rgen + hybridHit.rchit + miss.rmiss: shades from the
+ * accumulated shadow images.  d_out_rgba32f (W*H*4 floats) and
+ * d_out_bgra8 (the reference's B8G8R8A8 _rtImage) may each be NULL. */
+int hy_shade_pass(HyCtx* ctx, const HyGBuffer* gb, const HyCamera* cam,
+                  const HyPassConfig* cfg, const HyAccum* accum,
+                  float* d_out_rgba32f, uint8_t* d_out_bgra8, HyStats* stats);
+/* The three passes in order, fused where the data flow allows. */
+int hy_hybrid_forward(HyCtx* ctx, const HyGBuffer* gb, const HyCamera* cam,
+                      const HyPassConfig* cfg, HyAccum* accum,
+                      float* d_out_rgba32f, uint8_t* d_out_bgra8, HyStats* stats);
+/* Same, with host G-buffer planes and host outputs: the planes are copied in
+ * and the outputs copied back inside the call (pinned host memory makes the
+ * copies asynchronous).  The history stays on the device (accum). */
+int hy_hybrid_forward_host(HyCtx* ctx, const HyGBuffer* h_gb, const HyCamera* cam,
+                           const HyPassConfig* cfg, HyAccum* accum,
+                           float* h_out_rgba32f, uint8_t* h_out_bgra8, HyStats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HYBRIDRT_H */

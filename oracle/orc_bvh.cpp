@@ -1,0 +1,554 @@
+// ORACLE — test infrastructure only (see orc_math.hpp).
+//
+// CPU restatement of the acceleration structure that replaces the driver's
+// BLAS/TLAS (src/renderer.cpp:1696-1865) and of its traversal (the hidden part
+// of traceRayEXT at shadowRaygen.rgen:78, hybridRaygen.rgen:158,
+// hybridHit.rchit:322).  The algorithm is written down here in plain C++ so the
+// product's GPU build can be compared with it array for array:
+//
+//   1. world triangles: M * v with the fixed, unfused order ((m0 x + m1 y) + m2 z) + m3
+//   2. 30-bit Morton codes of the AABB centroids over the centroid bounds
+//   3. stable sort by Morton code (ties keep triangle order)
+//   4. Karras 2012 binary radix tree over the 64-bit keys (morton << 32 | id)
+//   5. bottom-up box refit
+//   6. BFS collapse into 8-wide nodes: greedily open the child with the
+//      largest surface area, then assign children to octant slots by a
+//      greedy maximum of dot(child centroid - node centroid, slot corner)
+//   7. quantise child boxes to 8 bits per axis against a power-of-two scale
+//      (Ylitie, Karras & Laine 2017 node format), rounding outwards
+//
+// Compiled with -ffp-contract=off -frounding-math: every float operation is a
+// single IEEE-rounded op, as the CUDA build writes them with __f*_rn/_rd/_ru.
+#include <algorithm>
+#include <cfenv>
+#include <cstdio>
+#include <numeric>
+
+#include "orc_scene.hpp"
+
+namespace orc {
+
+static inline float fmin2(float a, float b) { return std::fmin(a, b); }
+static inline float fmax2(float a, float b) { return std::fmax(a, b); }
+
+static float sub_dir(float a, float b, int mode) {
+    std::fesetround(mode);
+    volatile float va = a, vb = b;
+    volatile float r = va - vb;
+    std::fesetround(FE_TONEAREST);
+    return r;
+}
+static float div_up(float a, float b) {
+    std::fesetround(FE_UPWARD);
+    volatile float va = a, vb = b;
+    volatile float r = va / vb;
+    std::fesetround(FE_TONEAREST);
+    return r;
+}
+
+static void inverse4(const double* m, double* inv) {
+    // cofactor expansion, column-major in and out
+    double a[16];
+    for (int i = 0; i < 16; i++) a[i] = m[i];
+    inv[0] = a[5] * a[10] * a[15] - a[5] * a[11] * a[14] - a[9] * a[6] * a[15] + a[9] * a[7] * a[14] + a[13] * a[6] * a[11] - a[13] * a[7] * a[10];
+    inv[4] = -a[4] * a[10] * a[15] + a[4] * a[11] * a[14] + a[8] * a[6] * a[15] - a[8] * a[7] * a[14] - a[12] * a[6] * a[11] + a[12] * a[7] * a[10];
+    inv[8] = a[4] * a[9] * a[15] - a[4] * a[11] * a[13] - a[8] * a[5] * a[15] + a[8] * a[7] * a[13] + a[12] * a[5] * a[11] - a[12] * a[7] * a[9];
+    inv[12] = -a[4] * a[9] * a[14] + a[4] * a[10] * a[13] + a[8] * a[5] * a[14] - a[8] * a[6] * a[13] - a[12] * a[5] * a[10] + a[12] * a[6] * a[9];
+    inv[1] = -a[1] * a[10] * a[15] + a[1] * a[11] * a[14] + a[9] * a[2] * a[15] - a[9] * a[3] * a[14] - a[13] * a[2] * a[11] + a[13] * a[3] * a[10];
+    inv[5] = a[0] * a[10] * a[15] - a[0] * a[11] * a[14] - a[8] * a[2] * a[15] + a[8] * a[3] * a[14] + a[12] * a[2] * a[11] - a[12] * a[3] * a[10];
+    inv[9] = -a[0] * a[9] * a[15] + a[0] * a[11] * a[13] + a[8] * a[1] * a[15] - a[8] * a[3] * a[13] - a[12] * a[1] * a[11] + a[12] * a[3] * a[9];
+    inv[13] = a[0] * a[9] * a[14] - a[0] * a[10] * a[13] - a[8] * a[1] * a[14] + a[8] * a[2] * a[13] + a[12] * a[1] * a[10] - a[12] * a[2] * a[9];
+    inv[2] = a[1] * a[6] * a[15] - a[1] * a[7] * a[14] - a[5] * a[2] * a[15] + a[5] * a[3] * a[14] + a[13] * a[2] * a[7] - a[13] * a[3] * a[6];
+    inv[6] = -a[0] * a[6] * a[15] + a[0] * a[7] * a[14] + a[4] * a[2] * a[15] - a[4] * a[3] * a[14] - a[12] * a[2] * a[7] + a[12] * a[3] * a[6];
+    inv[10] = a[0] * a[5] * a[15] - a[0] * a[7] * a[13] - a[4] * a[1] * a[15] + a[4] * a[3] * a[13] + a[12] * a[1] * a[7] - a[12] * a[3] * a[5];
+    inv[14] = -a[0] * a[5] * a[14] + a[0] * a[6] * a[13] + a[4] * a[1] * a[14] - a[4] * a[2] * a[13] - a[12] * a[1] * a[6] + a[12] * a[2] * a[5];
+    inv[3] = -a[1] * a[6] * a[11] + a[1] * a[7] * a[10] + a[5] * a[2] * a[11] - a[5] * a[3] * a[10] - a[9] * a[2] * a[7] + a[9] * a[3] * a[6];
+    inv[7] = a[0] * a[6] * a[11] - a[0] * a[7] * a[10] - a[4] * a[2] * a[11] + a[4] * a[3] * a[10] + a[8] * a[2] * a[7] - a[8] * a[3] * a[6];
+    inv[11] = -a[0] * a[5] * a[11] + a[0] * a[7] * a[9] + a[4] * a[1] * a[11] - a[4] * a[3] * a[9] - a[8] * a[1] * a[7] + a[8] * a[3] * a[5];
+    inv[15] = a[0] * a[5] * a[10] - a[0] * a[6] * a[9] - a[4] * a[1] * a[10] + a[4] * a[2] * a[9] + a[8] * a[1] * a[6] - a[8] * a[2] * a[5];
+    double det = a[0] * inv[0] + a[1] * inv[4] + a[2] * inv[8] + a[3] * inv[12];
+    double r = 1.0 / det;
+    for (int i = 0; i < 16; i++) inv[i] *= r;
+}
+
+void scene_derive(Scene& s) {
+    // normal matrices: mat3(transpose(inverse(model))) (hybridHit.rchit:26, basic.vert:44)
+    size_t nx = s.xf.size() / 16;
+    s.nrm.assign(nx * 9, 0.f);
+    for (size_t t = 0; t < nx; t++) {
+        double m[16], inv[16];
+        for (int i = 0; i < 16; i++) m[i] = s.xf[t * 16 + i];
+        inverse4(m, inv);
+        // nrm(r, c) = inv(c, r); column-major: nrm[c*3 + r] = inv[r*4 + c]
+        for (int c = 0; c < 3; c++)
+            for (int r = 0; r < 3; r++) s.nrm[t * 9 + c * 3 + r] = (float)inv[r * 4 + c];
+    }
+    s.prim_tri0.resize(s.prims.size());
+    uint32_t nt = 0;
+    for (size_t p = 0; p < s.prims.size(); p++) { s.prim_tri0[p] = nt; nt += s.prims[p].index_count / 3; }
+    s.ntri = nt;
+    s.world.assign((size_t)nt * 9, 0.f);
+    s.tri_prim.assign(nt, 0);
+    for (size_t p = 0; p < s.prims.size(); p++) {
+        const HyPrimitive& pr = s.prims[p];
+        const float* M = &s.xf[(size_t)pr.transform_id * 16];
+        for (uint32_t k = 0; k < pr.index_count / 3; k++) {
+            uint32_t t = s.prim_tri0[p] + k;
+            s.tri_prim[t] = (uint32_t)p;
+            for (int v = 0; v < 3; v++) {
+                uint32_t vi = s.idx[pr.first_index + 3 * k + v] + pr.vertex_offset;
+                const float* P = s.verts[vi].pos;
+                for (int r = 0; r < 3; r++) {
+                    float acc = M[0 * 4 + r] * P[0];
+                    acc = acc + M[1 * 4 + r] * P[1];
+                    acc = acc + M[2 * 4 + r] * P[2];
+                    acc = acc + M[3 * 4 + r];
+                    s.world[(size_t)t * 9 + v * 3 + r] = acc;
+                }
+            }
+        }
+    }
+    s.bvh_ok = false;
+}
+
+static inline uint32_t expand10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+static inline int clz64(uint64_t x) { return x ? __builtin_clzll(x) : 64; }
+
+struct Box { float lo[3], hi[3]; };
+
+static inline float surface(const Box& b) {
+    float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+    float a = dx * dy;
+    a = a + dy * dz;
+    a = a + dz * dx;
+    return a;
+}
+
+void bvh_build(Scene& s) {
+    Bvh& B = s.bvh;
+    B = Bvh();
+    const uint32_t n = s.ntri;
+    B.n = n;
+    if (n == 0) { s.bvh_ok = false; return; }
+    std::vector<Box> tb(n);
+    std::vector<float> cen((size_t)n * 3);
+    for (int a = 0; a < 3; a++) { B.slo[a] = INFINITY; B.shi[a] = -INFINITY; }
+    for (uint32_t t = 0; t < n; t++) {
+        const float* w = &s.world[(size_t)t * 9];
+        for (int a = 0; a < 3; a++) {
+            tb[t].lo[a] = fmin2(fmin2(w[a], w[3 + a]), w[6 + a]);
+            tb[t].hi[a] = fmax2(fmax2(w[a], w[3 + a]), w[6 + a]);
+            float c = (tb[t].lo[a] + tb[t].hi[a]) * 0.5f;
+            cen[(size_t)t * 3 + a] = c;
+            B.slo[a] = fmin2(B.slo[a], c);
+            B.shi[a] = fmax2(B.shi[a], c);
+        }
+    }
+    float inv[3];
+    for (int a = 0; a < 3; a++) {
+        float ext = B.shi[a] - B.slo[a];
+        inv[a] = ext > 0.f ? 1024.0f / ext : 0.f;
+    }
+    std::vector<uint32_t> code(n);
+    for (uint32_t t = 0; t < n; t++) {
+        uint32_t q[3];
+        for (int a = 0; a < 3; a++) {
+            float v = (cen[(size_t)t * 3 + a] - B.slo[a]) * inv[a];
+            v = fmin2(fmax2(v, 0.f), 1023.f);
+            q[a] = (uint32_t)v;
+        }
+        code[t] = (expand10(q[0]) << 2) | (expand10(q[1]) << 1) | expand10(q[2]);
+    }
+    B.order.resize(n);
+    std::iota(B.order.begin(), B.order.end(), 0u);
+    std::stable_sort(B.order.begin(), B.order.end(), [&](uint32_t a, uint32_t b) { return code[a] < code[b]; });
+    B.morton.resize(n);
+    std::vector<uint64_t> key(n);
+    for (uint32_t i = 0; i < n; i++) {
+        B.morton[i] = code[B.order[i]];
+        key[i] = ((uint64_t)B.morton[i] << 32) | B.order[i];
+    }
+    // ---- Karras 2012 ----
+    auto delta = [&](int64_t i, int64_t j) -> int {
+        if (j < 0 || j >= (int64_t)n) return -1;
+        return clz64(key[i] ^ key[j]);
+    };
+    if (n > 1) {
+        B.bvh2.resize(n - 1);
+        for (int64_t i = 0; i < (int64_t)n - 1; i++) {
+            int d = (delta(i, i + 1) - delta(i, i - 1)) >= 0 ? 1 : -1;
+            int dmin = delta(i, i - d);
+            int64_t lmax = 2;
+            while (delta(i, i + lmax * d) > dmin) lmax *= 2;
+            int64_t l = 0;
+            for (int64_t t = lmax / 2; t >= 1; t /= 2)
+                if (delta(i, i + (l + t) * d) > dmin) l += t;
+            int64_t j = i + l * d;
+            int dnode = delta(i, j);
+            int64_t sp = 0;
+            for (int64_t div = 2;; div *= 2) {
+                int64_t t = (l + div - 1) / div;
+                if (delta(i, i + (sp + t) * d) > dnode) sp += t;
+                if (t == 1) break;
+            }
+            int64_t gamma = i + sp * d + std::min(d, 0);
+            int64_t lo = std::min(i, j), hi = std::max(i, j);
+            Bvh2Node& nd = B.bvh2[i];
+            nd.left = (lo == gamma) ? (kLeafBit | (uint32_t)gamma) : (uint32_t)gamma;
+            nd.right = (hi == gamma + 1) ? (kLeafBit | (uint32_t)(gamma + 1)) : (uint32_t)(gamma + 1);
+            nd.first = (uint32_t)lo;
+            nd.last = (uint32_t)hi;
+        }
+        // ---- refit (recursive post-order; union is order independent) ----
+        std::vector<uint32_t> stack;
+        std::vector<uint8_t> done(n - 1, 0);
+        stack.push_back(0);
+        while (!stack.empty()) {
+            uint32_t i = stack.back();
+            Bvh2Node& nd = B.bvh2[i];
+            bool ready = true;
+            for (uint32_t c : {nd.left, nd.right})
+                if (!(c & kLeafBit) && !done[c]) { stack.push_back(c); ready = false; }
+            if (!ready) continue;
+            stack.pop_back();
+            for (int a = 0; a < 3; a++) {
+                float lo2[2], hi2[2];
+                int k = 0;
+                for (uint32_t c : {nd.left, nd.right}) {
+                    if (c & kLeafBit) {
+                        const Box& b = tb[B.order[c & ~kLeafBit]];
+                        lo2[k] = b.lo[a]; hi2[k] = b.hi[a];
+                    } else {
+                        lo2[k] = B.bvh2[c].lo[a]; hi2[k] = B.bvh2[c].hi[a];
+                    }
+                    k++;
+                }
+                nd.lo[a] = fmin2(lo2[0], lo2[1]);
+                nd.hi[a] = fmax2(hi2[0], hi2[1]);
+            }
+            done[i] = 1;
+        }
+    }
+    auto ref_box = [&](uint32_t r) -> Box {
+        if (r & kLeafBit) return tb[B.order[r & ~kLeafBit]];
+        Box b;
+        for (int a = 0; a < 3; a++) { b.lo[a] = B.bvh2[r].lo[a]; b.hi[a] = B.bvh2[r].hi[a]; }
+        return b;
+    };
+    auto ref_count = [&](uint32_t r) -> uint32_t {
+        if (r & kLeafBit) return 1;
+        return B.bvh2[r].last - B.bvh2[r].first + 1;
+    };
+    auto ref_first = [&](uint32_t r) -> uint32_t {
+        if (r & kLeafBit) return r & ~kLeafBit;
+        return B.bvh2[r].first;
+    };
+    // ---- BFS collapse to BVH8 ----
+    std::vector<uint32_t> queue;       // BVH2 ref of each BVH8 node, BFS order
+    std::vector<uint32_t> level;       // level of each node
+    queue.push_back(n > 1 ? 0u : (kLeafBit | 0u));
+    level.push_back(0);
+    uint32_t tri_count = 0;
+    B.tris.assign((size_t)n * 12, 0.f);
+    for (size_t k = 0; k < queue.size(); k++) {
+        uint32_t r = queue[k];
+        // children list
+        uint32_t C[8];
+        int nc = 0;
+        if (r & kLeafBit) { C[nc++] = r; }
+        else { C[nc++] = B.bvh2[r].left; C[nc++] = B.bvh2[r].right; }
+        while (nc < 8) {
+            int best = -1;
+            float bestA = -1.f;
+            for (int i = 0; i < nc; i++) {
+                if (C[i] & kLeafBit) continue;
+                float A = surface(ref_box(C[i]));
+                if (best < 0 || A > bestA || (A == bestA && C[i] < C[best])) { best = i; bestA = A; }
+            }
+            if (best < 0) break;
+            uint32_t open = C[best];
+            C[best] = B.bvh2[open].left;
+            C[nc++] = B.bvh2[open].right;
+        }
+        // slot assignment
+        Box nb = ref_box(r);
+        float pc[3];
+        for (int a = 0; a < 3; a++) pc[a] = (nb.lo[a] + nb.hi[a]) * 0.5f;
+        float cost[8][8];
+        for (int i = 0; i < nc; i++) {
+            Box cb = ref_box(C[i]);
+            float dd[3];
+            for (int a = 0; a < 3; a++) dd[a] = (cb.lo[a] + cb.hi[a]) * 0.5f - pc[a];
+            for (int sl = 0; sl < 8; sl++) {
+                float c0 = (sl & 1) ? dd[0] : -dd[0];
+                float c1 = (sl & 2) ? dd[1] : -dd[1];
+                float c2 = (sl & 4) ? dd[2] : -dd[2];
+                cost[i][sl] = (c0 + c1) + c2;
+            }
+        }
+        int slot_of[8];
+        int child_in_slot[8];
+        for (int i = 0; i < 8; i++) { slot_of[i] = -1; child_in_slot[i] = -1; }
+        for (int it = 0; it < nc; it++) {
+            int bi = -1, bs = -1;
+            float bc = 0.f;
+            for (int i = 0; i < nc; i++) {
+                if (slot_of[i] >= 0) continue;
+                for (int sl = 0; sl < 8; sl++) {
+                    if (child_in_slot[sl] >= 0) continue;
+                    if (bi < 0 || cost[i][sl] > bc) { bi = i; bs = sl; bc = cost[i][sl]; }
+                }
+            }
+            slot_of[bi] = bs;
+            child_in_slot[bs] = bi;
+        }
+        // encode
+        Bvh8Node node;
+        std::memset(&node, 0, sizeof(node));
+        uint32_t e[3];
+        float inv_s[3];
+        for (int a = 0; a < 3; a++) {
+            node.w[a] = fbits(nb.lo[a]);
+            float ext = sub_dir(nb.hi[a], nb.lo[a], FE_UPWARD);
+            float t = div_up(ext, 255.0f);
+            uint32_t tb_ = fbits(t);
+            int E = (int)((tb_ >> 23) & 0xffu);
+            int ex = (E == 0) ? -100 : (E - 127 + ((tb_ & 0x7fffffu) ? 1 : 0));
+            ex = std::max(-100, std::min(100, ex));
+            e[a] = (uint32_t)(ex + 127);
+            inv_s[a] = bitsf((uint32_t)(127 - ex) << 23);
+        }
+        uint32_t imask = 0;
+        uint8_t meta[8] = {0}, qlo[3][8], qhi[3][8];
+        std::memset(qlo, 0, sizeof(qlo));
+        std::memset(qhi, 0, sizeof(qhi));
+        uint32_t child_base = (uint32_t)queue.size();
+        uint32_t tri_base = tri_count;
+        uint32_t toff = 0;
+        for (int sl = 0; sl < 8; sl++) {
+            int i = child_in_slot[sl];
+            if (i < 0) continue;
+            uint32_t c = C[i];
+            Box cb = ref_box(c);
+            for (int a = 0; a < 3; a++) {
+                float lo = std::floor(sub_dir(cb.lo[a], nb.lo[a], FE_DOWNWARD) * inv_s[a]);
+                float hi = std::ceil(sub_dir(cb.hi[a], nb.lo[a], FE_UPWARD) * inv_s[a]);
+                lo = fmin2(fmax2(lo, 0.f), 255.f);
+                hi = fmin2(fmax2(hi, 0.f), 255.f);
+                qlo[a][sl] = (uint8_t)lo;
+                qhi[a][sl] = (uint8_t)hi;
+            }
+            uint32_t cnt = ref_count(c);
+            if (cnt > (uint32_t)kLeafMax) {
+                imask |= 1u << sl;
+                meta[sl] = 0x80;
+                queue.push_back(c);
+                level.push_back(level[k] + 1);
+            } else {
+                meta[sl] = (uint8_t)((cnt << 5) | toff);
+                uint32_t f = ref_first(c);
+                for (uint32_t j = 0; j < cnt; j++) {
+                    uint32_t tid = B.order[f + j];
+                    float* dst = &B.tris[(size_t)(tri_count + toff + j) * 12];
+                    const float* w = &s.world[(size_t)tid * 9];
+                    dst[0] = w[0]; dst[1] = w[1]; dst[2] = w[2]; dst[3] = bitsf(tid);
+                    dst[4] = w[3]; dst[5] = w[4]; dst[6] = w[5]; dst[7] = 0.f;
+                    dst[8] = w[6]; dst[9] = w[7]; dst[10] = w[8]; dst[11] = 0.f;
+                }
+                toff += cnt;
+            }
+        }
+        tri_count += toff;
+        node.w[3] = e[0] | (e[1] << 8) | (e[2] << 16) | (imask << 24);
+        node.w[4] = child_base;
+        node.w[5] = tri_base;
+        auto pack4 = [](const uint8_t* b) { return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24); };
+        node.w[6] = pack4(meta); node.w[7] = pack4(meta + 4);
+        node.w[8] = pack4(qlo[0]); node.w[9] = pack4(qlo[0] + 4);
+        node.w[10] = pack4(qlo[1]); node.w[11] = pack4(qlo[1] + 4);
+        node.w[12] = pack4(qlo[2]); node.w[13] = pack4(qlo[2] + 4);
+        node.w[14] = pack4(qhi[0]); node.w[15] = pack4(qhi[0] + 4);
+        node.w[16] = pack4(qhi[1]); node.w[17] = pack4(qhi[1] + 4);
+        node.w[18] = pack4(qhi[2]); node.w[19] = pack4(qhi[2] + 4);
+        B.bvh8.push_back(node);
+    }
+    B.depth = level.empty() ? 0 : level.back() + 1;
+    s.bvh_ok = true;
+}
+
+// ---- watertight ray/triangle test (Woop, Benthin & Wald, JCGT 2013) -----------
+struct RayPre {
+    float o[3], d[3];
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+
+static RayPre ray_pre(const float o[3], const float d[3]) {
+    RayPre r;
+    for (int a = 0; a < 3; a++) { r.o[a] = o[a]; r.d[a] = d[a]; }
+    float ax = std::fabs(d[0]), ay = std::fabs(d[1]), az = std::fabs(d[2]);
+    r.kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
+    r.kx = r.kz + 1; if (r.kx == 3) r.kx = 0;
+    r.ky = r.kx + 1; if (r.ky == 3) r.ky = 0;
+    if (d[r.kz] < 0.f) std::swap(r.kx, r.ky);
+    r.Sx = d[r.kx] / d[r.kz];
+    r.Sy = d[r.ky] / d[r.kz];
+    r.Sz = 1.0f / d[r.kz];
+    return r;
+}
+
+// returns true and t/b1/b2 when the triangle is hit with tmin <= t <= tmax
+static bool tri_test(const RayPre& r, const float* v0, const float* v1, const float* v2, float tmin, float tmax,
+                     float& t, float& b1, float& b2) {
+    float A[3], Bv[3], Cv[3];
+    for (int a = 0; a < 3; a++) { A[a] = v0[a] - r.o[a]; Bv[a] = v1[a] - r.o[a]; Cv[a] = v2[a] - r.o[a]; }
+    float Ax = A[r.kx] - r.Sx * A[r.kz], Ay = A[r.ky] - r.Sy * A[r.kz];
+    float Bx = Bv[r.kx] - r.Sx * Bv[r.kz], By = Bv[r.ky] - r.Sy * Bv[r.kz];
+    float Cx = Cv[r.kx] - r.Sx * Cv[r.kz], Cy = Cv[r.ky] - r.Sy * Cv[r.kz];
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if (U == 0.f || V == 0.f || W == 0.f) {
+        double CxBy = (double)Cx * (double)By, CyBx = (double)Cy * (double)Bx;
+        U = (float)(CxBy - CyBx);
+        double AxCy = (double)Ax * (double)Cy, AyCx = (double)Ay * (double)Cx;
+        V = (float)(AxCy - AyCx);
+        double BxAy = (double)Bx * (double)Ay, ByAx = (double)By * (double)Ax;
+        W = (float)(BxAy - ByAx);
+    }
+    if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return false;
+    float det = U + V;
+    det = det + W;
+    if (det == 0.f) return false;
+    float Az = r.Sz * A[r.kz], Bz = r.Sz * Bv[r.kz], Cz = r.Sz * Cv[r.kz];
+    float T = U * Az;
+    T = T + V * Bz;
+    T = T + W * Cz;
+    float tt = T / det;
+    if (!(tt >= tmin && tt <= tmax)) return false;
+    t = tt;
+    b1 = V / det;
+    b2 = W / det;
+    return true;
+}
+
+static inline bool better(float t, uint32_t id, const Hit& h) {
+    return t < h.t || (t == h.t && id < h.id);
+}
+
+static Hit trace_brute(const Scene& s, const float o[3], const float d[3], float tmin, float tmax, bool any_hit,
+                       Counters* c) {
+    Hit h{tmax, HY_NO_HIT, 0.f, 0.f};
+    RayPre r = ray_pre(o, d);
+    for (uint32_t t = 0; t < s.ntri; t++) {
+        const float* w = &s.world[(size_t)t * 9];
+        float tt, b1, b2;
+        if (c) c->tris++;
+        if (tri_test(r, w, w + 3, w + 6, tmin, h.id == HY_NO_HIT ? tmax : h.t, tt, b1, b2)) {
+            if (h.id == HY_NO_HIT || better(tt, t, h)) h = Hit{tt, t, b1, b2};
+            if (any_hit) return h;
+        }
+    }
+    return h;
+}
+
+static inline uint8_t byte_of(const uint32_t* w, int word0, int slot) {
+    return (uint8_t)(w[word0 + (slot >> 2)] >> ((slot & 3) * 8));
+}
+
+static Hit trace_bvh8(const Scene& s, const float o[3], const float d[3], float tmin, float tmax, bool any_hit,
+                      Counters* c) {
+    const Bvh& B = s.bvh;
+    Hit h{tmax, HY_NO_HIT, 0.f, 0.f};
+    RayPre r = ray_pre(o, d);
+    float invd[3];
+    for (int a = 0; a < 3; a++) {
+        float dd = std::fabs(d[a]) > 1e-20f ? d[a] : std::copysign(1e-20f, d[a]);
+        invd[a] = 1.0f / dd;
+    }
+    uint32_t near = (invd[0] < 0.f ? 1u : 0u) | (invd[1] < 0.f ? 2u : 0u) | (invd[2] < 0.f ? 4u : 0u);
+    uint32_t stk_base[kStackMax], stk_bits[kStackMax];
+    int sp = 0;
+    uint32_t g_base = 0, g_bits = (1u << 24) | (1u << near);
+    float cur_tmax = tmax;
+    for (uint32_t iter = 0;; iter++) {
+        if (iter >= kMaxIters) { if (c) c->status |= HY_STATUS_TIMEOUT; break; }
+        if ((g_bits & 0xff000000u) == 0) {
+            if (sp == 0) break;
+            --sp;
+            g_base = stk_base[sp];
+            g_bits = stk_bits[sp];
+        }
+        uint32_t rb = (uint32_t)__builtin_ctz(g_bits >> 24);
+        g_bits &= ~(1u << (24 + rb));
+        uint32_t sl = rb ^ near;
+        uint32_t idx = g_base + (uint32_t)__builtin_popcount(g_bits & 0xffu & ((1u << sl) - 1u));
+        if (g_bits & 0xff000000u) {
+            if (sp >= kStackMax) { if (c) c->status |= HY_STATUS_STACK_OVERFLOW; break; }
+            stk_base[sp] = g_base;
+            stk_bits[sp] = g_bits;
+            sp++;
+        }
+        const uint32_t* w = B.bvh8[idx].w;
+        if (c) c->nodes++;
+        float adj[3], org[3];
+        for (int a = 0; a < 3; a++) {
+            uint32_t ea = (w[3] >> (8 * a)) & 0xffu;
+            float sc = bitsf(ea << 23);
+            adj[a] = sc * invd[a];
+            org[a] = (bitsf(w[a]) - o[a]) * invd[a];
+        }
+        uint32_t imask = w[3] >> 24;
+        uint32_t hit_int = 0, hit_tri = 0;
+        for (int slot = 0; slot < 8; slot++) {
+            uint8_t m = byte_of(w, 6, slot);
+            if (m == 0) continue;
+            float tn[3], tf[3];
+            for (int a = 0; a < 3; a++) {
+                float ql = (float)byte_of(w, 8 + 2 * a, slot);
+                float qh = (float)byte_of(w, 14 + 2 * a, slot);
+                float lo = invd[a] < 0.f ? qh : ql;
+                float hi = invd[a] < 0.f ? ql : qh;
+                tn[a] = std::fma(lo, adj[a], org[a]);
+                tf[a] = std::fma(hi, adj[a], org[a]);
+            }
+            float tnear = fmax2(fmax2(tn[0], tn[1]), fmax2(tn[2], tmin));
+            float tfar = fmin2(fmin2(tf[0], tf[1]), fmin2(tf[2], cur_tmax));
+            if (!(tnear <= tfar * 1.0000003f)) continue;
+            if (imask & (1u << slot)) hit_int |= 1u << (slot ^ near);
+            else hit_tri |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+        }
+        uint32_t tri_base = w[5];
+        while (hit_tri) {
+            uint32_t b = (uint32_t)__builtin_ctz(hit_tri);
+            hit_tri &= hit_tri - 1u;
+            const float* tr = &B.tris[(size_t)(tri_base + b) * 12];
+            uint32_t id = fbits(tr[3]);
+            if (c) c->tris++;
+            float tt, b1, b2;
+            if (tri_test(r, tr, tr + 4, tr + 8, tmin, cur_tmax, tt, b1, b2)) {
+                if (h.id == HY_NO_HIT || better(tt, id, h)) { h = Hit{tt, id, b1, b2}; cur_tmax = tt; }
+                if (any_hit) return h;
+            }
+        }
+        g_base = w[4];
+        g_bits = (hit_int << 24) | imask;
+    }
+    return h;
+}
+
+Hit trace(const Scene& s, const float o[3], const float d[3], float tmin, float tmax, bool any_hit, int mode,
+          Counters* c) {
+    if (mode == 1 && s.bvh_ok) return trace_bvh8(s, o, d, tmin, tmax, any_hit, c);
+    return trace_brute(s, o, d, tmin, tmax, any_hit, c);
+}
+
+}  // namespace orc

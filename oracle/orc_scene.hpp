@@ -1,0 +1,66 @@
+// ORACLE — test infrastructure only (see orc_math.hpp).  Scene state, BVH and
+// traversal of the CPU restatement.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "../include/hybridrt.h"
+#include "orc_math.hpp"
+
+namespace orc {
+
+constexpr int kLeafMax = 3;           // triangles per BVH8 leaf slot
+constexpr int kStackMax = 64;         // traversal stack entries
+constexpr uint32_t kMaxIters = 1u << 22;  // node visits per ray before giving up
+
+struct Env { uint32_t w = 0, h = 0; std::vector<uint8_t> px; };
+
+struct Bvh2Node { uint32_t left, right, first, last; float lo[3], hi[3]; };
+constexpr uint32_t kLeafBit = 0x80000000u;
+
+// 80-byte compressed BVH8 node as 20 words (the product's layout):
+//  w0-2 p.xyz | w3 e.x | e.y<<8 | e.z<<16 | imask<<24 | w4 child_base | w5 tri_base
+//  w6-7 meta[8] | w8-9 qlo_x[8] | w10-11 qlo_y | w12-13 qlo_z | w14-15 qhi_x | w16-17 qhi_y | w18-19 qhi_z
+struct Bvh8Node { uint32_t w[20]; };
+
+struct Bvh {
+    uint32_t n = 0;
+    float slo[3], shi[3];
+    std::vector<uint32_t> morton, order;   // sorted morton codes and triangle ids
+    std::vector<Bvh2Node> bvh2;            // n-1 internal nodes (Karras)
+    std::vector<Bvh8Node> bvh8;            // BFS order
+    std::vector<float> tris;               // 12 floats per packed triangle
+    uint32_t depth = 0;
+};
+
+struct Counters { uint64_t nodes = 0, tris = 0; uint32_t status = 0; };
+
+struct Hit { float t; uint32_t id; float b1, b2; };
+
+struct Scene {
+    std::vector<HyVertex> verts;
+    std::vector<uint32_t> idx;
+    std::vector<HyPrimitive> prims;
+    std::vector<float> xf;        // 16 per transform (column-major)
+    std::vector<float> nrm;       // 9 per transform: mat3(transpose(inverse(M))), column-major
+    std::vector<HyMaterial> mats;
+    std::vector<HyLight> lights;
+    Env env[2];
+    // derived geometry
+    uint32_t ntri = 0;
+    std::vector<float> world;        // 9 floats per triangle (v0, v1, v2) in world space
+    std::vector<uint32_t> tri_prim;  // primitive of each triangle
+    std::vector<uint32_t> prim_tri0; // first global triangle of each primitive
+    Bvh bvh;
+    bool bvh_ok = false;
+};
+
+// geometry / BVH
+void scene_derive(Scene& s);
+void bvh_build(Scene& s);
+// traversal: mode 0 = brute force over all triangles, 1 = BVH8 (op-for-op the
+// product's traversal, so node/triangle counts are comparable)
+Hit trace(const Scene& s, const float o[3], const float d[3], float tmin, float tmax, bool any_hit,
+          int mode, Counters* c);
+
+}  // namespace orc

@@ -1,0 +1,269 @@
+"""ORACLE — test infrastructure only.
+
+ctypes front end of liboracle.so, the CPU restatement of the hybrid pass.
+Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use it, as
+the checker; the product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+
+P = C.c_void_p
+U32 = C.c_uint32
+_lib = None
+
+
+def build() -> Path:
+    r = subprocess.run(["make", "-C", str(HERE)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB.exists():
+        build()
+    lib = C.CDLL(str(LIB))
+    sig = {
+        "orc_scene_create": (P, []),
+        "orc_scene_destroy": (None, [P]),
+        "orc_set_threads": (None, [C.c_int]),
+        "orc_get_threads": (C.c_int, []),
+        "orc_scene_set_geometry": (C.c_int, [P, P, U32, P, U32, P, U32, P, U32]),
+        "orc_scene_set_materials": (C.c_int, [P, P, U32]),
+        "orc_scene_set_lights": (C.c_int, [P, P, U32]),
+        "orc_scene_set_env": (C.c_int, [P, C.c_int, P, U32, U32]),
+        "orc_num_tris": (U32, [P]),
+        "orc_world_tris": (None, [P, P]),
+        "orc_bvh_build": (C.c_int, [P, P, P]),
+        "orc_bvh_download": (None, [P, P, P, P, P, P]),
+        "orc_trace": (None, [P, P, U32, C.c_int, C.c_int, P, P]),
+        "orc_tea": (U32, [U32, U32]),
+        "orc_rnd_seq": (None, [U32, U32, P, P]),
+        "orc_sample_disk": (None, [P, P, P, U32, P]),
+        "orc_brdf": (None, [P, P, P, C.c_float, P, C.c_float, P]),
+        "orc_gbuffer_primary": (C.c_int, [P, P, U32, U32, P, C.c_int]),
+        "orc_shadow_pass": (C.c_int, [P, P, P, P, U32, P, C.c_int, P]),
+        "orc_accumulate": (C.c_int, [P, P, P, P, P]),
+        "orc_shade": (C.c_int, [P, P, P, P, P, P, P, C.c_int, P]),
+    }
+    for k, (r, a) in sig.items():
+        f = getattr(lib, k)
+        f.restype = r
+        f.argtypes = a
+    _lib = lib
+    return lib
+
+
+def _p(a: np.ndarray):
+    assert a.flags["C_CONTIGUOUS"], "arrays must be C-contiguous"
+    return C.c_void_p(a.ctypes.data)
+
+
+# mirrors of the C structs (same layout as include/hybridrt.h)
+class _GBuf(C.Structure):
+    _fields_ = [("width", U32), ("height", U32), ("plane", C.c_void_p * 6), ("format", U32 * 6)]
+
+
+class _Cfg(C.Structure):
+    _fields_ = [("shadow_spp", U32), ("max_bounces", U32), ("rng_mode", U32), ("accum_frame", C.c_int32),
+                ("flags", U32), ("block_size", U32), ("queue_chunk", U32), ("stack_depth", U32)]
+
+
+class _Accum(C.Structure):
+    _fields_ = [("format", U32), ("num_lights", U32), ("history", C.c_void_p)]
+
+
+class _Stats(C.Structure):
+    _fields_ = [("shadow_rays", C.c_uint64), ("reflection_rays", C.c_uint64), ("hit_shadow_rays", C.c_uint64),
+                ("nodes_visited", C.c_uint64), ("tris_tested", C.c_uint64), ("error_flags", U32), ("_pad", U32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("_")}
+
+
+FP32_FORMATS = (0, 0, 0, 1, 0, 0)
+TRACE_BRUTE, TRACE_BVH8 = 0, 1
+
+
+def set_threads(n: int):
+    load().orc_set_threads(n)
+
+
+def threads() -> int:
+    return load().orc_get_threads()
+
+
+def tea(a: int, b: int) -> int:
+    return int(load().orc_tea(a, b))
+
+
+def rnd_seq(seed: int, n: int):
+    st = np.zeros(n, np.uint32)
+    v = np.zeros(n, np.float32)
+    load().orc_rnd_seq(seed, n, _p(st), _p(v))
+    return st, v
+
+
+def sample_disk(radius: float, pos, L, seed: int) -> np.ndarray:
+    r = np.array([radius], np.float32)
+    p = np.ascontiguousarray(pos, np.float32)
+    l = np.ascontiguousarray(L, np.float32)
+    out = np.zeros(3, np.float32)
+    load().orc_sample_disk(_p(r), _p(p), _p(l), seed, _p(out))
+    return out
+
+
+def brdf(N, V, L, roughness, F0, cos_theta):
+    out = np.zeros(5, np.float32)
+    a = [np.ascontiguousarray(x, np.float32) for x in (N, V, L, F0)]
+    load().orc_brdf(_p(a[0]), _p(a[1]), _p(a[2]), float(roughness), _p(a[3]), float(cos_theta), _p(out))
+    return out
+
+
+class OracleScene:
+    def __init__(self):
+        self.lib = load()
+        self.h = self.lib.orc_scene_create()
+        self.num_lights = 0
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.lib.orc_scene_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def set_scene_arrays(self, verts, idx, prims, xf, mats, lights, env=None):
+        self._keep = (verts, idx, prims, xf, mats, lights)
+        self.lib.orc_scene_set_geometry(self.h, _p(verts), len(verts), _p(idx), len(idx), _p(prims), len(prims),
+                                        _p(xf), len(xf))
+        self.lib.orc_scene_set_materials(self.h, _p(mats), len(mats))
+        self.lib.orc_scene_set_lights(self.h, _p(lights) if len(lights) else None, len(lights))
+        for slot, e in enumerate(env or []):
+            e = np.ascontiguousarray(e, np.uint8)
+            self.lib.orc_scene_set_env(self.h, slot, _p(e), e.shape[1], e.shape[0])
+        self.num_lights = len(lights)
+
+    def set_scene(self, scene):
+        self.set_scene_arrays(*scene.pack(), scene.env)
+
+    def set_lights(self, lights):
+        lights = np.ascontiguousarray(lights, np.float32)
+        self._lights = lights
+        self.lib.orc_scene_set_lights(self.h, _p(lights), len(lights))
+        self.num_lights = len(lights)
+
+    def set_materials(self, mats):
+        mats = np.ascontiguousarray(mats, np.float32)
+        self._mats = mats
+        self.lib.orc_scene_set_materials(self.h, _p(mats), len(mats))
+
+    @property
+    def num_tris(self) -> int:
+        return int(self.lib.orc_num_tris(self.h))
+
+    def world_tris(self) -> np.ndarray:
+        out = np.zeros((self.num_tris, 9), np.float32)
+        self.lib.orc_world_tris(self.h, _p(out))
+        return out
+
+    def build_bvh(self):
+        info = np.zeros(4, np.uint32)
+        b = np.zeros(6, np.float32)
+        rc = self.lib.orc_bvh_build(self.h, _p(info), _p(b))
+        if rc != 0:
+            raise RuntimeError("oracle bvh build failed")
+        return {"num_tris": int(info[0]), "num_bvh2_nodes": int(info[1]), "num_bvh8_nodes": int(info[2]),
+                "depth": int(info[3]), "scene_lo": b[:3].tolist(), "scene_hi": b[3:].tolist()}
+
+    def download_bvh(self, n_bvh8: int):
+        n = self.num_tris
+        morton = np.zeros(n, np.uint32)
+        order = np.zeros(n, np.uint32)
+        bvh2 = np.zeros((max(n - 1, 0), 10), np.uint32)
+        bvh8 = np.zeros((n_bvh8, 20), np.uint32)
+        tris = np.zeros((n, 12), np.float32)
+        self.lib.orc_bvh_download(self.h, _p(morton), _p(order), _p(bvh2), _p(bvh8), _p(tris))
+        return morton, order, bvh2, bvh8, tris
+
+    def trace(self, rays: np.ndarray, any_hit: bool, mode: int = TRACE_BVH8):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = len(rays)
+        hits = np.zeros((n, 4), np.float32)
+        cnt = np.zeros((n, 2), np.uint32)
+        self.lib.orc_trace(self.h, _p(rays), n, int(any_hit), mode, _p(hits), _p(cnt))
+        return hits, cnt
+
+    def gbuffer(self, cam36, width, height, mode=TRACE_BVH8):
+        planes = [np.zeros((height, width, 4 if i != 3 else 2), np.float32) for i in range(6)]
+        arr = (C.c_void_p * 6)(*[p.ctypes.data for p in planes])
+        cam = np.ascontiguousarray(cam36, np.float32)
+        self.lib.orc_gbuffer_primary(self.h, _p(cam), width, height, arr, mode)
+        return planes
+
+    @staticmethod
+    def _gb(planes, formats=FP32_FORMATS):
+        g = _GBuf()
+        g.width, g.height = planes[0].shape[1], planes[0].shape[0]
+        for i in range(6):
+            g.plane[i] = planes[i].ctypes.data
+            g.format[i] = formats[i]
+        return g
+
+    def shadow_pass(self, planes, cam36, cfg: dict, fmt: int, mode=TRACE_BVH8, formats=FP32_FORMATS):
+        H, W = planes[0].shape[:2]
+        dt = np.uint8 if fmt == 0 else np.float32
+        out = np.zeros((self.num_lights, H, W), dt)
+        st = _Stats()
+        cam = np.ascontiguousarray(cam36, np.float32)
+        self.lib.orc_shadow_pass(self.h, C.byref(self._gb(planes, formats)), _p(cam), C.byref(_Cfg(**cfg)), fmt,
+                                 _p(out), mode, C.byref(st))
+        return out, st.as_dict()
+
+    def accumulate(self, planes, cfg: dict, shadow: np.ndarray, hist: np.ndarray, fmt: int, formats=FP32_FORMATS):
+        acc = _Accum(fmt, hist.shape[0], hist.ctypes.data)
+        self.lib.orc_accumulate(self.h, C.byref(self._gb(planes, formats)), C.byref(_Cfg(**cfg)), _p(shadow),
+                                C.byref(acc))
+
+    def shade(self, planes, cam36, cfg: dict, hist: np.ndarray, fmt: int, mode=TRACE_BVH8, formats=FP32_FORMATS):
+        H, W = planes[0].shape[:2]
+        out_f = np.zeros((H, W, 4), np.float32)
+        out_8 = np.zeros((H, W, 4), np.uint8)
+        acc = _Accum(fmt, hist.shape[0], hist.ctypes.data)
+        st = _Stats()
+        cam = np.ascontiguousarray(cam36, np.float32)
+        self.lib.orc_shade(self.h, C.byref(self._gb(planes, formats)), _p(cam), C.byref(_Cfg(**cfg)), C.byref(acc),
+                           _p(out_f), _p(out_8), mode, C.byref(st))
+        return out_f, out_8, st.as_dict()
+
+    def forward(self, planes, cam36, cfg: dict, hist: np.ndarray, fmt: int, mode=TRACE_BVH8,
+                formats=FP32_FORMATS):
+        """shadow -> accumulate -> shade, the order of Renderer::rasterize_hybrid."""
+        flags = cfg.get("flags", 0)
+        shadow, st1 = self.shadow_pass(planes, cam36, cfg, fmt, mode, formats)
+        if flags & 0x2:  # HY_FLAG_NO_ACCUM: shade from the raw images
+            src = shadow
+        else:
+            self.accumulate(planes, cfg, shadow, hist, fmt, formats)
+            src = hist
+        out_f, out_8, st2 = self.shade(planes, cam36, cfg, src, fmt, mode, formats)
+        st = {k: st1[k] + st2[k] for k in st1 if k != "error_flags"}
+        st["error_flags"] = st1["error_flags"] | st2["error_flags"]
+        return out_f, out_8, shadow, st
+
+
+def cfg_dict(spp=1, max_bounces=8, rng_mode=0, accum_frame=0, flags=0):
+    return dict(shadow_spp=spp, max_bounces=max_bounces, rng_mode=rng_mode, accum_frame=accum_frame, flags=flags,
+                block_size=0, queue_chunk=0, stack_depth=0)

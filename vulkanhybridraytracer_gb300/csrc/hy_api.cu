@@ -1,0 +1,620 @@
+// C ABI of libhybridrt: context, scene upload, acceleration structure, passes.
+//
+// The three submissions of Renderer::rasterize_hybrid (src/renderer.cpp:559-580)
+// become stream-ordered kernel launches on the context's stream; there is no
+// host round trip between them (the reference waits for the queue to idle
+// after each).  Scene upload mirrors Renderer::load_data_to_gpu
+// (src/renderer.cpp:1477-1530) and the per-entity buffers of
+// create_hybrid_descriptors (src/renderer.cpp:3015-3048).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "hy_internal.h"
+#include "hy_pass.h"
+
+using namespace hy;
+
+namespace hy {
+
+int ctx_alloc(HyCtx* c, DevBuf& b, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (b.p && b.bytes >= bytes) return HY_OK;
+    c->alloc_calls++;
+    if (c->fail_after && c->alloc_calls >= c->fail_after) { c->fail_after = 0; return HY_ERR_OOM; }
+    size_t old = b.bytes;
+    if (c->max_bytes && c->used_bytes - old + bytes > c->max_bytes) return HY_ERR_OOM;
+    if (b.p) { cudaFree(b.p); b.p = nullptr; b.bytes = 0; c->used_bytes -= old; }
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        b.p = nullptr;
+        return e == cudaErrorMemoryAllocation ? HY_ERR_OOM : HY_ERR_CUDA;
+    }
+    b.bytes = bytes;
+    c->used_bytes += bytes;
+    return HY_OK;
+}
+
+void ctx_free(HyCtx* c, DevBuf& b) {
+    if (b.p) { cudaFree(b.p); c->used_bytes -= b.bytes; }
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+}  // namespace hy
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+template <class T> int upload(HyCtx* c, DevBuf& b, const T* src, size_t count) {
+    int rc = ctx_alloc(c, b, count * sizeof(T));
+    if (rc) return rc;
+    if (count) HY_CUDA_TRY(cudaMemcpyAsync(b.p, src, count * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+    HY_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return HY_OK;
+}
+
+inline bool finite_all(const float* p, size_t n) {
+    for (size_t i = 0; i < n; i++)
+        if (!std::isfinite(p[i])) return false;
+    return true;
+}
+
+void inverse4(const double* a, double* inv) {
+    inv[0] = a[5] * a[10] * a[15] - a[5] * a[11] * a[14] - a[9] * a[6] * a[15] + a[9] * a[7] * a[14] + a[13] * a[6] * a[11] - a[13] * a[7] * a[10];
+    inv[4] = -a[4] * a[10] * a[15] + a[4] * a[11] * a[14] + a[8] * a[6] * a[15] - a[8] * a[7] * a[14] - a[12] * a[6] * a[11] + a[12] * a[7] * a[10];
+    inv[8] = a[4] * a[9] * a[15] - a[4] * a[11] * a[13] - a[8] * a[5] * a[15] + a[8] * a[7] * a[13] + a[12] * a[5] * a[11] - a[12] * a[7] * a[9];
+    inv[12] = -a[4] * a[9] * a[14] + a[4] * a[10] * a[13] + a[8] * a[5] * a[14] - a[8] * a[6] * a[13] - a[12] * a[5] * a[10] + a[12] * a[6] * a[9];
+    inv[1] = -a[1] * a[10] * a[15] + a[1] * a[11] * a[14] + a[9] * a[2] * a[15] - a[9] * a[3] * a[14] - a[13] * a[2] * a[11] + a[13] * a[3] * a[10];
+    inv[5] = a[0] * a[10] * a[15] - a[0] * a[11] * a[14] - a[8] * a[2] * a[15] + a[8] * a[3] * a[14] + a[12] * a[2] * a[11] - a[12] * a[3] * a[10];
+    inv[9] = -a[0] * a[9] * a[15] + a[0] * a[11] * a[13] + a[8] * a[1] * a[15] - a[8] * a[3] * a[13] - a[12] * a[1] * a[11] + a[12] * a[3] * a[9];
+    inv[13] = a[0] * a[9] * a[14] - a[0] * a[10] * a[13] - a[8] * a[1] * a[14] + a[8] * a[2] * a[13] + a[12] * a[1] * a[10] - a[12] * a[2] * a[9];
+    inv[2] = a[1] * a[6] * a[15] - a[1] * a[7] * a[14] - a[5] * a[2] * a[15] + a[5] * a[3] * a[14] + a[13] * a[2] * a[7] - a[13] * a[3] * a[6];
+    inv[6] = -a[0] * a[6] * a[15] + a[0] * a[7] * a[14] + a[4] * a[2] * a[15] - a[4] * a[3] * a[14] - a[12] * a[2] * a[7] + a[12] * a[3] * a[6];
+    inv[10] = a[0] * a[5] * a[15] - a[0] * a[7] * a[13] - a[4] * a[1] * a[15] + a[4] * a[3] * a[13] + a[12] * a[1] * a[7] - a[12] * a[3] * a[5];
+    inv[14] = -a[0] * a[5] * a[14] + a[0] * a[6] * a[13] + a[4] * a[1] * a[14] - a[4] * a[2] * a[13] - a[12] * a[1] * a[6] + a[12] * a[2] * a[5];
+    inv[3] = -a[1] * a[6] * a[11] + a[1] * a[7] * a[10] + a[5] * a[2] * a[11] - a[5] * a[3] * a[10] - a[9] * a[2] * a[7] + a[9] * a[3] * a[6];
+    inv[7] = a[0] * a[6] * a[11] - a[0] * a[7] * a[10] - a[4] * a[2] * a[11] + a[4] * a[3] * a[10] + a[8] * a[2] * a[7] - a[8] * a[3] * a[6];
+    inv[11] = -a[0] * a[5] * a[11] + a[0] * a[7] * a[9] + a[4] * a[1] * a[11] - a[4] * a[3] * a[9] - a[8] * a[1] * a[7] + a[8] * a[3] * a[5];
+    inv[15] = a[0] * a[5] * a[10] - a[0] * a[6] * a[9] - a[4] * a[1] * a[10] + a[4] * a[2] * a[9] + a[8] * a[1] * a[6] - a[8] * a[2] * a[5];
+    double det = a[0] * inv[0] + a[1] * inv[4] + a[2] * inv[8] + a[3] * inv[12];
+    double r = 1.0 / det;
+    for (int i = 0; i < 16; i++) inv[i] *= r;
+}
+
+// mat3(transpose(inverse(M))) of each transform, column-major 3x3
+std::vector<float> normal_matrices(const float* xf, uint32_t n) {
+    std::vector<float> out((size_t)n * 9);
+    for (uint32_t t = 0; t < n; t++) {
+        double m[16], inv[16];
+        for (int i = 0; i < 16; i++) m[i] = xf[(size_t)t * 16 + i];
+        inverse4(m, inv);
+        for (int c = 0; c < 3; c++)
+            for (int r = 0; r < 3; r++) out[(size_t)t * 9 + c * 3 + r] = (float)inv[r * 4 + c];
+    }
+    return out;
+}
+
+SceneDev scene_dev(HyCtx* c) {
+    SceneDev S;
+    S.nodes = c->nodes.as<Node8>();
+    S.tris = c->tris.as<float4>();
+    S.vattr = c->vattr.as<float4>();
+    S.idx = c->idx.as<uint32_t>();
+    S.prims = c->prims.as<HyPrimitive>();
+    S.tri_prim = c->tri_prim.as<uint32_t>();
+    S.prim_tri0 = c->prim_tri0.as<uint32_t>();
+    S.nrm = c->nrm.as<float>();
+    S.mats = c->mats.as<HyMaterial>();
+    S.lights = c->lights.as<HyLight>();
+    S.env0 = c->env[0].as<uchar4>();
+    S.env1 = c->env[1].as<uchar4>();
+    S.num_mats = c->nmats;
+    S.num_lights = c->nlights;
+    S.num_nodes = c->bvh_ok ? c->n_bvh8 : 0;
+    S.num_tris = c->bvh_ok ? c->ntri : 0;
+    for (int i = 0; i < 2; i++) { S.env_w[i] = c->env_w[i]; S.env_h[i] = c->env_h[i]; }
+    return S;
+}
+
+// zero the counters, status word and queue slots of a call
+int reset_counters(HyCtx* c) {
+    HY_CUDA_TRY(cudaMemsetAsync(c->dstats.p, 0, c->dstats.bytes, c->stream));
+    return HY_OK;
+}
+unsigned long long* dev_stats(HyCtx* c) { return c->dstats.as<unsigned long long>(); }
+uint32_t* dev_status(HyCtx* c) { return (uint32_t*)(c->dstats.as<unsigned long long>() + ST_COUNT); }
+uint32_t* dev_queue(HyCtx* c, int k) { return dev_status(c) + 1 + k; }
+
+int status_to_code(uint32_t s) {
+    if (s & HY_STATUS_STACK_OVERFLOW) return HY_ERR_STACK_OVERFLOW;
+    if (s & HY_STATUS_TIMEOUT) return HY_ERR_TIMEOUT;
+    if (s & HY_STATUS_QUEUE_OVERFLOW) return HY_ERR_QUEUE_OVERFLOW;
+    if (s & HY_STATUS_NAN_INPUT) return HY_ERR_NAN_INPUT;
+    if (s & HY_STATUS_BAD_INDEX) return HY_ERR_CUDA;
+    return HY_OK;
+}
+
+// read back counters + status (synchronises the stream)
+int finish_call(HyCtx* c, HyStats* st, bool sync) {
+    HY_CUDA_TRY(cudaGetLastError());
+    if (!sync && !st) return HY_OK;
+    HY_CUDA_TRY(cudaMemcpyAsync(c->h_stats, c->dstats.p, ST_COUNT * 8 + 4, cudaMemcpyDeviceToHost, c->stream));
+    HY_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    uint32_t status;
+    std::memcpy(&status, c->h_stats + ST_COUNT, 4);
+    if (st) {
+        st->shadow_rays = c->h_stats[ST_SHADOW];
+        st->reflection_rays = c->h_stats[ST_REFL];
+        st->hit_shadow_rays = c->h_stats[ST_HITSHADOW];
+        st->nodes_visited = c->h_stats[ST_NODES];
+        st->tris_tested = c->h_stats[ST_TRIS];
+        st->error_flags = status;
+        st->_pad = 0;
+    }
+    return status_to_code(status);
+}
+
+uint32_t fmt_bytes(uint32_t f) {
+    switch (f) {
+        case HY_FMT_RGBA32F: return 16;
+        case HY_FMT_RG32F: return 8;
+        case HY_FMT_RGBA16F: return 8;
+        case HY_FMT_RG16F: return 4;
+        case HY_FMT_RGBA8: return 4;
+        default: return 0;
+    }
+}
+
+int check_gbuffer(const HyGBuffer* gb, bool need_all) {
+    if (!gb || gb->width == 0 || gb->height == 0) return HY_ERR_INVALID_ARG;
+    if ((uint64_t)gb->width * gb->height >= (1ull << 31)) return HY_ERR_INVALID_ARG;
+    for (int p = 0; p < 6; p++) {
+        bool needed = need_all || p == 0 || p == 1 || p == 3;
+        if (!needed) continue;
+        if (!gb->plane[p] || fmt_bytes(gb->format[p]) == 0) return HY_ERR_INVALID_ARG;
+        if (((uintptr_t)gb->plane[p]) % fmt_bytes(gb->format[p]) != 0) return HY_ERR_INVALID_ARG;
+    }
+    return HY_OK;
+}
+
+int check_cfg(const HyPassConfig* cfg) {
+    if (!cfg) return HY_ERR_INVALID_ARG;
+    if (cfg->shadow_spp == 0 || cfg->shadow_spp > 4096) return HY_ERR_INVALID_ARG;
+    if (cfg->max_bounces > 64) return HY_ERR_INVALID_ARG;
+    if (cfg->rng_mode > HY_RNG_DECORRELATED) return HY_ERR_INVALID_ARG;
+    return HY_OK;
+}
+
+int check_scene_ready(HyCtx* c) {
+    if (!c->geometry_ok || !c->bvh_ok) return HY_ERR_NOT_READY;
+    if (c->nmats == 0) return HY_ERR_NOT_READY;
+    if (c->max_material_id >= c->nmats) return HY_ERR_INVALID_ARG;  // a primitive names a missing material
+    return HY_OK;
+}
+
+int grid_for(HyCtx* c, int mode, bool count, int block) {
+    int per = 0;
+    if (pixel_occupancy(mode, count, block, &per) != cudaSuccess || per <= 0) per = 1;
+    return per * c->num_sms;
+}
+
+PassParams make_params(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const HyPassConfig* cfg,
+                       uint32_t accum_fmt, void* shadow, void* hist, float* out_f, uint8_t* out_8) {
+    PassParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.W = gb->width;
+    P.H = gb->height;
+    for (int i = 0; i < 6; i++) { P.plane[i] = gb->plane[i]; P.fmt[i] = gb->format[i]; }
+    // viewInverse * vec4(0,0,0,1), same op order as the device mat-vec
+    float cp[3];
+    for (int i = 0; i < 3; i++) {
+        float a = cam->inv_view[0 * 4 + i] * 0.f;
+        a = a + cam->inv_view[1 * 4 + i] * 0.f;
+        a = a + cam->inv_view[2 * 4 + i] * 0.f;
+        a = a + cam->inv_view[3 * 4 + i] * 1.f;
+        cp[i] = a;
+    }
+    P.cam_pos = f3{cp[0], cp[1], cp[2]};
+    P.frame_u = (uint32_t)(int32_t)cam->frame[0];
+    P.spp = cfg->shadow_spp;
+    P.max_bounces = cfg->max_bounces;
+    P.rng_mode = cfg->rng_mode;
+    P.flags = cfg->flags;
+    P.accum_frame = cfg->accum_frame;
+    P.accum_fmt = accum_fmt;
+    P.shadow = shadow;
+    P.hist = hist;
+    P.out_f = out_f;
+    P.out_8 = out_8;
+    P.tiles_x = (P.W + 7) / 8;
+    P.ntiles = P.tiles_x * ((P.H + 3) / 4);
+    P.chunk = cfg->queue_chunk ? cfg->queue_chunk : 1;
+    if (cfg->flags & HY_FLAG_FULL_BLUR_DISPATCH) { P.blur_w = P.W; P.blur_h = P.H; }
+    else { P.blur_w = (P.W / 16) * 16; P.blur_h = (P.H / 16) * 16; }
+    P.stats = dev_stats(c);
+    P.status = dev_status(c);
+    return P;
+}
+
+int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg, int queue_slot) {
+    bool count = (cfg->flags & HY_FLAG_COUNT_TRAVERSAL) != 0;
+    int block = cfg->block_size ? (int)cfg->block_size : 128;
+    if (block % 32 || block > 128) return HY_ERR_INVALID_ARG;  // kernels are built for <= 128 threads
+    PassParams P = P0;
+    P.queue = dev_queue(c, queue_slot);
+    int grid = grid_for(c, mode, count, block);
+    grid = std::max(1, std::min<int>(grid, (int)((P.ntiles * 32ull + block - 1) / block)));
+    HY_CUDA_TRY(launch_pixels(mode, count, scene_dev(c), P, grid, block, c->stream));
+    return HY_OK;
+}
+
+int ensure_size(HyCtx* c, DevBuf& b, size_t bytes) { return ctx_alloc(c, b, bytes); }
+
+}  // namespace
+
+extern "C" {
+
+const char* hy_error_string(int code) {
+    switch (code) {
+        case HY_OK: return "ok";
+        case HY_ERR_INVALID_ARG: return "invalid argument";
+        case HY_ERR_OOM: return "out of device memory";
+        case HY_ERR_CUDA: return "CUDA error";
+        case HY_ERR_TIMEOUT: return "device loop exceeded its iteration budget";
+        case HY_ERR_STACK_OVERFLOW: return "traversal stack overflow";
+        case HY_ERR_QUEUE_OVERFLOW: return "ray queue overflow";
+        case HY_ERR_NAN_INPUT: return "non-finite input";
+        case HY_ERR_NOT_READY: return "scene or acceleration structure not ready";
+        case HY_ERR_UNSUPPORTED: return "unsupported";
+        default: return "unknown error";
+    }
+}
+
+int hy_get_abi_version(void) { return HY_ABI_VERSION; }
+
+int hy_create(HyCtx** out, const HyCreateInfo* info) {
+    if (!out) return HY_ERR_INVALID_ARG;
+    *out = nullptr;
+    int dev = info ? info->device : 0;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || dev < 0 || dev >= ndev) {
+        cudaGetLastError();
+        return HY_ERR_CUDA;
+    }
+    HyCtx* c = new (std::nothrow) HyCtx();
+    if (!c) return HY_ERR_OOM;
+    c->device = dev;
+    DeviceGuard g(dev);
+    if (info) c->max_bytes = info->max_device_bytes;
+    if (info && info->stream) {
+        c->stream = (cudaStream_t)info->stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return HY_ERR_CUDA; }
+        c->own_stream = true;
+    }
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (c->num_sms <= 0) c->num_sms = 1;
+    int rc = ctx_alloc(c, c->dstats, ST_COUNT * 8 + 4 + WQ_COUNT * 4);
+    if (rc == HY_OK && cudaMallocHost((void**)&c->h_stats, 64) != cudaSuccess) rc = HY_ERR_CUDA;
+    if (rc) { hy_destroy(c); return rc; }
+    *out = c;
+    return HY_OK;
+}
+
+void hy_destroy(HyCtx* c) {
+    if (!c) return;
+    DeviceGuard g(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    DevBuf* bufs[] = {&c->verts, &c->vattr, &c->idx, &c->prims, &c->xf, &c->nrm, &c->prim_tri0, &c->tri_prim,
+                      &c->mats, &c->lights, &c->env[0], &c->env[1], &c->world, &c->tribox, &c->centroid,
+                      &c->keys[0], &c->keys[1], &c->vals[0], &c->vals[1], &c->bvh2, &c->parent, &c->flags,
+                      &c->bounds, &c->lvl_ref[0], &c->lvl_ref[1], &c->plan, &c->ni, &c->nt, &c->ni_scan,
+                      &c->nt_scan, &c->scan_tmp, &c->hist, &c->total, &c->nodes, &c->tris, &c->dstats,
+                      &c->raw_shadow, &c->hist_prev, &c->host_in[0], &c->host_in[1], &c->host_in[2],
+                      &c->host_in[3], &c->host_in[4], &c->host_in[5], &c->host_out_f, &c->host_out_8};
+    for (DevBuf* b : bufs) ctx_free(c, *b);
+    if (c->h_stats) cudaFreeHost(c->h_stats);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int hy_synchronize(HyCtx* c) {
+    if (!c) return HY_ERR_INVALID_ARG;
+    DeviceGuard g(c->device);
+    HY_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return HY_OK;
+}
+
+int hy_debug_fail_alloc_after(HyCtx* c, uint32_t n) {
+    if (!c) return HY_ERR_INVALID_ARG;
+    c->fail_after = n ? c->alloc_calls + n : 0;
+    return HY_OK;
+}
+
+int hy_scene_set_geometry(HyCtx* c, const HyVertex* verts, uint32_t nv, const uint32_t* indices, uint32_t ni,
+                          const HyPrimitive* prims, uint32_t np, const float* xf, uint32_t nx) {
+    if (!c || (nv && !verts) || (ni && !indices) || (np && !prims) || (nx && !xf)) return HY_ERR_INVALID_ARG;
+    if (np == 0 || nx == 0) return HY_ERR_INVALID_ARG;
+    DeviceGuard g(c->device);
+    // validation: index ranges, transform ids, finiteness
+    std::vector<uint32_t> prim_tri0(np);
+    uint64_t nt = 0;
+    uint32_t max_mat = 0;
+    for (uint32_t p = 0; p < np; p++) {
+        const HyPrimitive& pr = prims[p];
+        if (pr.index_count % 3 != 0) return HY_ERR_INVALID_ARG;
+        if ((uint64_t)pr.first_index + pr.index_count > ni) return HY_ERR_INVALID_ARG;
+        if (pr.transform_id >= nx) return HY_ERR_INVALID_ARG;
+        max_mat = std::max(max_mat, pr.material_id);
+        for (uint32_t k = 0; k < pr.index_count; k++)
+            if ((uint64_t)indices[pr.first_index + k] + pr.vertex_offset >= nv) return HY_ERR_INVALID_ARG;
+        prim_tri0[p] = (uint32_t)nt;
+        nt += pr.index_count / 3;
+    }
+    if (nt == 0 || nt >= (1ull << 31)) return HY_ERR_INVALID_ARG;
+    for (uint32_t v = 0; v < nv; v++)
+        if (!finite_all(verts[v].pos, 3)) return HY_ERR_NAN_INPUT;
+    if (!finite_all(xf, (size_t)nx * 16)) return HY_ERR_NAN_INPUT;
+    std::vector<uint32_t> tri_prim((size_t)nt);
+    for (uint32_t p = 0; p < np; p++)
+        for (uint32_t k = 0; k < prims[p].index_count / 3; k++) tri_prim[prim_tri0[p] + k] = p;
+    std::vector<float> vattr((size_t)nv * 8, 0.f);
+    for (uint32_t v = 0; v < nv; v++) {
+        vattr[(size_t)v * 8 + 0] = verts[v].normal[0];
+        vattr[(size_t)v * 8 + 1] = verts[v].normal[1];
+        vattr[(size_t)v * 8 + 2] = verts[v].normal[2];
+        vattr[(size_t)v * 8 + 4] = verts[v].uv[0];
+        vattr[(size_t)v * 8 + 5] = verts[v].uv[1];
+    }
+    std::vector<float> nrm = normal_matrices(xf, nx);
+    int rc;
+    c->geometry_ok = false;
+    c->bvh_ok = false;
+    if ((rc = upload(c, c->verts, verts, nv)) || (rc = upload(c, c->vattr, vattr.data(), vattr.size())) ||
+        (rc = upload(c, c->idx, indices, ni)) || (rc = upload(c, c->prims, prims, np)) ||
+        (rc = upload(c, c->xf, xf, (size_t)nx * 16)) || (rc = upload(c, c->nrm, nrm.data(), nrm.size())) ||
+        (rc = upload(c, c->prim_tri0, prim_tri0.data(), np)) ||
+        (rc = upload(c, c->tri_prim, tri_prim.data(), tri_prim.size())))
+        return rc;
+    c->nverts = nv;
+    c->nidx = ni;
+    c->nprims = np;
+    c->nxf = nx;
+    c->ntri = (uint32_t)nt;
+    c->max_material_id = max_mat;
+    c->geometry_ok = true;
+    return HY_OK;
+}
+
+int hy_scene_set_materials(HyCtx* c, const HyMaterial* m, uint32_t n) {
+    if (!c || !m || n == 0) return HY_ERR_INVALID_ARG;
+    DeviceGuard g(c->device);
+    int rc = upload(c, c->mats, m, n);
+    if (rc) return rc;
+    c->nmats = n;
+    return HY_OK;
+}
+
+int hy_scene_set_lights(HyCtx* c, const HyLight* l, uint32_t n) {
+    if (!c || (n && !l)) return HY_ERR_INVALID_ARG;
+    DeviceGuard g(c->device);
+    for (uint32_t i = 0; i < n; i++)
+        if (!finite_all(l[i].pos, 4) || !finite_all(l[i].color, 4)) return HY_ERR_NAN_INPUT;
+    int rc = upload(c, c->lights, l, n);
+    if (rc) return rc;
+    c->nlights = n;
+    return HY_OK;
+}
+
+int hy_scene_set_env(HyCtx* c, int slot, const uint8_t* px, uint32_t w, uint32_t h) {
+    if (!c || slot < 0 || slot > 1 || !px || w == 0 || h == 0) return HY_ERR_INVALID_ARG;
+    DeviceGuard g(c->device);
+    int rc = upload(c, c->env[slot], px, (size_t)w * h * 4);
+    if (rc) return rc;
+    c->env_w[slot] = w;
+    c->env_h[slot] = h;
+    return HY_OK;
+}
+
+int hy_bvh_build(HyCtx* c, HyBvhStats* st) {
+    if (!c) return HY_ERR_INVALID_ARG;
+    if (!c->geometry_ok) return HY_ERR_NOT_READY;
+    DeviceGuard g(c->device);
+    c->bvh_ok = false;
+    return bvh_build_impl(c, st);
+}
+
+int hy_bvh_refit(HyCtx* c, const float* xf, uint32_t nx) {
+    if (!c || !xf || nx != c->nxf) return HY_ERR_INVALID_ARG;
+    if (!c->bvh_ok) return HY_ERR_NOT_READY;
+    if (!finite_all(xf, (size_t)nx * 16)) return HY_ERR_NAN_INPUT;
+    DeviceGuard g(c->device);
+    std::vector<float> nrm = normal_matrices(xf, nx);
+    int rc;
+    if ((rc = upload(c, c->xf, xf, (size_t)nx * 16)) || (rc = upload(c, c->nrm, nrm.data(), nrm.size()))) return rc;
+    return bvh_refit_impl(c);
+}
+
+int hy_bvh_download(HyCtx* c, uint32_t* morton, uint32_t* order, uint32_t* bvh2, uint32_t* bvh8, float* tris) {
+    if (!c) return HY_ERR_INVALID_ARG;
+    if (!c->bvh_ok) return HY_ERR_NOT_READY;
+    DeviceGuard g(c->device);
+    const size_t n = c->ntri;
+    HY_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (morton) HY_CUDA_TRY(cudaMemcpy(morton, c->keys[0].p, n * 4, cudaMemcpyDeviceToHost));
+    if (order) HY_CUDA_TRY(cudaMemcpy(order, c->vals[0].p, n * 4, cudaMemcpyDeviceToHost));
+    if (bvh2 && n > 1) HY_CUDA_TRY(cudaMemcpy(bvh2, c->bvh2.p, (n - 1) * 40, cudaMemcpyDeviceToHost));
+    if (bvh8) HY_CUDA_TRY(cudaMemcpy(bvh8, c->nodes.p, (size_t)c->n_bvh8 * 80, cudaMemcpyDeviceToHost));
+    if (tris) HY_CUDA_TRY(cudaMemcpy(tris, c->tris.p, n * 48, cudaMemcpyDeviceToHost));
+    return HY_OK;
+}
+
+int hy_trace_rays(HyCtx* c, const HyRay* rays, uint32_t n, int any_hit, HyHit* hits, HyStats* st) {
+    if (!c || (n && (!rays || !hits))) return HY_ERR_INVALID_ARG;
+    if (!c->bvh_ok) return HY_ERR_NOT_READY;
+    DeviceGuard g(c->device);
+    int rc = reset_counters(c);
+    if (rc) return rc;
+    bool count = st != nullptr;
+    int grid = std::max(1, std::min<int>(c->num_sms * 16, (int)((n + 127) / 128)));
+    HY_CUDA_TRY(launch_trace(scene_dev(c), rays, n, any_hit != 0, count, hits, dev_stats(c), dev_status(c), grid,
+                             c->stream));
+    return finish_call(c, st, true);
+}
+
+int hy_gbuffer_primary(HyCtx* c, const HyCamera* cam, uint32_t W, uint32_t H, float* planes[6]) {
+    if (!c || !cam || !planes || W == 0 || H == 0) return HY_ERR_INVALID_ARG;
+    for (int i = 0; i < 6; i++)
+        if (!planes[i]) return HY_ERR_INVALID_ARG;
+    int rc = check_scene_ready(c);
+    if (rc) return rc;
+    DeviceGuard g(c->device);
+    if ((rc = reset_counters(c))) return rc;
+    GbufParams G;
+    G.W = W;
+    G.H = H;
+    std::memcpy(G.inv_view, cam->inv_view, 64);
+    std::memcpy(G.inv_proj, cam->inv_proj, 64);
+    for (int i = 0; i < 6; i++) G.planes[i] = planes[i];
+    G.status = dev_status(c);
+    HY_CUDA_TRY(launch_gbuffer(scene_dev(c), G, c->stream));
+    return finish_call(c, nullptr, true);
+}
+
+int hy_shadow_pass(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const HyPassConfig* cfg,
+                   uint32_t accum_format, void* d_shadow, HyStats* st) {
+    if (!c || !cam || !d_shadow || accum_format > HY_ACCUM_F32) return HY_ERR_INVALID_ARG;
+    int rc;
+    if ((rc = check_gbuffer(gb, false)) || (rc = check_cfg(cfg)) || (rc = check_scene_ready(c))) return rc;
+    DeviceGuard g(c->device);
+    if ((rc = reset_counters(c))) return rc;
+    PassParams P = make_params(c, gb, cam, cfg, accum_format, d_shadow, nullptr, nullptr, nullptr);
+    if ((rc = run_pixels(c, MODE_SHADOW, P, cfg, WQ_SHADOW))) return rc;
+    return finish_call(c, st, !(cfg->flags & HY_FLAG_NO_STATUS_SYNC));
+}
+
+static int accumulate_impl(HyCtx* c, const HyGBuffer* gb, const HyPassConfig* cfg, const void* shadow,
+                           HyAccum* acc) {
+    AccumParams A;
+    A.W = gb->width;
+    A.H = gb->height;
+    A.num_lights = acc->num_lights;
+    A.fmt = acc->format;
+    A.frame = cfg->accum_frame;
+    if (cfg->flags & HY_FLAG_FULL_BLUR_DISPATCH) { A.blur_w = A.W; A.blur_h = A.H; }
+    else { A.blur_w = (A.W / 16) * 16; A.blur_h = (A.H / 16) * 16; }
+    A.motion = gb->plane[3];
+    A.motion_fmt = gb->format[3];
+    A.shadow = shadow;
+    A.hist = acc->history;
+    A.hist_prev = acc->history;
+    if (A.frame <= 0) {
+        // the reprojected read sees the history as it was before this pass
+        size_t bytes = (size_t)A.W * A.H * acc->num_lights * (acc->format == HY_ACCUM_U8 ? 1 : 4);
+        int rc = ensure_size(c, c->hist_prev, bytes);
+        if (rc) return rc;
+        HY_CUDA_TRY(cudaMemcpyAsync(c->hist_prev.p, acc->history, bytes, cudaMemcpyDeviceToDevice, c->stream));
+        A.hist_prev = c->hist_prev.p;
+    }
+    HY_CUDA_TRY(launch_accumulate(A, c->stream));
+    return HY_OK;
+}
+
+int hy_accumulate_pass(HyCtx* c, const HyGBuffer* gb, const HyPassConfig* cfg, const void* d_shadow, HyAccum* acc) {
+    if (!c || !d_shadow || !acc || !acc->history || acc->format > HY_ACCUM_F32) return HY_ERR_INVALID_ARG;
+    int rc;
+    if ((rc = check_gbuffer(gb, false)) || (rc = check_cfg(cfg))) return rc;
+    DeviceGuard g(c->device);
+    if ((rc = accumulate_impl(c, gb, cfg, d_shadow, acc))) return rc;
+    HY_CUDA_TRY(cudaGetLastError());
+    if (!(cfg->flags & HY_FLAG_NO_STATUS_SYNC)) HY_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return HY_OK;
+}
+
+int hy_shade_pass(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const HyPassConfig* cfg, const HyAccum* acc,
+                  float* out_f, uint8_t* out_8, HyStats* st) {
+    if (!c || !cam || !acc || !acc->history || acc->format > HY_ACCUM_F32) return HY_ERR_INVALID_ARG;
+    int rc;
+    if ((rc = check_gbuffer(gb, true)) || (rc = check_cfg(cfg)) || (rc = check_scene_ready(c))) return rc;
+    if (acc->num_lights != c->nlights) return HY_ERR_INVALID_ARG;
+    DeviceGuard g(c->device);
+    if ((rc = reset_counters(c))) return rc;
+    // with HY_FLAG_NO_ACCUM the history argument holds the raw shadow images
+    PassParams P = make_params(c, gb, cam, cfg, acc->format, acc->history, acc->history, out_f, out_8);
+    if ((rc = run_pixels(c, MODE_SHADE, P, cfg, WQ_SHADE))) return rc;
+    return finish_call(c, st, !(cfg->flags & HY_FLAG_NO_STATUS_SYNC));
+}
+
+static int forward_impl(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const HyPassConfig* cfg, HyAccum* acc,
+                        float* out_f, uint8_t* out_8) {
+    int rc;
+    const bool fused = (cfg->flags & HY_FLAG_NO_ACCUM) || cfg->accum_frame > 0;
+    if (fused) {
+        PassParams P = make_params(c, gb, cam, cfg, acc->format, nullptr, acc->history, out_f, out_8);
+        return run_pixels(c, MODE_FUSED, P, cfg, WQ_FUSED);
+    }
+    size_t bytes = (size_t)gb->width * gb->height * c->nlights * (acc->format == HY_ACCUM_U8 ? 1 : 4);
+    if ((rc = ensure_size(c, c->raw_shadow, bytes))) return rc;
+    PassParams P = make_params(c, gb, cam, cfg, acc->format, c->raw_shadow.p, acc->history, out_f, out_8);
+    if ((rc = run_pixels(c, MODE_SHADOW, P, cfg, WQ_SHADOW))) return rc;
+    if ((rc = accumulate_impl(c, gb, cfg, c->raw_shadow.p, acc))) return rc;
+    return run_pixels(c, MODE_SHADE, P, cfg, WQ_SHADE);
+}
+
+int hy_hybrid_forward(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const HyPassConfig* cfg, HyAccum* acc,
+                      float* out_f, uint8_t* out_8, HyStats* st) {
+    if (!c || !cam || !acc || !acc->history || acc->format > HY_ACCUM_F32) return HY_ERR_INVALID_ARG;
+    int rc;
+    if ((rc = check_gbuffer(gb, true)) || (rc = check_cfg(cfg)) || (rc = check_scene_ready(c))) return rc;
+    if (acc->num_lights != c->nlights) return HY_ERR_INVALID_ARG;
+    DeviceGuard g(c->device);
+    if ((rc = reset_counters(c))) return rc;
+    if ((rc = forward_impl(c, gb, cam, cfg, acc, out_f, out_8))) return rc;
+    return finish_call(c, st, !(cfg->flags & HY_FLAG_NO_STATUS_SYNC));
+}
+
+int hy_hybrid_forward_host(HyCtx* c, const HyGBuffer* hgb, const HyCamera* cam, const HyPassConfig* cfg,
+                           HyAccum* acc, float* h_out_f, uint8_t* h_out_8, HyStats* st) {
+    if (!c || !cam || !acc || !acc->history || acc->format > HY_ACCUM_F32) return HY_ERR_INVALID_ARG;
+    int rc;
+    if ((rc = check_gbuffer(hgb, true)) || (rc = check_cfg(cfg)) || (rc = check_scene_ready(c))) return rc;
+    if (acc->num_lights != c->nlights) return HY_ERR_INVALID_ARG;
+    DeviceGuard g(c->device);
+    const size_t npx = (size_t)hgb->width * hgb->height;
+    HyGBuffer dgb = *hgb;
+    for (int p = 0; p < 6; p++) {
+        size_t bytes = npx * fmt_bytes(hgb->format[p]);
+        if ((rc = ensure_size(c, c->host_in[p], bytes))) return rc;
+        HY_CUDA_TRY(cudaMemcpyAsync(c->host_in[p].p, hgb->plane[p], bytes, cudaMemcpyHostToDevice, c->stream));
+        dgb.plane[p] = c->host_in[p].p;
+    }
+    float* d_f = nullptr;
+    uint8_t* d_8 = nullptr;
+    if (h_out_f) { if ((rc = ensure_size(c, c->host_out_f, npx * 16))) return rc; d_f = c->host_out_f.as<float>(); }
+    if (h_out_8) { if ((rc = ensure_size(c, c->host_out_8, npx * 4))) return rc; d_8 = c->host_out_8.as<uint8_t>(); }
+    if ((rc = reset_counters(c))) return rc;
+    if ((rc = forward_impl(c, &dgb, cam, cfg, acc, d_f, d_8))) return rc;
+    if (h_out_f) HY_CUDA_TRY(cudaMemcpyAsync(h_out_f, d_f, npx * 16, cudaMemcpyDeviceToHost, c->stream));
+    if (h_out_8) HY_CUDA_TRY(cudaMemcpyAsync(h_out_8, d_8, npx * 4, cudaMemcpyDeviceToHost, c->stream));
+    return finish_call(c, st, true);
+}
+
+}  // extern "C"

@@ -1,0 +1,365 @@
+// Device-side building blocks of the hybrid pass (sm_103a).
+//
+//  * GLSL-semantics vector math, the reference RNG (random.glsl:3-33) and the
+//    shading helpers of helpers.glsl:33-93.
+//  * G-buffer texel decode for the reference's attachment formats.
+//  * The compressed 8-wide BVH node (80 B, 5 x 128-bit loads), the packed
+//    triangle record (48 B, 3 x 128-bit loads) and the stack traversal with
+//    a watertight ray/triangle test (Woop, Benthin & Wald, JCGT 2013).
+//
+// Traversal and BVH arithmetic is written with explicit __f*_rn intrinsics:
+// every operation is one IEEE-rounded op in a fixed order, so a CPU build of
+// the same algorithm visits the same nodes and returns the same hits.
+#pragma once
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "../../include/hybridrt.h"
+
+namespace hy {
+
+// ------------------------------------------------------------------------------
+// vector math
+// ------------------------------------------------------------------------------
+struct f3 { float x, y, z; };
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ f3 operator/(f3 a, f3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ f3 operator/(f3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ f3 splat(float s) { return {s, s, s}; }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ float length(f3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ f3 normalize(f3 a) { return a / length(a); }
+__device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
+__device__ __forceinline__ float mixf(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+__device__ __forceinline__ f3 mix3(f3 a, f3 b, float t) { return {mixf(a.x, b.x, t), mixf(a.y, b.y, t), mixf(a.z, b.z, t)}; }
+__device__ __forceinline__ f3 pow3(f3 a, float e) { return {powf(a.x, e), powf(a.y, e), powf(a.z, e)}; }
+__device__ __forceinline__ f3 reflect(f3 I, f3 N) { return I - 2.0f * dot(N, I) * N; }
+__device__ __forceinline__ f3 refract(f3 I, f3 N, float eta) {
+    float d = dot(N, I);
+    float k = 1.0f - eta * eta * (1.0f - d * d);
+    if (k < 0.0f) return splat(0.0f);
+    return eta * I - (eta * d + sqrtf(k)) * N;
+}
+
+// unfused variants for the ray-construction path (same op order as written)
+__device__ __forceinline__ float dot_rn(f3 a, f3 b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ f3 add_rn(f3 a, f3 b) { return {__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z)}; }
+__device__ __forceinline__ f3 sub_rn(f3 a, f3 b) { return {__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)}; }
+__device__ __forceinline__ f3 scale_rn(f3 a, float s) { return {__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s)}; }
+__device__ __forceinline__ float length_rn(f3 a) { return __fsqrt_rn(dot_rn(a, a)); }
+__device__ __forceinline__ f3 normalize_rn(f3 a) {
+    float l = length_rn(a);
+    return {__fdiv_rn(a.x, l), __fdiv_rn(a.y, l), __fdiv_rn(a.z, l)};
+}
+__device__ __forceinline__ f3 cross_rn(f3 a, f3 b) {
+    return {__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)), __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z)),
+            __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x))};
+}
+
+constexpr float PI = 3.14159265359f;       // helpers.glsl:5
+constexpr float PI_MISS = 3.141592f;       // miss.rmiss:11
+
+// ------------------------------------------------------------------------------
+// RNG (random.glsl:3-33)
+// ------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t tea(uint32_t val0, uint32_t val1) {
+    uint32_t v0 = val0, v1 = val1, s0 = 0;
+#pragma unroll
+    for (uint32_t n = 0; n < 16; n++) {
+        s0 += 0x9e3779b9u;
+        v0 += ((v1 << 4) + 0xa341316cu) ^ (v1 + s0) ^ ((v1 >> 5) + 0xc8013ea4u);
+        v1 += ((v0 << 4) + 0xad90777du) ^ (v0 + s0) ^ ((v0 >> 5) + 0x7e95761eu);
+    }
+    return v0;
+}
+__device__ __forceinline__ uint32_t lcg(uint32_t& prev) {
+    prev = 1664525u * prev + 1013904223u;
+    return prev & 0x00FFFFFFu;
+}
+__device__ __forceinline__ float rnd(uint32_t& prev) { return __fdiv_rn((float)lcg(prev), 16777216.0f); }
+
+// ------------------------------------------------------------------------------
+// shading helpers (helpers.glsl:33-93)
+// ------------------------------------------------------------------------------
+__device__ __forceinline__ float DistributionGGX(f3 N, f3 H, float roughness) {
+    float a = roughness * roughness;
+    float a2 = a * a;
+    float NdotH = fmaxf(dot(N, H), 0.0f);
+    float NdotH2 = NdotH * NdotH;
+    float denom = (NdotH2 * (a2 - 1.0f) + 1.0f);
+    denom = PI * denom * denom;
+    return a2 / denom;
+}
+__device__ __forceinline__ float GeometrySchlickGGX(float NdotV, float roughness) {
+    float r = roughness + 1.0f;
+    float k = (r * r) / 8.0f;
+    return NdotV / (NdotV * (1.0f - k) + k);
+}
+__device__ __forceinline__ float GeometrySmith(f3 N, f3 V, f3 L, float roughness) {
+    float NdotV = fmaxf(dot(N, V), 0.0f);
+    float NdotL = fmaxf(dot(N, L), 0.0f);
+    return GeometrySchlickGGX(NdotV, roughness) * GeometrySchlickGGX(NdotL, roughness);
+}
+__device__ __forceinline__ f3 FresnelSchlick(float cosTheta, f3 F0) {
+    float p = powf(1.0f - cosTheta, 5.0f);
+    return F0 + (splat(1.0f) - F0) * p;
+}
+// sampleDisk (helpers.glsl:82-93); `seed` advances (the caller passes a copy
+// for the reference's by-value semantics).
+__device__ __forceinline__ f3 sampleDisk(float light_radius, f3 position, f3 L, uint32_t& seed) {
+    float r1 = rnd(seed);
+    float radius = __fmul_rn(light_radius, __fsqrt_rn(r1));
+    float r2 = rnd(seed);
+    float angle = __fmul_rn(__fmul_rn(r2, 2.0f), PI);
+    float px = __fmul_rn(radius, cosf(angle)), py = __fmul_rn(radius, sinf(angle));
+    f3 tangent = normalize_rn(cross_rn(L, mk(0.f, 1.f, 0.f)));
+    if (L.x == 0.f && L.y == 1.f && L.z == 0.f) tangent = mk(0.f, 0.f, 1.f);
+    f3 bitangent = normalize_rn(cross_rn(tangent, L));
+    f3 target = add_rn(add_rn(add_rn(position, L), scale_rn(tangent, px)), scale_rn(bitangent, py));
+    return normalize_rn(sub_rn(target, position));
+}
+
+// ------------------------------------------------------------------------------
+// texel decode
+// ------------------------------------------------------------------------------
+__device__ __forceinline__ float4 fetch_texel(const void* plane, uint32_t fmt, size_t i) {
+    switch (fmt) {
+        case HY_FMT_RGBA32F: return __ldg((const float4*)plane + i);
+        case HY_FMT_RG32F: { float2 v = __ldg((const float2*)plane + i); return make_float4(v.x, v.y, 0.f, 0.f); }
+        case HY_FMT_RGBA16F: {
+            uint2 u = __ldg((const uint2*)plane + i);
+            __half2 a = *reinterpret_cast<__half2*>(&u.x), b = *reinterpret_cast<__half2*>(&u.y);
+            return make_float4(__low2float(a), __high2float(a), __low2float(b), __high2float(b));
+        }
+        case HY_FMT_RG16F: {
+            uint32_t u = __ldg((const uint32_t*)plane + i);
+            __half2 a = *reinterpret_cast<__half2*>(&u);
+            return make_float4(__low2float(a), __high2float(a), 0.f, 0.f);
+        }
+        default: {
+            uint32_t u = __ldg((const uint32_t*)plane + i);
+            return make_float4(__fdiv_rn((float)(u & 0xffu), 255.f), __fdiv_rn((float)((u >> 8) & 0xffu), 255.f),
+                               __fdiv_rn((float)((u >> 16) & 0xffu), 255.f), __fdiv_rn((float)(u >> 24), 255.f));
+        }
+    }
+}
+
+__device__ __forceinline__ uint8_t quant8(float v) {
+    return (uint8_t)__float2uint_rn(__fmul_rn(fminf(fmaxf(v, 0.f), 1.f), 255.0f));
+}
+__device__ __forceinline__ float accum_load(uint32_t fmt, const void* buf, size_t i) {
+    if (fmt == HY_ACCUM_U8) return __fdiv_rn((float)((const uint8_t*)buf)[i], 255.0f);
+    return ((const float*)buf)[i];
+}
+__device__ __forceinline__ void accum_store(uint32_t fmt, void* buf, size_t i, float v) {
+    if (fmt == HY_ACCUM_U8) ((uint8_t*)buf)[i] = quant8(v);
+    else ((float*)buf)[i] = v;
+}
+
+// ------------------------------------------------------------------------------
+// BVH8 node / triangle layout
+// ------------------------------------------------------------------------------
+// node words (uint4 q[5]):
+//  q0 = p.x, p.y, p.z, e.x | e.y<<8 | e.z<<16 | imask<<24
+//  q1 = child_base, tri_base, meta[0..3], meta[4..7]
+//  q2 = qlo_x[0..3], qlo_x[4..7], qlo_y[0..3], qlo_y[4..7]
+//  q3 = qlo_z[0..3], qlo_z[4..7], qhi_x[0..3], qhi_x[4..7]
+//  q4 = qhi_y[0..3], qhi_y[4..7], qhi_z[0..3], qhi_z[4..7]
+// meta[s]: 0 = empty slot, 0x80 = internal child, else (count << 5) | triangle offset
+// triangle (float4 t[3]) = (v0, id bits), (v1, 0), (v2, 0)
+struct Node8 { uint4 q[5]; };
+constexpr int kLeafMax = 3;
+constexpr int kStackMax = 64;
+constexpr uint32_t kMaxIters = 1u << 22;
+
+struct SceneDev {
+    const Node8* nodes;
+    const float4* tris;          // 3 per triangle
+    const float4* vattr;         // 2 per vertex: (normal.xyz, 0), (uv.xy, 0, 0)
+    const uint32_t* idx;
+    const HyPrimitive* prims;
+    const uint32_t* tri_prim;    // global triangle -> primitive
+    const uint32_t* prim_tri0;   // primitive -> first global triangle
+    const float* nrm;            // 9 floats per transform (column-major normal matrix)
+    const HyMaterial* mats;
+    const HyLight* lights;
+    const uchar4* env0;
+    const uchar4* env1;
+    uint32_t num_mats, num_lights;
+    uint32_t num_nodes, num_tris;
+    uint32_t env_w[2], env_h[2];
+};
+
+struct Hit { float t; uint32_t id; float b1, b2; };
+
+struct RayPre {
+    f3 o;
+    float d[3];
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+    float invd[3];
+    uint32_t near;
+};
+
+__device__ __forceinline__ float comp(f3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+__device__ __forceinline__ RayPre ray_pre(f3 o, f3 d) {
+    RayPre r;
+    r.o = o;
+    r.d[0] = d.x; r.d[1] = d.y; r.d[2] = d.z;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    r.kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
+    r.kx = r.kz + 1; if (r.kx == 3) r.kx = 0;
+    r.ky = r.kx + 1; if (r.ky == 3) r.ky = 0;
+    if (comp(d, r.kz) < 0.f) { int t = r.kx; r.kx = r.ky; r.ky = t; }
+    float dz = comp(d, r.kz);
+    r.Sx = __fdiv_rn(comp(d, r.kx), dz);
+    r.Sy = __fdiv_rn(comp(d, r.ky), dz);
+    r.Sz = __fdiv_rn(1.0f, dz);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        float dd = fabsf(r.d[a]) > 1e-20f ? r.d[a] : copysignf(1e-20f, r.d[a]);
+        r.invd[a] = __fdiv_rn(1.0f, dd);
+    }
+    r.near = (r.invd[0] < 0.f ? 1u : 0u) | (r.invd[1] < 0.f ? 2u : 0u) | (r.invd[2] < 0.f ? 4u : 0u);
+    return r;
+}
+
+__device__ __forceinline__ float sel3(const float* a, int k) { return k == 0 ? a[0] : (k == 1 ? a[1] : a[2]); }
+
+// Woop et al. 2013 with a double-precision fallback on zero edge functions.
+__device__ __forceinline__ bool tri_test(const RayPre& r, float4 v0, float4 v1, float4 v2, float tmin, float tmax,
+                                         float& t, float& b1, float& b2) {
+    float A[3] = {__fsub_rn(v0.x, r.o.x), __fsub_rn(v0.y, r.o.y), __fsub_rn(v0.z, r.o.z)};
+    float B[3] = {__fsub_rn(v1.x, r.o.x), __fsub_rn(v1.y, r.o.y), __fsub_rn(v1.z, r.o.z)};
+    float C[3] = {__fsub_rn(v2.x, r.o.x), __fsub_rn(v2.y, r.o.y), __fsub_rn(v2.z, r.o.z)};
+    float Akz = sel3(A, r.kz), Bkz = sel3(B, r.kz), Ckz = sel3(C, r.kz);
+    float Ax = __fsub_rn(sel3(A, r.kx), __fmul_rn(r.Sx, Akz)), Ay = __fsub_rn(sel3(A, r.ky), __fmul_rn(r.Sy, Akz));
+    float Bx = __fsub_rn(sel3(B, r.kx), __fmul_rn(r.Sx, Bkz)), By = __fsub_rn(sel3(B, r.ky), __fmul_rn(r.Sy, Bkz));
+    float Cx = __fsub_rn(sel3(C, r.kx), __fmul_rn(r.Sx, Ckz)), Cy = __fsub_rn(sel3(C, r.ky), __fmul_rn(r.Sy, Ckz));
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.f || V == 0.f || W == 0.f) {
+        U = __double2float_rn(__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx)));
+        V = __double2float_rn(__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx)));
+        W = __double2float_rn(__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax)));
+    }
+    if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return false;
+    float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.f) return false;
+    float Az = __fmul_rn(r.Sz, Akz), Bz = __fmul_rn(r.Sz, Bkz), Cz = __fmul_rn(r.Sz, Ckz);
+    float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+    float tt = __fdiv_rn(T, det);
+    if (!(tt >= tmin && tt <= tmax)) return false;
+    t = tt;
+    b1 = __fdiv_rn(V, det);
+    b2 = __fdiv_rn(W, det);
+    return true;
+}
+
+__device__ __forceinline__ uint32_t byte_at(uint32_t lo4, uint32_t hi4, int slot) {
+    uint32_t w = slot < 4 ? lo4 : hi4;
+    return (w >> ((slot & 3) * 8)) & 0xffu;
+}
+
+// Stack traversal of the 8-wide BVH.  ANY: TerminateOnFirstHit semantics.
+// COUNT: accumulate node visits / triangle tests.
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ Hit traverse(const SceneDev& S, const RayPre& r, float tmin, float tmax,
+                                        uint32_t* nodes_ctr, uint32_t* tris_ctr, uint32_t* status) {
+    Hit h{tmax, HY_NO_HIT, 0.f, 0.f};
+    uint2 stk[kStackMax];
+    int sp = 0;
+    uint32_t g_base = 0, g_bits = (1u << 24) | (1u << r.near);
+    float cur_tmax = tmax;
+    for (uint32_t iter = 0;; iter++) {
+        if (iter >= kMaxIters) { atomicOr(status, HY_STATUS_TIMEOUT); break; }
+        if ((g_bits & 0xff000000u) == 0) {
+            if (sp == 0) break;
+            --sp;
+            g_base = stk[sp].x;
+            g_bits = stk[sp].y;
+        }
+        uint32_t rb = __ffs(g_bits >> 24) - 1;
+        g_bits &= ~(1u << (24 + rb));
+        uint32_t sl = rb ^ r.near;
+        uint32_t idx = g_base + __popc(g_bits & 0xffu & ((1u << sl) - 1u));
+        if (g_bits & 0xff000000u) {
+            if (sp >= kStackMax) { atomicOr(status, HY_STATUS_STACK_OVERFLOW); break; }
+            stk[sp] = make_uint2(g_base, g_bits);
+            sp++;
+        }
+        if (idx >= S.num_nodes) { atomicOr(status, HY_STATUS_BAD_INDEX); break; }
+        const uint4* np = S.nodes[idx].q;
+        uint4 q0 = __ldg(np + 0), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3), q4 = __ldg(np + 4);
+        if (COUNT) (*nodes_ctr)++;
+        float adj[3], org[3];
+        float p[3] = {__uint_as_float(q0.x), __uint_as_float(q0.y), __uint_as_float(q0.z)};
+        float oo[3] = {r.o.x, r.o.y, r.o.z};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            uint32_t ea = (q0.w >> (8 * a)) & 0xffu;
+            adj[a] = __fmul_rn(__uint_as_float(ea << 23), r.invd[a]);
+            org[a] = __fmul_rn(__fsub_rn(p[a], oo[a]), r.invd[a]);
+        }
+        uint32_t imask = q0.w >> 24;
+        uint32_t qlo[3][2] = {{q2.x, q2.y}, {q2.z, q2.w}, {q3.x, q3.y}};
+        uint32_t qhi[3][2] = {{q3.z, q3.w}, {q4.x, q4.y}, {q4.z, q4.w}};
+        uint32_t hit_int = 0, hit_tri = 0;
+#pragma unroll
+        for (int slot = 0; slot < 8; slot++) {
+            uint32_t m = byte_at(q1.z, q1.w, slot);
+            if (m == 0) continue;
+            float tn[3], tf[3];
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                float ql = (float)byte_at(qlo[a][0], qlo[a][1], slot);
+                float qh = (float)byte_at(qhi[a][0], qhi[a][1], slot);
+                float lo = r.invd[a] < 0.f ? qh : ql;
+                float hi = r.invd[a] < 0.f ? ql : qh;
+                tn[a] = __fmaf_rn(lo, adj[a], org[a]);
+                tf[a] = __fmaf_rn(hi, adj[a], org[a]);
+            }
+            float tnear = fmaxf(fmaxf(tn[0], tn[1]), fmaxf(tn[2], tmin));
+            float tfar = fminf(fminf(tf[0], tf[1]), fminf(tf[2], cur_tmax));
+            if (!(tnear <= __fmul_rn(tfar, 1.0000003f))) continue;
+            if (imask & (1u << slot)) hit_int |= 1u << (slot ^ r.near);
+            else hit_tri |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+        }
+        uint32_t tri_base = q1.y;
+        while (hit_tri) {
+            uint32_t b = __ffs(hit_tri) - 1;
+            hit_tri &= hit_tri - 1u;
+            if (tri_base + b >= S.num_tris) { atomicOr(status, HY_STATUS_BAD_INDEX); break; }
+            const float4* tp = S.tris + (size_t)(tri_base + b) * 3;
+            float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+            uint32_t id = __float_as_uint(v0.w);
+            if (COUNT) (*tris_ctr)++;
+            float tt, b1, b2;
+            if (tri_test(r, v0, v1, v2, tmin, cur_tmax, tt, b1, b2)) {
+                if (h.id == HY_NO_HIT || tt < h.t || (tt == h.t && id < h.id)) {
+                    h = Hit{tt, id, b1, b2};
+                    cur_tmax = tt;
+                }
+                if (ANY) return h;
+            }
+        }
+        g_base = q1.x;
+        g_bits = (hit_int << 24) | imask;
+    }
+    return h;
+}
+
+}  // namespace hy

@@ -1,0 +1,82 @@
+// Host-side context of libhybridrt (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/hybridrt.h"
+
+struct HyCtx;
+
+namespace hy {
+
+// Device allocation owned by the context; grows on demand, never shrinks.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    template <class T> T* as() const { return (T*)p; }
+};
+
+int ctx_alloc(HyCtx* c, DevBuf& b, size_t bytes);  // HY_OK / HY_ERR_OOM / HY_ERR_CUDA
+void ctx_free(HyCtx* c, DevBuf& b);
+
+// Accumulated per-pass device counters (u64 each)
+enum { ST_SHADOW = 0, ST_REFL, ST_HITSHADOW, ST_NODES, ST_TRIS, ST_COUNT };
+// work-queue counters (u32 each)
+enum { WQ_SHADOW = 0, WQ_SHADE, WQ_FUSED, WQ_MISC, WQ_COUNT };
+
+}  // namespace hy
+
+struct HyCtx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    uint64_t max_bytes = 0, used_bytes = 0;
+    uint32_t fail_after = 0, alloc_calls = 0;
+    int num_sms = 0;
+
+    // ---- scene ----
+    hy::DevBuf verts, vattr, idx, prims, xf, nrm, prim_tri0, tri_prim, mats, lights, env[2];
+    uint32_t nverts = 0, nidx = 0, nprims = 0, nxf = 0, ntri = 0, nmats = 0, nlights = 0;
+    uint32_t max_material_id = 0;
+    uint32_t env_w[2] = {0, 0}, env_h[2] = {0, 0};
+    bool geometry_ok = false;
+
+    // ---- acceleration structure ----
+    hy::DevBuf world;       // float4 x3 per triangle (world-space vertices)
+    hy::DevBuf tribox;      // float lo[3], hi[3] per triangle
+    hy::DevBuf centroid;    // float4 per triangle
+    hy::DevBuf keys[2], vals[2];
+    hy::DevBuf bvh2;        // 10 words per internal node: left,right,first,last, lo[3], hi[3]
+    hy::DevBuf parent;      // n-1 internal + n leaves
+    hy::DevBuf flags;       // refit arrival counters
+    hy::DevBuf bounds;      // 6 orderable ints + build scratch
+    hy::DevBuf lvl_ref[2], plan, ni, nt, ni_scan, nt_scan;
+    hy::DevBuf scan_tmp, hist, total;
+    hy::DevBuf nodes, tris;
+    uint32_t n_bvh8 = 0, depth = 0;
+    bool bvh_ok = false;
+    HyBvhStats last_build{};
+
+    // ---- pass scratch ----
+    hy::DevBuf dstats;      // u64[ST_COUNT] + u32 status + u32 queue counters
+    hy::DevBuf raw_shadow;  // per-light raw shadow images (unfused path)
+    hy::DevBuf hist_prev;   // history snapshot for the reprojection read
+    hy::DevBuf host_in[6], host_out_f, host_out_8;  // device staging of hy_hybrid_forward_host
+    uint32_t* h_status = nullptr;   // pinned readback slot
+    unsigned long long* h_stats = nullptr;
+};
+
+namespace hy {
+int bvh_build_impl(HyCtx* c, HyBvhStats* st);
+int bvh_refit_impl(HyCtx* c);
+int world_tris_impl(HyCtx* c);
+int scan_exclusive(HyCtx* c, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* d_total);
+}  // namespace hy
+
+#define HY_CUDA_TRY(expr)                               \
+    do {                                                \
+        cudaError_t _e = (expr);                        \
+        if (_e != cudaSuccess) return HY_ERR_CUDA;      \
+    } while (0)

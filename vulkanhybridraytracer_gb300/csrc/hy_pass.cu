@@ -1,0 +1,575 @@
+// The hybrid pass on sm_103a.
+//
+// One persistent kernel template covers the three reference programs:
+//   MODE_SHADOW  shadowRaygen.rgen:28-93   -> raw per-light shadow images
+//   MODE_SHADE   hybridRaygen.rgen:27-186 (+ hybridHit.rchit, miss.rmiss)
+//                reading the accumulated shadow images
+//   MODE_FUSED   both per light in one pass: shadow rays -> running-mean
+//                accumulation (blur.comp:41-48, frame > 0) -> shading, so
+//                the raw images never touch memory
+// and k_accumulate is blur.comp:35-81 for the reset frame (frame <= 0),
+// whose 3x3 neighbourhood clamp needs the whole raw image first.
+//
+// Work distribution: warps pull 8x4 pixel tiles from a global queue
+// (warp-aggregated atomicAdd, `chunk` tiles per pull) until it is drained;
+// the grid is sized to the resident-block capacity of the GPU.
+#include <cuda_runtime.h>
+
+#include "hy_device.cuh"
+#include "hy_pass.h"
+
+namespace hy {
+
+struct LaneStats {
+    uint32_t shadow = 0, refl = 0, hshadow = 0;
+    unsigned long long nodes = 0, tris = 0;
+};
+
+__device__ __forceinline__ void flush_stats(const LaneStats& s, unsigned long long* out) {
+    unsigned long long v[5] = {s.shadow, s.refl, s.hshadow, s.nodes, s.tris};
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        unsigned long long x = v[k];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0 && x) atomicAdd(out + k, x);
+    }
+}
+
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ Hit trace(const SceneDev& S, f3 o, f3 d, float tmin, float tmax, LaneStats& ls,
+                                     uint32_t* status) {
+    RayPre r = ray_pre(o, d);
+    uint32_t nn = 0, nt = 0;
+    Hit h = traverse<ANY, COUNT>(S, r, tmin, tmax, &nn, &nt, status);
+    if (COUNT) { ls.nodes += nn; ls.tris += nt; }
+    return h;
+}
+
+// equirect NEAREST / REPEAT lookup of an RGBA8 map
+__device__ __forceinline__ f3 env_lookup(const uchar4* px, uint32_t w, uint32_t h, float u, float v) {
+    if (w == 0 || h == 0) return mk(0.f, 0.f, 0.f);
+    if (!(u == u)) u = 0.f;
+    if (!(v == v)) v = 0.f;
+    float fx = floorf(u * (float)w), fy = floorf(v * (float)h);
+    fx = fminf(fmaxf(fx, -1e9f), 1e9f);
+    fy = fminf(fmaxf(fy, -1e9f), 1e9f);
+    long long ix = (long long)fx % (long long)w, iy = (long long)fy % (long long)h;
+    if (ix < 0) ix += w;
+    if (iy < 0) iy += h;
+    uchar4 c = px[(size_t)iy * w + (size_t)ix];
+    return mk(__fdiv_rn((float)c.x, 255.f), __fdiv_rn((float)c.y, 255.f), __fdiv_rn((float)c.z, 255.f));
+}
+__device__ __forceinline__ f3 irradiance_at(const SceneDev& S, f3 N) {
+    float u = 0.5f + atan2f(N.x, N.z) / (2.0f * PI);
+    float v = 0.5f - asinf(N.y) / PI;
+    return env_lookup(S.env1, S.env_w[1], S.env_h[1], u, v);
+}
+__device__ __forceinline__ f3 miss_color(const SceneDev& S, f3 d) {
+    f3 dir = normalize(d);
+    float u = 0.5f + atan2f(dir.x, dir.z) / (2.0f * PI_MISS);
+    float v = 0.5f - asinf(dir.y) / PI_MISS;
+    return pow3(env_lookup(S.env0, S.env_w[0], S.env_h[0], u, v), 2.2f);
+}
+
+__device__ __forceinline__ int mat_index(float f, uint32_t n) {
+    if (!(f > -1.f && f < (float)n)) return -1;
+    return (int)f;
+}
+
+struct LightGeo { f3 L; float dist, maxd, NdotL; bool isDir; };
+
+__device__ __forceinline__ LightGeo light_geo(const HyLight& lt, f3 position, f3 N) {
+    LightGeo g;
+    g.isDir = lt.pos[3] < 0.f;
+    f3 lp = mk(lt.pos[0], lt.pos[1], lt.pos[2]);
+    f3 L = g.isDir ? lp : sub_rn(lp, position);
+    g.maxd = lt.pos[3];
+    g.dist = length_rn(L);
+    g.L = normalize_rn(L);
+    g.NdotL = clampf(dot_rn(N, g.L), 0.f, 1.f);
+    return g;
+}
+
+struct HitAttr { f3 N; uint32_t prim; };
+
+__device__ __forceinline__ HitAttr hit_attributes(const SceneDev& S, const Hit& h) {
+    uint32_t p = S.tri_prim[h.id];
+    HyPrimitive pr = S.prims[p];
+    uint32_t local = h.id - S.prim_tri0[p];
+    float b0 = __fsub_rn(__fsub_rn(1.0f, h.b1), h.b2);
+    float bw[3] = {b0, h.b1, h.b2};
+    f3 n = mk(0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        uint32_t vi = S.idx[pr.first_index + 3 * local + k] + pr.vertex_offset;
+        float4 a = __ldg(S.vattr + (size_t)vi * 2);
+        n = n + mk(a.x, a.y, a.z) * bw[k];
+    }
+    const float* nm = S.nrm + (size_t)pr.transform_id * 9;
+    f3 tn = mk(nm[0] * n.x + nm[3] * n.y + nm[6] * n.z, nm[1] * n.x + nm[4] * n.y + nm[7] * n.z,
+               nm[2] * n.x + nm[5] * n.y + nm[8] * n.z);
+    return HitAttr{normalize(tn), p};
+}
+
+struct Payload { f3 color; float t; f3 dir; float scattered; f3 origin; };
+
+// hybridHit.rchit:24-183
+template <bool COUNT>
+__device__ Payload closest_hit(const SceneDev& S, const PassParams& P, const Hit& h, f3 ro, f3 rd, uint32_t& seed,
+                               LaneStats& ls) {
+    HitAttr a = hit_attributes(S, h);
+    f3 N = a.N;
+    f3 V = normalize(-rd);
+    float NdotV = clampf(dot(N, V), 0.f, 1.f);
+    f3 worldPos = ro + rd * h.t;
+    HyPrimitive pr = S.prims[a.prim];
+    const HyMaterial mat = S.mats[pr.material_id];
+    int smode = (int)mat.smr[0];
+    f3 albedo = pow3(mk(mat.diffuse[0], mat.diffuse[1], mat.diffuse[2]), 2.2f);
+    float roughness = mat.smr[2], metallic = mat.smr[1];
+    f3 F0 = mix3(splat(0.04f), albedo, metallic);
+    f3 irradiance = irradiance_at(S, N);
+    f3 direction = mk(1.f, 1.f, 1.f);
+    float dirw = 0.f;
+    f3 Lo = mk(0.f, 0.f, 0.f);
+    float attenuation = 1.0f;
+    for (uint32_t i = 0; i < S.num_lights; i++) {
+        const HyLight lt = S.lights[i];
+        bool isDir = lt.pos[3] < 0.f;
+        f3 lp = mk(lt.pos[0], lt.pos[1], lt.pos[2]);
+        f3 L = isDir ? lp : lp - worldPos;
+        float maxd = lt.pos[3];
+        float dist = length(L);
+        L = normalize(L);
+        float I = isDir ? 1.0f : (lt.color[3] / (dist * dist));
+        f3 H = normalize(V + L);
+        float NdotL = clampf(dot(N, L), 0.f, 1.f);
+        float NdotH = clampf(dot(N, H), 0.f, 1.f);
+        float shadowFactor = 1.0f;
+        if (I == 0.f) attenuation = 0.f;
+        else {
+            attenuation = maxd - dist;
+            attenuation /= maxd;
+            attenuation = fmaxf(attenuation, 0.f);
+            attenuation = isDir ? 0.3f : attenuation * attenuation;
+        }
+        f3 lc = mk(lt.color[0], lt.color[1], lt.color[2]);
+        if (smode == 0) {
+            if (NdotL > 0.f) {
+                bool shadowed = true;
+                if (dist < maxd) {
+                    uint32_t sd = seed;
+                    f3 dir = P.rng_mode == HY_RNG_REFERENCE ? sampleDisk(lt.radius, worldPos, L, sd)
+                                                            : sampleDisk(lt.radius, worldPos, L, seed);
+                    Hit sh = trace<true, COUNT>(S, add_rn(worldPos, scale_rn(dir, 1e-2f)), dir, 0.001f,
+                                                __fadd_rn(dist, 1.0f), ls, P.status);
+                    ls.hshadow++;
+                    shadowed = sh.id != HY_NO_HIT;
+                }
+                if (!shadowed) shadowFactor += 1.0f;
+            }
+            f3 radiance = I * lc * attenuation * shadowFactor;
+            f3 F = FresnelSchlick(NdotH, F0);
+            float D = DistributionGGX(N, H, roughness);
+            float G = GeometrySmith(N, V, L, roughness);
+            f3 numerator = D * G * F;
+            float denominator = fmaxf(4.0f * clampf(dot(N, V), 0.f, 1.f) * NdotL, 0.000001f);
+            f3 specular = numerator / denominator;
+            f3 kD = (splat(1.0f) - F) * (1.0f - metallic);
+            Lo = Lo + (kD * albedo / PI + specular) * radiance * NdotL;
+            direction = mk(1.f, 1.f, 1.f);
+            dirw = 0.f;
+        } else if (smode == 3) {
+            f3 reflected = reflect(normalize(rd), N);
+            bool sc = dot(reflected, N) > 0.f;
+            Lo = Lo + ((NdotL > 0.f && I > 0.f) ? I * lc * attenuation * albedo * metallic
+                                                : irradiance * albedo * metallic);
+            direction = reflected;
+            dirw = sc ? 1.f : 0.f;
+        } else if (smode == 4) {
+            float ior = mat.diffuse[3];
+            float NdV = dot(N, normalize(rd));
+            f3 refrN = NdV > 0.f ? -N : N;
+            float eta = NdV > 0.f ? 1.0f / ior : ior;
+            Lo = Lo + ((I > 0.f) ? I * lc * attenuation * albedo * metallic : irradiance * albedo * metallic);
+            float radicand = 1.0f + powf(eta, 2.0f) * (NdV * NdV - 1.0f);
+            direction = radicand < 0.f ? reflect(rd, N) : refract(normalize(rd), refrN, eta);
+            dirw = 1.f;
+        }
+    }
+    f3 F = FresnelSchlick(NdotV, F0);
+    f3 kD = (splat(1.0f) - F) * (1.0f - metallic);
+    f3 ambient = kD * albedo * irradiance;
+    Payload p;
+    p.color = Lo + ambient;  // emissive is vec3(0) without an emissive texture
+    p.t = h.t;
+    p.dir = direction;
+    p.scattered = dirw;
+    p.origin = worldPos;
+    return p;
+}
+
+__device__ __forceinline__ float roundtrip(uint32_t fmt, float v) {
+    return fmt == HY_ACCUM_U8 ? __fdiv_rn((float)quant8(v), 255.0f) : v;
+}
+
+template <int MODE, bool COUNT>
+__device__ __forceinline__ void do_pixel(const SceneDev& S, const PassParams& P, uint32_t x, uint32_t y,
+                                         LaneStats& ls) {
+    const size_t pix = (size_t)y * P.W + x;
+    const size_t plane = (size_t)P.W * P.H;
+    const float4 g0 = fetch_texel(P.plane[0], P.fmt[0], pix);
+    const float4 g1 = fetch_texel(P.plane[1], P.fmt[1], pix);
+    const f3 position = mk(g0.x, g0.y, g0.z);
+    const f3 normal = mk(__fsub_rn(__fmul_rn(g1.x, 2.0f), 1.0f), __fsub_rn(__fmul_rn(g1.y, 2.0f), 1.0f),
+                         __fsub_rn(__fmul_rn(g1.z, 2.0f), 1.0f));
+    const int mi = mat_index(g0.w, S.num_mats);
+    const int smode = mi >= 0 ? (int)S.mats[mi].smr[0] : 0;
+    const float ior = mi >= 0 ? S.mats[mi].diffuse[3] : 1.f;
+    const f3 N = normalize_rn(normal);
+    uint32_t seed_s = tea(y * P.W + x, P.frame_u);
+    uint32_t seed_h = seed_s;
+    const bool background = g0.w == 0.f && g1.w == 0.f;
+    const bool shading = MODE != MODE_SHADOW && !background;
+    const bool in_blur = x < P.blur_w && y < P.blur_h;
+
+    // shading state (hybridRaygen.rgen:35-72)
+    f3 albedo = mk(0.f, 0.f, 0.f), emissive = mk(0.f, 0.f, 0.f), V = mk(0.f, 0.f, 1.f), F0 = splat(0.04f);
+    f3 irradiance = mk(0.f, 0.f, 0.f), origin = mk(0.f, 0.f, 0.f), direction = mk(0.f, 0.f, 0.f);
+    f3 rayColor = mk(0.f, 0.f, 0.f);
+    float roughness = 0.f, metallic = 0.f, NdotV = 0.f, attenuation = 1.0f;
+    if (MODE != MODE_SHADOW) {
+        const float4 g2 = fetch_texel(P.plane[2], P.fmt[2], pix);
+        albedo = pow3(mk(g2.x, g2.y, g2.z), 2.2f);
+        if (shading) {
+            const float4 g4 = fetch_texel(P.plane[4], P.fmt[4], pix);
+            const float4 g5 = fetch_texel(P.plane[5], P.fmt[5], pix);
+            emissive = mk(g5.x, g5.y, g5.z);
+            roughness = g4.y;
+            metallic = g4.z;
+            F0 = mix3(splat(0.04f), albedo, metallic);
+            V = normalize(P.cam_pos - position);
+            NdotV = clampf(dot(N, V), 0.f, 1.f);
+            irradiance = irradiance_at(S, N);
+        }
+    }
+
+    for (uint32_t i = 0; i < S.num_lights; i++) {
+        const HyLight lt = S.lights[i];
+        const LightGeo lg = light_geo(lt, position, N);
+        const size_t li = i * plane + pix;
+        float sfac = 0.f;
+        if (MODE != MODE_SHADE) {
+            // shadowRaygen.rgen:52-93
+            float sf = 0.f;
+            if (smode == 4) {
+                sf = 1.0f;
+            } else if (lg.NdotL > 0.f) {
+                const int spp = (int)P.spp;
+                if (lg.dist < lg.maxd && P.rng_mode == HY_RNG_REFERENCE) {
+                    uint32_t sd = seed_s;
+                    f3 dir = sampleDisk(lt.radius, position, lg.L, sd);
+                    Hit h = trace<true, COUNT>(S, add_rn(position, scale_rn(dir, 1e-1f)), dir, 0.001f,
+                                               __fadd_rn(lg.dist, 1.0f), ls, P.status);
+                    ls.shadow++;
+                    sf = h.id == HY_NO_HIT ? (float)spp : 0.f;
+                } else {
+                    for (int k = 0; k < spp; k++) {
+                        bool shadowed = false;
+                        if (lg.dist < lg.maxd) {
+                            f3 dir = sampleDisk(lt.radius, position, lg.L, seed_s);
+                            Hit h = trace<true, COUNT>(S, add_rn(position, scale_rn(dir, 1e-1f)), dir, 0.001f,
+                                                       __fadd_rn(lg.dist, 1.0f), ls, P.status);
+                            ls.shadow++;
+                            shadowed = h.id != HY_NO_HIT;
+                        }
+                        if (!shadowed) sf = __fadd_rn(sf, 1.0f);
+                    }
+                }
+                sf = __fdiv_rn(sf, (float)spp);
+            }
+            if (MODE == MODE_SHADOW) {
+                accum_store(P.accum_fmt, P.shadow, li, sf);
+                continue;
+            }
+            // MODE_FUSED: accumulation (blur.comp:41-48) of the stored value
+            const float center = roundtrip(P.accum_fmt, sf);
+            if (P.flags & HY_FLAG_NO_ACCUM) {
+                sfac = center;
+            } else if (in_blur) {
+                const float old = accum_load(P.accum_fmt, P.hist, li);
+                const float a = __fdiv_rn(1.0f, __fadd_rn((float)P.accum_frame, 1.0f));
+                const float out = __fadd_rn(__fmul_rn(old, __fsub_rn(1.0f, a)), __fmul_rn(center, a));
+                accum_store(P.accum_fmt, P.hist, li, out);
+                sfac = roundtrip(P.accum_fmt, out);
+            } else {
+                sfac = accum_load(P.accum_fmt, P.hist, li);
+            }
+        } else {
+            sfac = accum_load(P.accum_fmt, (P.flags & HY_FLAG_NO_ACCUM) ? P.shadow : P.hist, li);
+        }
+        if (!shading) continue;
+        // hybridRaygen.rgen:73-149
+        const float I = lg.isDir ? 1.0f : (lt.color[3] / (lg.dist * lg.dist));
+        const f3 L = lg.L;
+        const float NdotL = lg.NdotL;
+        if (NdotL > 0.f) {
+            if (I == 0.f) attenuation = 0.f;
+            else {
+                attenuation = lg.maxd - lg.dist;
+                attenuation /= lg.maxd;
+                attenuation = fmaxf(attenuation, 0.f);
+                attenuation = lg.isDir ? 0.3f : (attenuation * attenuation);
+            }
+        }
+        const f3 lc = mk(lt.color[0], lt.color[1], lt.color[2]);
+        if (smode == 0) {
+            f3 radiance = lc * I * attenuation * sfac;
+            f3 H = normalize(V + L);
+            float D = DistributionGGX(N, H, roughness);
+            float G = GeometrySmith(N, V, L, roughness);
+            f3 F = FresnelSchlick(fmaxf(dot(H, V), 0.f), F0);
+            f3 kD = (splat(1.0f) - F) * (1.0f - metallic);
+            f3 numerator = D * G * F;
+            float denominator = 4.0f * NdotV * NdotL;
+            f3 specular = numerator / fmaxf(denominator, 0.001f);
+            rayColor = rayColor + (kD * albedo / PI + specular) * radiance * NdotL;
+        }
+        if (smode == 3) {
+            direction = reflect(normalize(-V), N);
+            origin = position;
+            rayColor = rayColor + ((NdotL > 0.f && I > 0.f) ? lc * I * attenuation * sfac * albedo * metallic
+                                                            : irradiance * albedo * metallic);
+        }
+        if (smode == 4) {
+            origin = position;
+            float cosAlpha = dot(N, V);
+            f3 Iv = -V;
+            float NdotI = dot(N, Iv);
+            f3 refrN = NdotI > 0.f ? -N : N;
+            float eta = NdotI > 0.f ? 1.0f / ior : ior;
+            float radicand = 1.0f + powf(eta, 2.0f) * (cosAlpha * cosAlpha - 1.0f);
+            direction = radicand < 0.f ? reflect(Iv, N) : refract(Iv, refrN, eta);
+            rayColor = rayColor + ((I > 0.f) ? I * lc * attenuation * albedo * metallic : irradiance * albedo * metallic);
+        }
+    }
+    if (MODE == MODE_SHADOW) return;
+
+    f3 fc;
+    if (!shading) {
+        fc = albedo;  // background: hybridRaygen.rgen:182-183
+    } else {
+        // hybridRaygen.rgen:151-170
+        for (uint32_t depth = 0; depth < P.max_bounces; depth++) {
+            if (smode == 0) break;
+            f3 ro = origin + direction * 1e-2f;
+            Hit h = trace<false, COUNT>(S, ro, direction, 0.001f, 1000.0f, ls, P.status);
+            ls.refl++;
+            f3 pc, pdir = direction, porg = origin;
+            float pt, pw = 0.f;
+            if (h.id == HY_NO_HIT) {
+                pc = miss_color(S, direction);
+                pt = -1.f;
+            } else {
+                Payload p = closest_hit<COUNT>(S, P, h, ro, direction, seed_h, ls);
+                pc = p.color; pt = p.t; pdir = p.dir; pw = p.scattered; porg = p.origin;
+            }
+            rayColor = rayColor * pc;
+            if (pt < 0.f || !(pw > 0.f)) break;
+            origin = porg;
+            direction = pdir;
+        }
+        f3 F = FresnelSchlick(NdotV, F0);
+        f3 kD = (splat(1.0f) - F) * (1.0f - metallic);
+        fc = rayColor + kD * albedo * irradiance + emissive;
+    }
+    if (P.out_f) reinterpret_cast<float4*>(P.out_f)[pix] = make_float4(fc.x, fc.y, fc.z, 1.f);
+    if (P.out_8) reinterpret_cast<uchar4*>(P.out_8)[pix] = make_uchar4(quant8(fc.z), quant8(fc.y), quant8(fc.x), 255);
+}
+
+template <int MODE, bool COUNT>
+__global__ void __launch_bounds__(128) k_pixels(const SceneDev S, const PassParams P) {
+    LaneStats ls;
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t* queue = P.queue;
+    for (;;) {
+        uint32_t t0 = 0;
+        if (lane == 0) t0 = atomicAdd(queue, P.chunk);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= P.ntiles) break;
+        uint32_t t1 = min(t0 + P.chunk, P.ntiles);
+        for (uint32_t t = t0; t < t1; t++) {
+            uint32_t tx = t % P.tiles_x, ty = t / P.tiles_x;
+            uint32_t x = tx * 8 + (lane & 7), y = ty * 4 + (lane >> 3);
+            if (x < P.W && y < P.H) do_pixel<MODE, COUNT>(S, P, x, y, ls);
+        }
+    }
+    flush_stats(ls, P.stats);
+}
+
+// blur.comp:35-81, reset-frame branch and running mean, one texel per thread
+__global__ void k_accumulate(const AccumParams A) {
+    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= A.blur_w || y >= A.blur_h) return;
+    const size_t plane = (size_t)A.W * A.H, pix = (size_t)y * A.W + x;
+    float rx = 0.f;
+    if (A.frame <= 0) {
+        float4 mo = fetch_texel(A.motion, A.motion_fmt, pix);
+        rx = __fsub_rn(__fmul_rn(mo.x, 2.0f), 1.0f);
+    }
+    for (uint32_t l = 0; l < A.num_lights; l++) {
+        const size_t o = l * plane;
+        const float center = accum_load(A.fmt, A.shadow, o + pix);
+        float out;
+        if (A.frame > 0) {
+            const float old = accum_load(A.fmt, A.hist, o + pix);
+            const float a = __fdiv_rn(1.0f, __fadd_rn((float)A.frame, 1.0f));
+            out = __fadd_rn(__fmul_rn(old, __fsub_rn(1.0f, a)), __fmul_rn(center, a));
+        } else {
+            // blur.comp:53: the y term reuses the x motion (vec2(float, vec2) constructor)
+            const float lx = __fadd_rn((float)x, __fmul_rn(rx, (float)A.W));
+            const float ly = __fadd_rn((float)y, __fmul_rn(rx, (float)A.H));
+            float mn = center, mx = center;
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    if (dx == 0 && dy == 0) continue;
+                    int xx = (int)x + dx, yy = (int)y + dy;
+                    float c = 0.f;
+                    if (xx >= 0 && yy >= 0 && xx < (int)A.W && yy < (int)A.H)
+                        c = accum_load(A.fmt, A.shadow, o + (size_t)yy * A.W + xx);
+                    mn = fminf(mn, c);
+                    mx = fmaxf(mx, c);
+                }
+            float old = 0.f;
+            if (lx > -2147483648.f && lx < 2147483647.f && ly > -2147483648.f && ly < 2147483647.f) {
+                int ix = (int)lx, iy = (int)ly;
+                if (ix >= 0 && iy >= 0 && ix < (int)A.W && iy < (int)A.H)
+                    old = accum_load(A.fmt, A.hist_prev, o + (size_t)iy * A.W + ix);
+            }
+            old = fmaxf(mn, old);
+            old = fminf(mx, old);
+            out = __fadd_rn(__fmul_rn(old, __fsub_rn(1.0f, 0.4f)), __fmul_rn(center, 0.4f));
+        }
+        accum_store(A.fmt, A.hist, o + pix, out);
+    }
+}
+
+// generic ray queries (32 B ray in, 16 B hit out)
+template <bool ANY, bool COUNT>
+__global__ void __launch_bounds__(128) k_trace(const SceneDev S, const HyRay* __restrict__ rays, uint32_t n,
+                                               HyHit* __restrict__ hits, unsigned long long* stats, uint32_t* status) {
+    LaneStats ls;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i - threadIdx.x < n; i += gridDim.x * blockDim.x) {
+        if (i < n) {
+            HyRay r = rays[i];
+            Hit h = trace<ANY, COUNT>(S, mk(r.org[0], r.org[1], r.org[2]), mk(r.dir[0], r.dir[1], r.dir[2]), r.tmin,
+                                      r.tmax, ls, status);
+            ls.shadow++;
+            HyHit o;
+            o.t = h.id == HY_NO_HIT ? 0.f : h.t;
+            o.tri_id = h.id;
+            o.b1 = h.id == HY_NO_HIT ? 0.f : h.b1;
+            o.b2 = h.id == HY_NO_HIT ? 0.f : h.b2;
+            hits[i] = o;
+        }
+    }
+    flush_stats(ls, stats);
+}
+
+// primary-ray G-buffer (raygen.rgen:29-40 camera, geometry_shader.frag:54-76 encoding)
+__device__ __forceinline__ f3 mat_vec3(const float* m, float x, float y, float z, float w) {
+    float r[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float a = __fmul_rn(m[0 * 4 + i], x);
+        a = __fadd_rn(a, __fmul_rn(m[1 * 4 + i], y));
+        a = __fadd_rn(a, __fmul_rn(m[2 * 4 + i], z));
+        a = __fadd_rn(a, __fmul_rn(m[3 * 4 + i], w));
+        r[i] = a;
+    }
+    return mk(r[0], r[1], r[2]);
+}
+
+__global__ void __launch_bounds__(128) k_gbuffer(const SceneDev S, const GbufParams G) {
+    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= G.W || y >= G.H) return;
+    size_t i = (size_t)y * G.W + x;
+    float ux = __fdiv_rn(__fadd_rn((float)x, 0.5f), (float)G.W), uy = __fdiv_rn(__fadd_rn((float)y, 0.5f), (float)G.H);
+    float dx = __fsub_rn(__fmul_rn(ux, 2.0f), 1.0f), dy = __fsub_rn(__fmul_rn(uy, 2.0f), 1.0f);
+    f3 org = mat_vec3(G.inv_view, 0.f, 0.f, 0.f, 1.f);
+    f3 tgt = mat_vec3(G.inv_proj, dx, dy, 1.f, 1.f);
+    f3 tn = normalize_rn(tgt);
+    f3 dir = mat_vec3(G.inv_view, tn.x, tn.y, tn.z, 0.f);
+    f3 o = add_rn(org, scale_rn(dir, 1e-2f));
+    LaneStats ls;
+    Hit h = trace<false, false>(S, o, dir, 0.001f, 10000.0f, ls, G.status);
+    float4* p0 = (float4*)G.planes[0]; float4* p1 = (float4*)G.planes[1]; float4* p2 = (float4*)G.planes[2];
+    float2* p3 = (float2*)G.planes[3]; float4* p4 = (float4*)G.planes[4]; float4* p5 = (float4*)G.planes[5];
+    if (h.id == HY_NO_HIT) {
+        float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        p0[i] = z; p1[i] = z; p2[i] = z; p3[i] = make_float2(0.f, 0.f); p4[i] = z; p5[i] = z;
+        return;
+    }
+    HitAttr a = hit_attributes(S, h);
+    const HyMaterial m = S.mats[S.prims[a.prim].material_id];
+    f3 wp = add_rn(o, scale_rn(dir, h.t));
+    p0[i] = make_float4(wp.x, wp.y, wp.z, m.smr[3]);
+    p1[i] = make_float4(__fadd_rn(__fmul_rn(a.N.x, 0.5f), 0.5f), __fadd_rn(__fmul_rn(a.N.y, 0.5f), 0.5f),
+                        __fadd_rn(__fmul_rn(a.N.z, 0.5f), 0.5f), 1.f);
+    p2[i] = make_float4(m.diffuse[0], m.diffuse[1], m.diffuse[2], 1.f);
+    p3[i] = make_float2(0.5f, 0.5f);
+    p4[i] = make_float4(0.f, m.smr[2], m.smr[1], 1.f);
+    p5[i] = make_float4(0.f, 0.f, 0.f, 1.f);
+}
+
+// ---------------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------------
+template <int MODE>
+static void* pixel_kernel(bool count) {
+    return count ? (void*)k_pixels<MODE, true> : (void*)k_pixels<MODE, false>;
+}
+
+cudaError_t launch_pixels(int mode, bool count, const SceneDev& S, const PassParams& P, int grid, int block,
+                          cudaStream_t s) {
+    void* fn = mode == MODE_SHADOW ? pixel_kernel<MODE_SHADOW>(count)
+             : mode == MODE_SHADE  ? pixel_kernel<MODE_SHADE>(count)
+                                   : pixel_kernel<MODE_FUSED>(count);
+    void* args[] = {(void*)&S, (void*)&P};
+    return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, s);
+}
+
+cudaError_t pixel_occupancy(int mode, bool count, int block, int* blocks_per_sm) {
+    void* fn = mode == MODE_SHADOW ? pixel_kernel<MODE_SHADOW>(count)
+             : mode == MODE_SHADE  ? pixel_kernel<MODE_SHADE>(count)
+                                   : pixel_kernel<MODE_FUSED>(count);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, 0);
+}
+
+cudaError_t launch_accumulate(const AccumParams& A, cudaStream_t s) {
+    dim3 b(16, 16), g((A.blur_w + 15) / 16, (A.blur_h + 15) / 16);
+    if (g.x == 0 || g.y == 0) return cudaSuccess;
+    k_accumulate<<<g, b, 0, s>>>(A);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace(const SceneDev& S, const HyRay* rays, uint32_t n, bool any, bool count, HyHit* hits,
+                         unsigned long long* stats, uint32_t* status, int grid, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    if (any) {
+        if (count) k_trace<true, true><<<grid, 128, 0, s>>>(S, rays, n, hits, stats, status);
+        else k_trace<true, false><<<grid, 128, 0, s>>>(S, rays, n, hits, stats, status);
+    } else {
+        if (count) k_trace<false, true><<<grid, 128, 0, s>>>(S, rays, n, hits, stats, status);
+        else k_trace<false, false><<<grid, 128, 0, s>>>(S, rays, n, hits, stats, status);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gbuffer(const SceneDev& S, const GbufParams& G, cudaStream_t s) {
+    dim3 b(16, 8), g((G.W + 15) / 16, (G.H + 7) / 8);
+    k_gbuffer<<<g, b, 0, s>>>(S, G);
+    return cudaGetLastError();
+}
+
+}  // namespace hy

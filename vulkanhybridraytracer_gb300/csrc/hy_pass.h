@@ -1,0 +1,58 @@
+// Launch parameters shared by hy_pass.cu (device) and hy_api.cu (host).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hy_device.cuh"
+
+namespace hy {
+
+enum { MODE_SHADOW = 0, MODE_SHADE = 1, MODE_FUSED = 2 };
+
+struct PassParams {
+    uint32_t W, H;
+    const void* plane[6];
+    uint32_t fmt[6];
+    f3 cam_pos;              // viewInverse * (0,0,0,1)
+    uint32_t frame_u;        // uint(int(cam.frame.x)): the per-pixel RNG frame
+    uint32_t spp, max_bounces, rng_mode, flags;
+    int32_t accum_frame;     // blur.comp frame
+    uint32_t accum_fmt;
+    void* shadow;            // raw shadow images
+    void* hist;              // accumulated history
+    float* out_f;
+    uint8_t* out_8;
+    uint32_t tiles_x, ntiles, chunk;
+    uint32_t blur_w, blur_h; // texels the blur dispatch covers
+    unsigned long long* stats;
+    uint32_t* status;
+    uint32_t* queue;
+};
+
+struct AccumParams {
+    uint32_t W, H, num_lights, fmt;
+    int32_t frame;
+    uint32_t blur_w, blur_h;
+    const void* motion;
+    uint32_t motion_fmt;
+    const void* shadow;
+    void* hist;
+    const void* hist_prev;
+};
+
+struct GbufParams {
+    uint32_t W, H;
+    float inv_view[16], inv_proj[16];
+    float* planes[6];
+    uint32_t* status;
+};
+
+cudaError_t launch_pixels(int mode, bool count, const SceneDev& S, const PassParams& P, int grid, int block,
+                          cudaStream_t s);
+cudaError_t pixel_occupancy(int mode, bool count, int block, int* blocks_per_sm);
+cudaError_t launch_accumulate(const AccumParams& A, cudaStream_t s);
+cudaError_t launch_trace(const SceneDev& S, const HyRay* rays, uint32_t n, bool any, bool count, HyHit* hits,
+                         unsigned long long* stats, uint32_t* status, int grid, cudaStream_t s);
+cudaError_t launch_gbuffer(const SceneDev& S, const GbufParams& G, cudaStream_t s);
+
+}  // namespace hy

@@ -1,0 +1,218 @@
+"""Python host API over the C ABI (include/hybridrt.h).
+
+``HybridContext`` is the counterpart of the hybrid part of VkPinut's
+``Renderer``: it takes a ``Scene`` (what Renderer::load_data_to_gpu and
+create_hybrid_descriptors upload, src/renderer.cpp:1477-1530, 3015-3048),
+builds the acceleration structure (create_bottom/top_acceleration_structure,
+src/renderer.cpp:1643-1688) and runs the pass that rasterize_hybrid submits
+(src/renderer.cpp:559-580).  Device buffers are torch CUDA tensors, used as
+plain memory; every computation runs in libhybridrt's CUDA kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .scene import Scene
+
+
+def _ptr(t) -> int:
+    return t.data_ptr() if hasattr(t, "data_ptr") else t.ctypes.data
+
+
+def _np_ptr(a: np.ndarray):
+    assert a.flags["C_CONTIGUOUS"]
+    return C.c_void_p(a.ctypes.data)
+
+
+def camera_struct(cam36) -> L.HyCamera:
+    cam = np.ascontiguousarray(cam36, np.float32)
+    c = L.HyCamera()
+    C.memmove(C.byref(c), cam.ctypes.data, 144)
+    return c
+
+
+def pass_config(spp=1, max_bounces=8, rng_mode=L.HY_RNG_REFERENCE, accum_frame=0, flags=0, block_size=0,
+                queue_chunk=0, stack_depth=0) -> L.HyPassConfig:
+    return L.HyPassConfig(spp, max_bounces, rng_mode, accum_frame, flags, block_size, queue_chunk, stack_depth)
+
+
+GBUF_FP32_FORMATS = (L.HY_FMT_RGBA32F, L.HY_FMT_RGBA32F, L.HY_FMT_RGBA32F, L.HY_FMT_RG32F, L.HY_FMT_RGBA32F,
+                     L.HY_FMT_RGBA32F)
+
+
+def gbuffer_struct(planes, width, height, formats=GBUF_FP32_FORMATS) -> L.HyGBuffer:
+    g = L.HyGBuffer()
+    g.width, g.height = width, height
+    for i in range(6):
+        g.plane[i] = _ptr(planes[i])
+        g.format[i] = formats[i]
+    return g
+
+
+class HybridContext:
+    """One device context: scene, BVH, and the hybrid pass."""
+
+    def __init__(self, device: int = 0, stream: int | None = None, max_device_bytes: int = 0):
+        self.lib = L.load()
+        self.device = device
+        info = L.HyCreateInfo(device, 0, stream, max_device_bytes)
+        h = C.c_void_p()
+        L.check(self.lib.hy_create(C.byref(h), C.byref(info)), "hy_create")
+        self.h = h
+        self.num_lights = 0
+        self.num_tris = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.hy_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- scene ----
+    def set_scene_arrays(self, verts, idx, prims, xf, mats, lights, env=None):
+        self._keep = (verts, idx, prims, xf, mats, lights)
+        L.check(self.lib.hy_scene_set_geometry(self.h, _np_ptr(verts), len(verts), _np_ptr(idx), len(idx),
+                                               _np_ptr(prims), len(prims), _np_ptr(xf), len(xf)), "geometry")
+        L.check(self.lib.hy_scene_set_materials(self.h, _np_ptr(mats), len(mats)), "materials")
+        L.check(self.lib.hy_scene_set_lights(self.h, _np_ptr(lights) if len(lights) else None, len(lights)),
+                "lights")
+        for slot, e in enumerate(env or []):
+            e = np.ascontiguousarray(e, np.uint8)
+            L.check(self.lib.hy_scene_set_env(self.h, slot, _np_ptr(e), e.shape[1], e.shape[0]), "env")
+        self.num_lights = len(lights)
+        self.num_tris = int(sum(int(p[1]) // 3 for p in prims))
+
+    def set_scene(self, scene: Scene):
+        verts, idx, prims, xf, mats, lights = scene.pack()
+        self.set_scene_arrays(verts, idx, prims, xf, mats, lights, scene.env)
+
+    def set_lights(self, lights: np.ndarray):
+        lights = np.ascontiguousarray(lights, np.float32)
+        L.check(self.lib.hy_scene_set_lights(self.h, _np_ptr(lights), len(lights)), "lights")
+        self.num_lights = len(lights)
+
+    def set_materials(self, mats: np.ndarray):
+        mats = np.ascontiguousarray(mats, np.float32)
+        L.check(self.lib.hy_scene_set_materials(self.h, _np_ptr(mats), len(mats)), "materials")
+
+    def build_bvh(self) -> dict:
+        st = L.HyBvhStats()
+        L.check(self.lib.hy_bvh_build(self.h, C.byref(st)), "bvh_build")
+        return {"num_tris": st.num_tris, "num_bvh2_nodes": st.num_bvh2_nodes, "num_bvh8_nodes": st.num_bvh8_nodes,
+                "depth": st.depth, "build_ms": st.build_ms, "scene_lo": list(st.scene_lo),
+                "scene_hi": list(st.scene_hi)}
+
+    def download_bvh(self, n_bvh8: int):
+        n = self.num_tris
+        morton = np.zeros(n, np.uint32)
+        order = np.zeros(n, np.uint32)
+        bvh2 = np.zeros((max(n - 1, 0), 10), np.uint32)
+        bvh8 = np.zeros((n_bvh8, 20), np.uint32)
+        tris = np.zeros((n, 12), np.float32)
+        L.check(self.lib.hy_bvh_download(self.h, _np_ptr(morton), _np_ptr(order), _np_ptr(bvh2), _np_ptr(bvh8),
+                                         _np_ptr(tris)), "bvh_download")
+        return morton, order, bvh2, bvh8, tris
+
+    # ---- queries ----
+    def trace(self, rays, any_hit: bool, count: bool = False):
+        """rays: CUDA float32 tensor (n, 8); returns (hits int32/float32 view (n, 4) tensor, stats)."""
+        import torch
+        n = rays.shape[0]
+        hits = torch.empty((n, 4), dtype=torch.float32, device=rays.device)
+        st = L.HyStats()
+        L.check(self.lib.hy_trace_rays(self.h, C.c_void_p(rays.data_ptr()), n, int(any_hit),
+                                       C.c_void_p(hits.data_ptr()), C.byref(st) if count else None), "trace")
+        return hits, st.as_dict()
+
+    def gbuffer(self, cam36, width: int, height: int):
+        import torch
+        dev = torch.device("cuda", self.device)
+        planes = [torch.empty((height, width, 4 if i != 3 else 2), dtype=torch.float32, device=dev)
+                  for i in range(6)]
+        arr = (C.c_void_p * 6)(*[p.data_ptr() for p in planes])
+        cam = camera_struct(cam36)
+        L.check(self.lib.hy_gbuffer_primary(self.h, C.byref(cam), width, height, arr), "gbuffer")
+        return planes
+
+    # ---- the pass ----
+    def new_history(self, width, height, fmt=L.HY_ACCUM_U8, fill=0):
+        import torch
+        dt = torch.uint8 if fmt == L.HY_ACCUM_U8 else torch.float32
+        return torch.full((self.num_lights, height, width), fill, dtype=dt, device=torch.device("cuda", self.device))
+
+    @staticmethod
+    def _accum(hist, fmt):
+        return L.HyAccum(fmt, hist.shape[0], hist.data_ptr())
+
+    def forward(self, planes, cam36, cfg: L.HyPassConfig, hist, fmt=L.HY_ACCUM_U8, out_f=None, out_8=None,
+                formats=GBUF_FP32_FORMATS):
+        h, w = planes[0].shape[0], planes[0].shape[1]
+        gb = gbuffer_struct(planes, w, h, formats)
+        cam = camera_struct(cam36)
+        acc = self._accum(hist, fmt)
+        st = L.HyStats()
+        L.check(self.lib.hy_hybrid_forward(self.h, C.byref(gb), C.byref(cam), C.byref(cfg), C.byref(acc),
+                                           C.c_void_p(out_f.data_ptr()) if out_f is not None else None,
+                                           C.c_void_p(out_8.data_ptr()) if out_8 is not None else None,
+                                           C.byref(st)), "hybrid_forward")
+        return st.as_dict()
+
+    def forward_host(self, planes_np, cam36, cfg, hist, fmt=L.HY_ACCUM_U8, out_f=None, out_8=None,
+                     formats=GBUF_FP32_FORMATS, stats=True):
+        """Host planes / outputs (numpy or pinned CPU tensors); history stays on the device."""
+        h, w = planes_np[0].shape[0], planes_np[0].shape[1]
+        gb = gbuffer_struct(planes_np, w, h, formats)
+        cam = camera_struct(cam36)
+        acc = self._accum(hist, fmt)
+        st = L.HyStats()
+        L.check(self.lib.hy_hybrid_forward_host(self.h, C.byref(gb), C.byref(cam), C.byref(cfg), C.byref(acc),
+                                                C.c_void_p(_ptr(out_f)) if out_f is not None else None,
+                                                C.c_void_p(_ptr(out_8)) if out_8 is not None else None,
+                                                C.byref(st) if stats else None), "hybrid_forward_host")
+        return st.as_dict()
+
+    def shadow_pass(self, planes, cam36, cfg, shadow, fmt=L.HY_ACCUM_U8, formats=GBUF_FP32_FORMATS):
+        h, w = planes[0].shape[0], planes[0].shape[1]
+        gb = gbuffer_struct(planes, w, h, formats)
+        cam = camera_struct(cam36)
+        st = L.HyStats()
+        L.check(self.lib.hy_shadow_pass(self.h, C.byref(gb), C.byref(cam), C.byref(cfg), fmt,
+                                        C.c_void_p(shadow.data_ptr()), C.byref(st)), "shadow_pass")
+        return st.as_dict()
+
+    def accumulate_pass(self, planes, cfg, shadow, hist, fmt=L.HY_ACCUM_U8, formats=GBUF_FP32_FORMATS):
+        h, w = planes[0].shape[0], planes[0].shape[1]
+        gb = gbuffer_struct(planes, w, h, formats)
+        acc = self._accum(hist, fmt)
+        L.check(self.lib.hy_accumulate_pass(self.h, C.byref(gb), C.byref(cfg), C.c_void_p(shadow.data_ptr()),
+                                            C.byref(acc)), "accumulate_pass")
+
+    def shade_pass(self, planes, cam36, cfg, hist, fmt=L.HY_ACCUM_U8, out_f=None, out_8=None,
+                   formats=GBUF_FP32_FORMATS):
+        h, w = planes[0].shape[0], planes[0].shape[1]
+        gb = gbuffer_struct(planes, w, h, formats)
+        cam = camera_struct(cam36)
+        acc = self._accum(hist, fmt)
+        st = L.HyStats()
+        L.check(self.lib.hy_shade_pass(self.h, C.byref(gb), C.byref(cam), C.byref(cfg), C.byref(acc),
+                                       C.c_void_p(out_f.data_ptr()) if out_f is not None else None,
+                                       C.c_void_p(out_8.data_ptr()) if out_8 is not None else None,
+                                       C.byref(st)), "shade_pass")
+        return st.as_dict()
+
+    def synchronize(self):
+        L.check(self.lib.hy_synchronize(self.h), "synchronize")

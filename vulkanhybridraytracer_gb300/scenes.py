@@ -1,0 +1,228 @@
+"""Seeded synthetic scenes for the hybrid pass.
+
+The reference's meshes and environment maps (sphere.obj, lucy.obj,
+DamagedHelmet.gltf, the LA_Downtown HDR/JPG) are not part of its repository,
+so seeded synthetic scenes of the stated shapes stand in for them:
+
+* ``small``   256x256, 20x20 ground quad + 16 icospheres (subdivision 2),
+              one point light (2,6,2) intensity 20 + one directional light,
+              1 shadow ray per light per pixel, 1 mirror bounce.
+* ``hd``      1920x1080, 512x512-vertex fBm terrain (522,242 triangles) +
+              48 icospheres (subdivision 5, 20,480 triangles each): 1,505,282
+              triangles, 256 materials, 4 spherical area lights (radius 0.5,
+              intensity U[10, 50]), 16 shadow samples per light per pixel,
+              1 mirror bounce.
+* ``diff``    512x512, ground + 64 icospheres (subdivision 3), 64 materials,
+              8 point lights, 16 shadow samples.
+
+Materials: albedo U[0,1]^3, roughness U[0,1], metallic Bernoulli(0.3);
+shading model 3 (mirror) when roughness < 0.3, else 0 (PBR).  Draws come
+from numpy's PCG64 generator in the order written below.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .scene import (DIRECTIONAL_LIGHT, POINT_LIGHT, SHADING_MIRROR, SHADING_PBR, Camera, Light, Material,
+                    Mesh, Object, Scene)
+
+
+# ---- meshes ----------------------------------------------------------------------
+def _vertices(pos, nrm, uv) -> np.ndarray:
+    n = len(pos)
+    v = np.zeros((n, 11), np.float32)
+    v[:, 0:3] = pos
+    v[:, 3:6] = nrm
+    v[:, 6:9] = 1.0
+    v[:, 9:11] = uv
+    return v
+
+
+def icosphere(subdiv: int) -> Mesh:
+    """Unit icosphere: 20 * 4^subdiv triangles, outward normals."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+             (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5),
+             (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    v = np.array(verts, np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    f = np.array(faces, np.int64)
+    for _ in range(subdiv):
+        e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]])
+        e.sort(axis=1)
+        uniq, inv = np.unique(e, axis=0, return_inverse=True)
+        mid = (v[uniq[:, 0]] + v[uniq[:, 1]]) * 0.5
+        mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+        base = len(v)
+        v = np.concatenate([v, mid])
+        nf = len(f)
+        a = base + inv[:nf]
+        b = base + inv[nf:2 * nf]
+        c = base + inv[2 * nf:]
+        f = np.concatenate([np.stack([f[:, 0], a, c], 1), np.stack([f[:, 1], b, a], 1),
+                            np.stack([f[:, 2], c, b], 1), np.stack([a, b, c], 1)])
+    uv = np.stack([0.5 + np.arctan2(v[:, 0], v[:, 2]) / (2 * np.pi), 0.5 - np.arcsin(np.clip(v[:, 1], -1, 1)) / np.pi], 1)
+    return Mesh(_vertices(v, v, uv), f.reshape(-1).astype(np.uint32))
+
+
+def quad(size: float) -> Mesh:
+    h = size / 2.0
+    pos = np.array([[-h, 0, -h], [h, 0, -h], [h, 0, h], [-h, 0, h]], np.float64)
+    nrm = np.tile([0.0, 1.0, 0.0], (4, 1))
+    uv = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float64)
+    return Mesh(_vertices(pos, nrm, uv), np.array([0, 2, 1, 0, 3, 2], np.uint32))
+
+
+def _value_noise(rng: np.random.Generator, n: int, cells: int) -> np.ndarray:
+    g = rng.random((cells + 1, cells + 1))
+    x = np.linspace(0, cells, n, endpoint=False)
+    i = np.floor(x).astype(np.int64)
+    f = x - i
+    f = f * f * (3 - 2 * f)
+    a = g[i][:, i]
+    b = g[i][:, i + 1]
+    c = g[i + 1][:, i]
+    d = g[i + 1][:, i + 1]
+    fx = f[None, :]
+    fy = f[:, None]
+    return (a * (1 - fx) + b * fx) * (1 - fy) + (c * (1 - fx) + d * fx) * fy
+
+
+def terrain(rng: np.random.Generator, n: int = 512, extent: float = 50.0, amplitude: float = 2.0,
+            octaves: int = 6) -> Mesh:
+    """n x n vertex fBm heightfield over [-extent, extent]^2: 2 (n-1)^2 triangles."""
+    h = np.zeros((n, n))
+    amp, cells, norm = 1.0, 4, 0.0
+    for _ in range(octaves):
+        h += amp * (_value_noise(rng, n, cells) - 0.5)
+        norm += amp
+        amp *= 0.5   # gain
+        cells *= 2   # lacunarity
+    h *= amplitude / norm * 2.0
+    xs = np.linspace(-extent, extent, n)
+    X, Z = np.meshgrid(xs, xs)
+    pos = np.stack([X, h, Z], -1).reshape(-1, 3)
+    dx = xs[1] - xs[0]
+    gx = np.gradient(h, dx, axis=1)
+    gz = np.gradient(h, dx, axis=0)
+    nrm = np.stack([-gx, np.ones_like(h), -gz], -1).reshape(-1, 3)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    uv = np.stack([(X + extent) / (2 * extent), (Z + extent) / (2 * extent)], -1).reshape(-1, 2)
+    i = np.arange(n - 1)
+    I, J = np.meshgrid(i, i)
+    a = (J * n + I).reshape(-1)
+    b = a + 1
+    c = a + n
+    d = c + 1
+    idx = np.stack([a, c, b, b, c, d], 1).reshape(-1).astype(np.uint32)
+    return Mesh(_vertices(pos, nrm, uv), idx), h
+
+
+def trs(t=(0, 0, 0), s=1.0) -> np.ndarray:
+    """Translate * uniform scale in glm storage (m[col][row])."""
+    m = np.eye(4) * s
+    m[3, 3] = 1.0
+    m[3, 0:3] = t
+    return m
+
+
+def random_materials(rng: np.random.Generator, n: int) -> list:
+    out = []
+    for _ in range(n):
+        albedo = rng.random(3)
+        rough = float(rng.random())
+        metal = float(rng.random() < 0.3)
+        model = SHADING_MIRROR if rough < 0.3 else SHADING_PBR
+        out.append(Material(shading_model=model, diffuse_color=(*albedo, 1.0), metallic_factor=metal,
+                            roughness_factor=rough, ior=1.0))
+    return out
+
+
+def env_map(rng: np.random.Generator, w: int = 1024, h: int = 512, sun=True) -> np.ndarray:
+    """Procedural equirect RGBA8 sky: vertical gradient, low-frequency noise, a sun disk."""
+    v = (np.arange(h) + 0.5) / h
+    u = (np.arange(w) + 0.5) / w
+    U, V = np.meshgrid(u, v)
+    elev = (0.5 - V) * np.pi
+    sky = np.stack([0.35 + 0.3 * np.sin(elev).clip(0), 0.55 + 0.25 * np.sin(elev).clip(0), 0.85 + 0.1 * np.sin(elev)], -1)
+    ground = np.array([0.25, 0.22, 0.2])
+    col = np.where((elev > 0)[..., None], sky, ground)
+    col = col * (0.85 + 0.3 * _value_noise(rng, max(w, h), 8)[:h, :w][..., None])
+    if sun:
+        su, sv = rng.random() , 0.25 + 0.1 * rng.random()
+        d = np.hypot((U - su) * 2, V - sv)
+        col = col + (d < 0.02)[..., None] * 1.0
+    rgba = np.concatenate([np.clip(col, 0, 1), np.ones((h, w, 1))], -1)
+    return np.round(rgba * 255).astype(np.uint8)
+
+
+# ---- configurations ---------------------------------------------------------------
+@dataclass
+class Workload:
+    name: str
+    scene: Scene
+    width: int
+    height: int
+    spp: int
+    max_bounces: int
+    rng_mode: int   # HY_RNG_*
+
+    def camera(self, frame: float = 0.0) -> np.ndarray:
+        return self.scene.camera.rt_camera(self.width, self.height, frame)
+
+
+def small(seed: int = 0, width: int = 256, height: int = 256) -> Workload:
+    rng = np.random.default_rng(seed)
+    sc = Scene()
+    sc.entities.append(Object(quad(20.0), 0, trs()))
+    ico = icosphere(2)
+    for i in range(16):
+        r = rng.uniform(0.3, 0.8)
+        c = (rng.uniform(-5, 5), rng.uniform(0.5, 1.5), rng.uniform(-5, 5))
+        sc.entities.append(Object(ico, i + 1, trs(c, r)))
+    sc.materials = random_materials(rng, 17)
+    sc.lights = [Light(POINT_LIGHT, (1, 1, 1), (2, 6, 2), 20.0, 500.0, 0.1),
+                 Light(DIRECTIONAL_LIGHT, (1, 1, 1), (0.3, 1.0, 0.2), 1.0, 500.0, 0.1)]
+    sc.camera = Camera((0.0, 4.0, 10.0), (0.0, 0.0, 0.0), 60.0)
+    sc.env = [env_map(rng), env_map(rng, sun=False)]
+    return Workload("small-256x256-5k", sc, width, height, 1, 1, 0)
+
+
+def hd(seed: int = 1, width: int = 1920, height: int = 1080, n_spheres: int = 48, sphere_subdiv: int = 5,
+       terrain_n: int = 512, spp: int = 16) -> Workload:
+    rng = np.random.default_rng(seed)
+    sc = Scene()
+    ter, hmap = terrain(rng, terrain_n)
+    sc.materials = random_materials(rng, 256)
+    sc.entities.append(Object(ter, int(rng.integers(256)), trs()))
+    ico = icosphere(sphere_subdiv)
+    for _ in range(n_spheres):
+        s = rng.uniform(0.5, 3.0)
+        x, z = rng.uniform(-40, 40), rng.uniform(-40, 40)
+        sc.entities.append(Object(ico, int(rng.integers(256)), trs((x, s + 1.0, z), s)))
+    sc.lights = [Light(POINT_LIGHT, (1, 1, 1), (rng.uniform(-30, 30), rng.uniform(8, 16), rng.uniform(-30, 30)),
+                       float(rng.uniform(10, 50)), 500.0, 0.5) for _ in range(4)]
+    sc.camera = Camera((0.0, 18.0, 55.0), (0.0, 0.0, 0.0), 60.0)
+    sc.env = [env_map(rng), env_map(rng, sun=False)]
+    return Workload(f"hd-{width}x{height}-{sc.num_tris // 1000}k", sc, width, height, spp, 1, 1)
+
+
+def diff(seed: int = 3, width: int = 512, height: int = 512) -> Workload:
+    rng = np.random.default_rng(seed)
+    sc = Scene()
+    sc.entities.append(Object(quad(30.0), 0, trs()))
+    ico = icosphere(3)
+    sc.materials = random_materials(rng, 64)
+    for i in range(64):
+        r = rng.uniform(0.3, 0.8)
+        c = (rng.uniform(-8, 8), rng.uniform(0.5, 1.5), rng.uniform(-8, 8))
+        sc.entities.append(Object(ico, int(rng.integers(64)), trs(c, r)))
+    sc.lights = [Light(POINT_LIGHT, (1, 1, 1), (rng.uniform(-8, 8), rng.uniform(4, 8), rng.uniform(-8, 8)),
+                       float(rng.uniform(10, 50)), 500.0, 0.3) for _ in range(8)]
+    sc.camera = Camera((0.0, 8.0, 16.0), (0.0, 0.0, 0.0), 60.0)
+    sc.env = [env_map(rng), env_map(rng, sun=False)]
+    return Workload("diff-512x512-82k", sc, width, height, 16, 1, 1)
