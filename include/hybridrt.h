@@ -168,6 +168,7 @@ typedef struct HyPassConfig {
     uint32_t block_size;    /* threads per block; 0 = default / autotuned */
     uint32_t queue_chunk;   /* work items fetched per warp from the ray queue; 0 = default */
     uint32_t stack_depth;   /* traversal stack entries; 0 = default (max 64) */
+    uint32_t min_blocks;    /* shadow-kernel variant compiled for 4/5/6/8 resident blocks per SM; 0 = 5 */
 } HyPassConfig;
 
 typedef struct HyStats {

@@ -1,0 +1,380 @@
+"""GPU parity of libhybridrt against the CPU oracle, through the C ABI.
+
+Integer/index outputs (Morton codes, sort order, BVH arrays, packed
+triangles, hit ids, traversal counts, R8 shadow/history images) must be
+bit-exact.  Radiance follows the pass's stated tolerance: relative RMS
+<= 1e-3 and per-pixel max |err| <= 1e-2 on pixels whose shadow decisions
+agree; decisions may differ on at most 1e-4 of the shadow texels (a shadow
+ray direction built from cosf/sinf can differ by an ulp between CUDA and
+libm and graze an edge differently).
+"""
+import numpy as np
+import pytest
+
+import pyoracle as po
+from vulkanhybridraytracer_gb300 import _lib as L
+from vulkanhybridraytracer_gb300 import scenes
+from vulkanhybridraytracer_gb300.scene import Material
+
+pytestmark = pytest.mark.gpu
+
+RMS_TOL, MAX_TOL, FLIP_TOL = 1e-3, 1e-2, 1e-4
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class Pair:
+    """The same scene in the GPU context and in the oracle."""
+
+    def __init__(self, wl, build=True):
+        from vulkanhybridraytracer_gb300.hybrid import HybridContext
+        self.wl = wl
+        self.ctx = HybridContext(0)
+        self.ctx.set_scene(wl.scene)
+        self.orc = po.OracleScene()
+        self.orc.set_scene(wl.scene)
+        if build:
+            self.gi = self.ctx.build_bvh()
+            self.oi = self.orc.build_bvh()
+
+
+def glass_workload(w=96, h=96):
+    wl = scenes.small(0, w, h)
+    for i in (2, 5, 9):
+        wl.scene.materials[i] = Material(4, (0.9, 0.95, 1.0, 1), 1.0, 0.0, 1.5)
+    for i in (3, 7):
+        wl.scene.materials[i] = Material(3, (0.8, 0.8, 0.8, 1), 1.0, 0.05, 1.0)
+    wl.scene.materials[0] = Material(3, (0.6, 0.6, 0.6, 1), 1.0, 0.1, 1.0)  # mirror floor
+    wl.max_bounces = 8
+    return wl
+
+
+@pytest.fixture(scope="module")
+def small(gpu_lib, oracle_lib):
+    return Pair(scenes.small(0))
+
+
+@pytest.fixture(scope="module")
+def glass(gpu_lib, oracle_lib):
+    return Pair(glass_workload())
+
+
+def assert_bvh_equal(p: Pair):
+    assert p.gi["num_bvh8_nodes"] == p.oi["num_bvh8_nodes"] and p.gi["depth"] == p.oi["depth"]
+    g = p.ctx.download_bvh(p.gi["num_bvh8_nodes"])
+    o = p.orc.download_bvh(p.oi["num_bvh8_nodes"])
+    for name, a, b in zip(["morton", "order", "bvh2", "bvh8", "tris"], g, o):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), name
+
+
+def test_bvh_bitexact_small(small):
+    assert_bvh_equal(small)
+    assert small.gi["scene_lo"] == small.oi["scene_lo"] and small.gi["scene_hi"] == small.oi["scene_hi"]
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 17, 33, 1000])
+def test_bvh_bitexact_tiny_and_degenerate(gpu_lib, oracle_lib, n):
+    """Few triangles, duplicated positions (equal Morton codes) and zero-area triangles."""
+    from vulkanhybridraytracer_gb300.hybrid import HybridContext
+    rng = np.random.default_rng(100 + n)
+    v = np.zeros((3 * n, 11), np.float32)
+    base = rng.uniform(-1, 1, (n, 3))
+    base[n // 2:] = base[0]
+    for t in range(n):
+        for k in range(3):
+            v[3 * t + k, 0:3] = base[t] + (rng.uniform(-0.5, 0.5, 3) if t % 5 else 0)  # every 5th is a point
+            v[3 * t + k, 4] = 1
+    idx = np.arange(3 * n, dtype=np.uint32)
+    prims = np.array([[0, 3 * n, 0, 0, 0, 0]], np.uint32)
+    xf = np.eye(4, dtype=np.float32).reshape(1, 16)
+    mats = Material().to_shader(0)[None]
+    lights = np.zeros((0, 12), np.float32)
+    ctx = HybridContext(0)
+    ctx.set_scene_arrays(v, idx, prims, xf, mats, lights)
+    orc = po.OracleScene()
+    orc.set_scene_arrays(v, idx, prims, xf, mats, lights)
+    p = Pair.__new__(Pair)
+    p.ctx, p.orc, p.gi, p.oi = ctx, orc, ctx.build_bvh(), orc.build_bvh()
+    assert_bvh_equal(p)
+    rays = _rays(rng, 3000, -2, 2)
+    torch = _torch()
+    for any_hit in (False, True):
+        hg, sg = ctx.trace(torch.from_numpy(rays).cuda(), any_hit, count=True)
+        ho, co = orc.trace(rays, any_hit)
+        assert np.array_equal(hg.cpu().numpy().view(np.uint32), ho.view(np.uint32))
+        assert sg["nodes_visited"] == co[:, 0].sum() and sg["tris_tested"] == co[:, 1].sum()
+    ctx.close()
+
+
+def _rays(rng, n, lo=-6, hi=6):
+    org = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    org[:, 1] = rng.uniform(0.1, 4, n)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = np.zeros((n, 8), np.float32)
+    r[:, 0:3], r[:, 3], r[:, 4:7], r[:, 7] = org, 0.001, d, 1000.0
+    return r
+
+
+@pytest.mark.parametrize("any_hit", [False, True])
+def test_trace_bitexact(small, any_hit):
+    torch = _torch()
+    rays = _rays(np.random.default_rng(7), 50000)
+    rays[::7, 4:7] = [0, -1, 0]   # axis-aligned directions (zero components)
+    rays[::11, 7] = 0.5           # short rays
+    hg, sg = small.ctx.trace(torch.from_numpy(rays).cuda(), any_hit, count=True)
+    ho, co = small.orc.trace(rays, any_hit)
+    assert np.array_equal(hg.cpu().numpy().view(np.uint32), ho.view(np.uint32))
+    assert sg["nodes_visited"] == int(co[:, 0].sum()) and sg["tris_tested"] == int(co[:, 1].sum())
+    assert sg["error_flags"] == 0
+    # against brute force (the reference's semantics without any BVH)
+    hb, _ = small.orc.trace(rays, any_hit, po.TRACE_BRUTE)
+    ig, ib = hg.cpu().numpy().view(np.uint32)[:, 1], hb.view(np.uint32)[:, 1]
+    assert np.mean((ig != 0xFFFFFFFF) == (ib != 0xFFFFFFFF)) >= 0.9999
+    if not any_hit:
+        assert np.mean(ig == ib) >= 0.9999
+
+
+def test_gbuffer_primary(small):
+    torch = _torch()
+    cam = small.wl.camera(0.0)
+    W, H = small.wl.width, small.wl.height
+    g = [p.cpu().numpy() for p in small.ctx.gbuffer(cam, W, H)]
+    o = small.orc.gbuffer(cam, W, H)
+    for i in (0, 2, 3, 4, 5):
+        assert np.array_equal(g[i], o[i]), f"plane {i}"
+    np.testing.assert_allclose(g[1], o[1], atol=2e-6)
+    torch.cuda.synchronize()
+
+
+def run_both(p: Pair, frame, spp, rng_mode, fmt, flags=0, max_bounces=None, hist0=None, planes=None,
+             formats=None):
+    from vulkanhybridraytracer_gb300.hybrid import GBUF_FP32_FORMATS, pass_config
+    torch = _torch()
+    wl = p.wl
+    W, H = wl.width, wl.height
+    mb = wl.max_bounces if max_bounces is None else max_bounces
+    cam = wl.camera(float(frame))
+    if planes is None:
+        planes = p.orc.gbuffer(cam, W, H)
+    formats = formats or GBUF_FP32_FORMATS
+    nl = len(wl.scene.lights)
+    dt = np.uint8 if fmt == L.HY_ACCUM_U8 else np.float32
+    if hist0 is None:
+        rng = np.random.default_rng(frame + 17)
+        hist0 = (rng.integers(0, 256, (nl, H, W)).astype(np.uint8) if fmt == L.HY_ACCUM_U8
+                 else rng.random((nl, H, W)).astype(np.float32))
+    hist_g = torch.from_numpy(hist0.copy()).cuda()
+    out_f = torch.zeros((H, W, 4), device="cuda")
+    out_8 = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
+    dplanes = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in planes]
+    st = p.ctx.forward(dplanes, cam, pass_config(spp, mb, rng_mode, frame, flags), hist_g, fmt, out_f=out_f,
+                       out_8=out_8, formats=formats)
+    hist_o = hist0.copy().astype(dt)
+    of, o8, osh, ost = p.orc.forward(planes, cam, po.cfg_dict(spp, mb, rng_mode, frame, flags), hist_o, fmt,
+                                     formats=formats)
+    return (out_f.cpu().numpy(), out_8.cpu().numpy(), hist_g.cpu().numpy(), st), (of, o8, hist_o, osh, ost)
+
+
+def check_parity(g, o, fmt):
+    out_f, out_8, hist_g, st = g
+    of, o8, hist_o, osh, ost = o
+    assert st["error_flags"] == 0
+    flips = np.mean(hist_g != hist_o)
+    assert flips <= FLIP_TOL, f"history differs on {flips:.2e} of texels"
+    agree = np.all(hist_g == hist_o, axis=0)
+    err = np.abs(out_f[..., :3].astype(np.float64) - of[..., :3])
+    rms = np.sqrt((err ** 2).sum() / max((of[..., :3].astype(np.float64) ** 2).sum(), 1e-30))
+    assert rms <= RMS_TOL, f"relative RMS {rms:.3e}"
+    assert err[agree].max(initial=0) <= MAX_TOL, f"max |err| {err[agree].max():.3e}"
+    assert np.all(out_f[..., 3] == 1)
+    bad8 = np.abs(out_8.astype(int) - o8.astype(int)) > 1
+    assert bad8[agree].mean() <= 1e-3
+    for k in ("shadow_rays", "reflection_rays"):
+        assert abs(st[k] - ost[k]) <= max(2, 1e-4 * ost[k]), (k, st[k], ost[k])
+
+
+@pytest.mark.parametrize("frame", [0, 1, 5])
+@pytest.mark.parametrize("rng_mode,spp", [(L.HY_RNG_REFERENCE, 1), (L.HY_RNG_REFERENCE, 8),
+                                          (L.HY_RNG_DECORRELATED, 4)])
+def test_forward_small(small, frame, rng_mode, spp):
+    g, o = run_both(small, frame, spp, rng_mode, L.HY_ACCUM_U8)
+    check_parity(g, o, L.HY_ACCUM_U8)
+
+
+@pytest.mark.parametrize("flags", [0, L.HY_FLAG_NO_ACCUM, L.HY_FLAG_FULL_BLUR_DISPATCH])
+@pytest.mark.parametrize("frame", [0, 3])
+def test_forward_f32_history_and_flags(small, flags, frame):
+    g, o = run_both(small, frame, 4, L.HY_RNG_DECORRELATED, L.HY_ACCUM_F32, flags)
+    check_parity(g, o, L.HY_ACCUM_F32)
+
+
+@pytest.mark.parametrize("frame", [0, 2])
+def test_forward_glass_mirror_bounces(glass, frame):
+    g, o = run_both(glass, frame, 2, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8)
+    assert g[3]["reflection_rays"] > g[3]["hit_shadow_rays"] > 0
+    check_parity(g, o, L.HY_ACCUM_U8)
+
+
+def test_packed_reference_formats(small):
+    """The reference's own attachment formats: RGBA16F, RGBA16F, RGBA8, RG16F, RGBA8, RGBA8."""
+    cam = small.wl.camera(2.0)
+    W, H = small.wl.width, small.wl.height
+    f = small.orc.gbuffer(cam, W, H)
+    p = [f[0].astype(np.float16), f[1].astype(np.float16),
+         np.round(np.clip(f[2], 0, 1) * 255).astype(np.uint8), f[3].astype(np.float16),
+         np.round(np.clip(f[4], 0, 1) * 255).astype(np.uint8), np.round(np.clip(f[5], 0, 1) * 255).astype(np.uint8)]
+    fmts = (L.HY_FMT_RGBA16F, L.HY_FMT_RGBA16F, L.HY_FMT_RGBA8, L.HY_FMT_RG16F, L.HY_FMT_RGBA8, L.HY_FMT_RGBA8)
+    g, o = run_both(small, 2, 1, L.HY_RNG_REFERENCE, L.HY_ACCUM_U8, planes=p, formats=fmts)
+    check_parity(g, o, L.HY_ACCUM_U8)
+
+
+def test_stagewise_matches_fused(small):
+    """shadow -> accumulate -> shade called one by one equals hy_hybrid_forward's fused kernel."""
+    from vulkanhybridraytracer_gb300.hybrid import pass_config
+    torch = _torch()
+    wl = small.wl
+    W, H, nl = wl.width, wl.height, len(wl.scene.lights)
+    cam = wl.camera(4.0)
+    planes = [torch.from_numpy(x).cuda() for x in small.orc.gbuffer(cam, W, H)]
+    h0 = torch.from_numpy(np.random.default_rng(1).integers(0, 256, (nl, H, W)).astype(np.uint8)).cuda()
+    cfg = pass_config(4, 1, L.HY_RNG_DECORRELATED, 4, 0)
+    ha, hb = h0.clone(), h0.clone()
+    fa, fb = torch.zeros((H, W, 4), device="cuda"), torch.zeros((H, W, 4), device="cuda")
+    small.ctx.forward(planes, cam, cfg, ha, L.HY_ACCUM_U8, out_f=fa)
+    shadow = torch.zeros((nl, H, W), dtype=torch.uint8, device="cuda")
+    small.ctx.shadow_pass(planes, cam, cfg, shadow, L.HY_ACCUM_U8)
+    small.ctx.accumulate_pass(planes, cfg, shadow, hb, L.HY_ACCUM_U8)
+    small.ctx.shade_pass(planes, cam, cfg, hb, L.HY_ACCUM_U8, out_f=fb)
+    assert torch.equal(ha, hb)
+    assert torch.equal(fa, fb)
+
+
+def test_accumulate_reprojection(small):
+    """blur.comp reset branch with non-zero motion: reads the pre-pass history at
+    (x + r.x W, y + r.x H), clamps to the 3x3 range, mixes 0.4; bit-exact."""
+    torch = _torch()
+    from vulkanhybridraytracer_gb300.hybrid import pass_config
+    W, H, nl = 72, 40, 2
+    rng = np.random.default_rng(3)
+    planes = [np.zeros((H, W, 4), np.float32) for _ in range(6)]
+    planes[3] = (0.5 + rng.integers(-3, 4, (H, W, 2)) / (2.0 * W)).astype(np.float32)
+    shadow = rng.integers(0, 256, (nl, H, W)).astype(np.uint8)
+    hist = rng.integers(0, 256, (nl, H, W)).astype(np.uint8)
+    for frame in (0, -1, 6):
+        hg = torch.from_numpy(hist.copy()).cuda()
+        small.ctx.accumulate_pass([torch.from_numpy(x).cuda() for x in planes], pass_config(accum_frame=frame),
+                                  torch.from_numpy(shadow).cuda(), hg, L.HY_ACCUM_U8)
+        ho = hist.copy()
+        small.orc.accumulate(planes, po.cfg_dict(accum_frame=frame), shadow, ho, 0)
+        assert np.array_equal(hg.cpu().numpy(), ho), frame
+
+
+def test_host_buffers_equal_device(small):
+    from vulkanhybridraytracer_gb300.hybrid import pass_config
+    torch = _torch()
+    wl = small.wl
+    W, H, nl = wl.width, wl.height, len(wl.scene.lights)
+    cam = wl.camera(3.0)
+    pn = small.orc.gbuffer(cam, W, H)
+    cfg = pass_config(2, 1, L.HY_RNG_DECORRELATED, 3, 0)
+    h1 = torch.zeros((nl, H, W), dtype=torch.uint8, device="cuda")
+    h2 = h1.clone()
+    o1 = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
+    small.ctx.forward([torch.from_numpy(x).cuda() for x in pn], cam, cfg, h1, L.HY_ACCUM_U8, out_8=o1)
+    o2 = np.zeros((H, W, 4), np.uint8)
+    st = small.ctx.forward_host(pn, cam, cfg, h2, L.HY_ACCUM_U8, out_8=o2)
+    assert np.array_equal(o1.cpu().numpy(), o2) and torch.equal(h1, h2)
+    assert st["shadow_rays"] > 0
+
+
+def test_deterministic(small):
+    a = run_both(small, 3, 4, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8)[0]
+    b = run_both(small, 3, 4, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8)[0]
+    for x, y in zip(a[:3], b[:3]):
+        assert np.array_equal(x, y)
+
+
+def test_counts_match_oracle_pass(small):
+    """With HY_FLAG_COUNT_TRAVERSAL the pass's node/triangle counts equal the
+    oracle's BVH8 traversal of the same frame (REFERENCE RNG, exact rays)."""
+    g, o = run_both(small, 1, 1, L.HY_RNG_REFERENCE, L.HY_ACCUM_U8, flags=L.HY_FLAG_COUNT_TRAVERSAL)
+    st, ost = g[3], o[4]
+    assert abs(st["nodes_visited"] - ost["nodes_visited"]) <= 1e-3 * ost["nodes_visited"]
+    assert abs(st["tris_tested"] - ost["tris_tested"]) <= 1e-3 * ost["tris_tested"]
+
+
+def test_error_paths(gpu_lib, oracle_lib):
+    from vulkanhybridraytracer_gb300.hybrid import HybridContext, pass_config
+    torch = _torch()
+    wl = scenes.small(0, 32, 32)
+    ctx = HybridContext(0)
+    planes = [torch.zeros((32, 32, 4 if i != 3 else 2), device="cuda") for i in range(6)]
+    hist = torch.zeros((2, 32, 32), dtype=torch.uint8, device="cuda")
+    cam = wl.camera(0.0)
+    with pytest.raises(L.HyError) as e:
+        ctx.forward(planes, cam, pass_config(1), hist)
+    assert e.value.code == L.HY_ERR_NOT_READY
+    ctx.set_scene(wl.scene)
+    with pytest.raises(L.HyError) as e:
+        ctx.forward(planes, cam, pass_config(1), hist)
+    assert e.value.code == L.HY_ERR_NOT_READY   # no BVH yet
+    ctx.build_bvh()
+    with pytest.raises(L.HyError) as e:
+        ctx.forward(planes, cam, pass_config(0), hist)
+    assert e.value.code == L.HY_ERR_INVALID_ARG  # spp 0
+    with pytest.raises(L.HyError) as e:
+        ctx.forward(planes, cam, pass_config(1), hist[:1])
+    assert e.value.code == L.HY_ERR_INVALID_ARG  # history for the wrong light count
+    # forced allocation failure surfaces as HY_ERR_OOM and leaves the context usable
+    assert ctx.lib.hy_debug_fail_alloc_after(ctx.h, 1) == 0
+    with pytest.raises(L.HyError) as e:
+        ctx.forward(planes, cam, pass_config(1, accum_frame=0), hist)   # reset frame allocates scratch
+    assert e.value.code == L.HY_ERR_OOM
+    ctx.forward(planes, cam, pass_config(1, accum_frame=0), hist)
+    # non-finite geometry is rejected at upload
+    verts, idx, prims, xf, mats, lights = wl.scene.pack()
+    bad = verts.copy()
+    bad[0, 0] = np.nan
+    with pytest.raises(L.HyError) as e:
+        ctx.set_scene_arrays(bad, idx, prims, xf, mats, lights)
+    assert e.value.code == L.HY_ERR_NAN_INPUT
+    badp = prims.copy()
+    badp[0, 3] = 99   # material id past the material table
+    ctx.set_scene_arrays(verts, idx, badp, xf, mats, lights)
+    ctx.build_bvh()
+    with pytest.raises(L.HyError) as e:
+        ctx.forward(planes, cam, pass_config(1), hist)
+    assert e.value.code == L.HY_ERR_INVALID_ARG
+    ctx.close()
+
+
+def test_device_memory_cap(gpu_lib):
+    from vulkanhybridraytracer_gb300.hybrid import HybridContext
+    wl = scenes.small(0, 32, 32)
+    ctx = HybridContext(0, max_device_bytes=1 << 16)
+    with pytest.raises(L.HyError) as e:
+        ctx.set_scene(wl.scene)
+        ctx.build_bvh()
+    assert e.value.code == L.HY_ERR_OOM
+    ctx.close()
+
+
+# ---- full size: the 1080p / 1.5M-triangle workload -------------------------------------------
+@pytest.fixture(scope="module")
+def hd(gpu_lib, oracle_lib):
+    return Pair(scenes.hd(1))
+
+
+def test_hd_bvh_bitexact(hd):
+    assert hd.gi["num_tris"] == 1505282
+    assert_bvh_equal(hd)
+
+
+def test_hd_forward_parity(hd):
+    """Whole 1920x1080 frame, 4 lights x 16 decorrelated samples, against the oracle."""
+    g, o = run_both(hd, 3, 16, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8)
+    check_parity(g, o, L.HY_ACCUM_U8)

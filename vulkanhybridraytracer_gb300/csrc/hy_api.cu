@@ -210,9 +210,9 @@ int check_scene_ready(HyCtx* c) {
     return HY_OK;
 }
 
-int grid_for(HyCtx* c, int mode, bool count, int block) {
+int grid_for(HyCtx* c, int mode, bool count, int minb, int block) {
     int per = 0;
-    if (pixel_occupancy(mode, count, block, &per) != cudaSuccess || per <= 0) per = 1;
+    if (pixel_occupancy(mode, count, minb, block, &per) != cudaSuccess || per <= 0) per = 1;
     return per * c->num_sms;
 }
 
@@ -260,9 +260,10 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
     if (block % 32 || block > 128) return HY_ERR_INVALID_ARG;  // kernels are built for <= 128 threads
     PassParams P = P0;
     P.queue = dev_queue(c, queue_slot);
-    int grid = grid_for(c, mode, count, block);
+    int minb = cfg->min_blocks ? (int)cfg->min_blocks : 5;
+    int grid = grid_for(c, mode, count, minb, block);
     grid = std::max(1, std::min<int>(grid, (int)((P.ntiles * 32ull + block - 1) / block)));
-    HY_CUDA_TRY(launch_pixels(mode, count, scene_dev(c), P, grid, block, c->stream));
+    HY_CUDA_TRY(launch_pixels(mode, count, minb, scene_dev(c), P, grid, block, c->stream));
     return HY_OK;
 }
 
@@ -566,16 +567,18 @@ int hy_shade_pass(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const HyPa
 static int forward_impl(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const HyPassConfig* cfg, HyAccum* acc,
                         float* out_f, uint8_t* out_8) {
     int rc;
-    const bool fused = (cfg->flags & HY_FLAG_NO_ACCUM) || cfg->accum_frame > 0;
-    if (fused) {
+    if (!(cfg->flags & HY_FLAG_NO_ACCUM) && cfg->accum_frame > 0) {
+        // steady state: the running mean is pointwise, so the shadow kernel folds
+        // each light's factor straight into the history (no raw images)
         PassParams P = make_params(c, gb, cam, cfg, acc->format, nullptr, acc->history, out_f, out_8);
-        return run_pixels(c, MODE_FUSED, P, cfg, WQ_FUSED);
+        if ((rc = run_pixels(c, MODE_SHADOW_ACCUM, P, cfg, WQ_SHADOW))) return rc;
+        return run_pixels(c, MODE_SHADE, P, cfg, WQ_SHADE);
     }
     size_t bytes = (size_t)gb->width * gb->height * c->nlights * (acc->format == HY_ACCUM_U8 ? 1 : 4);
     if ((rc = ensure_size(c, c->raw_shadow, bytes))) return rc;
     PassParams P = make_params(c, gb, cam, cfg, acc->format, c->raw_shadow.p, acc->history, out_f, out_8);
     if ((rc = run_pixels(c, MODE_SHADOW, P, cfg, WQ_SHADOW))) return rc;
-    if ((rc = accumulate_impl(c, gb, cfg, c->raw_shadow.p, acc))) return rc;
+    if (!(cfg->flags & HY_FLAG_NO_ACCUM) && (rc = accumulate_impl(c, gb, cfg, c->raw_shadow.p, acc))) return rc;
     return run_pixels(c, MODE_SHADE, P, cfg, WQ_SHADE);
 }
 

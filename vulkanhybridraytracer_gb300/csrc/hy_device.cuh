@@ -276,90 +276,120 @@ __device__ __forceinline__ uint32_t byte_at(uint32_t lo4, uint32_t hi4, int slot
 
 // Stack traversal of the 8-wide BVH.  ANY: TerminateOnFirstHit semantics.
 // COUNT: accumulate node visits / triangle tests.
+//
+// Traversal state of one ray.  A node group is (first child index, bits):
+// bits[31:24] hold the not-yet-visited hit children in traversal rank order
+// (rank = slot ^ near-octant), bits[7:0] the node's internal-child slot mask.
+struct Trav {
+    uint32_t g_base, g_bits;
+    int sp;
+    uint32_t iters;
+    float tmax;
+    Hit h;
+};
+
+__device__ __forceinline__ void trav_init(Trav& t, const RayPre& r, float tmax) {
+    t.g_base = 0;
+    t.g_bits = (1u << 24) | (1u << r.near);  // a virtual group holding the root
+    t.sp = 0;
+    t.iters = 0;
+    t.tmax = tmax;
+    t.h = Hit{tmax, HY_NO_HIT, 0.f, 0.f};
+}
+
+// One node visit (its box tests and the triangles of its leaf slots).
+// Returns true when the ray is finished: t.h holds the hit, or id HY_NO_HIT.
 template <bool ANY, bool COUNT>
-__device__ __forceinline__ Hit traverse(const SceneDev& S, const RayPre& r, float tmin, float tmax,
-                                        uint32_t* nodes_ctr, uint32_t* tris_ctr, uint32_t* status) {
-    Hit h{tmax, HY_NO_HIT, 0.f, 0.f};
-    uint2 stk[kStackMax];
-    int sp = 0;
-    uint32_t g_base = 0, g_bits = (1u << 24) | (1u << r.near);
-    float cur_tmax = tmax;
-    for (uint32_t iter = 0;; iter++) {
-        if (iter >= kMaxIters) { atomicOr(status, HY_STATUS_TIMEOUT); break; }
-        if ((g_bits & 0xff000000u) == 0) {
-            if (sp == 0) break;
-            --sp;
-            g_base = stk[sp].x;
-            g_bits = stk[sp].y;
-        }
-        uint32_t rb = __ffs(g_bits >> 24) - 1;
-        g_bits &= ~(1u << (24 + rb));
-        uint32_t sl = rb ^ r.near;
-        uint32_t idx = g_base + __popc(g_bits & 0xffu & ((1u << sl) - 1u));
-        if (g_bits & 0xff000000u) {
-            if (sp >= kStackMax) { atomicOr(status, HY_STATUS_STACK_OVERFLOW); break; }
-            stk[sp] = make_uint2(g_base, g_bits);
-            sp++;
-        }
-        if (idx >= S.num_nodes) { atomicOr(status, HY_STATUS_BAD_INDEX); break; }
-        const uint4* np = S.nodes[idx].q;
-        uint4 q0 = __ldg(np + 0), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3), q4 = __ldg(np + 4);
-        if (COUNT) (*nodes_ctr)++;
-        float adj[3], org[3];
-        float p[3] = {__uint_as_float(q0.x), __uint_as_float(q0.y), __uint_as_float(q0.z)};
-        float oo[3] = {r.o.x, r.o.y, r.o.z};
+__device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& r, float tmin, Trav& t, uint2* stk,
+                                          uint32_t& nodes_ctr, uint32_t& tris_ctr, uint32_t* status) {
+    if (++t.iters > kMaxIters) { atomicOr(status, HY_STATUS_TIMEOUT); return true; }
+    if ((t.g_bits & 0xff000000u) == 0) {
+        if (t.sp == 0) return true;
+        --t.sp;
+        t.g_base = stk[t.sp].x;
+        t.g_bits = stk[t.sp].y;
+    }
+    const uint32_t rb = __ffs(t.g_bits >> 24) - 1;
+    t.g_bits &= ~(1u << (24 + rb));
+    const uint32_t sl = rb ^ r.near;
+    const uint32_t idx = t.g_base + __popc(t.g_bits & 0xffu & ((1u << sl) - 1u));
+    if (t.g_bits & 0xff000000u) {
+        if (t.sp >= kStackMax) { atomicOr(status, HY_STATUS_STACK_OVERFLOW); return true; }
+        stk[t.sp] = make_uint2(t.g_base, t.g_bits);
+        t.sp++;
+    }
+    if (idx >= S.num_nodes) { atomicOr(status, HY_STATUS_BAD_INDEX); return true; }
+    const uint4* np = S.nodes[idx].q;
+    const uint4 q0 = __ldg(np + 0), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3), q4 = __ldg(np + 4);
+    if (COUNT) nodes_ctr++;
+    float adj[3], org[3];
+    const float p[3] = {__uint_as_float(q0.x), __uint_as_float(q0.y), __uint_as_float(q0.z)};
+    const float oo[3] = {r.o.x, r.o.y, r.o.z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const uint32_t ea = (q0.w >> (8 * a)) & 0xffu;
+        adj[a] = __fmul_rn(__uint_as_float(ea << 23), r.invd[a]);
+        org[a] = __fmul_rn(__fsub_rn(p[a], oo[a]), r.invd[a]);
+    }
+    const uint32_t imask = q0.w >> 24;
+    const uint32_t qlo[3][2] = {{q2.x, q2.y}, {q2.z, q2.w}, {q3.x, q3.y}};
+    const uint32_t qhi[3][2] = {{q3.z, q3.w}, {q4.x, q4.y}, {q4.z, q4.w}};
+    uint32_t hit_int = 0, hit_tri = 0;
+#pragma unroll
+    for (int slot = 0; slot < 8; slot++) {
+        const uint32_t m = byte_at(q1.z, q1.w, slot);
+        float tn[3], tf[3];
 #pragma unroll
         for (int a = 0; a < 3; a++) {
-            uint32_t ea = (q0.w >> (8 * a)) & 0xffu;
-            adj[a] = __fmul_rn(__uint_as_float(ea << 23), r.invd[a]);
-            org[a] = __fmul_rn(__fsub_rn(p[a], oo[a]), r.invd[a]);
+            const float ql = (float)byte_at(qlo[a][0], qlo[a][1], slot);
+            const float qh = (float)byte_at(qhi[a][0], qhi[a][1], slot);
+            const float lo = r.invd[a] < 0.f ? qh : ql;
+            const float hi = r.invd[a] < 0.f ? ql : qh;
+            tn[a] = __fmaf_rn(lo, adj[a], org[a]);
+            tf[a] = __fmaf_rn(hi, adj[a], org[a]);
         }
-        uint32_t imask = q0.w >> 24;
-        uint32_t qlo[3][2] = {{q2.x, q2.y}, {q2.z, q2.w}, {q3.x, q3.y}};
-        uint32_t qhi[3][2] = {{q3.z, q3.w}, {q4.x, q4.y}, {q4.z, q4.w}};
-        uint32_t hit_int = 0, hit_tri = 0;
-#pragma unroll
-        for (int slot = 0; slot < 8; slot++) {
-            uint32_t m = byte_at(q1.z, q1.w, slot);
-            if (m == 0) continue;
-            float tn[3], tf[3];
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                float ql = (float)byte_at(qlo[a][0], qlo[a][1], slot);
-                float qh = (float)byte_at(qhi[a][0], qhi[a][1], slot);
-                float lo = r.invd[a] < 0.f ? qh : ql;
-                float hi = r.invd[a] < 0.f ? ql : qh;
-                tn[a] = __fmaf_rn(lo, adj[a], org[a]);
-                tf[a] = __fmaf_rn(hi, adj[a], org[a]);
-            }
-            float tnear = fmaxf(fmaxf(tn[0], tn[1]), fmaxf(tn[2], tmin));
-            float tfar = fminf(fminf(tf[0], tf[1]), fminf(tf[2], cur_tmax));
-            if (!(tnear <= __fmul_rn(tfar, 1.0000003f))) continue;
+        const float tnear = fmaxf(fmaxf(tn[0], tn[1]), fmaxf(tn[2], tmin));
+        const float tfar = fminf(fminf(tf[0], tf[1]), fminf(tf[2], t.tmax));
+        const bool hit = m != 0 && tnear <= __fmul_rn(tfar, 1.0000003f);
+        if (hit) {
             if (imask & (1u << slot)) hit_int |= 1u << (slot ^ r.near);
             else hit_tri |= ((1u << (m >> 5)) - 1u) << (m & 31u);
         }
-        uint32_t tri_base = q1.y;
-        while (hit_tri) {
-            uint32_t b = __ffs(hit_tri) - 1;
-            hit_tri &= hit_tri - 1u;
-            if (tri_base + b >= S.num_tris) { atomicOr(status, HY_STATUS_BAD_INDEX); break; }
-            const float4* tp = S.tris + (size_t)(tri_base + b) * 3;
-            float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
-            uint32_t id = __float_as_uint(v0.w);
-            if (COUNT) (*tris_ctr)++;
-            float tt, b1, b2;
-            if (tri_test(r, v0, v1, v2, tmin, cur_tmax, tt, b1, b2)) {
-                if (h.id == HY_NO_HIT || tt < h.t || (tt == h.t && id < h.id)) {
-                    h = Hit{tt, id, b1, b2};
-                    cur_tmax = tt;
-                }
-                if (ANY) return h;
-            }
-        }
-        g_base = q1.x;
-        g_bits = (hit_int << 24) | imask;
     }
-    return h;
+    const uint32_t tri_base = q1.y;
+    while (hit_tri) {
+        const uint32_t b = __ffs(hit_tri) - 1;
+        hit_tri &= hit_tri - 1u;
+        if (tri_base + b >= S.num_tris) { atomicOr(status, HY_STATUS_BAD_INDEX); return true; }
+        const float4* tp = S.tris + (size_t)(tri_base + b) * 3;
+        const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+        const uint32_t id = __float_as_uint(v0.w);
+        if (COUNT) tris_ctr++;
+        float tt, b1, b2;
+        if (tri_test(r, v0, v1, v2, tmin, t.tmax, tt, b1, b2)) {
+            if (t.h.id == HY_NO_HIT || tt < t.h.t || (tt == t.h.t && id < t.h.id)) {
+                t.h = Hit{tt, id, b1, b2};
+                t.tmax = tt;
+            }
+            if (ANY) return true;
+        }
+    }
+    t.g_base = q1.x;
+    t.g_bits = (hit_int << 24) | imask;
+    return false;
+}
+
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ Hit traverse(const SceneDev& S, const RayPre& r, float tmin, float tmax,
+                                        uint32_t* nodes_ctr, uint32_t* tris_ctr, uint32_t* status) {
+    uint2 stk[kStackMax];
+    Trav t;
+    trav_init(t, r, tmax);
+    uint32_t nn = 0, nt = 0;
+    while (!trav_step<ANY, COUNT>(S, r, tmin, t, stk, nn, nt, status)) {
+    }
+    if (COUNT) { *nodes_ctr += nn; *tris_ctr += nt; }
+    return t.h;
 }
 
 }  // namespace hy

@@ -24,7 +24,7 @@ void ctx_free(HyCtx* c, DevBuf& b);
 // Accumulated per-pass device counters (u64 each)
 enum { ST_SHADOW = 0, ST_REFL, ST_HITSHADOW, ST_NODES, ST_TRIS, ST_COUNT };
 // work-queue counters (u32 each)
-enum { WQ_SHADOW = 0, WQ_SHADE, WQ_FUSED, WQ_MISC, WQ_COUNT };
+enum { WQ_SHADOW = 0, WQ_SHADE, WQ_MISC, WQ_COUNT };
 
 }  // namespace hy
 

@@ -1,18 +1,18 @@
 // The hybrid pass on sm_103a.
 //
-// One persistent kernel template covers the three reference programs:
-//   MODE_SHADOW  shadowRaygen.rgen:28-93   -> raw per-light shadow images
-//   MODE_SHADE   hybridRaygen.rgen:27-186 (+ hybridHit.rchit, miss.rmiss)
-//                reading the accumulated shadow images
-//   MODE_FUSED   both per light in one pass: shadow rays -> running-mean
-//                accumulation (blur.comp:41-48, frame > 0) -> shading, so
-//                the raw images never touch memory
-// and k_accumulate is blur.comp:35-81 for the reset frame (frame <= 0),
-// whose 3x3 neighbourhood clamp needs the whole raw image first.
+// Kernels of the three reference programs:
+//   k_shadow<ACCUM=false>  shadowRaygen.rgen:28-93 -> raw per-light shadow images
+//   k_shadow<ACCUM=true>   the same rays folded straight into the history with
+//                          blur.comp's running mean (frame > 0), so the raw
+//                          images never touch memory in the steady state
+//   k_accumulate           blur.comp:35-81 for the reset frame (frame <= 0),
+//                          whose 3x3 clamp needs the whole raw image first
+//   k_pixels<MODE_SHADE>   hybridRaygen.rgen:27-186 + hybridHit.rchit +
+//                          miss.rmiss, reading the accumulated images
 //
-// Work distribution: warps pull 8x4 pixel tiles from a global queue
-// (warp-aggregated atomicAdd, `chunk` tiles per pull) until it is drained;
-// the grid is sized to the resident-block capacity of the GPU.
+// Work distribution: persistent warps pull 8x4 pixel tiles from a global
+// queue (one atomicAdd per `chunk` tiles) until it is drained; grids are
+// sized to the resident-block capacity of the GPU.
 #include <cuda_runtime.h>
 
 #include "hy_device.cuh"
@@ -227,88 +227,38 @@ __device__ __forceinline__ void do_pixel(const SceneDev& S, const PassParams& P,
     const int smode = mi >= 0 ? (int)S.mats[mi].smr[0] : 0;
     const float ior = mi >= 0 ? S.mats[mi].diffuse[3] : 1.f;
     const f3 N = normalize_rn(normal);
-    uint32_t seed_s = tea(y * P.W + x, P.frame_u);
-    uint32_t seed_h = seed_s;
+    uint32_t seed_h = tea(y * P.W + x, P.frame_u);
     const bool background = g0.w == 0.f && g1.w == 0.f;
-    const bool shading = MODE != MODE_SHADOW && !background;
-    const bool in_blur = x < P.blur_w && y < P.blur_h;
+    const float4 g2 = fetch_texel(P.plane[2], P.fmt[2], pix);
+    const f3 albedo = pow3(mk(g2.x, g2.y, g2.z), 2.2f);
+    if (background) {
+        // hybridRaygen.rgen:182-183 overwrites everything computed before with albedo
+        if (P.out_f) reinterpret_cast<float4*>(P.out_f)[pix] = make_float4(albedo.x, albedo.y, albedo.z, 1.f);
+        if (P.out_8)
+            reinterpret_cast<uchar4*>(P.out_8)[pix] =
+                make_uchar4(quant8(albedo.z), quant8(albedo.y), quant8(albedo.x), 255);
+        return;
+    }
 
     // shading state (hybridRaygen.rgen:35-72)
-    f3 albedo = mk(0.f, 0.f, 0.f), emissive = mk(0.f, 0.f, 0.f), V = mk(0.f, 0.f, 1.f), F0 = splat(0.04f);
-    f3 irradiance = mk(0.f, 0.f, 0.f), origin = mk(0.f, 0.f, 0.f), direction = mk(0.f, 0.f, 0.f);
+    const float4 g4 = fetch_texel(P.plane[4], P.fmt[4], pix);
+    const float4 g5 = fetch_texel(P.plane[5], P.fmt[5], pix);
+    const f3 emissive = mk(g5.x, g5.y, g5.z);
+    const float roughness = g4.y, metallic = g4.z;
+    const f3 F0 = mix3(splat(0.04f), albedo, metallic);
+    const f3 V = normalize(P.cam_pos - position);
+    const float NdotV = clampf(dot(N, V), 0.f, 1.f);
+    const f3 irradiance = irradiance_at(S, N);
+    f3 origin = mk(0.f, 0.f, 0.f), direction = mk(0.f, 0.f, 0.f);
     f3 rayColor = mk(0.f, 0.f, 0.f);
-    float roughness = 0.f, metallic = 0.f, NdotV = 0.f, attenuation = 1.0f;
-    if (MODE != MODE_SHADOW) {
-        const float4 g2 = fetch_texel(P.plane[2], P.fmt[2], pix);
-        albedo = pow3(mk(g2.x, g2.y, g2.z), 2.2f);
-        if (shading) {
-            const float4 g4 = fetch_texel(P.plane[4], P.fmt[4], pix);
-            const float4 g5 = fetch_texel(P.plane[5], P.fmt[5], pix);
-            emissive = mk(g5.x, g5.y, g5.z);
-            roughness = g4.y;
-            metallic = g4.z;
-            F0 = mix3(splat(0.04f), albedo, metallic);
-            V = normalize(P.cam_pos - position);
-            NdotV = clampf(dot(N, V), 0.f, 1.f);
-            irradiance = irradiance_at(S, N);
-        }
-    }
+    float attenuation = 1.0f;
 
     for (uint32_t i = 0; i < S.num_lights; i++) {
         const HyLight lt = S.lights[i];
         const LightGeo lg = light_geo(lt, position, N);
         const size_t li = i * plane + pix;
-        float sfac = 0.f;
-        if (MODE != MODE_SHADE) {
-            // shadowRaygen.rgen:52-93
-            float sf = 0.f;
-            if (smode == 4) {
-                sf = 1.0f;
-            } else if (lg.NdotL > 0.f) {
-                const int spp = (int)P.spp;
-                if (lg.dist < lg.maxd && P.rng_mode == HY_RNG_REFERENCE) {
-                    uint32_t sd = seed_s;
-                    f3 dir = sampleDisk(lt.radius, position, lg.L, sd);
-                    Hit h = trace<true, COUNT>(S, add_rn(position, scale_rn(dir, 1e-1f)), dir, 0.001f,
-                                               __fadd_rn(lg.dist, 1.0f), ls, P.status);
-                    ls.shadow++;
-                    sf = h.id == HY_NO_HIT ? (float)spp : 0.f;
-                } else {
-                    for (int k = 0; k < spp; k++) {
-                        bool shadowed = false;
-                        if (lg.dist < lg.maxd) {
-                            f3 dir = sampleDisk(lt.radius, position, lg.L, seed_s);
-                            Hit h = trace<true, COUNT>(S, add_rn(position, scale_rn(dir, 1e-1f)), dir, 0.001f,
-                                                       __fadd_rn(lg.dist, 1.0f), ls, P.status);
-                            ls.shadow++;
-                            shadowed = h.id != HY_NO_HIT;
-                        }
-                        if (!shadowed) sf = __fadd_rn(sf, 1.0f);
-                    }
-                }
-                sf = __fdiv_rn(sf, (float)spp);
-            }
-            if (MODE == MODE_SHADOW) {
-                accum_store(P.accum_fmt, P.shadow, li, sf);
-                continue;
-            }
-            // MODE_FUSED: accumulation (blur.comp:41-48) of the stored value
-            const float center = roundtrip(P.accum_fmt, sf);
-            if (P.flags & HY_FLAG_NO_ACCUM) {
-                sfac = center;
-            } else if (in_blur) {
-                const float old = accum_load(P.accum_fmt, P.hist, li);
-                const float a = __fdiv_rn(1.0f, __fadd_rn((float)P.accum_frame, 1.0f));
-                const float out = __fadd_rn(__fmul_rn(old, __fsub_rn(1.0f, a)), __fmul_rn(center, a));
-                accum_store(P.accum_fmt, P.hist, li, out);
-                sfac = roundtrip(P.accum_fmt, out);
-            } else {
-                sfac = accum_load(P.accum_fmt, P.hist, li);
-            }
-        } else {
-            sfac = accum_load(P.accum_fmt, (P.flags & HY_FLAG_NO_ACCUM) ? P.shadow : P.hist, li);
-        }
-        if (!shading) continue;
+        // the accumulated shadow image (or the raw one without the denoise pass)
+        const float sfac = accum_load(P.accum_fmt, (P.flags & HY_FLAG_NO_ACCUM) ? P.shadow : P.hist, li);
         // hybridRaygen.rgen:73-149
         const float I = lg.isDir ? 1.0f : (lt.color[3] / (lg.dist * lg.dist));
         const f3 L = lg.L;
@@ -353,38 +303,171 @@ __device__ __forceinline__ void do_pixel(const SceneDev& S, const PassParams& P,
             rayColor = rayColor + ((I > 0.f) ? I * lc * attenuation * albedo * metallic : irradiance * albedo * metallic);
         }
     }
-    if (MODE == MODE_SHADOW) return;
-
-    f3 fc;
-    if (!shading) {
-        fc = albedo;  // background: hybridRaygen.rgen:182-183
-    } else {
-        // hybridRaygen.rgen:151-170
-        for (uint32_t depth = 0; depth < P.max_bounces; depth++) {
-            if (smode == 0) break;
-            f3 ro = origin + direction * 1e-2f;
-            Hit h = trace<false, COUNT>(S, ro, direction, 0.001f, 1000.0f, ls, P.status);
-            ls.refl++;
-            f3 pc, pdir = direction, porg = origin;
-            float pt, pw = 0.f;
-            if (h.id == HY_NO_HIT) {
-                pc = miss_color(S, direction);
-                pt = -1.f;
-            } else {
-                Payload p = closest_hit<COUNT>(S, P, h, ro, direction, seed_h, ls);
-                pc = p.color; pt = p.t; pdir = p.dir; pw = p.scattered; porg = p.origin;
-            }
-            rayColor = rayColor * pc;
-            if (pt < 0.f || !(pw > 0.f)) break;
-            origin = porg;
-            direction = pdir;
+    // hybridRaygen.rgen:151-170
+    for (uint32_t depth = 0; depth < P.max_bounces; depth++) {
+        if (smode == 0) break;
+        f3 ro = origin + direction * 1e-2f;
+        Hit h = trace<false, COUNT>(S, ro, direction, 0.001f, 1000.0f, ls, P.status);
+        ls.refl++;
+        f3 pc, pdir = direction, porg = origin;
+        float pt, pw = 0.f;
+        if (h.id == HY_NO_HIT) {
+            pc = miss_color(S, direction);
+            pt = -1.f;
+        } else {
+            Payload p = closest_hit<COUNT>(S, P, h, ro, direction, seed_h, ls);
+            pc = p.color; pt = p.t; pdir = p.dir; pw = p.scattered; porg = p.origin;
         }
-        f3 F = FresnelSchlick(NdotV, F0);
-        f3 kD = (splat(1.0f) - F) * (1.0f - metallic);
-        fc = rayColor + kD * albedo * irradiance + emissive;
+        rayColor = rayColor * pc;
+        if (pt < 0.f || !(pw > 0.f)) break;
+        origin = porg;
+        direction = pdir;
     }
+    const f3 F = FresnelSchlick(NdotV, F0);
+    const f3 kD = (splat(1.0f) - F) * (1.0f - metallic);
+    const f3 fc = rayColor + kD * albedo * irradiance + emissive;
     if (P.out_f) reinterpret_cast<float4*>(P.out_f)[pix] = make_float4(fc.x, fc.y, fc.z, 1.f);
     if (P.out_8) reinterpret_cast<uchar4*>(P.out_8)[pix] = make_uchar4(quant8(fc.z), quant8(fc.y), quant8(fc.x), 255);
+}
+
+// ---------------------------------------------------------------------------------
+// shadowRaygen.rgen:28-93 as a persistent state machine.
+//
+// Each lane owns one pixel and walks its rays (lights in order, samples in
+// order, the RNG advancing exactly as the per-pixel loop would) one BVH node
+// per iteration; a lane whose ray ends starts the next one in the same
+// iteration, and a lane whose pixel is done takes the next pixel of the
+// warp's pool (8x4 tiles pulled from the global queue).  Warps therefore stay
+// converged on node visits instead of waiting for each ray's slowest lane.
+// ACCUM: fold each light's factor into the history with blur.comp's running
+// mean (frame > 0) instead of writing the raw image.
+// ---------------------------------------------------------------------------------
+struct ShadowLane {
+    f3 position, N, L;
+    float dist, radius;
+    uint32_t pix, seed, light, k, nrays;
+    float sf;
+    int smode;
+    bool in_blur, setup;
+};
+
+template <bool ACCUM>
+__device__ __forceinline__ void shadow_finalize(const PassParams& P, const ShadowLane& s, size_t plane, float v) {
+    const size_t li = (size_t)s.light * plane + s.pix;
+    if (!ACCUM) {
+        accum_store(P.accum_fmt, P.shadow, li, v);
+    } else if (s.in_blur) {
+        const float center = roundtrip(P.accum_fmt, v);
+        const float old = accum_load(P.accum_fmt, P.hist, li);
+        const float a = __fdiv_rn(1.0f, __fadd_rn((float)P.accum_frame, 1.0f));
+        accum_store(P.accum_fmt, P.hist, li, __fadd_rn(__fmul_rn(old, __fsub_rn(1.0f, a)), __fmul_rn(center, a)));
+    }
+}
+
+template <bool COUNT, bool ACCUM, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_shadow(const SceneDev S, const PassParams P) {
+    LaneStats ls;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    const size_t plane = (size_t)P.W * P.H;
+    const bool reference = P.rng_mode == HY_RNG_REFERENCE;
+    uint2 stk[kStackMax];
+    ShadowLane s;
+    Trav t;
+    RayPre r;
+    bool has_px = false, live = false, queue_empty = false;
+    uint32_t pool_cur = 0, pool_end = 0;
+    uint32_t nn = 0, nt = 0;
+    for (;;) {
+        // ---- give idle lanes a pixel from the warp's pool ----
+        uint32_t need = __ballot_sync(0xffffffffu, !has_px);
+        while (need && !queue_empty) {
+            if (pool_cur == pool_end) {
+                uint32_t t0 = 0;
+                if (lane == 0) t0 = atomicAdd(P.queue, P.chunk);
+                t0 = __shfl_sync(0xffffffffu, t0, 0);
+                if (t0 >= P.ntiles) { queue_empty = true; break; }
+                pool_cur = t0 * 32;
+                pool_end = min(t0 + P.chunk, P.ntiles) * 32;
+            }
+            const uint32_t take = min((uint32_t)__popc(need), pool_end - pool_cur);
+            const uint32_t rank = __popc(need & lt_mask);
+            if (!has_px && rank < take) {
+                const uint32_t slot = pool_cur + rank, tile = slot >> 5, l = slot & 31;
+                const uint32_t x = (tile % P.tiles_x) * 8 + (l & 7), y = (tile / P.tiles_x) * 4 + (l >> 3);
+                if (x < P.W && y < P.H) {
+                    has_px = true;
+                    s.pix = y * P.W + x;
+                    const float4 g0 = fetch_texel(P.plane[0], P.fmt[0], s.pix);
+                    const float4 g1 = fetch_texel(P.plane[1], P.fmt[1], s.pix);
+                    s.position = mk(g0.x, g0.y, g0.z);
+                    s.N = normalize_rn(mk(__fsub_rn(__fmul_rn(g1.x, 2.0f), 1.0f), __fsub_rn(__fmul_rn(g1.y, 2.0f), 1.0f),
+                                          __fsub_rn(__fmul_rn(g1.z, 2.0f), 1.0f)));
+                    const int mi = mat_index(g0.w, S.num_mats);
+                    s.smode = mi >= 0 ? (int)S.mats[mi].smr[0] : 0;
+                    s.seed = tea(s.pix, P.frame_u);
+                    s.light = 0;
+                    s.setup = true;
+                    s.in_blur = x < P.blur_w && y < P.blur_h;
+                }
+            }
+            pool_cur += take;
+            need = __ballot_sync(0xffffffffu, !has_px);
+        }
+        if (queue_empty && __ballot_sync(0xffffffffu, has_px) == 0) break;
+
+        // ---- a lane without a ray starts its pixel's next one ----
+        if (has_px && !live) {
+            for (;;) {
+                if (s.setup) {
+                    if (s.light >= S.num_lights) { has_px = false; break; }
+                    const HyLight lt = S.lights[s.light];
+                    const LightGeo lg = light_geo(lt, s.position, s.N);
+                    s.L = lg.L;
+                    s.dist = lg.dist;
+                    s.radius = lt.radius;
+                    s.k = 0;
+                    s.sf = 0.f;
+                    float v = -1.f;
+                    if (s.smode == 4) v = 1.0f;                       // glass: fully lit, no rays
+                    else if (!(lg.NdotL > 0.f)) v = 0.0f;             // facing away
+                    else if (!(lg.dist < lg.maxd)) v = 1.0f;          // out of range / directional: all lit
+                    if (v >= 0.f) {
+                        shadow_finalize<ACCUM>(P, s, plane, v);
+                        s.light++;
+                        continue;
+                    }
+                    s.nrays = reference ? 1u : P.spp;
+                    s.setup = false;
+                }
+                if (s.k < s.nrays) {
+                    uint32_t sd = s.seed;
+                    const f3 dir = reference ? sampleDisk(s.radius, s.position, s.L, sd)
+                                             : sampleDisk(s.radius, s.position, s.L, s.seed);
+                    r = ray_pre(add_rn(s.position, scale_rn(dir, 1e-1f)), dir);
+                    trav_init(t, r, __fadd_rn(s.dist, 1.0f));
+                    s.k++;
+                    live = true;
+                    ls.shadow++;
+                    break;
+                }
+                // every sample of this light is in: REFERENCE traced the one shared ray
+                shadow_finalize<ACCUM>(P, s, plane, reference ? s.sf : __fdiv_rn(s.sf, (float)P.spp));
+                s.light++;
+                s.setup = true;
+            }
+        }
+
+        // ---- one node visit ----
+        if (live) {
+            if (trav_step<true, COUNT>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
+                live = false;
+                if (t.h.id == HY_NO_HIT) s.sf = __fadd_rn(s.sf, 1.0f);
+            }
+        }
+    }
+    if (COUNT) { ls.nodes += nn; ls.tris += nt; }
+    flush_stats(ls, P.stats);
 }
 
 template <int MODE, bool COUNT>
@@ -525,25 +608,34 @@ __global__ void __launch_bounds__(128) k_gbuffer(const SceneDev S, const GbufPar
 // ---------------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------------
-template <int MODE>
-static void* pixel_kernel(bool count) {
-    return count ? (void*)k_pixels<MODE, true> : (void*)k_pixels<MODE, false>;
+template <bool ACCUM, int MINB>
+static void* shadow_kernel(bool count) {
+    return count ? (void*)k_shadow<true, ACCUM, MINB> : (void*)k_shadow<false, ACCUM, MINB>;
+}
+template <bool ACCUM>
+static void* shadow_kernel(bool count, int minb) {
+    switch (minb) {
+        case 4: return shadow_kernel<ACCUM, 4>(count);
+        case 6: return shadow_kernel<ACCUM, 6>(count);
+        case 8: return shadow_kernel<ACCUM, 8>(count);
+        default: return shadow_kernel<ACCUM, 5>(count);
+    }
+}
+// minb: resident blocks per SM the shadow kernel is compiled for (register cap)
+static void* pixel_kernel(int mode, bool count, int minb) {
+    if (mode == MODE_SHADOW) return shadow_kernel<false>(count, minb);
+    if (mode == MODE_SHADOW_ACCUM) return shadow_kernel<true>(count, minb);
+    return count ? (void*)k_pixels<MODE_SHADE, true> : (void*)k_pixels<MODE_SHADE, false>;
 }
 
-cudaError_t launch_pixels(int mode, bool count, const SceneDev& S, const PassParams& P, int grid, int block,
+cudaError_t launch_pixels(int mode, bool count, int minb, const SceneDev& S, const PassParams& P, int grid, int block,
                           cudaStream_t s) {
-    void* fn = mode == MODE_SHADOW ? pixel_kernel<MODE_SHADOW>(count)
-             : mode == MODE_SHADE  ? pixel_kernel<MODE_SHADE>(count)
-                                   : pixel_kernel<MODE_FUSED>(count);
     void* args[] = {(void*)&S, (void*)&P};
-    return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, s);
+    return cudaLaunchKernel(pixel_kernel(mode, count, minb), dim3(grid), dim3(block), args, 0, s);
 }
 
-cudaError_t pixel_occupancy(int mode, bool count, int block, int* blocks_per_sm) {
-    void* fn = mode == MODE_SHADOW ? pixel_kernel<MODE_SHADOW>(count)
-             : mode == MODE_SHADE  ? pixel_kernel<MODE_SHADE>(count)
-                                   : pixel_kernel<MODE_FUSED>(count);
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, 0);
+cudaError_t pixel_occupancy(int mode, bool count, int minb, int block, int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pixel_kernel(mode, count, minb), block, 0);
 }
 
 cudaError_t launch_accumulate(const AccumParams& A, cudaStream_t s) {

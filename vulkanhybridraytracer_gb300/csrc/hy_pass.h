@@ -7,7 +7,7 @@
 
 namespace hy {
 
-enum { MODE_SHADOW = 0, MODE_SHADE = 1, MODE_FUSED = 2 };
+enum { MODE_SHADOW = 0, MODE_SHADE = 1, MODE_SHADOW_ACCUM = 2 };
 
 struct PassParams {
     uint32_t W, H;
@@ -47,9 +47,9 @@ struct GbufParams {
     uint32_t* status;
 };
 
-cudaError_t launch_pixels(int mode, bool count, const SceneDev& S, const PassParams& P, int grid, int block,
+cudaError_t launch_pixels(int mode, bool count, int minb, const SceneDev& S, const PassParams& P, int grid, int block,
                           cudaStream_t s);
-cudaError_t pixel_occupancy(int mode, bool count, int block, int* blocks_per_sm);
+cudaError_t pixel_occupancy(int mode, bool count, int minb, int block, int* blocks_per_sm);
 cudaError_t launch_accumulate(const AccumParams& A, cudaStream_t s);
 cudaError_t launch_trace(const SceneDev& S, const HyRay* rays, uint32_t n, bool any, bool count, HyHit* hits,
                          unsigned long long* stats, uint32_t* status, int grid, cudaStream_t s);
