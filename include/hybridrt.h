@@ -158,6 +158,8 @@ enum { HY_RNG_REFERENCE = 0, HY_RNG_DECORRELATED = 1 };
 #define HY_FLAG_NO_ACCUM           0x2u /* shade from the raw shadow images, no denoise pass */
 #define HY_FLAG_COUNT_TRAVERSAL    0x4u /* count BVH nodes visited / triangles tested into HyStats */
 #define HY_FLAG_NO_STATUS_SYNC     0x8u /* do not read back the status word (no host sync) */
+#define HY_FLAG_PIXEL_PARALLEL     0x10u /* one lane per pixel for DECORRELATED shadow rays (default: one lane
+                                            group per pixel-light, the samples on adjacent lanes) */
 
 typedef struct HyPassConfig {
     uint32_t shadow_spp;    /* samplesBuffer.samples (1..64, src/renderer.cpp:656) */
@@ -168,7 +170,8 @@ typedef struct HyPassConfig {
     uint32_t block_size;    /* threads per block; 0 = default / autotuned */
     uint32_t queue_chunk;   /* work items fetched per warp from the ray queue; 0 = default */
     uint32_t stack_depth;   /* traversal stack entries; 0 = default (max 64) */
-    uint32_t min_blocks;    /* shadow-kernel variant compiled for 4/5/6/8 resident blocks per SM; 0 = 5 */
+    uint32_t min_blocks;    /* shadow-kernel variant: compiled for 5 (96 registers) or 8 (64 registers)
+                               resident blocks per SM; 0 = 8 */
 } HyPassConfig;
 
 typedef struct HyStats {

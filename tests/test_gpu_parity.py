@@ -378,3 +378,21 @@ def test_hd_forward_parity(hd):
     """Whole 1920x1080 frame, 4 lights x 16 decorrelated samples, against the oracle."""
     g, o = run_both(hd, 3, 16, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8)
     check_parity(g, o, L.HY_ACCUM_U8)
+
+
+@pytest.mark.parametrize("spp", [2, 3, 16, 40])
+def test_group_kernel_equals_pixel_kernel(small, spp):
+    """The sample-parallel shadow kernel (LCG jump-ahead per sample) writes the
+    same shadow images as the one-lane-per-pixel kernel, bit for bit."""
+    from vulkanhybridraytracer_gb300.hybrid import pass_config
+    torch = _torch()
+    wl = small.wl
+    W, H, nl = wl.width, wl.height, len(wl.scene.lights)
+    cam = wl.camera(5.0)
+    planes = [torch.from_numpy(x).cuda() for x in small.orc.gbuffer(cam, W, H)]
+    a = torch.zeros((nl, H, W), dtype=torch.uint8, device="cuda")
+    b = torch.zeros_like(a)
+    sa = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, 0), a)
+    sb = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, L.HY_FLAG_PIXEL_PARALLEL), b)
+    assert torch.equal(a, b)
+    assert sa["shadow_rays"] == sb["shadow_rays"] > 0

@@ -260,7 +260,16 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
     if (block % 32 || block > 128) return HY_ERR_INVALID_ARG;  // kernels are built for <= 128 threads
     PassParams P = P0;
     P.queue = dev_queue(c, queue_slot);
-    int minb = cfg->min_blocks ? (int)cfg->min_blocks : 5;
+    // DECORRELATED samples of one pixel-light go to one lane group
+    if ((mode == MODE_SHADOW || mode == MODE_SHADOW_ACCUM) && P.rng_mode == HY_RNG_DECORRELATED && P.spp >= 2 &&
+        !(cfg->flags & HY_FLAG_PIXEL_PARALLEL)) {
+        mode = mode == MODE_SHADOW ? MODE_SHADOW_G : MODE_SHADOW_ACCUM_G;
+        uint32_t G = 2;
+        while (G < P.spp && G < 32) G <<= 1;
+        P.group = G;
+    }
+    // 8 resident blocks (64 registers) measured fastest on the 1080p workload
+    int minb = cfg->min_blocks ? (int)cfg->min_blocks : 8;
     int grid = grid_for(c, mode, count, minb, block);
     grid = std::max(1, std::min<int>(grid, (int)((P.ntiles * 32ull + block - 1) / block)));
     HY_CUDA_TRY(launch_pixels(mode, count, minb, scene_dev(c), P, grid, block, c->stream));

@@ -332,19 +332,34 @@ __device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& r, fl
         org[a] = __fmul_rn(__fsub_rn(p[a], oo[a]), r.invd[a]);
     }
     const uint32_t imask = q0.w >> 24;
-    const uint32_t qlo[3][2] = {{q2.x, q2.y}, {q2.z, q2.w}, {q3.x, q3.y}};
-    const uint32_t qhi[3][2] = {{q3.z, q3.w}, {q4.x, q4.y}, {q4.z, q4.w}};
+    // near/far planes per axis: a ray going in -a enters through the max plane,
+    // so the quantised lo/hi byte planes swap once per node, not per child
+    uint32_t qn[3][2], qf[3][2];
+    {
+        const uint32_t qlo[3][2] = {{q2.x, q2.y}, {q2.z, q2.w}, {q3.x, q3.y}};
+        const uint32_t qhi[3][2] = {{q3.z, q3.w}, {q4.x, q4.y}, {q4.z, q4.w}};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const bool neg = r.invd[a] < 0.f;
+#pragma unroll
+            for (int w = 0; w < 2; w++) {
+                qn[a][w] = neg ? qhi[a][w] : qlo[a][w];
+                qf[a][w] = neg ? qlo[a][w] : qhi[a][w];
+            }
+        }
+    }
     uint32_t hit_int = 0, hit_tri = 0;
 #pragma unroll
     for (int slot = 0; slot < 8; slot++) {
         const uint32_t m = byte_at(q1.z, q1.w, slot);
         float tn[3], tf[3];
+        // byte -> float without I2F: PRMT builds 0x4B0000qq (= 2^23 + q), the
+        // FADD removes 2^23 exactly
+        const uint32_t kSel = 0x7540u | (uint32_t)(slot & 3);  // an immediate once the loop unrolls
 #pragma unroll
         for (int a = 0; a < 3; a++) {
-            const float ql = (float)byte_at(qlo[a][0], qlo[a][1], slot);
-            const float qh = (float)byte_at(qhi[a][0], qhi[a][1], slot);
-            const float lo = r.invd[a] < 0.f ? qh : ql;
-            const float hi = r.invd[a] < 0.f ? ql : qh;
+            const float lo = __fsub_rn(__uint_as_float(__byte_perm(qn[a][slot >> 2], 0x4B000000u, kSel)), 8388608.0f);
+            const float hi = __fsub_rn(__uint_as_float(__byte_perm(qf[a][slot >> 2], 0x4B000000u, kSel)), 8388608.0f);
             tn[a] = __fmaf_rn(lo, adj[a], org[a]);
             tf[a] = __fmaf_rn(hi, adj[a], org[a]);
         }

@@ -470,6 +470,140 @@ __global__ void __launch_bounds__(128, MINB) k_shadow(const SceneDev S, const Pa
     flush_stats(ls, P.stats);
 }
 
+// ---------------------------------------------------------------------------------
+// DECORRELATED shadow rays, sample-parallel: a group of G lanes (G = spp
+// rounded up to a power of two, at most 32) traces the samples of one
+// pixel-light together.  The samples share their origin and fall in the
+// light's small cone, so the group walks nearly the same nodes: its node
+// loads coalesce into one request and its lanes stay converged.  Sample n of
+// a pixel starts from the pixel's TEA seed advanced 2n LCG steps (LCG
+// jump-ahead), which is exactly the state the sequential per-pixel loop
+// reaches, so the rays equal those of k_shadow.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t lcg_jump(uint32_t s, uint32_t n) {
+    uint32_t A = 1664525u, C = 1013904223u;  // x -> A x + C, one step of random.glsl:21-27
+    while (n) {
+        if (n & 1u) s = A * s + C;
+        C = (A + 1u) * C;                    // the map composed with itself
+        A = A * A;
+        n >>= 1;
+    }
+    return s;
+}
+
+template <bool COUNT, bool ACCUM, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, const PassParams P) {
+    LaneStats ls;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t G = P.group;                  // power of two, 2..32
+    const uint32_t g = lane & (G - 1), base = lane & ~(G - 1);
+    const uint32_t gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << base;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    const size_t plane = (size_t)P.W * P.H;
+    const uint32_t spp = P.spp;
+    uint2 stk[kStackMax];
+    ShadowLane s;
+    Trav t;
+    RayPre r;
+    bool has_px = false, live = false, queue_empty = false;
+    uint32_t pool_cur = 0, pool_end = 0, rays_before = 0, seed0 = 0;
+    uint32_t nn = 0, nt = 0;
+    for (;;) {
+        // ---- idle groups take the next pixel of the warp's pool ----
+        uint32_t need = __ballot_sync(0xffffffffu, g == 0 && !has_px);
+        while (need && !queue_empty) {
+            if (pool_cur == pool_end) {
+                uint32_t t0 = 0;
+                if (lane == 0) t0 = atomicAdd(P.queue, P.chunk);
+                t0 = __shfl_sync(0xffffffffu, t0, 0);
+                if (t0 >= P.ntiles) { queue_empty = true; break; }
+                pool_cur = t0 * 32;
+                pool_end = min(t0 + P.chunk, P.ntiles) * 32;
+            }
+            const uint32_t take = min((uint32_t)__popc(need), pool_end - pool_cur);
+            const uint32_t rank = __popc(need & lt_mask);
+            const uint32_t my_slot = (g == 0 && !has_px && rank < take) ? pool_cur + rank : 0xffffffffu;
+            const uint32_t slot = __shfl_sync(0xffffffffu, my_slot, base);
+            if (slot != 0xffffffffu) {
+                const uint32_t tile = slot >> 5, l = slot & 31;
+                const uint32_t x = (tile % P.tiles_x) * 8 + (l & 7), y = (tile / P.tiles_x) * 4 + (l >> 3);
+                if (x < P.W && y < P.H) {
+                    has_px = true;
+                    s.pix = y * P.W + x;
+                    const float4 g0 = fetch_texel(P.plane[0], P.fmt[0], s.pix);
+                    const float4 g1 = fetch_texel(P.plane[1], P.fmt[1], s.pix);
+                    s.position = mk(g0.x, g0.y, g0.z);
+                    s.N = normalize_rn(mk(__fsub_rn(__fmul_rn(g1.x, 2.0f), 1.0f), __fsub_rn(__fmul_rn(g1.y, 2.0f), 1.0f),
+                                          __fsub_rn(__fmul_rn(g1.z, 2.0f), 1.0f)));
+                    const int mi = mat_index(g0.w, S.num_mats);
+                    s.smode = mi >= 0 ? (int)S.mats[mi].smr[0] : 0;
+                    seed0 = tea(s.pix, P.frame_u);
+                    rays_before = 0;
+                    s.light = 0;
+                    s.setup = true;
+                    s.in_blur = x < P.blur_w && y < P.blur_h;
+                }
+            }
+            pool_cur += take;
+            need = __ballot_sync(0xffffffffu, g == 0 && !has_px);
+        }
+        if (queue_empty && __ballot_sync(0xffffffffu, has_px) == 0) break;
+
+        // ---- light set-up (group-uniform) ----
+        if (has_px && s.setup) {
+            for (;;) {
+                if (s.light >= S.num_lights) { has_px = false; break; }
+                const HyLight lt = S.lights[s.light];
+                const LightGeo lg = light_geo(lt, s.position, s.N);
+                float v = -1.f;
+                if (s.smode == 4) v = 1.0f;
+                else if (!(lg.NdotL > 0.f)) v = 0.0f;
+                else if (!(lg.dist < lg.maxd)) v = 1.0f;
+                if (v >= 0.f) {
+                    if (g == 0) shadow_finalize<ACCUM>(P, s, plane, v);
+                    s.light++;
+                    continue;
+                }
+                s.L = lg.L;
+                s.dist = lg.dist;
+                s.radius = lt.radius;
+                s.k = g;
+                s.sf = 0.f;
+                s.setup = false;
+                break;
+            }
+        }
+        // ---- start this lane's next sample of the current light ----
+        if (has_px && !s.setup && !live && s.k < spp) {
+            uint32_t sd = lcg_jump(seed0, 2u * (rays_before + s.k));
+            const f3 dir = sampleDisk(s.radius, s.position, s.L, sd);
+            r = ray_pre(add_rn(s.position, scale_rn(dir, 1e-1f)), dir);
+            trav_init(t, r, __fadd_rn(s.dist, 1.0f));
+            s.k += G;
+            live = true;
+            ls.shadow++;
+        }
+        // ---- one node visit ----
+        if (live) {
+            if (trav_step<true, COUNT>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
+                live = false;
+                if (t.h.id == HY_NO_HIT) s.sf = __fadd_rn(s.sf, 1.0f);
+            }
+        }
+        // ---- a group whose samples are all in folds them into the light's factor ----
+        const uint32_t busy = __ballot_sync(0xffffffffu, has_px && !s.setup && (live || s.k < spp));
+        if (has_px && !s.setup && (busy & gmask) == 0) {
+            const uint32_t unocc = __reduce_add_sync(gmask, (uint32_t)s.sf);
+            if (g == 0) shadow_finalize<ACCUM>(P, s, plane, __fdiv_rn((float)unocc, (float)spp));
+            rays_before += spp;
+            s.light++;
+            s.setup = true;
+        }
+    }
+    if (COUNT) { ls.nodes += nn; ls.tris += nt; }
+    flush_stats(ls, P.stats);
+}
+
 template <int MODE, bool COUNT>
 __global__ void __launch_bounds__(128) k_pixels(const SceneDev S, const PassParams P) {
     LaneStats ls;
@@ -608,24 +742,24 @@ __global__ void __launch_bounds__(128) k_gbuffer(const SceneDev S, const GbufPar
 // ---------------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------------
-template <bool ACCUM, int MINB>
+template <bool GROUP, bool ACCUM, int MINB>
 static void* shadow_kernel(bool count) {
+    if (GROUP) return count ? (void*)k_shadow_group<true, ACCUM, MINB> : (void*)k_shadow_group<false, ACCUM, MINB>;
     return count ? (void*)k_shadow<true, ACCUM, MINB> : (void*)k_shadow<false, ACCUM, MINB>;
 }
-template <bool ACCUM>
+template <bool GROUP, bool ACCUM>
 static void* shadow_kernel(bool count, int minb) {
-    switch (minb) {
-        case 4: return shadow_kernel<ACCUM, 4>(count);
-        case 6: return shadow_kernel<ACCUM, 6>(count);
-        case 8: return shadow_kernel<ACCUM, 8>(count);
-        default: return shadow_kernel<ACCUM, 5>(count);
-    }
+    return minb >= 8 ? shadow_kernel<GROUP, ACCUM, 8>(count) : shadow_kernel<GROUP, ACCUM, 5>(count);
 }
 // minb: resident blocks per SM the shadow kernel is compiled for (register cap)
 static void* pixel_kernel(int mode, bool count, int minb) {
-    if (mode == MODE_SHADOW) return shadow_kernel<false>(count, minb);
-    if (mode == MODE_SHADOW_ACCUM) return shadow_kernel<true>(count, minb);
-    return count ? (void*)k_pixels<MODE_SHADE, true> : (void*)k_pixels<MODE_SHADE, false>;
+    switch (mode) {
+        case MODE_SHADOW: return shadow_kernel<false, false>(count, minb);
+        case MODE_SHADOW_ACCUM: return shadow_kernel<false, true>(count, minb);
+        case MODE_SHADOW_G: return shadow_kernel<true, false>(count, minb);
+        case MODE_SHADOW_ACCUM_G: return shadow_kernel<true, true>(count, minb);
+        default: return count ? (void*)k_pixels<MODE_SHADE, true> : (void*)k_pixels<MODE_SHADE, false>;
+    }
 }
 
 cudaError_t launch_pixels(int mode, bool count, int minb, const SceneDev& S, const PassParams& P, int grid, int block,

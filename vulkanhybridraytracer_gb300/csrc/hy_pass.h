@@ -7,7 +7,8 @@
 
 namespace hy {
 
-enum { MODE_SHADOW = 0, MODE_SHADE = 1, MODE_SHADOW_ACCUM = 2 };
+// *_G: the sample-parallel shadow kernel (DECORRELATED rays, spp >= 2)
+enum { MODE_SHADOW = 0, MODE_SHADE = 1, MODE_SHADOW_ACCUM = 2, MODE_SHADOW_G = 3, MODE_SHADOW_ACCUM_G = 4 };
 
 struct PassParams {
     uint32_t W, H;
@@ -24,6 +25,7 @@ struct PassParams {
     uint8_t* out_8;
     uint32_t tiles_x, ntiles, chunk;
     uint32_t blur_w, blur_h; // texels the blur dispatch covers
+    uint32_t group;          // lanes per pixel-light in the sample-parallel shadow kernel
     unsigned long long* stats;
     uint32_t* status;
     uint32_t* queue;
