@@ -49,7 +49,8 @@ enum {
     HY_ERR_QUEUE_OVERFLOW  = -6,
     HY_ERR_NAN_INPUT       = -7,
     HY_ERR_NOT_READY       = -8,  /* scene or BVH missing */
-    HY_ERR_UNSUPPORTED     = -9
+    HY_ERR_UNSUPPORTED     = -9,
+    HY_ERR_TOO_LARGE       = -10  /* input exceeds the fixed scratch of an allocation-free entry point */
 };
 
 /* device status-word bits (HyStats.error_flags) */
@@ -270,6 +271,31 @@ int hy_hybrid_forward(HyCtx* ctx, const HyGBuffer* gb, const HyCamera* cam,
 int hy_hybrid_forward_host(HyCtx* ctx, const HyGBuffer* h_gb, const HyCamera* cam,
                            const HyPassConfig* cfg, HyAccum* accum,
                            float* h_out_rgba32f, uint8_t* h_out_bgra8, HyStats* stats);
+
+/* ---- allocation-free accumulation (no counterpart in the reference) ----
+ *
+ * hy_accumulate_pass without a context and without any device allocation,
+ * for callers that may not allocate device memory themselves or have it
+ * allocated for them: an engine whose allocator owns and budgets every
+ * device allocation (as VMA does for VkPinut), or a frame loop that cannot
+ * afford the device-wide wait of cudaFree.  It computes exactly what
+ * hy_accumulate_pass computes, on the calling thread's current device and on
+ * `stream` (a cudaStream_t; NULL is the default stream), and returns without
+ * synchronising.
+ *
+ * The reset-frame branch (accum_frame <= 0) snapshots the history into a
+ * fixed scratch array of HY_NOALLOC_SCRATCH_BYTES that lives in the library
+ * and is held by every GPU that loads it until the process exits.  Calls
+ * whose history (width * height * num_lights * 1 or 4 bytes) exceeds it
+ * return HY_ERR_TOO_LARGE.  The first call on a device looks up the array's
+ * device address (once per device); make that first call before any stream
+ * capture.  All calls on a device share the one array, so calls whose work
+ * overlaps on the GPU (different streams, not ordered) race on it; order
+ * them on one stream.  The array keeps the last call's contents; nothing in
+ * it needs to start at zero. */
+#define HY_NOALLOC_SCRATCH_BYTES (16u << 20)
+int hy_accumulate_pass_noalloc(const HyGBuffer* gb, const HyPassConfig* cfg, const void* d_shadow,
+                               HyAccum* accum, void* stream);
 
 #ifdef __cplusplus
 }

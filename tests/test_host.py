@@ -37,7 +37,7 @@ def test_library_exports_every_header_symbol(lib):
 
 
 def test_error_strings(lib):
-    for code in range(0, -10, -1):
+    for code in range(0, -11, -1):
         s = lib.hy_error_string(code).decode()
         assert s and s != "unknown error"
 

@@ -22,6 +22,8 @@ HY_ERR_QUEUE_OVERFLOW = -6
 HY_ERR_NAN_INPUT = -7
 HY_ERR_NOT_READY = -8
 HY_ERR_UNSUPPORTED = -9
+HY_ERR_TOO_LARGE = -10
+HY_NOALLOC_SCRATCH_BYTES = 16 << 20
 
 HY_FMT_RGBA32F, HY_FMT_RG32F, HY_FMT_RGBA16F, HY_FMT_RG16F, HY_FMT_RGBA8 = range(5)
 HY_ACCUM_U8, HY_ACCUM_F32 = 0, 1
@@ -125,6 +127,7 @@ PROTOTYPES = {
                                 C.POINTER(HyAccum), P, P, C.POINTER(HyStats)]),
     "hy_hybrid_forward_host": (I32, [P, C.POINTER(HyGBuffer), C.POINTER(HyCamera), C.POINTER(HyPassConfig),
                                      C.POINTER(HyAccum), P, P, C.POINTER(HyStats)]),
+    "hy_accumulate_pass_noalloc": (I32, [C.POINTER(HyGBuffer), C.POINTER(HyPassConfig), P, C.POINTER(HyAccum), P]),
 }
 
 _lib = None

@@ -294,6 +294,7 @@ const char* hy_error_string(int code) {
         case HY_ERR_NAN_INPUT: return "non-finite input";
         case HY_ERR_NOT_READY: return "scene or acceleration structure not ready";
         case HY_ERR_UNSUPPORTED: return "unsupported";
+        case HY_ERR_TOO_LARGE: return "input exceeds the fixed scratch of the allocation-free entry point";
         default: return "unknown error";
     }
 }
