@@ -1,8 +1,9 @@
 // ORACLE — test infrastructure only.  CPU restatement of the reference's GLSL
 // math for the hybrid pass.  Nothing in the product links or calls this code;
 // tests, __graft_entry__.smoke() and bench.py's cpu_baseline leg use it as the
-// checker.  Parity of this file with the reference is pinned against the
-// reference's own random.glsl / helpers.glsl compiled as C++ (oracle/glsl_ref).
+// checker.  Pinned against the reference's own shader sources: oracle/glsl_ref
+// compiles them as C++ (from the reference checkout, into oracle/_ref) and
+// tests/golden holds their outputs; the oracle reproduces them bit for bit.
 #pragma once
 #include <cmath>
 #include <cstdint>

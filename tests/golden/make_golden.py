@@ -1,23 +1,38 @@
 """Generates the golden vectors in this directory.
 
-rng_kat.json — TEA seeds, LCG states and rnd() values of random.glsl:3-33,
-computed here by an independent pure-Python restatement (mod 2^32 integer
-arithmetic, exact float division by 2^24) and, when the reference's own
-random.glsl/helpers.glsl have been compiled as C++ into oracle/_ref
-(oracle/glsl_ref/Makefile, needs /root/reference), cross-checked against
-that build before anything is written.
+rng_kat.json      TEA seeds, LCG states and rnd() values of random.glsl:3-33,
+                  from an independent pure-Python restatement (mod 2^32
+                  integer arithmetic, exact float division by 2^24),
+                  cross-checked against the reference's own random.glsl.
+ref_kat.json      sampleDisk directions and GGX / Smith / Fresnel values
+                  computed by the reference's own helpers.glsl.
+ref_pass_small.npz
+                  the reference's own shadowRaygen.rgen, blur.comp and
+                  hybridRaygen.rgen + hybridHit.rchit + miss.rmiss +
+                  shadow.rmiss run on the 48x48 small_glass workload (glass,
+                  mirrors, 8 bounces), with its inputs (G-buffer, camera).
+
+"The reference's own" = the reference checkout's shader sources rewritten
+into C++ and compiled by oracle/glsl_ref (Makefile, translate.py,
+harness.cpp) into oracle/_ref/libglslref.so; that build needs the reference
+checkout, so this script runs where it exists.  The fixtures let every other
+machine check the oracle and the GPU path against the reference's output.
 
 Run:  python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
-import ctypes
 import json
+import sys
 from pathlib import Path
+
+import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 M32 = 0xFFFFFFFF
+for p in (ROOT, ROOT / "oracle", ROOT / "oracle" / "glsl_ref"):
+    sys.path.insert(0, str(p))
 
 
 def tea(v0: int, v1: int) -> int:
@@ -33,7 +48,7 @@ def lcg(state: int) -> int:
     return (1664525 * state + 1013904223) & M32
 
 
-def make():
+def rng_kat(ref=None):
     W = 1700  # the reference window width (src/vk_engine.cpp:27)
     kat = {"width": W, "frames": {}, "rnd": {}}
     for frame in (0, 1, 7, -1):
@@ -50,20 +65,85 @@ def make():
             states.append(st)
             vals.append((st & 0xFFFFFF) / float(1 << 24))
         kat["rnd"][str(s)] = {"states": states, "values": vals}
-    ref = ROOT / "oracle" / "_ref" / "libglslref.so"
-    if ref.exists():
-        lib = ctypes.CDLL(str(ref))
-        lib.ref_tea.restype = ctypes.c_uint32
-        lib.ref_tea.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+    if ref is not None:
         for frame, seeds in kat["frames"].items():
             for e in seeds:
-                got = lib.ref_tea((e["y"] * W + e["x"]) & M32, int(frame) & M32)
-                assert got == e["seed"], (frame, e, got)
+                assert ref.tea((e["y"] * W + e["x"]) & M32, int(frame) & M32) == e["seed"]
+        for s, d in kat["rnd"].items():
+            st, v = ref.rnd_seq(int(s), 8)
+            assert st.tolist() == d["states"] and np.array_equal(v, np.float32(d["values"]))
         kat["checked_against"] = "reference random.glsl compiled as C++ (oracle/_ref/libglslref.so)"
-    (HERE / "rng_kat.json").write_text(json.dumps(kat, indent=1) + "\n")
     return kat
 
 
+def ref_kat(ref):
+    rng = np.random.default_rng(20261203)
+    disk, brdf = [], []
+    for i in range(64):
+        pos = rng.normal(size=3).astype(np.float32)
+        L = rng.normal(size=3).astype(np.float32)
+        L /= np.linalg.norm(L)
+        if i == 0:
+            L = np.array([0, 1, 0], np.float32)  # the tangent special case
+        radius, seed = float(np.float32(rng.uniform(0.05, 1.0))), int(rng.integers(0, 2**32))
+        d = ref.sample_disk(radius, pos, L, seed)
+        disk.append({"radius": radius, "pos": pos.tolist(), "L": L.tolist(), "seed": seed, "dir": d.tolist()})
+    for i in range(64):
+        N, V, L = [(lambda x: (x / np.linalg.norm(x)).astype(np.float32))(rng.normal(size=3)) for _ in range(3)]
+        r, c = float(np.float32(rng.uniform(0.05, 1))), float(np.float32(rng.uniform(0, 1)))
+        F0 = rng.uniform(0, 1, 3).astype(np.float32)
+        out = ref.brdf(N, V, L, r, F0, c)
+        brdf.append({"N": N.tolist(), "V": V.tolist(), "L": L.tolist(), "roughness": r, "F0": F0.tolist(),
+                     "cos": c, "D_G_F": out.tolist()})
+    return {"source": "reference helpers.glsl compiled as C++ (oracle/_ref/libglslref.so)", "sampleDisk": disk,
+            "brdf": brdf}
+
+
+def ref_pass(ref):
+    """Reference shaders on the small_glass workload (brute-force traversal of the harness)."""
+    import pyoracle as po
+    from vulkanhybridraytracer_gb300 import scenes
+
+    wl = scenes.small_glass()
+    cam = wl.camera(3.0)
+    orc = po.OracleScene()
+    orc.set_scene(wl.scene)
+    planes = orc.gbuffer(cam, wl.width, wl.height, po.TRACE_BRUTE)  # G-buffer input (the raster pass's job)
+    rs = ref.RefScene(wl.scene)
+    shadow1 = rs.shadow_pass(planes, cam, 1)
+    shadow4 = rs.shadow_pass(planes, cam, 4)
+    # blur.comp: reset frame then a running-mean frame, on 3 images of 120x72 (not multiples of 16)
+    bh, bw = 72, 120
+    g = np.random.default_rng(7)
+    motion = np.full((bh, bw, 2), 0.5, np.float32)
+    blur_in = g.integers(0, 256, (3, bh, bw)).astype(np.uint8)
+    blur_hist0 = g.integers(0, 256, (3, bh, bw)).astype(np.uint8)
+    blur_f0 = ref.blur(0, motion, blur_in.copy(), blur_hist0.copy())
+    blur_f3 = ref.blur(3, motion, blur_in.copy(), blur_f0.copy())
+    hybrid = rs.hybrid_pass(planes, cam, shadow4)
+    return dict(camera=cam, **{f"plane{i}": planes[i] for i in range(6)}, shadow_spp1=shadow1, shadow_spp4=shadow4,
+                hybrid_rgba=hybrid, blur_motion=motion, blur_in=blur_in, blur_hist0=blur_hist0,
+                blur_after_frame0=blur_f0, blur_after_frame3=blur_f3)
+
+
+def make():
+    ref = None
+    try:
+        import pyref
+
+        if pyref.available():
+            pyref.load()
+            ref = pyref
+    except Exception as e:  # the reference checkout is not on every machine
+        print("reference shaders unavailable:", e)
+    (HERE / "rng_kat.json").write_text(json.dumps(rng_kat(ref), indent=1) + "\n")
+    if ref is None:
+        print("wrote rng_kat.json (not cross-checked); ref_kat.json / ref_pass_small.npz need the reference")
+        return
+    (HERE / "ref_kat.json").write_text(json.dumps(ref_kat(ref)) + "\n")
+    np.savez_compressed(HERE / "ref_pass_small.npz", **ref_pass(ref))
+    print("wrote rng_kat.json, ref_kat.json, ref_pass_small.npz from the reference's shader code")
+
+
 if __name__ == "__main__":
-    k = make()
-    print("wrote rng_kat.json", k.get("checked_against", "(not cross-checked: oracle/_ref not built)"))
+    make()

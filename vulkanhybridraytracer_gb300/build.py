@@ -82,12 +82,31 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_LIB
 
 
+REFERENCE_DIR = Path(os.environ.get("HY_REFERENCE_DIR", "/root/reference"))
+
+
+def build_reference_pin(force: bool = False):
+    """The reference's own shaders compiled as C++ into oracle/_ref (test
+    infrastructure); only where the reference checkout exists."""
+    if not (REFERENCE_DIR / "data" / "shaders").exists():
+        return None
+    args = ["make", "-C", str(ORACLE_DIR / "glsl_ref"), f"REF={REFERENCE_DIR}"]
+    if force:
+        args.insert(1, "-B")
+    r = subprocess.run(args, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference shader build failed:\n" + r.stdout + r.stderr)
+    return ORACLE_DIR / "_ref" / "libglslref.so"
+
+
 def build_all(force: bool = False) -> None:
-    with ThreadPoolExecutor(max_workers=2) as ex:
+    with ThreadPoolExecutor(max_workers=3) as ex:
         f1 = ex.submit(build_cuda, force)
         f2 = ex.submit(build_oracle, force)
+        f3 = ex.submit(build_reference_pin, force)
         f1.result()
         f2.result()
+        f3.result()
 
 
 if __name__ == "__main__":

@@ -211,6 +211,20 @@ def hd(seed: int = 1, width: int = 1920, height: int = 1080, n_spheres: int = 48
     return Workload(f"hd-{width}x{height}-{sc.num_tris // 1000}k", sc, width, height, spp, 1, 1)
 
 
+def small_glass(width: int = 48, height: int = 48) -> Workload:
+    """The small scene with glass spheres (ior 1.5), mirror spheres and a mirror
+    floor, 8 bounces: exercises every shading model of hybridHit.rchit."""
+    wl = small(0, width, height)
+    for i in (2, 5, 9):
+        wl.scene.materials[i] = Material(4, (0.9, 0.95, 1.0, 1), 1.0, 0.0, 1.5)
+    for i in (3, 7):
+        wl.scene.materials[i] = Material(3, (0.8, 0.8, 0.8, 1), 1.0, 0.05, 1.0)
+    wl.scene.materials[0] = Material(3, (0.6, 0.6, 0.6, 1), 1.0, 0.1, 1.0)
+    wl.max_bounces = 8
+    wl.name = f"small-glass-{width}x{height}"
+    return wl
+
+
 def diff(seed: int = 3, width: int = 512, height: int = 512) -> Workload:
     rng = np.random.default_rng(seed)
     sc = Scene()
