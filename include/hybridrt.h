@@ -146,7 +146,7 @@ enum { HY_ACCUM_U8 = 0, HY_ACCUM_F32 = 1 };
 
 typedef struct HyAccum {
     uint32_t format;
-    uint32_t num_lights;
+    uint32_t num_lights;   /* the pass shades with the scene's first num_lights lights (<= its count) */
     void*    history;      /* device, caller-owned: the reference's _denoisedImages */
 } HyAccum;
 
@@ -271,6 +271,39 @@ int hy_hybrid_forward(HyCtx* ctx, const HyGBuffer* gb, const HyCamera* cam,
 int hy_hybrid_forward_host(HyCtx* ctx, const HyGBuffer* h_gb, const HyCamera* cam,
                            const HyPassConfig* cfg, HyAccum* accum,
                            float* h_out_rgba32f, uint8_t* h_out_bgra8, HyStats* stats);
+
+/* ---- batches: many views of several scenes in one persistent launch ----
+ *
+ * Each view is one hybrid pass (its own G-buffer, camera, configuration,
+ * history and outputs) over one of the scene contexts in `scenes` (contexts
+ * that hold a scene and a built BVH; `ctx` itself may be one of them).  The
+ * shadow rays of all views run in one persistent launch over a global queue
+ * of (view, 8x4 tile) units, then all views are shaded in one launch; views
+ * on their reset frame (accum_frame <= 0) get blur.comp's reset branch in
+ * between.  By default the sequence is captured as a CUDA graph the first
+ * time a batch of this shape (view count, tile count, reset views, tuning) is
+ * seen and replayed afterwards; the per-view parameters travel through a
+ * pinned table copied in by the graph, so cameras, frames and buffers may
+ * change between replays.  Runs on ctx's stream; all contexts must share
+ * its device.  tuning->queue_chunk / min_blocks select the launch shape
+ * (NULL: defaults); its other fields are ignored. */
+typedef struct HyView {
+    uint32_t     scene;        /* index into scenes[] */
+    uint32_t     _pad;
+    HyGBuffer    gbuffer;      /* device planes */
+    HyCamera     camera;
+    HyPassConfig config;       /* the view's spp, bounces, RNG mode, accumulation frame, flags */
+    HyAccum      accum;        /* the view's history (device) */
+    float*       out_rgba32f;  /* device, may be NULL */
+    uint8_t*     out_bgra8;    /* device, may be NULL */
+} HyView;
+
+#define HY_BATCH_NO_GRAPH       0x1u /* enqueue the launches directly instead of replaying a captured graph */
+#define HY_BATCH_NO_STATUS_SYNC 0x2u /* return without reading back the status word (stats must be NULL) */
+#define HY_BATCH_MAX_VIEWS 1024u
+
+int hy_batch_forward(HyCtx* ctx, HyCtx* const* scenes, uint32_t num_scenes, const HyView* views,
+                     uint32_t num_views, uint32_t batch_flags, const HyPassConfig* tuning, HyStats* stats);
 
 /* ---- allocation-free accumulation (no counterpart in the reference) ----
  *

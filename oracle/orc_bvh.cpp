@@ -72,6 +72,18 @@ static void inverse4(const double* m, double* inv) {
 }
 
 void scene_derive(Scene& s) {
+    s.prim_tri0.resize(s.prims.size());
+    uint32_t nt = 0;
+    for (size_t p = 0; p < s.prims.size(); p++) { s.prim_tri0[p] = nt; nt += s.prims[p].index_count / 3; }
+    s.ntri = nt;
+    s.tri_prim.assign(nt, 0);
+    for (size_t p = 0; p < s.prims.size(); p++)
+        for (uint32_t k = 0; k < s.prims[p].index_count / 3; k++) s.tri_prim[s.prim_tri0[p] + k] = (uint32_t)p;
+    derive_world(s);
+    s.bvh_ok = false;
+}
+
+void derive_world(Scene& s) {
     // normal matrices: mat3(transpose(inverse(model))) (hybridHit.rchit:26, basic.vert:44)
     size_t nx = s.xf.size() / 16;
     s.nrm.assign(nx * 9, 0.f);
@@ -83,18 +95,12 @@ void scene_derive(Scene& s) {
         for (int c = 0; c < 3; c++)
             for (int r = 0; r < 3; r++) s.nrm[t * 9 + c * 3 + r] = (float)inv[r * 4 + c];
     }
-    s.prim_tri0.resize(s.prims.size());
-    uint32_t nt = 0;
-    for (size_t p = 0; p < s.prims.size(); p++) { s.prim_tri0[p] = nt; nt += s.prims[p].index_count / 3; }
-    s.ntri = nt;
-    s.world.assign((size_t)nt * 9, 0.f);
-    s.tri_prim.assign(nt, 0);
+    s.world.assign((size_t)s.ntri * 9, 0.f);
     for (size_t p = 0; p < s.prims.size(); p++) {
         const HyPrimitive& pr = s.prims[p];
         const float* M = &s.xf[(size_t)pr.transform_id * 16];
         for (uint32_t k = 0; k < pr.index_count / 3; k++) {
             uint32_t t = s.prim_tri0[p] + k;
-            s.tri_prim[t] = (uint32_t)p;
             for (int v = 0; v < 3; v++) {
                 uint32_t vi = s.idx[pr.first_index + 3 * k + v] + pr.vertex_offset;
                 const float* P = s.verts[vi].pos;
@@ -108,7 +114,6 @@ void scene_derive(Scene& s) {
             }
         }
     }
-    s.bvh_ok = false;
 }
 
 static inline uint32_t expand10(uint32_t v) {
@@ -123,6 +128,104 @@ static inline uint32_t expand10(uint32_t v) {
 static inline int clz64(uint64_t x) { return x ? __builtin_clzll(x) : 64; }
 
 struct Box { float lo[3], hi[3]; };
+
+// boxes of the binary tree, bottom-up (the union is order independent)
+static void refit_bvh2(Bvh& B, const std::vector<Box>& tb) {
+    const uint32_t n = B.n;
+    if (n < 2) return;
+    std::vector<uint32_t> stack;
+    std::vector<uint8_t> done(n - 1, 0);
+    stack.push_back(0);
+    while (!stack.empty()) {
+        uint32_t i = stack.back();
+        Bvh2Node& nd = B.bvh2[i];
+        bool ready = true;
+        for (uint32_t c : {nd.left, nd.right})
+            if (!(c & kLeafBit) && !done[c]) { stack.push_back(c); ready = false; }
+        if (!ready) continue;
+        stack.pop_back();
+        for (int a = 0; a < 3; a++) {
+            float lo2[2], hi2[2];
+            int k = 0;
+            for (uint32_t c : {nd.left, nd.right}) {
+                if (c & kLeafBit) {
+                    const Box& b = tb[B.order[c & ~kLeafBit]];
+                    lo2[k] = b.lo[a]; hi2[k] = b.hi[a];
+                } else {
+                    lo2[k] = B.bvh2[c].lo[a]; hi2[k] = B.bvh2[c].hi[a];
+                }
+                k++;
+            }
+            nd.lo[a] = fmin2(lo2[0], lo2[1]);
+            nd.hi[a] = fmax2(hi2[0], hi2[1]);
+        }
+        done[i] = 1;
+    }
+}
+
+static std::vector<Box> tri_boxes(const Scene& s) {
+    std::vector<Box> tb(s.ntri);
+    for (uint32_t t = 0; t < s.ntri; t++) {
+        const float* w = &s.world[(size_t)t * 9];
+        for (int a = 0; a < 3; a++) {
+            tb[t].lo[a] = fmin2(fmin2(w[a], w[3 + a]), w[6 + a]);
+            tb[t].hi[a] = fmax2(fmax2(w[a], w[3 + a]), w[6 + a]);
+        }
+    }
+    return tb;
+}
+
+static Box ref_box_of(const Bvh& B, const std::vector<Box>& tb, uint32_t r) {
+    if (r & kLeafBit) return tb[B.order[r & ~kLeafBit]];
+    Box b;
+    for (int a = 0; a < 3; a++) { b.lo[a] = B.bvh2[r].lo[a]; b.hi[a] = B.bvh2[r].hi[a]; }
+    return b;
+}
+
+// Node origin p = the node box's lo corner, per-axis power-of-two scale 2^e
+// with 255 * 2^e >= extent (extent and division rounded up), child boxes
+// quantised outwards.  Writes w[0..2], the exponent bytes of w[3] (keeping
+// its internal mask byte) and w[8..19].
+static void quantize_node(const Bvh& B, const std::vector<Box>& tb, uint32_t ref, const uint32_t* slots,
+                          uint32_t* w) {
+    Box nb = ref_box_of(B, tb, ref);
+    uint32_t e3 = 0;
+    float inv_s[3];
+    for (int a = 0; a < 3; a++) {
+        w[a] = fbits(nb.lo[a]);
+        float ext = sub_dir(nb.hi[a], nb.lo[a], FE_UPWARD);
+        float t = div_up(ext, 255.0f);
+        uint32_t tb_ = fbits(t);
+        int E = (int)((tb_ >> 23) & 0xffu);
+        int ex = (E == 0) ? -100 : (E - 127 + ((tb_ & 0x7fffffu) ? 1 : 0));
+        ex = std::max(-100, std::min(100, ex));
+        e3 |= (uint32_t)(ex + 127) << (8 * a);
+        inv_s[a] = bitsf((uint32_t)(127 - ex) << 23);
+    }
+    w[3] = (w[3] & 0xff000000u) | e3;
+    uint8_t qlo[3][8], qhi[3][8];
+    std::memset(qlo, 0, sizeof(qlo));
+    std::memset(qhi, 0, sizeof(qhi));
+    for (int sl = 0; sl < 8; sl++) {
+        if (slots[sl] == 0xffffffffu) continue;
+        Box cb = ref_box_of(B, tb, slots[sl]);
+        for (int a = 0; a < 3; a++) {
+            float lo = std::floor(sub_dir(cb.lo[a], nb.lo[a], FE_DOWNWARD) * inv_s[a]);
+            float hi = std::ceil(sub_dir(cb.hi[a], nb.lo[a], FE_UPWARD) * inv_s[a]);
+            qlo[a][sl] = (uint8_t)fmin2(fmax2(lo, 0.f), 255.f);
+            qhi[a][sl] = (uint8_t)fmin2(fmax2(hi, 0.f), 255.f);
+        }
+    }
+    auto pack4 = [](const uint8_t* b) {
+        return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
+    };
+    for (int a = 0; a < 3; a++) {
+        w[8 + 2 * a] = pack4(qlo[a]);
+        w[9 + 2 * a] = pack4(qlo[a] + 4);
+        w[14 + 2 * a] = pack4(qhi[a]);
+        w[15 + 2 * a] = pack4(qhi[a] + 4);
+    }
+}
 
 static inline float surface(const Box& b) {
     float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
@@ -207,35 +310,7 @@ void bvh_build(Scene& s) {
             nd.first = (uint32_t)lo;
             nd.last = (uint32_t)hi;
         }
-        // ---- refit (recursive post-order; union is order independent) ----
-        std::vector<uint32_t> stack;
-        std::vector<uint8_t> done(n - 1, 0);
-        stack.push_back(0);
-        while (!stack.empty()) {
-            uint32_t i = stack.back();
-            Bvh2Node& nd = B.bvh2[i];
-            bool ready = true;
-            for (uint32_t c : {nd.left, nd.right})
-                if (!(c & kLeafBit) && !done[c]) { stack.push_back(c); ready = false; }
-            if (!ready) continue;
-            stack.pop_back();
-            for (int a = 0; a < 3; a++) {
-                float lo2[2], hi2[2];
-                int k = 0;
-                for (uint32_t c : {nd.left, nd.right}) {
-                    if (c & kLeafBit) {
-                        const Box& b = tb[B.order[c & ~kLeafBit]];
-                        lo2[k] = b.lo[a]; hi2[k] = b.hi[a];
-                    } else {
-                        lo2[k] = B.bvh2[c].lo[a]; hi2[k] = B.bvh2[c].hi[a];
-                    }
-                    k++;
-                }
-                nd.lo[a] = fmin2(lo2[0], lo2[1]);
-                nd.hi[a] = fmax2(hi2[0], hi2[1]);
-            }
-            done[i] = 1;
-        }
+        refit_bvh2(B, tb);
     }
     auto ref_box = [&](uint32_t r) -> Box {
         if (r & kLeafBit) return tb[B.order[r & ~kLeafBit]];
@@ -313,23 +388,12 @@ void bvh_build(Scene& s) {
         // encode
         Bvh8Node node;
         std::memset(&node, 0, sizeof(node));
-        uint32_t e[3];
-        float inv_s[3];
-        for (int a = 0; a < 3; a++) {
-            node.w[a] = fbits(nb.lo[a]);
-            float ext = sub_dir(nb.hi[a], nb.lo[a], FE_UPWARD);
-            float t = div_up(ext, 255.0f);
-            uint32_t tb_ = fbits(t);
-            int E = (int)((tb_ >> 23) & 0xffu);
-            int ex = (E == 0) ? -100 : (E - 127 + ((tb_ & 0x7fffffu) ? 1 : 0));
-            ex = std::max(-100, std::min(100, ex));
-            e[a] = (uint32_t)(ex + 127);
-            inv_s[a] = bitsf((uint32_t)(127 - ex) << 23);
-        }
+        uint32_t slots[8];
+        for (int sl = 0; sl < 8; sl++) slots[sl] = child_in_slot[sl] < 0 ? 0xffffffffu : C[child_in_slot[sl]];
+        B.node_ref.push_back(r);
+        B.node_plan.insert(B.node_plan.end(), slots, slots + 8);
         uint32_t imask = 0;
-        uint8_t meta[8] = {0}, qlo[3][8], qhi[3][8];
-        std::memset(qlo, 0, sizeof(qlo));
-        std::memset(qhi, 0, sizeof(qhi));
+        uint8_t meta[8] = {0};
         uint32_t child_base = (uint32_t)queue.size();
         uint32_t tri_base = tri_count;
         uint32_t toff = 0;
@@ -337,15 +401,6 @@ void bvh_build(Scene& s) {
             int i = child_in_slot[sl];
             if (i < 0) continue;
             uint32_t c = C[i];
-            Box cb = ref_box(c);
-            for (int a = 0; a < 3; a++) {
-                float lo = std::floor(sub_dir(cb.lo[a], nb.lo[a], FE_DOWNWARD) * inv_s[a]);
-                float hi = std::ceil(sub_dir(cb.hi[a], nb.lo[a], FE_UPWARD) * inv_s[a]);
-                lo = fmin2(fmax2(lo, 0.f), 255.f);
-                hi = fmin2(fmax2(hi, 0.f), 255.f);
-                qlo[a][sl] = (uint8_t)lo;
-                qhi[a][sl] = (uint8_t)hi;
-            }
             uint32_t cnt = ref_count(c);
             if (cnt > (uint32_t)kLeafMax) {
                 imask |= 1u << sl;
@@ -367,21 +422,36 @@ void bvh_build(Scene& s) {
             }
         }
         tri_count += toff;
-        node.w[3] = e[0] | (e[1] << 8) | (e[2] << 16) | (imask << 24);
+        node.w[3] = imask << 24;
+        quantize_node(B, tb, r, slots, node.w);
         node.w[4] = child_base;
         node.w[5] = tri_base;
         auto pack4 = [](const uint8_t* b) { return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24); };
         node.w[6] = pack4(meta); node.w[7] = pack4(meta + 4);
-        node.w[8] = pack4(qlo[0]); node.w[9] = pack4(qlo[0] + 4);
-        node.w[10] = pack4(qlo[1]); node.w[11] = pack4(qlo[1] + 4);
-        node.w[12] = pack4(qlo[2]); node.w[13] = pack4(qlo[2] + 4);
-        node.w[14] = pack4(qhi[0]); node.w[15] = pack4(qhi[0] + 4);
-        node.w[16] = pack4(qhi[1]); node.w[17] = pack4(qhi[1] + 4);
-        node.w[18] = pack4(qhi[2]); node.w[19] = pack4(qhi[2] + 4);
         B.bvh8.push_back(node);
     }
+    (void)ref_box;
     B.depth = level.empty() ? 0 : level.back() + 1;
     s.bvh_ok = true;
+}
+
+// New transforms, same topology: re-transformed triangles, refitted binary
+// tree, every 8-wide node re-quantised with its stored slot plan, packed
+// triangles rewritten (the GPU refit computes exactly this).
+void bvh_refit(Scene& s) {
+    Bvh& B = s.bvh;
+    if (!s.bvh_ok) return;
+    std::vector<Box> tb = tri_boxes(s);
+    refit_bvh2(B, tb);
+    for (size_t k = 0; k < B.bvh8.size(); k++) quantize_node(B, tb, B.node_ref[k], &B.node_plan[k * 8], B.bvh8[k].w);
+    for (uint32_t i = 0; i < B.n; i++) {
+        float* dst = &B.tris[(size_t)i * 12];
+        const uint32_t tid = fbits(dst[3]);
+        const float* w = &s.world[(size_t)tid * 9];
+        dst[0] = w[0]; dst[1] = w[1]; dst[2] = w[2];
+        dst[4] = w[3]; dst[5] = w[4]; dst[6] = w[5];
+        dst[8] = w[6]; dst[9] = w[7]; dst[10] = w[8];
+    }
 }
 
 // ---- watertight ray/triangle test (Woop, Benthin & Wald, JCGT 2013) -----------

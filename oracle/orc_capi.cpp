@@ -58,6 +58,16 @@ int orc_bvh_build(void* sp, uint32_t* info, float* bounds6) {
         for (int a = 0; a < 3; a++) { bounds6[a] = s.bvh.slo[a]; bounds6[3 + a] = s.bvh.shi[a]; }
     return s.bvh_ok ? 0 : -8;
 }
+// new transforms, same topology (hy_bvh_refit's counterpart)
+int orc_bvh_refit(void* sp, const float* xf, uint32_t nx) {
+    Scene& s = *(Scene*)sp;
+    if (!s.bvh_ok || (size_t)nx * 16 != s.xf.size()) return -1;
+    s.xf.assign(xf, xf + (size_t)nx * 16);
+    derive_world(s);
+    bvh_refit(s);
+    return 0;
+}
+
 void orc_bvh_download(void* sp, uint32_t* morton, uint32_t* order, uint32_t* bvh2, uint32_t* bvh8, float* tris) {
     Bvh& B = ((Scene*)sp)->bvh;
     if (morton) std::memcpy(morton, B.morton.data(), B.morton.size() * 4);

@@ -31,6 +31,8 @@ struct Bvh {
     std::vector<Bvh8Node> bvh8;            // BFS order
     std::vector<float> tris;               // 12 floats per packed triangle
     uint32_t depth = 0;
+    std::vector<uint32_t> node_ref;        // BVH2 subtree of each BVH8 node (refits)
+    std::vector<uint32_t> node_plan;       // its 8 slot children, 0xffffffff = empty (refits)
 };
 
 struct Counters { uint64_t nodes = 0, tris = 0; uint32_t status = 0; };
@@ -57,7 +59,9 @@ struct Scene {
 
 // geometry / BVH
 void scene_derive(Scene& s);
+void derive_world(Scene& s);   // normal matrices and world triangles from the current transforms
 void bvh_build(Scene& s);
+void bvh_refit(Scene& s);
 // traversal: mode 0 = brute force over all triangles, 1 = BVH8 (op-for-op the
 // product's traversal, so node/triangle counts are comparable)
 Hit trace(const Scene& s, const float o[3], const float d[3], float tmin, float tmax, bool any_hit,

@@ -47,6 +47,7 @@ def load():
         "orc_world_tris": (None, [P, P]),
         "orc_bvh_build": (C.c_int, [P, P, P]),
         "orc_bvh_download": (None, [P, P, P, P, P, P]),
+        "orc_bvh_refit": (C.c_int, [P, P, U32]),
         "orc_trace": (None, [P, P, U32, C.c_int, C.c_int, P, P]),
         "orc_tea": (U32, [U32, U32]),
         "orc_rnd_seq": (None, [U32, U32, P, P]),
@@ -187,6 +188,12 @@ class OracleScene:
             raise RuntimeError("oracle bvh build failed")
         return {"num_tris": int(info[0]), "num_bvh2_nodes": int(info[1]), "num_bvh8_nodes": int(info[2]),
                 "depth": int(info[3]), "scene_lo": b[:3].tolist(), "scene_hi": b[3:].tolist()}
+
+    def refit_bvh(self, xf: np.ndarray):
+        xf = np.ascontiguousarray(xf, np.float32)
+        self._xf = xf
+        if self.lib.orc_bvh_refit(self.h, _p(xf), len(xf)) != 0:
+            raise RuntimeError("oracle refit needs a built BVH and the same transform count")
 
     def download_bvh(self, n_bvh8: int):
         n = self.num_tris

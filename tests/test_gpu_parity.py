@@ -244,8 +244,9 @@ def test_stagewise_matches_fused(small):
     cfg = pass_config(4, 1, L.HY_RNG_DECORRELATED, 4, 0)
     ha, hb = h0.clone(), h0.clone()
     fa, fb = torch.zeros((H, W, 4), device="cuda"), torch.zeros((H, W, 4), device="cuda")
-    small.ctx.forward(planes, cam, cfg, ha, L.HY_ACCUM_U8, out_f=fa)
     shadow = torch.zeros((nl, H, W), dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()   # torch's stream vs the context's own stream
+    small.ctx.forward(planes, cam, cfg, ha, L.HY_ACCUM_U8, out_f=fa)
     small.ctx.shadow_pass(planes, cam, cfg, shadow, L.HY_ACCUM_U8)
     small.ctx.accumulate_pass(planes, cfg, shadow, hb, L.HY_ACCUM_U8)
     small.ctx.shade_pass(planes, cam, cfg, hb, L.HY_ACCUM_U8, out_f=fb)
@@ -284,6 +285,7 @@ def test_host_buffers_equal_device(small):
     h1 = torch.zeros((nl, H, W), dtype=torch.uint8, device="cuda")
     h2 = h1.clone()
     o1 = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()   # torch's stream vs the context's own stream
     small.ctx.forward([torch.from_numpy(x).cuda() for x in pn], cam, cfg, h1, L.HY_ACCUM_U8, out_8=o1)
     o2 = np.zeros((H, W, 4), np.uint8)
     st = small.ctx.forward_host(pn, cam, cfg, h2, L.HY_ACCUM_U8, out_8=o2)
@@ -327,8 +329,8 @@ def test_error_paths(gpu_lib, oracle_lib):
         ctx.forward(planes, cam, pass_config(0), hist)
     assert e.value.code == L.HY_ERR_INVALID_ARG  # spp 0
     with pytest.raises(L.HyError) as e:
-        ctx.forward(planes, cam, pass_config(1), hist[:1])
-    assert e.value.code == L.HY_ERR_INVALID_ARG  # history for the wrong light count
+        ctx.forward(planes, cam, pass_config(1), torch.zeros((3, 32, 32), dtype=torch.uint8, device="cuda"))
+    assert e.value.code == L.HY_ERR_INVALID_ARG  # history for more lights than the scene has
     # forced allocation failure surfaces as HY_ERR_OOM and leaves the context usable
     assert ctx.lib.hy_debug_fail_alloc_after(ctx.h, 1) == 0
     with pytest.raises(L.HyError) as e:

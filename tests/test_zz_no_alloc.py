@@ -44,6 +44,7 @@ def test_noalloc_accumulate_matches_context_pass(gpu_lib):
     for frame in (0, -1, 4):
         shadow = torch.from_numpy(rng.integers(0, 256, (nl, H, W)).astype(np.uint8)).cuda()
         cfg = pass_config(accum_frame=frame)
+        torch.cuda.synchronize()   # the context runs on its own stream
         ctx.accumulate_pass(planes, cfg, shadow, h_ref, L.HY_ACCUM_U8)
         acc = L.HyAccum(L.HY_ACCUM_U8, nl, h_new.data_ptr())
         rc = lib.hy_accumulate_pass_noalloc(C.byref(gb), C.byref(cfg), C.c_void_p(shadow.data_ptr()), C.byref(acc),
@@ -56,6 +57,7 @@ def test_noalloc_accumulate_matches_context_pass(gpu_lib):
     hf_new = hf_ref.clone()
     shadow_f = torch.rand((nl, H, W), device="cuda")
     cfg = pass_config(accum_frame=0)
+    torch.cuda.synchronize()
     ctx.accumulate_pass(planes, cfg, shadow_f, hf_ref, L.HY_ACCUM_F32)
     acc = L.HyAccum(L.HY_ACCUM_F32, nl, hf_new.data_ptr())
     assert lib.hy_accumulate_pass_noalloc(C.byref(gb), C.byref(cfg), C.c_void_p(shadow_f.data_ptr()), C.byref(acc),

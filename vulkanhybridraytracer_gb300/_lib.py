@@ -88,6 +88,16 @@ class HyStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("_")}
 
 
+class HyView(C.Structure):
+    _fields_ = [("scene", C.c_uint32), ("_pad", C.c_uint32), ("gbuffer", HyGBuffer), ("camera", HyCamera),
+                ("config", HyPassConfig), ("accum", HyAccum), ("out_rgba32f", C.c_void_p),
+                ("out_bgra8", C.c_void_p)]
+
+
+HY_BATCH_NO_GRAPH = 0x1
+HY_BATCH_NO_STATUS_SYNC = 0x2
+
+
 class HyBvhStats(C.Structure):
     _fields_ = [("num_tris", C.c_uint32), ("num_bvh2_nodes", C.c_uint32), ("num_bvh8_nodes", C.c_uint32),
                 ("depth", C.c_uint32), ("build_ms", C.c_float), ("scene_lo", C.c_float * 3),
@@ -128,6 +138,8 @@ PROTOTYPES = {
     "hy_hybrid_forward_host": (I32, [P, C.POINTER(HyGBuffer), C.POINTER(HyCamera), C.POINTER(HyPassConfig),
                                      C.POINTER(HyAccum), P, P, C.POINTER(HyStats)]),
     "hy_accumulate_pass_noalloc": (I32, [C.POINTER(HyGBuffer), C.POINTER(HyPassConfig), P, C.POINTER(HyAccum), P]),
+    "hy_batch_forward": (I32, [P, C.POINTER(P), U32, C.POINTER(HyView), U32, U32, C.POINTER(HyPassConfig),
+                               C.POINTER(HyStats)]),
 }
 
 _lib = None

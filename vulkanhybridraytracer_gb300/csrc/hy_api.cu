@@ -250,6 +250,7 @@ PassParams make_params(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const
     if (cfg->flags & HY_FLAG_FULL_BLUR_DISPATCH) { P.blur_w = P.W; P.blur_h = P.H; }
     else { P.blur_w = (P.W / 16) * 16; P.blur_h = (P.H / 16) * 16; }
     P.stats = dev_stats(c);
+    P.num_lights = c->nlights;
     P.status = dev_status(c);
     return P;
 }
@@ -338,11 +339,16 @@ void hy_destroy(HyCtx* c) {
                       &c->mats, &c->lights, &c->env[0], &c->env[1], &c->world, &c->tribox, &c->centroid,
                       &c->keys[0], &c->keys[1], &c->vals[0], &c->vals[1], &c->bvh2, &c->parent, &c->flags,
                       &c->bounds, &c->lvl_ref[0], &c->lvl_ref[1], &c->plan, &c->ni, &c->nt, &c->ni_scan,
-                      &c->nt_scan, &c->scan_tmp, &c->hist, &c->total, &c->nodes, &c->tris, &c->dstats,
+                      &c->nt_scan, &c->scan_tmp, &c->hist, &c->total, &c->nodes, &c->tris, &c->node_ref,
+                      &c->node_plan, &c->dstats,
                       &c->raw_shadow, &c->hist_prev, &c->host_in[0], &c->host_in[1], &c->host_in[2],
                       &c->host_in[3], &c->host_in[4], &c->host_in[5], &c->host_out_f, &c->host_out_8};
     for (DevBuf* b : bufs) ctx_free(c, *b);
     if (c->h_stats) cudaFreeHost(c->h_stats);
+    if (c->batch_exec) cudaGraphExecDestroy(c->batch_exec);
+    if (c->batch_done) cudaEventDestroy(c->batch_done);
+    if (c->h_batch_tab) cudaFreeHost(c->h_batch_tab);
+    ctx_free(c, c->batch_tab);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -565,11 +571,12 @@ int hy_shade_pass(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const HyPa
     if (!c || !cam || !acc || !acc->history || acc->format > HY_ACCUM_F32) return HY_ERR_INVALID_ARG;
     int rc;
     if ((rc = check_gbuffer(gb, true)) || (rc = check_cfg(cfg)) || (rc = check_scene_ready(c))) return rc;
-    if (acc->num_lights != c->nlights) return HY_ERR_INVALID_ARG;
+    if (acc->num_lights > c->nlights) return HY_ERR_INVALID_ARG;  // the pass uses the first num_lights lights
     DeviceGuard g(c->device);
     if ((rc = reset_counters(c))) return rc;
     // with HY_FLAG_NO_ACCUM the history argument holds the raw shadow images
     PassParams P = make_params(c, gb, cam, cfg, acc->format, acc->history, acc->history, out_f, out_8);
+    P.num_lights = acc->num_lights;
     if ((rc = run_pixels(c, MODE_SHADE, P, cfg, WQ_SHADE))) return rc;
     return finish_call(c, st, !(cfg->flags & HY_FLAG_NO_STATUS_SYNC));
 }
@@ -581,12 +588,14 @@ static int forward_impl(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, cons
         // steady state: the running mean is pointwise, so the shadow kernel folds
         // each light's factor straight into the history (no raw images)
         PassParams P = make_params(c, gb, cam, cfg, acc->format, nullptr, acc->history, out_f, out_8);
+        P.num_lights = acc->num_lights;
         if ((rc = run_pixels(c, MODE_SHADOW_ACCUM, P, cfg, WQ_SHADOW))) return rc;
         return run_pixels(c, MODE_SHADE, P, cfg, WQ_SHADE);
     }
-    size_t bytes = (size_t)gb->width * gb->height * c->nlights * (acc->format == HY_ACCUM_U8 ? 1 : 4);
-    if ((rc = ensure_size(c, c->raw_shadow, bytes))) return rc;
+    size_t bytes = (size_t)gb->width * gb->height * acc->num_lights * (acc->format == HY_ACCUM_U8 ? 1 : 4);
+    if ((rc = ensure_size(c, c->raw_shadow, bytes ? bytes : 16))) return rc;
     PassParams P = make_params(c, gb, cam, cfg, acc->format, c->raw_shadow.p, acc->history, out_f, out_8);
+    P.num_lights = acc->num_lights;
     if ((rc = run_pixels(c, MODE_SHADOW, P, cfg, WQ_SHADOW))) return rc;
     if (!(cfg->flags & HY_FLAG_NO_ACCUM) && (rc = accumulate_impl(c, gb, cfg, c->raw_shadow.p, acc))) return rc;
     return run_pixels(c, MODE_SHADE, P, cfg, WQ_SHADE);
@@ -597,7 +606,7 @@ int hy_hybrid_forward(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const 
     if (!c || !cam || !acc || !acc->history || acc->format > HY_ACCUM_F32) return HY_ERR_INVALID_ARG;
     int rc;
     if ((rc = check_gbuffer(gb, true)) || (rc = check_cfg(cfg)) || (rc = check_scene_ready(c))) return rc;
-    if (acc->num_lights != c->nlights) return HY_ERR_INVALID_ARG;
+    if (acc->num_lights > c->nlights) return HY_ERR_INVALID_ARG;  // the pass uses the first num_lights lights
     DeviceGuard g(c->device);
     if ((rc = reset_counters(c))) return rc;
     if ((rc = forward_impl(c, gb, cam, cfg, acc, out_f, out_8))) return rc;
@@ -609,7 +618,7 @@ int hy_hybrid_forward_host(HyCtx* c, const HyGBuffer* hgb, const HyCamera* cam, 
     if (!c || !cam || !acc || !acc->history || acc->format > HY_ACCUM_F32) return HY_ERR_INVALID_ARG;
     int rc;
     if ((rc = check_gbuffer(hgb, true)) || (rc = check_cfg(cfg)) || (rc = check_scene_ready(c))) return rc;
-    if (acc->num_lights != c->nlights) return HY_ERR_INVALID_ARG;
+    if (acc->num_lights > c->nlights) return HY_ERR_INVALID_ARG;  // the pass uses the first num_lights lights
     DeviceGuard g(c->device);
     const size_t npx = (size_t)hgb->width * hgb->height;
     HyGBuffer dgb = *hgb;
@@ -628,6 +637,150 @@ int hy_hybrid_forward_host(HyCtx* c, const HyGBuffer* hgb, const HyCamera* cam, 
     if (h_out_f) HY_CUDA_TRY(cudaMemcpyAsync(h_out_f, d_f, npx * 16, cudaMemcpyDeviceToHost, c->stream));
     if (h_out_8) HY_CUDA_TRY(cudaMemcpyAsync(h_out_8, d_8, npx * 4, cudaMemcpyDeviceToHost, c->stream));
     return finish_call(c, st, true);
+}
+
+// ---- batches -------------------------------------------------------------------
+static int batch_enqueue(HyCtx* c, const std::vector<PassParams>& pv, const std::vector<SceneDev>& sd,
+                         const HyView* views, const std::vector<uint32_t>& reset_views, const BatchParams& B,
+                         bool count, int minb, size_t tab_bytes) {
+    cudaStream_t s = c->stream;
+    HY_CUDA_TRY(cudaMemcpyAsync(c->batch_tab.p, c->h_batch_tab, tab_bytes, cudaMemcpyHostToDevice, s));
+    HY_CUDA_TRY(cudaMemsetAsync(c->dstats.p, 0, c->dstats.bytes, s));
+    int per = 0;
+    if (batch_occupancy(false, count, minb, &per) != cudaSuccess || per <= 0) per = 1;
+    int grid = std::max(1, std::min<int>(per * c->num_sms, (int)((B.total_tiles * 32ull + 127) / 128)));
+    BatchParams Bs = B;
+    Bs.queue = dev_queue(c, WQ_SHADOW);
+    HY_CUDA_TRY(launch_batch(false, count, minb, Bs, grid, s));
+    for (uint32_t v : reset_views) {
+        const HyView& vw = views[v];
+        HyAccum acc = vw.accum;
+        int rc = accumulate_impl(c, &vw.gbuffer, &vw.config, pv[v].shadow, &acc);
+        if (rc) return rc;
+    }
+    if (batch_occupancy(true, count, minb, &per) != cudaSuccess || per <= 0) per = 1;
+    grid = std::max(1, std::min<int>(per * c->num_sms, (int)((B.total_tiles * 32ull + 127) / 128)));
+    BatchParams Bh = B;
+    Bh.queue = dev_queue(c, WQ_SHADE);
+    HY_CUDA_TRY(launch_batch(true, count, minb, Bh, grid, s));
+    (void)sd;
+    return HY_OK;
+}
+
+int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* views, uint32_t nv,
+                     uint32_t bflags, const HyPassConfig* tuning, HyStats* st) {
+    if (!c || !scenes || ns == 0 || !views || nv == 0 || nv > kMaxBatchViews) return HY_ERR_INVALID_ARG;
+    int rc;
+    for (uint32_t i = 0; i < ns; i++) {
+        if (!scenes[i]) return HY_ERR_INVALID_ARG;
+        if (scenes[i]->device != c->device) return HY_ERR_INVALID_ARG;
+        if ((rc = check_scene_ready(scenes[i]))) return rc;
+    }
+    DeviceGuard g(c->device);
+    const bool count = tuning && (tuning->flags & HY_FLAG_COUNT_TRAVERSAL);
+    const uint32_t chunk = tuning && tuning->queue_chunk ? tuning->queue_chunk : 1;
+    const int minb = tuning && tuning->min_blocks ? (int)tuning->min_blocks : 8;
+    // per-view parameters
+    std::vector<PassParams> pv(nv);
+    std::vector<uint32_t> reset_views;
+    size_t raw_bytes = 0, snap_bytes = 0;
+    std::vector<size_t> raw_off(nv, (size_t)-1);
+    uint32_t total = 0;
+    for (uint32_t i = 0; i < nv; i++) {
+        const HyView& v = views[i];
+        if (v.scene >= ns) return HY_ERR_INVALID_ARG;
+        if ((rc = check_gbuffer(&v.gbuffer, true)) || (rc = check_cfg(&v.config))) return rc;
+        const HyCtx* sc = scenes[v.scene];
+        if (!v.accum.history || v.accum.format > HY_ACCUM_F32 || v.accum.num_lights > sc->nlights)
+            return HY_ERR_INVALID_ARG;
+        const size_t hbytes = (size_t)v.gbuffer.width * v.gbuffer.height * v.accum.num_lights *
+                              (v.accum.format == HY_ACCUM_U8 ? 1 : 4);
+        const bool accum = !(v.config.flags & HY_FLAG_NO_ACCUM) && v.config.accum_frame > 0;
+        if (!accum) {
+            raw_off[i] = raw_bytes;
+            raw_bytes += (hbytes + 255) & ~(size_t)255;
+            if (!(v.config.flags & HY_FLAG_NO_ACCUM)) {
+                reset_views.push_back(i);
+                snap_bytes = std::max(snap_bytes, hbytes);
+            }
+        }
+        pv[i] = make_params(c, &v.gbuffer, &v.camera, &v.config, v.accum.format, nullptr, v.accum.history,
+                            v.out_rgba32f, v.out_bgra8);
+        pv[i].scene = v.scene;
+        pv[i].tile_begin = total;
+        pv[i].num_lights = v.accum.num_lights;
+        uint32_t G = 1;
+        if (v.config.rng_mode == HY_RNG_DECORRELATED)
+            while (G < v.config.shadow_spp && G < 32) G <<= 1;
+        pv[i].group = G;
+        total += pv[i].ntiles;
+    }
+    if ((rc = ensure_size(c, c->raw_shadow, raw_bytes ? raw_bytes : 16))) return rc;
+    if (snap_bytes && (rc = ensure_size(c, c->hist_prev, snap_bytes))) return rc;
+    for (uint32_t i = 0; i < nv; i++) {
+        if (raw_off[i] == (size_t)-1) continue;
+        pv[i].shadow = (uint8_t*)c->raw_shadow.p + raw_off[i];
+    }
+    std::vector<SceneDev> sd(ns);
+    for (uint32_t i = 0; i < ns; i++) sd[i] = scene_dev(scenes[i]);
+    // the tables: device copy + pinned host mirror
+    const size_t tab_bytes = nv * sizeof(PassParams) + ns * sizeof(SceneDev);
+    if ((rc = ensure_size(c, c->batch_tab, tab_bytes))) return rc;
+    if (c->batch_done) HY_CUDA_TRY(cudaEventSynchronize(c->batch_done));  // the last replay has read the mirror
+    if (c->h_batch_tab_bytes < tab_bytes) {
+        if (c->h_batch_tab) cudaFreeHost(c->h_batch_tab);
+        c->h_batch_tab = nullptr;
+        c->h_batch_tab_bytes = 0;
+        HY_CUDA_TRY(cudaMallocHost(&c->h_batch_tab, tab_bytes));
+        c->h_batch_tab_bytes = tab_bytes;
+        if (c->batch_exec) { cudaGraphExecDestroy(c->batch_exec); c->batch_exec = nullptr; c->batch_key.clear(); }
+    }
+    std::memcpy(c->h_batch_tab, pv.data(), nv * sizeof(PassParams));
+    std::memcpy((uint8_t*)c->h_batch_tab + nv * sizeof(PassParams), sd.data(), ns * sizeof(SceneDev));
+    BatchParams B;
+    B.views = c->batch_tab.as<PassParams>();
+    B.scenes = (const SceneDev*)((uint8_t*)c->batch_tab.p + nv * sizeof(PassParams));
+    B.nviews = nv;
+    B.total_tiles = total;
+    B.chunk = chunk;
+    B.stats = dev_stats(c);
+    B.status = dev_status(c);
+    B.queue = nullptr;
+    if (bflags & HY_BATCH_NO_GRAPH) {
+        if ((rc = batch_enqueue(c, pv, sd, views, reset_views, B, count, minb, tab_bytes))) return rc;
+    } else {
+        // the graph bakes pointers of the tables, scratch and reset-view launches
+        std::vector<uint64_t> key = {nv, ns, total, chunk, (uint64_t)minb, (uint64_t)count, (uint64_t)(uintptr_t)c->batch_tab.p,
+                                     (uint64_t)(uintptr_t)c->h_batch_tab, (uint64_t)(uintptr_t)c->raw_shadow.p,
+                                     (uint64_t)(uintptr_t)c->hist_prev.p, (uint64_t)(uintptr_t)c->stream};
+        for (uint32_t v : reset_views) {
+            const HyView& vw = views[v];
+            key.push_back(v);
+            key.push_back((uint64_t)(uintptr_t)vw.accum.history);
+            key.push_back((uint64_t)(uintptr_t)vw.gbuffer.plane[3]);
+            key.push_back(((uint64_t)vw.gbuffer.width << 32) | vw.gbuffer.height);
+            key.push_back(((uint64_t)(uint32_t)vw.config.accum_frame << 32) | vw.config.flags);
+            key.push_back(((uint64_t)vw.accum.format << 32) | vw.gbuffer.format[3]);
+        }
+        if (!c->batch_exec || key != c->batch_key) {
+            if (c->batch_exec) { cudaGraphExecDestroy(c->batch_exec); c->batch_exec = nullptr; }
+            c->batch_key.clear();
+            cudaGraph_t graph = nullptr;
+            HY_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            rc = batch_enqueue(c, pv, sd, views, reset_views, B, count, minb, tab_bytes);
+            cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+            if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+            if (e != cudaSuccess) { cudaGetLastError(); return HY_ERR_CUDA; }
+            e = cudaGraphInstantiate(&c->batch_exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) { cudaGetLastError(); c->batch_exec = nullptr; return HY_ERR_CUDA; }
+            c->batch_key = key;
+        }
+        HY_CUDA_TRY(cudaGraphLaunch(c->batch_exec, c->stream));
+    }
+    if (!c->batch_done) HY_CUDA_TRY(cudaEventCreateWithFlags(&c->batch_done, cudaEventDisableTiming));
+    HY_CUDA_TRY(cudaEventRecord(c->batch_done, c->stream));
+    return finish_call(c, st, !(bflags & HY_BATCH_NO_STATUS_SYNC));
 }
 
 }  // extern "C"

@@ -434,19 +434,14 @@ __global__ void k_collapse_plan(const uint32_t* __restrict__ lvl, uint32_t m, co
     nt[k] = n_tri;
 }
 
-__global__ void k_collapse_emit(uint32_t m, uint32_t level_start, uint32_t tri_start,
-                                const uint32_t* __restrict__ lvl, const uint32_t* __restrict__ plan,
-                                const uint32_t* __restrict__ ni_scan, const uint32_t* __restrict__ nt_scan,
-                                const uint32_t* __restrict__ bvh2, const uint32_t* __restrict__ order,
-                                const float* __restrict__ tribox, const float4* __restrict__ world,
-                                Node8* __restrict__ nodes, float4* __restrict__ tris, uint32_t* __restrict__ next) {
-    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= m) return;
-    Ref nb = load_ref(lvl[k], bvh2, order, tribox);
-    uint32_t child_base = level_start + m + ni_scan[k];
-    uint32_t tri_base = tri_start + nt_scan[k];
-    uint32_t e[3];
+// Node origin p = the node box's lo corner, per-axis power-of-two scale 2^e
+// with 255 * 2^e >= extent (extent and division rounded up), child boxes
+// quantised outwards: floor((lo - p)_rd / 2^e), ceil((hi - p)_ru / 2^e).
+__device__ __forceinline__ void quantize_node(const Ref& nb, const uint32_t* slots, const uint32_t* bvh2,
+                                              const uint32_t* order, const float* tribox, uint32_t& e3,
+                                              uint32_t qlo[3][2], uint32_t qhi[3][2]) {
     float inv_s[3];
+    e3 = 0;
     for (int a = 0; a < 3; a++) {
         float ext = __fsub_ru(nb.hi[a], nb.lo[a]);
         float t = __fdiv_ru(ext, 255.0f);
@@ -454,13 +449,12 @@ __global__ void k_collapse_emit(uint32_t m, uint32_t level_start, uint32_t tri_s
         int E = (int)((tb >> 23) & 0xffu);
         int ex = (E == 0) ? -100 : (E - 127 + ((tb & 0x7fffffu) ? 1 : 0));
         ex = max(-100, min(100, ex));
-        e[a] = (uint32_t)(ex + 127);
+        e3 |= (uint32_t)(ex + 127) << (8 * a);
         inv_s[a] = __uint_as_float((uint32_t)(127 - ex) << 23);
+        qlo[a][0] = qlo[a][1] = qhi[a][0] = qhi[a][1] = 0;
     }
-    uint32_t imask = 0, meta[2] = {0, 0}, qlo[3][2] = {{0, 0}, {0, 0}, {0, 0}}, qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
-    uint32_t toff = 0, rank = 0;
     for (int sl = 0; sl < 8; sl++) {
-        uint32_t c = plan[(size_t)k * 8 + sl];
+        uint32_t c = slots[sl];
         if (c == 0xffffffffu) continue;
         Ref cb = load_ref(c, bvh2, order, tribox);
         int wsel = sl >> 2, sh = (sl & 3) * 8;
@@ -472,6 +466,34 @@ __global__ void k_collapse_emit(uint32_t m, uint32_t level_start, uint32_t tri_s
             qlo[a][wsel] |= (uint32_t)lo << sh;
             qhi[a][wsel] |= (uint32_t)hi << sh;
         }
+    }
+}
+
+__global__ void k_collapse_emit(uint32_t m, uint32_t level_start, uint32_t tri_start,
+                                const uint32_t* __restrict__ lvl, const uint32_t* __restrict__ plan,
+                                const uint32_t* __restrict__ ni_scan, const uint32_t* __restrict__ nt_scan,
+                                const uint32_t* __restrict__ bvh2, const uint32_t* __restrict__ order,
+                                const float* __restrict__ tribox, const float4* __restrict__ world,
+                                Node8* __restrict__ nodes, float4* __restrict__ tris, uint32_t* __restrict__ next,
+                                uint32_t* __restrict__ node_ref, uint32_t* __restrict__ node_plan) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    Ref nb = load_ref(lvl[k], bvh2, order, tribox);
+    uint32_t child_base = level_start + m + ni_scan[k];
+    uint32_t tri_base = tri_start + nt_scan[k];
+    const uint32_t* slots = plan + (size_t)k * 8;
+    // kept for refits: the node's BVH2 subtree and its children in slot order
+    node_ref[level_start + k] = lvl[k];
+    for (int sl = 0; sl < 8; sl++) node_plan[(size_t)(level_start + k) * 8 + sl] = slots[sl];
+    uint32_t e3, qlo[3][2], qhi[3][2];
+    quantize_node(nb, slots, bvh2, order, tribox, e3, qlo, qhi);
+    uint32_t imask = 0, meta[2] = {0, 0};
+    uint32_t toff = 0, rank = 0;
+    for (int sl = 0; sl < 8; sl++) {
+        uint32_t c = slots[sl];
+        if (c == 0xffffffffu) continue;
+        Ref cb = load_ref(c, bvh2, order, tribox);
+        int wsel = sl >> 2, sh = (sl & 3) * 8;
         if (cb.count > (uint32_t)kLeafMax) {
             imask |= 1u << sl;
             meta[wsel] |= 0x80u << sh;
@@ -493,12 +515,46 @@ __global__ void k_collapse_emit(uint32_t m, uint32_t level_start, uint32_t tri_s
     }
     Node8 nd;
     nd.q[0] = make_uint4(__float_as_uint(nb.lo[0]), __float_as_uint(nb.lo[1]), __float_as_uint(nb.lo[2]),
-                         e[0] | (e[1] << 8) | (e[2] << 16) | (imask << 24));
+                         e3 | (imask << 24));
     nd.q[1] = make_uint4(child_base, tri_base, meta[0], meta[1]);
     nd.q[2] = make_uint4(qlo[0][0], qlo[0][1], qlo[1][0], qlo[1][1]);
     nd.q[3] = make_uint4(qlo[2][0], qlo[2][1], qhi[0][0], qhi[0][1]);
     nd.q[4] = make_uint4(qhi[1][0], qhi[1][1], qhi[2][0], qhi[2][1]);
     nodes[level_start + k] = nd;
+}
+
+// Refit: the same topology, slot order and child/triangle bases; only the
+// node origin, exponents and quantised child boxes are recomputed from the
+// refitted binary tree.
+__global__ void k_requantize(uint32_t n_nodes, const uint32_t* __restrict__ node_ref,
+                             const uint32_t* __restrict__ node_plan, const uint32_t* __restrict__ bvh2,
+                             const uint32_t* __restrict__ order, const float* __restrict__ tribox,
+                             Node8* __restrict__ nodes) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_nodes) return;
+    Ref nb = load_ref(node_ref[k], bvh2, order, tribox);
+    uint32_t e3, qlo[3][2], qhi[3][2];
+    quantize_node(nb, node_plan + (size_t)k * 8, bvh2, order, tribox, e3, qlo, qhi);
+    Node8& nd = nodes[k];
+    const uint32_t imask = nd.q[0].w >> 24;
+    nd.q[0] = make_uint4(__float_as_uint(nb.lo[0]), __float_as_uint(nb.lo[1]), __float_as_uint(nb.lo[2]),
+                         e3 | (imask << 24));
+    nd.q[2] = make_uint4(qlo[0][0], qlo[0][1], qlo[1][0], qlo[1][1]);
+    nd.q[3] = make_uint4(qlo[2][0], qlo[2][1], qhi[0][0], qhi[0][1]);
+    nd.q[4] = make_uint4(qhi[1][0], qhi[1][1], qhi[2][0], qhi[2][1]);
+}
+
+// packed triangles take their (new) world vertices by the id they carry
+__global__ void k_repack_tris(uint32_t n, const float4* __restrict__ world, float4* __restrict__ tris) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4* t = tris + (size_t)i * 3;
+    const uint32_t id = __float_as_uint(t[0].w);
+    float4 v0 = world[(size_t)id * 3], v1 = world[(size_t)id * 3 + 1], v2 = world[(size_t)id * 3 + 2];
+    v0.w = __uint_as_float(id);
+    v1.w = 0.f;
+    v2.w = 0.f;
+    t[0] = v0; t[1] = v1; t[2] = v2;
 }
 
 // ---------------------------------------------------------------------------------
@@ -540,7 +596,9 @@ int bvh_build_impl(HyCtx* c, HyBvhStats* st) {
         (rc = ctx_alloc(c, c->lvl_ref[0], (size_t)n * 4)) || (rc = ctx_alloc(c, c->lvl_ref[1], (size_t)n * 4)) ||
         (rc = ctx_alloc(c, c->plan, (size_t)n * 32)) || (rc = ctx_alloc(c, c->ni, (size_t)n * 4)) ||
         (rc = ctx_alloc(c, c->nt, (size_t)n * 4)) || (rc = ctx_alloc(c, c->ni_scan, (size_t)n * 4)) ||
-        (rc = ctx_alloc(c, c->nt_scan, (size_t)n * 4)))
+        (rc = ctx_alloc(c, c->nt_scan, (size_t)n * 4)) ||
+        (rc = ctx_alloc(c, c->node_ref, (size_t)std::max<uint32_t>(n, 1) * 4)) ||
+        (rc = ctx_alloc(c, c->node_plan, (size_t)std::max<uint32_t>(n, 1) * 32)))
         return rc;
     cudaStream_t s = c->stream;
     int* bnd = c->bounds.as<int>();
@@ -588,7 +646,8 @@ int bvh_build_impl(HyCtx* c, HyBvhStats* st) {
                                                      c->ni_scan.as<uint32_t>(), c->nt_scan.as<uint32_t>(), bvh2, ord,
                                                      c->tribox.as<float>(), c->world.as<float4>(),
                                                      c->nodes.as<Node8>(), c->tris.as<float4>(),
-                                                     c->lvl_ref[lv ^ 1].as<uint32_t>());
+                                                     c->lvl_ref[lv ^ 1].as<uint32_t>(), c->node_ref.as<uint32_t>(),
+                                                     c->node_plan.as<uint32_t>());
         HY_CUDA_TRY(cudaGetLastError());
         uint32_t h_tot[2];
         HY_CUDA_TRY(cudaMemcpyAsync(h_tot, tot, 8, cudaMemcpyDeviceToHost, s));
@@ -634,8 +693,24 @@ int bvh_build_impl(HyCtx* c, HyBvhStats* st) {
 // the binary tree and re-encodes every 8-wide node and triangle record level by
 // level with the stored plan of the last build.
 int bvh_refit_impl(HyCtx* c) {
-    (void)c;
-    return HY_ERR_UNSUPPORTED;
+    const uint32_t n = c->ntri;
+    int rc;
+    cudaStream_t s = c->stream;
+    if ((rc = world_tris_impl(c))) return rc;
+    if (n > 1) {
+        HY_CUDA_TRY(cudaMemsetAsync(c->flags.p, 0, (size_t)n * 4, s));
+        k_refit<<<cdiv(n, 256), 256, 0, s>>>(c->vals[0].as<uint32_t>(), c->tribox.as<float>(), n,
+                                             c->bvh2.as<uint32_t>(), c->parent.as<uint32_t>(),
+                                             c->flags.as<uint32_t>());
+    }
+    k_requantize<<<cdiv(c->n_bvh8, 128), 128, 0, s>>>(c->n_bvh8, c->node_ref.as<uint32_t>(),
+                                                      c->node_plan.as<uint32_t>(), c->bvh2.as<uint32_t>(),
+                                                      c->vals[0].as<uint32_t>(), c->tribox.as<float>(),
+                                                      c->nodes.as<Node8>());
+    k_repack_tris<<<cdiv(n, 256), 256, 0, s>>>(n, c->world.as<float4>(), c->tris.as<float4>());
+    HY_CUDA_TRY(cudaGetLastError());
+    HY_CUDA_TRY(cudaStreamSynchronize(s));
+    return HY_OK;
 }
 
 }  // namespace hy

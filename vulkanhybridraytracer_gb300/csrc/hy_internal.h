@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/hybridrt.h"
 
@@ -55,6 +56,7 @@ struct HyCtx {
     hy::DevBuf lvl_ref[2], plan, ni, nt, ni_scan, nt_scan;
     hy::DevBuf scan_tmp, hist, total;
     hy::DevBuf nodes, tris;
+    hy::DevBuf node_ref, node_plan;  // per BVH8 node: its BVH2 subtree, its 8 slot children (refits)
     uint32_t n_bvh8 = 0, depth = 0;
     bool bvh_ok = false;
     HyBvhStats last_build{};
@@ -66,6 +68,14 @@ struct HyCtx {
     hy::DevBuf host_in[6], host_out_f, host_out_8;  // device staging of hy_hybrid_forward_host
     uint32_t* h_status = nullptr;   // pinned readback slot
     unsigned long long* h_stats = nullptr;
+
+    // ---- batches ----
+    hy::DevBuf batch_tab;           // PassParams[num_views] + SceneDev[num_scenes]
+    void* h_batch_tab = nullptr;    // pinned mirror, copied in by the captured graph
+    size_t h_batch_tab_bytes = 0;
+    cudaGraphExec_t batch_exec = nullptr;
+    std::vector<uint64_t> batch_key;
+    cudaEvent_t batch_done = nullptr;
 };
 
 namespace hy {

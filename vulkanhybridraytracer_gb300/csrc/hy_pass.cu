@@ -133,7 +133,7 @@ __device__ Payload closest_hit(const SceneDev& S, const PassParams& P, const Hit
     float dirw = 0.f;
     f3 Lo = mk(0.f, 0.f, 0.f);
     float attenuation = 1.0f;
-    for (uint32_t i = 0; i < S.num_lights; i++) {
+    for (uint32_t i = 0; i < P.num_lights; i++) {
         const HyLight lt = S.lights[i];
         bool isDir = lt.pos[3] < 0.f;
         f3 lp = mk(lt.pos[0], lt.pos[1], lt.pos[2]);
@@ -253,7 +253,7 @@ __device__ __forceinline__ void do_pixel(const SceneDev& S, const PassParams& P,
     f3 rayColor = mk(0.f, 0.f, 0.f);
     float attenuation = 1.0f;
 
-    for (uint32_t i = 0; i < S.num_lights; i++) {
+    for (uint32_t i = 0; i < P.num_lights; i++) {
         const HyLight lt = S.lights[i];
         const LightGeo lg = light_geo(lt, position, N);
         const size_t li = i * plane + pix;
@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(128, MINB) k_shadow(const SceneDev S, const Pa
         if (has_px && !live) {
             for (;;) {
                 if (s.setup) {
-                    if (s.light >= S.num_lights) { has_px = false; break; }
+                    if (s.light >= P.num_lights) { has_px = false; break; }
                     const HyLight lt = S.lights[s.light];
                     const LightGeo lg = light_geo(lt, s.position, s.N);
                     s.L = lg.L;
@@ -552,7 +552,7 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, co
         // ---- light set-up (group-uniform) ----
         if (has_px && s.setup) {
             for (;;) {
-                if (s.light >= S.num_lights) { has_px = false; break; }
+                if (s.light >= P.num_lights) { has_px = false; break; }
                 const HyLight lt = S.lights[s.light];
                 const LightGeo lg = light_geo(lt, s.position, s.N);
                 float v = -1.f;
@@ -740,6 +740,206 @@ __global__ void __launch_bounds__(128) k_gbuffer(const SceneDev S, const GbufPar
 }
 
 // ---------------------------------------------------------------------------------
+// Batches: many views of several scenes in one persistent launch.  The global
+// queue hands out (view, 8x4 tile) units; a warp finishes its tile before it
+// takes the next one, so lane-group size (from the view's spp), scene and
+// G-buffer stay uniform across the warp while different warps work on
+// different views.  REFERENCE views run with one lane per pixel (their
+// samples are one ray), DECORRELATED views with spp lanes per pixel-light.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t view_of_tile(const uint32_t* s_begin, uint32_t nviews, uint32_t tile) {
+    uint32_t lo = 0, hi = nviews;  // s_begin[lo] <= tile < s_begin[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (s_begin[mid] <= tile) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void finalize_rt(const PassParams& P, bool accum, const ShadowLane& s, size_t plane,
+                                            float v) {
+    if (accum) shadow_finalize<true>(P, s, plane, v);
+    else shadow_finalize<false>(P, s, plane, v);
+}
+
+template <bool COUNT, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_shadow_batch(const BatchParams B) {
+    __shared__ uint32_t s_begin[kMaxBatchViews + 1];
+    for (uint32_t i = threadIdx.x; i <= B.nviews; i += blockDim.x)
+        s_begin[i] = i < B.nviews ? B.views[i].tile_begin : B.total_tiles;
+    __syncthreads();
+    LaneStats ls;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    uint2 stk[kStackMax];
+    ShadowLane s;
+    Trav t;
+    RayPre r;
+    bool has_px = false, live = false;
+    uint32_t rays_before = 0, seed0 = 0, nn = 0, nt = 0;
+    // warp-uniform: the current unit and its view's parameters
+    uint32_t slot_cur = 0, slot_end = 0, chunk_cur = 0, chunk_end = 0;
+    uint32_t G = 1, g = 0, base = lane, gmask = 1u << lane, spp = 1, nrays = 1;
+    uint32_t cur_view = 0xffffffffu, pending = 0xffffffffu;
+    bool reference = true, accum = false, queue_empty = false;
+    size_t plane = 0;
+    const PassParams* P = B.views;
+    const SceneDev* S = B.scenes;
+    for (;;) {
+        // ---- the next unit once the current tile is handed out and every lane is
+        //      idle: a warp's lanes stay on one 8x4 tile (coherent rays), and group
+        //      size and G-buffer may change with the view.  (Letting a warp run
+        //      into its next tile early measured 4 % slower: with one tile per
+        //      pull that tile lies far away in the image.) ----
+        if (slot_cur == slot_end && __ballot_sync(0xffffffffu, has_px) == 0) {
+            if (pending == 0xffffffffu && !queue_empty) {
+                if (chunk_cur == chunk_end) {
+                    uint32_t t0 = 0;
+                    if (lane == 0) t0 = atomicAdd(B.queue, B.chunk);
+                    t0 = __shfl_sync(0xffffffffu, t0, 0);
+                    if (t0 >= B.total_tiles) queue_empty = true;
+                    else { chunk_cur = t0; chunk_end = min(t0 + B.chunk, B.total_tiles); }
+                }
+                if (!queue_empty) pending = chunk_cur++;
+            }
+            const bool idle = __ballot_sync(0xffffffffu, has_px) == 0;
+            if (pending == 0xffffffffu) {
+                if (idle) break;  // queue drained, every lane done
+            } else {
+                const uint32_t v = view_of_tile(s_begin, B.nviews, pending);
+                if (v != cur_view && idle) {
+                    cur_view = v;
+                    P = B.views + v;
+                    S = B.scenes + P->scene;
+                    reference = P->rng_mode == HY_RNG_REFERENCE;
+                    spp = P->spp;
+                    nrays = reference ? 1u : spp;
+                    G = P->group;
+                    g = lane & (G - 1);
+                    base = lane & ~(G - 1);
+                    gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << base;
+                    accum = !(P->flags & HY_FLAG_NO_ACCUM) && P->accum_frame > 0;
+                    plane = (size_t)P->W * P->H;
+                }
+                if (v == cur_view) {
+                    slot_cur = (pending - P->tile_begin) * 32;
+                    slot_end = slot_cur + 32;
+                    pending = 0xffffffffu;
+                }
+            }
+        }
+        // ---- idle groups take the tile's next pixel ----
+        uint32_t need = __ballot_sync(0xffffffffu, g == 0 && !has_px);
+        while (need && slot_cur < slot_end) {
+            const uint32_t take = min((uint32_t)__popc(need), slot_end - slot_cur);
+            const uint32_t rank = __popc(need & lt_mask);
+            const uint32_t my_slot = (g == 0 && !has_px && rank < take) ? slot_cur + rank : 0xffffffffu;
+            const uint32_t slot = __shfl_sync(0xffffffffu, my_slot, base);
+            if (slot != 0xffffffffu) {
+                const uint32_t tl = slot >> 5, l = slot & 31;
+                const uint32_t x = (tl % P->tiles_x) * 8 + (l & 7), y = (tl / P->tiles_x) * 4 + (l >> 3);
+                if (x < P->W && y < P->H) {
+                    has_px = true;
+                    s.pix = y * P->W + x;
+                    const float4 g0 = fetch_texel(P->plane[0], P->fmt[0], s.pix);
+                    const float4 g1 = fetch_texel(P->plane[1], P->fmt[1], s.pix);
+                    s.position = mk(g0.x, g0.y, g0.z);
+                    s.N = normalize_rn(mk(__fsub_rn(__fmul_rn(g1.x, 2.0f), 1.0f), __fsub_rn(__fmul_rn(g1.y, 2.0f), 1.0f),
+                                          __fsub_rn(__fmul_rn(g1.z, 2.0f), 1.0f)));
+                    const int mi = mat_index(g0.w, S->num_mats);
+                    s.smode = mi >= 0 ? (int)S->mats[mi].smr[0] : 0;
+                    seed0 = tea(s.pix, P->frame_u);
+                    rays_before = 0;
+                    s.light = 0;
+                    s.setup = true;
+                    s.in_blur = x < P->blur_w && y < P->blur_h;
+                }
+            }
+            slot_cur += take;
+            need = __ballot_sync(0xffffffffu, g == 0 && !has_px);
+        }
+        // ---- light set-up (group-uniform) ----
+        if (has_px && s.setup) {
+            for (;;) {
+                if (s.light >= P->num_lights) { has_px = false; break; }
+                const HyLight lt = S->lights[s.light];
+                const LightGeo lg = light_geo(lt, s.position, s.N);
+                float v = -1.f;
+                if (s.smode == 4) v = 1.0f;
+                else if (!(lg.NdotL > 0.f)) v = 0.0f;
+                else if (!(lg.dist < lg.maxd)) v = 1.0f;
+                if (v >= 0.f) {
+                    if (g == 0) finalize_rt(*P, accum, s, plane, v);
+                    s.light++;
+                    continue;
+                }
+                s.L = lg.L;
+                s.dist = lg.dist;
+                s.radius = lt.radius;
+                s.k = g;
+                s.sf = 0.f;
+                s.setup = false;
+                break;
+            }
+        }
+        // ---- this lane's next sample ----
+        if (has_px && !s.setup && !live && s.k < nrays) {
+            uint32_t sd = reference ? seed0 : lcg_jump(seed0, 2u * (rays_before + s.k));
+            const f3 dir = sampleDisk(s.radius, s.position, s.L, sd);
+            r = ray_pre(add_rn(s.position, scale_rn(dir, 1e-1f)), dir);
+            trav_init(t, r, __fadd_rn(s.dist, 1.0f));
+            s.k += G;
+            live = true;
+            ls.shadow++;
+        }
+        // ---- one node visit ----
+        if (live) {
+            if (trav_step<true, COUNT>(*S, r, 0.001f, t, stk, nn, nt, P->status)) {
+                live = false;
+                if (t.h.id == HY_NO_HIT) s.sf = __fadd_rn(s.sf, 1.0f);
+            }
+        }
+        // ---- groups whose samples are all in fold them into the light's factor ----
+        const uint32_t busy = __ballot_sync(0xffffffffu, has_px && !s.setup && (live || s.k < nrays));
+        if (has_px && !s.setup && (busy & gmask) == 0) {
+            const uint32_t unocc = __reduce_add_sync(gmask, (uint32_t)s.sf);
+            const float v = reference ? (float)unocc : __fdiv_rn((float)unocc, (float)spp);
+            if (g == 0) finalize_rt(*P, accum, s, plane, v);
+            rays_before += spp;
+            s.light++;
+            s.setup = true;
+        }
+    }
+    if (COUNT) { ls.nodes += nn; ls.tris += nt; }
+    flush_stats(ls, B.stats);
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_pixels_batch(const BatchParams B) {
+    __shared__ uint32_t s_begin[kMaxBatchViews + 1];
+    for (uint32_t i = threadIdx.x; i <= B.nviews; i += blockDim.x)
+        s_begin[i] = i < B.nviews ? B.views[i].tile_begin : B.total_tiles;
+    __syncthreads();
+    LaneStats ls;
+    const uint32_t lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t t0 = 0;
+        if (lane == 0) t0 = atomicAdd(B.queue, B.chunk);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= B.total_tiles) break;
+        const uint32_t t1 = min(t0 + B.chunk, B.total_tiles);
+        for (uint32_t tile = t0; tile < t1; tile++) {
+            const PassParams& P = B.views[view_of_tile(s_begin, B.nviews, tile)];
+            const uint32_t tl = tile - P.tile_begin;
+            const uint32_t x = (tl % P.tiles_x) * 8 + (lane & 7), y = (tl / P.tiles_x) * 4 + (lane >> 3);
+            if (x < P.W && y < P.H) do_pixel<MODE_SHADE, COUNT>(B.scenes[P.scene], P, x, y, ls);
+        }
+    }
+    flush_stats(ls, B.stats);
+}
+
+// ---------------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------------
 template <bool GROUP, bool ACCUM, int MINB>
@@ -796,6 +996,21 @@ cudaError_t launch_gbuffer(const SceneDev& S, const GbufParams& G, cudaStream_t 
     dim3 b(16, 8), g((G.W + 15) / 16, (G.H + 7) / 8);
     k_gbuffer<<<g, b, 0, s>>>(S, G);
     return cudaGetLastError();
+}
+
+static void* batch_kernel(bool shade, bool count, int minb) {
+    if (shade) return count ? (void*)k_pixels_batch<true> : (void*)k_pixels_batch<false>;
+    if (minb >= 8) return count ? (void*)k_shadow_batch<true, 8> : (void*)k_shadow_batch<false, 8>;
+    return count ? (void*)k_shadow_batch<true, 5> : (void*)k_shadow_batch<false, 5>;
+}
+
+cudaError_t launch_batch(bool shade, bool count, int minb, const BatchParams& B, int grid, cudaStream_t s) {
+    void* args[] = {(void*)&B};
+    return cudaLaunchKernel(batch_kernel(shade, count, minb), dim3(grid), dim3(128), args, 0, s);
+}
+
+cudaError_t batch_occupancy(bool shade, bool count, int minb, int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, batch_kernel(shade, count, minb), 128, 0);
 }
 
 }  // namespace hy

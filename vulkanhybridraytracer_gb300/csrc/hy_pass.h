@@ -29,6 +29,21 @@ struct PassParams {
     unsigned long long* stats;
     uint32_t* status;
     uint32_t* queue;
+    // batches: the view's scene and its first tile in the batch's global tile range
+    uint32_t scene, tile_begin;
+    uint32_t num_lights;     // the pass uses the scene's first num_lights lights
+};
+
+// A batch: a device table of per-view PassParams over a device table of
+// scenes; persistent warps pull (view, tile) units from one global queue.
+constexpr uint32_t kMaxBatchViews = 1024;
+struct BatchParams {
+    const PassParams* views;
+    const SceneDev* scenes;
+    uint32_t nviews, total_tiles, chunk;
+    unsigned long long* stats;
+    uint32_t* status;
+    uint32_t* queue;
 };
 
 struct AccumParams {
@@ -56,5 +71,7 @@ cudaError_t launch_accumulate(const AccumParams& A, cudaStream_t s);
 cudaError_t launch_trace(const SceneDev& S, const HyRay* rays, uint32_t n, bool any, bool count, HyHit* hits,
                          unsigned long long* stats, uint32_t* status, int grid, cudaStream_t s);
 cudaError_t launch_gbuffer(const SceneDev& S, const GbufParams& G, cudaStream_t s);
+cudaError_t launch_batch(bool shade, bool count, int minb, const BatchParams& B, int grid, cudaStream_t s);
+cudaError_t batch_occupancy(bool shade, bool count, int minb, int* blocks_per_sm);
 
 }  // namespace hy

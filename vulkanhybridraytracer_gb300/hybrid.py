@@ -117,6 +117,11 @@ class HybridContext:
                 "depth": st.depth, "build_ms": st.build_ms, "scene_lo": list(st.scene_lo),
                 "scene_hi": list(st.scene_hi)}
 
+    def refit_bvh(self, transforms: np.ndarray):
+        """New column-major transforms, same topology (the per-frame TLAS update)."""
+        xf = np.ascontiguousarray(transforms, np.float32).reshape(-1, 16)
+        L.check(self.lib.hy_bvh_refit(self.h, _np_ptr(xf), len(xf)), "bvh_refit")
+
     def download_bvh(self, n_bvh8: int):
         n = self.num_tris
         morton = np.zeros(n, np.uint32)
@@ -160,7 +165,8 @@ class HybridContext:
         return L.HyAccum(fmt, hist.shape[0], hist.data_ptr())
 
     def forward(self, planes, cam36, cfg: L.HyPassConfig, hist, fmt=L.HY_ACCUM_U8, out_f=None, out_8=None,
-                formats=GBUF_FP32_FORMATS):
+                formats=GBUF_FP32_FORMATS, stats: bool = True):
+        """hy_hybrid_forward.  stats=False with HY_FLAG_NO_STATUS_SYNC in cfg returns without a host sync."""
         h, w = planes[0].shape[0], planes[0].shape[1]
         gb = gbuffer_struct(planes, w, h, formats)
         cam = camera_struct(cam36)
@@ -169,7 +175,7 @@ class HybridContext:
         L.check(self.lib.hy_hybrid_forward(self.h, C.byref(gb), C.byref(cam), C.byref(cfg), C.byref(acc),
                                            C.c_void_p(out_f.data_ptr()) if out_f is not None else None,
                                            C.c_void_p(out_8.data_ptr()) if out_8 is not None else None,
-                                           C.byref(st)), "hybrid_forward")
+                                           C.byref(st) if stats else None), "hybrid_forward")
         return st.as_dict()
 
     def forward_host(self, planes_np, cam36, cfg, hist, fmt=L.HY_ACCUM_U8, out_f=None, out_8=None,
@@ -213,6 +219,34 @@ class HybridContext:
                                        C.c_void_p(out_f.data_ptr()) if out_f is not None else None,
                                        C.c_void_p(out_8.data_ptr()) if out_8 is not None else None,
                                        C.byref(st)), "shade_pass")
+        return st.as_dict()
+
+    def batch_forward(self, scenes, views, graph: bool = True, tuning: L.HyPassConfig | None = None,
+                      sync: bool = True):
+        """One batch of views over scene contexts (hy_batch_forward).
+
+        views: list of dicts with keys scene, planes, camera (36 floats), config
+        (HyPassConfig), hist, fmt and optionally out_f / out_8 (device tensors).
+        """
+        arr = (C.c_void_p * len(scenes))(*[s.h.value for s in scenes])
+        vs = (L.HyView * len(views))()
+        keep = []
+        for i, v in enumerate(views):
+            planes = v["planes"]
+            h, w = planes[0].shape[0], planes[0].shape[1]
+            vs[i].scene = v["scene"]
+            vs[i].gbuffer = gbuffer_struct(planes, w, h, v.get("formats", GBUF_FP32_FORMATS))
+            vs[i].camera = camera_struct(v["camera"])
+            vs[i].config = v["config"]
+            vs[i].accum = self._accum(v["hist"], v.get("fmt", L.HY_ACCUM_U8))
+            vs[i].out_rgba32f = v["out_f"].data_ptr() if v.get("out_f") is not None else None
+            vs[i].out_bgra8 = v["out_8"].data_ptr() if v.get("out_8") is not None else None
+            keep.append(planes)
+        flags = (0 if graph else L.HY_BATCH_NO_GRAPH) | (0 if sync else L.HY_BATCH_NO_STATUS_SYNC)
+        st = L.HyStats()
+        L.check(self.lib.hy_batch_forward(self.h, arr, len(scenes), vs, len(views), flags,
+                                          C.byref(tuning) if tuning is not None else None,
+                                          C.byref(st) if sync else None), "batch_forward")
         return st.as_dict()
 
     def synchronize(self):

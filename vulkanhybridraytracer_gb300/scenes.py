@@ -240,3 +240,50 @@ def diff(seed: int = 3, width: int = 512, height: int = 512) -> Workload:
     sc.camera = Camera((0.0, 8.0, 16.0), (0.0, 0.0, 0.0), 60.0)
     sc.env = [env_map(rng), env_map(rng, sun=False)]
     return Workload("diff-512x512-82k", sc, width, height, 16, 1, 1)
+
+
+# ---- the mixed batch ------------------------------------------------------------------
+BATCH_RESOLUTIONS = ((320, 240), (640, 480), (1280, 720), (1920, 1080))
+BATCH_SPP = (1, 4, 16, 64)
+
+
+def batch_scene(rng: np.random.Generator, n_tris: int) -> Scene:
+    """A terrain + icosphere scene built like the 1080p one with about n_tris
+    triangles (35 % terrain, 65 % spheres of 5,120 triangles), 256 materials
+    and 8 area lights (a view uses the first 1..8)."""
+    sc = Scene()
+    n_ter = max(8, int(round(np.sqrt(0.35 * n_tris / 2.0))) + 1)
+    ter, _ = terrain(rng, n_ter)
+    sc.materials = random_materials(rng, 256)
+    sc.entities.append(Object(ter, int(rng.integers(256)), trs()))
+    ico = icosphere(4)
+    for _ in range(max(1, int(round(0.65 * n_tris / ico.num_tris)))):
+        s = rng.uniform(0.5, 3.0)
+        x, z = rng.uniform(-40, 40), rng.uniform(-40, 40)
+        sc.entities.append(Object(ico, int(rng.integers(256)), trs((x, s + 1.0, z), s)))
+    sc.lights = [Light(POINT_LIGHT, (1, 1, 1), (rng.uniform(-30, 30), rng.uniform(8, 16), rng.uniform(-30, 30)),
+                       float(rng.uniform(10, 50)), 500.0, 0.5) for _ in range(8)]
+    sc.env = [env_map(rng), env_map(rng, sun=False)]
+    return sc
+
+
+def batch(seed: int = 2, n_scenes: int = 8, n_views: int = 64, tri_range=(50_000, 2_000_000)):
+    """64 views over 8 scenes: triangle counts log-uniform in [50k, 2M],
+    resolution uniform in {320x240, 640x480, 1280x720, 1920x1080}, shadow spp
+    uniform in {1, 4, 16, 64} (DECORRELATED), light count uniform in [1, 8],
+    cameras on a ring around each scene.  Returns (scenes, view specs); a view
+    spec holds scene, width, height, spp, lights, camera (Camera)."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log(tri_range[0]), np.log(tri_range[1])
+    counts = np.exp(rng.uniform(lo, hi, n_scenes)).astype(int)
+    scs = [batch_scene(rng, int(n)) for n in counts]
+    views = []
+    for _ in range(n_views):
+        si = int(rng.integers(n_scenes))
+        w, h = BATCH_RESOLUTIONS[int(rng.integers(len(BATCH_RESOLUTIONS)))]
+        spp = BATCH_SPP[int(rng.integers(len(BATCH_SPP)))]
+        nl = int(rng.integers(1, 9))
+        ang = rng.uniform(0, 2 * np.pi)
+        cam = Camera((55.0 * np.sin(ang), float(rng.uniform(12, 24)), 55.0 * np.cos(ang)), (0.0, 0.0, 0.0), 60.0)
+        views.append(dict(scene=si, width=w, height=h, spp=spp, lights=nl, camera=cam))
+    return scs, views
