@@ -46,8 +46,9 @@ def parse():
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--minb", type=int, default=0, help="shadow-kernel variant: resident blocks per SM")
-    ap.add_argument("--workload", default="hd", choices=["hd", "batch"],
-                    help="hd: the 1080p frame (headline); batch: 64 mixed views over 8 scenes, batched vs per view")
+    ap.add_argument("--workload", default="hd", choices=["hd", "batch", "diff"],
+                    help="hd: the 1080p frame (headline); batch: 64 mixed views over 8 scenes, batched vs per "
+                         "view; diff: 512x512 forward + adjoint")
     ap.add_argument("--views", type=int, default=64)
     return ap.parse_args()
 
@@ -192,6 +193,76 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_diff(args):
+    """Differentiable form: 512x512, 64 icospheres (subdivision 3), 64 materials, 8 point
+    lights, 16 shadow samples; L2 loss against a target rendered from parameters perturbed
+    by N(0, 0.05).  Forward = G-buffer + shadow pass + shading at the current parameters;
+    backward = hy_hybrid_backward (visibility held fixed)."""
+    import torch
+
+    from vulkanhybridraytracer_gb300 import diffrender, scenes
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    wl = scenes.diff(3, 512, 512)
+    r = diffrender.DiffRenderer(wl.scene, wl.camera(0.0), wl.width, wl.height, spp=wl.spp,
+                                max_bounces=wl.max_bounces)
+    mp0, lp0 = r.params0
+    rng = np.random.default_rng(3)
+    mp_t = np.clip(mp0 + rng.normal(0, 0.05, mp0.shape), 0.0, 1.0).astype(np.float32)
+    lp_t = (lp0 + rng.normal(0, 0.05, lp0.shape)).astype(np.float32)
+    target, _ = r.render(mp_t, lp_t)
+    target = target.clone()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def step(timed):
+        r.set_params(mp0, lp0)
+        flush.zero_()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        e[0].record(stream)
+        planes = r.ctx.gbuffer(r.cam, r.W, r.H)
+        shadow = torch.zeros((r.ctx.num_lights, r.H, r.W), dtype=torch.float32, device=dev)
+        r.ctx.shadow_pass(planes, r.cam, r.cfg, shadow, r.fmt)
+        img = torch.empty((r.H, r.W, 4), dtype=torch.float32, device=dev)
+        r.ctx.shade_pass(planes, r.cam, r.cfg, shadow, r.fmt, out_f=img)
+        e[1].record(stream)
+        grad = 2.0 * (img - target)
+        grad[..., 3] = 0.0
+        e[2].record(stream)
+        gm, gl, st = r.backward((planes, shadow), grad)
+        e[3].record(stream)
+        torch.cuda.synchronize()
+        return e[0].elapsed_time(e[1]), e[2].elapsed_time(e[3]), st, float(((img - target)[..., :3] ** 2).sum())
+
+    for _ in range(args.warmup):
+        step(False)
+    fw, bw = [], []
+    clocks = Clocks(0)
+    clocks.start()
+    for _ in range(args.steps):
+        f, b, st, loss = step(True)
+        fw.append(f)
+        bw.append(b)
+    clk = clocks.stop()
+    f_ms, b_ms = float(np.mean(fw)), float(np.mean(bw))
+    line = {"metric": "hybrid_backward_ms", "value": b_ms, "unit": "ms", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": b_ms, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": wl.name, "width": wl.width, "height": wl.height,
+                       "triangles": wl.scene.num_tris, "materials": len(wl.scene.materials),
+                       "lights": len(wl.scene.lights), "shadow_spp": wl.spp, "max_bounces": wl.max_bounces,
+                       "params": len(wl.scene.materials) * 5 + len(wl.scene.lights) * 4,
+                       "loss": "L2 vs target rendered from params + N(0, 0.05)",
+                       "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MB write)"},
+            "forward_ms": f_ms, "backward_over_forward": b_ms / f_ms,
+            "backward_rays": {"reflection_rays": st["reflection_rays"], "hit_shadow_rays": st["hit_shadow_rays"]},
+            "loss": loss, "clocks": clk, "gpu_launches": 2}
+    print(json.dumps(line))
+    r.close()
+
+
 def run_batch(args):
     """64 views over 8 scenes (50k-2M triangles, 320x240..1920x1080, spp 1/4/16/64,
     1-8 lights): the views one by one through hy_hybrid_forward, then as one
@@ -292,14 +363,16 @@ def main():
     if args.workload == "batch":
         run_batch(args)
         return
+    if args.workload == "diff":
+        run_diff(args)
+        return
     import torch
 
-    ws, rank, local = dist_env()
-    if ws > 1:
-        import torch.distributed as dist
+    from vulkanhybridraytracer_gb300 import replicas
 
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    ws, rank, local = replicas.env()
     torch.cuda.set_device(local)
+    replicas.init()  # replicas: each rank renders its own frames, no data-path collective
     dev = torch.device("cuda", local)
     from vulkanhybridraytracer_gb300 import _lib as L
     from vulkanhybridraytracer_gb300.hybrid import HybridContext, pass_config
@@ -328,6 +401,11 @@ def main():
     st_plain = ctx.forward(planes, wl.camera(1.0), cfg(1, 0), hist.clone(), L.HY_ACCUM_U8, out_f=out_f,
                            out_8=out_8)
     rays = st_plain["shadow_rays"] + st_plain["reflection_rays"] + st_plain["hit_shadow_rays"]
+    # the shadow kernel's own traversal counts (same rays as the fused frame)
+    shadow_tmp = torch.empty((len(wl.scene.lights), wl.height, wl.width), dtype=torch.uint8, device=dev)
+    st_shadow = ctx.shadow_pass(planes, wl.camera(1.0), cfg(1, L.HY_FLAG_COUNT_TRAVERSAL), shadow_tmp,
+                                L.HY_ACCUM_U8)
+    del shadow_tmp
 
     frame = 0
     for _ in range(args.warmup):
@@ -336,10 +414,10 @@ def main():
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     step_rays = []
-    if ws > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     torch.cuda.synchronize()
     clocks = Clocks(local)
+    ctx.profile(True)  # CUDA events around each kernel launch, on the library's (= torch's) stream
     clocks.start()
     t_wall = time.perf_counter()
     for k in range(args.steps):
@@ -352,35 +430,54 @@ def main():
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall
     clk = clocks.stop()
+    kernels = ctx.profile_read()
+    ctx.profile(False)
     ms = [a.elapsed_time(b) for a, b in ev]
-    t_dev = sum(ms) / 1e3
-    if ws > 1:
-        t = torch.tensor([t_dev], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
-    total_rays = rays * args.steps * ws
-    value = total_rays / t_dev / 1e6
+    t_dev = replicas.max_over_ranks(sum(ms) / 1e3, dev)
+    value = replicas.throughput(rays * args.steps, t_dev, ws) / 1e6
     ms_per_step = t_dev * 1e3 / args.steps
 
-    # roofline: algorithmic bytes per launch / launch time (the fused pass kernel)
+    # roofline of each kernel: algorithmic bytes per launch (48 B per ray record, 80 B per BVH8 node
+    # visited, 48 B per triangle tested, plus the compulsory pixel I/O) / its average launch time
     npx = wl.width * wl.height
     L_ = len(wl.scene.lights)
-    alg_bytes = (rays * (32 + 16) + 80 * st_count["nodes_visited"] + 48 * st_count["tris_tested"]
-                 + npx * (88 + 16 + 4 + 2 * L_))
-    achieved = alg_bytes / (ms_per_step / 1e3) / 1e9
+    sh_rays = st_shadow["shadow_rays"]
+    sh_nodes, sh_tris = st_shadow["nodes_visited"], st_shadow["tris_tested"]
+    alg = {
+        # G-buffer planes 0/1 (32 B/px), u8 history read + write per light
+        "k_shadow_group<accum>": sh_rays * 48 + 80 * sh_nodes + 48 * sh_tris + npx * (32 + 2 * L_),
+        # all six planes (88 B/px), RGBA32F + BGRA8 out, u8 history read per light
+        "k_pixels<shade>": ((rays - sh_rays) * 48 + 80 * (st_count["nodes_visited"] - sh_nodes)
+                            + 48 * (st_count["tris_tested"] - sh_tris) + npx * (88 + 16 + 4 + L_)),
+    }
+    alg_frame = sum(alg.values())
     peaks = {}
     try:
         peaks = json.load(open(ROOT / "MEASURED_PEAKS.json"))
     except Exception:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
+    per_kernel = {}
+    for name, k in kernels.items():
+        e = {"launches": k["launches"], "avg_ms": k["avg_ms"],
+             "share": k["total_ms"] / max(sum(x["total_ms"] for x in kernels.values()), 1e-9)}
+        if name in alg:
+            e["alg_bytes"] = alg[name]
+            e["achieved_gbs"] = alg[name] / (k["avg_ms"] / 1e3) / 1e9
+        per_kernel[name] = e
+    dom = max(kernels, key=lambda n: kernels[n]["total_ms"]) if kernels else None
+    if dom in alg:
+        achieved = per_kernel[dom]["achieved_gbs"]
+    else:  # no per-kernel record: the whole frame
+        dom = "frame"
+        achieved = alg_frame / (ms_per_step / 1e3) / 1e9
+    # DRAM bytes per launch from the committed ncu summary of the same workload
     traffic = None
-    tf = ROOT / "profiles" / "traffic_fused_hd.json"
-    if tf.exists():
-        try:
-            traffic = json.load(open(tf)).get("bytes_per_launch")
-        except Exception:
-            traffic = None
+    for f in sorted((ROOT / "profiles").glob(f"*-{wl.width}x{wl.height}_dram.md")):
+        for ln in f.read_text().splitlines():
+            parts = ln.split()
+            if len(parts) == 3 and parts[0] == "traffic_bytes_per_launch" and parts[1] == dom:
+                traffic = int(parts[2])
 
     # e2e: host G-buffer in, host BGRA8 image out, through hy_hybrid_forward_host
     planes_h = [p.cpu().pin_memory() for p in planes]
@@ -423,15 +520,15 @@ def main():
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": 1e3 * sum(e2e_t) / len(e2e_t)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_shadow (shadow rays + accumulation) and k_pixels<MODE_SHADE>, per frame",
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
+                         "frac": achieved / peak, "traffic": traffic, "kernel": dom,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
+                         "per_kernel": per_kernel,
+                         "frame": {"alg_bytes": alg_frame, "achieved": alg_frame / (ms_per_step / 1e3) / 1e9}},
             "cpu_baseline": cpu,
         }
         print(json.dumps(line))
     ctx.close()
-    if ws > 1:
-        torch.distributed.destroy_process_group()
+    replicas.finalize()
 
 
 if __name__ == "__main__":

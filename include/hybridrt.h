@@ -272,6 +272,59 @@ int hy_hybrid_forward_host(HyCtx* ctx, const HyGBuffer* h_gb, const HyCamera* ca
                            const HyPassConfig* cfg, HyAccum* accum,
                            float* h_out_rgba32f, uint8_t* h_out_bgra8, HyStats* stats);
 
+/* ---- per-kernel timing (the reference's only timer is the frame rate it
+ *      prints, src/renderer.cpp:614) ----
+ * While enabled, every kernel launch of the context's passes is bracketed by
+ * CUDA events on the context's stream (no host synchronisation).
+ * hy_profile_read waits for the stream, reports per kernel its launch count
+ * and summed device time, and clears the record; at most 4096 launches are
+ * kept between reads.  Enabling clears the record too. */
+typedef struct HyKernelTime {
+    char     kernel[40];
+    uint32_t launches;
+    float    total_ms;
+} HyKernelTime;
+int hy_profile_enable(HyCtx* ctx, int enable);
+int hy_profile_read(HyCtx* ctx, HyKernelTime* out, uint32_t capacity, uint32_t* count);
+
+/* ---- differentiation (no counterpart in the reference, whose passes are
+ *      forward only) ----
+ *
+ * hy_hybrid_backward is the adjoint of hy_shade_pass (hybridRaygen.rgen +
+ * hybridHit.rchit + miss.rmiss): given dLoss/dImage for the image that
+ * hy_shade_pass / hy_hybrid_forward produced from the same G-buffer, camera,
+ * configuration and shadow images (accum->history, exactly what the shading
+ * read), it returns the gradient of the loss with respect to
+ *   materials, HY_GRAD_MATERIAL_PARAMS floats each: diffuse[0..2] (the
+ *     shaders linearise it with pow(., 2.2)), roughness (smr[2]),
+ *     metallic (smr[1]);
+ *   lights, HY_GRAD_LIGHT_PARAMS floats each: pos[0..2] (a directional
+ *     light's direction), intensity (color[3]).
+ * Visibility is held fixed: the shadow images, which triangle each bounce ray
+ * hits and the bounce-hit shadow rays' outcomes are constants (edge and
+ * penumbra terms are not differentiated).  Branches of the shaders that
+ * switch on a light's side of the surface take the side they took in the
+ * forward pass.  The G-buffer's albedo (plane 2) and roughness/metallic
+ * (plane 4 .y/.z) are taken to be the material's own values at the texel's
+ * material index (plane 0 .w), as hy_gbuffer_primary writes them; their
+ * gradients go to that material.  Bounce rays and bounce-hit shadow rays are
+ * re-traced (nothing is stored by the forward pass).
+ *
+ * d_grad_rgba32f: device, W*H*4 floats laid out like hy_shade_pass's
+ * d_out_rgba32f (alpha ignored).  d_grad_materials (num_mats*5) and
+ * d_grad_lights (num_lights*4, the scene's light count; lights past
+ * accum->num_lights get 0) are device arrays, overwritten; either may be
+ * NULL.  cfg->max_bounces <= HY_GRAD_MAX_BOUNCES and accum->num_lights <=
+ * HY_GRAD_MAX_LIGHTS, else HY_ERR_UNSUPPORTED.  Sums over pixels use float
+ * atomics, so the last bits may vary from run to run. */
+#define HY_GRAD_MATERIAL_PARAMS 5
+#define HY_GRAD_LIGHT_PARAMS 4
+#define HY_GRAD_MAX_BOUNCES 8
+#define HY_GRAD_MAX_LIGHTS 64
+int hy_hybrid_backward(HyCtx* ctx, const HyGBuffer* gb, const HyCamera* cam, const HyPassConfig* cfg,
+                       const HyAccum* accum, const float* d_grad_rgba32f, float* d_grad_materials,
+                       float* d_grad_lights, HyStats* stats);
+
 /* ---- batches: many views of several scenes in one persistent launch ----
  *
  * Each view is one hybrid pass (its own G-buffer, camera, configuration,

@@ -242,6 +242,7 @@ struct image2D {
     void* data = nullptr;
     int w = 0, h = 0;
     bool unorm8 = true;  // R8/RGBA8 storage (first channel kept), else float
+    bool bgra8 = false;  // with unorm8: four channels stored as bytes B, G, R, A (a B8G8R8A8 image)
 };
 vec4 imageLoad(const image2D& im, const ivec2& p);
 void imageStore(image2D& im, const ivec2& p, const vec4& v);

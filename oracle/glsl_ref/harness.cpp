@@ -54,6 +54,10 @@ vec4 texture(const sampler2D& s, const vec2& uv) {
 vec4 imageLoad(const image2D& im, const ivec2& p) {
     if (!im.data || p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h) return vec4(0.f);
     size_t i = (size_t)p.y * im.w + p.x;
+    if (im.unorm8 && im.bgra8) {
+        const uint8_t* q = (const uint8_t*)im.data + i * 4;
+        return vec4((float)q[2] / 255.0f, (float)q[1] / 255.0f, (float)q[0] / 255.0f, (float)q[3] / 255.0f);
+    }
     if (im.unorm8) return vec4((float)((const uint8_t*)im.data)[i] / 255.0f, 0.f, 0.f, 1.f);
     const float* f = (const float*)im.data + i * 4;
     return vec4(f[0], f[1], f[2], f[3]);
@@ -62,6 +66,12 @@ vec4 imageLoad(const image2D& im, const ivec2& p) {
 void imageStore(image2D& im, const ivec2& p, const vec4& v) {
     if (!im.data || p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h) return;
     size_t i = (size_t)p.y * im.w + p.x;
+    auto u8 = [](float x) { return (uint8_t)std::nearbyint(std::fmin(std::fmax(x, 0.f), 1.f) * 255.0f); };
+    if (im.unorm8 && im.bgra8) {
+        uint8_t* q = (uint8_t*)im.data + i * 4;
+        q[0] = u8(v.z); q[1] = u8(v.y); q[2] = u8(v.x); q[3] = u8(v.w);
+        return;
+    }
     if (im.unorm8) {
         float c = std::fmin(std::fmax(v.x, 0.f), 1.f) * 255.0f;
         ((uint8_t*)im.data)[i] = (uint8_t)std::nearbyint(c);
@@ -113,6 +123,8 @@ void traceRayEXT(const accelerationStructureEXT&, uint flags, uint, uint, uint, 
 #include "hybridHit.rchit.hpp"
 #include "miss.rmiss.hpp"
 #include "blur.comp.hpp"
+#include "raygen.rgen.hpp"
+#include "closesthit.rchit.hpp"
 namespace sh_helpers {
 using namespace glsl;
 #include "helpers.glsl.hpp"
@@ -164,8 +176,19 @@ sampler2D plane_sampler(const float* data, int w, int h) {
 
 // ---- pipeline state for the trace hook ----
 RefScene* g_scene = nullptr;
-int g_pipeline = 0;  // 0 = shadow, 1 = hybrid
+int g_pipeline = 0;  // 0 = shadow, 1 = hybrid, 2 = path traced (raygen + closesthit)
 std::vector<PayloadTable*> g_callers;
+
+// the closest-hit program of the bound pipeline
+struct HitProgram {
+    PayloadTable* payloads;
+    vec3* attribs;
+    void (*main)();
+};
+HitProgram hit_program() {
+    if (g_pipeline == 2) return {&sh_closesthit::g_payloads, &sh_closesthit::attribs, sh_closesthit::main};
+    return {&sh_hybridHit::g_payloads, &sh_hybridHit::attribs, sh_hybridHit::main};
+}
 
 template <class T> void copy_in(PayloadTable& callee, PayloadTable& caller, int loc) {
     (void)sizeof(T);
@@ -194,22 +217,23 @@ void trace_hook(uint flags, uint miss, const vec3& o, float tmin, const vec3& d,
         return;
     }
     if (flags & gl_RayFlagsSkipClosestHitShaderEXT) return;
-    // closest hit: hybridHit.rchit
+    // closest hit: hybridHit.rchit or closesthit.rchit
+    const HitProgram hp = hit_program();
     const uint32_t p = g_scene->os.tri_prim[h.id];
-    PayloadTable& callee = sh_hybridHit::g_payloads;
+    PayloadTable& callee = *hp.payloads;
     std::memcpy(callee.in_ptr, caller.ptr[payload], caller.size[payload]);
     vec3 so = gl_WorldRayOriginEXT, sd = gl_WorldRayDirectionEXT;
     float st = gl_HitTEXT;
     int sp = gl_PrimitiveID, si = gl_InstanceCustomIndexEXT;
-    vec3 sa = sh_hybridHit::attribs;
+    vec3 sa = *hp.attribs;
     gl_WorldRayOriginEXT = o;
     gl_WorldRayDirectionEXT = d;
     gl_HitTEXT = h.t;
     gl_PrimitiveID = (int)(h.id - g_scene->os.prim_tri0[p]);
     gl_InstanceCustomIndexEXT = (int)p;
-    sh_hybridHit::attribs = vec3(h.b1, h.b2, 0.f);
+    *hp.attribs = vec3(h.b1, h.b2, 0.f);
     g_callers.push_back(&callee);
-    sh_hybridHit::main();
+    hp.main();
     g_callers.pop_back();
     std::memcpy(caller.ptr[payload], callee.in_ptr, caller.size[payload]);
     gl_WorldRayOriginEXT = so;
@@ -217,7 +241,7 @@ void trace_hook(uint flags, uint miss, const vec3& o, float tmin, const vec3& d,
     gl_HitTEXT = st;
     gl_PrimitiveID = sp;
     gl_InstanceCustomIndexEXT = si;
-    sh_hybridHit::attribs = sa;
+    *hp.attribs = sa;
 }
 
 void bind_env(Array<sampler2D>& arr, RefScene& s) {
@@ -407,6 +431,63 @@ int ref_hybrid_pass(void* sp, uint32_t W, uint32_t H, const float* const* planes
     bind_env(sh_miss::skybox, s);
     g_scene = &s;
     g_pipeline = 1;
+    g_trace = trace_hook;
+    g_callers.assign(1, &sh::g_payloads);
+    gl_LaunchSizeEXT = uvec3(W, H, 1);
+    for (uint32_t y = 0; y < H; y++)
+        for (uint32_t x = 0; x < W; x++) {
+            gl_LaunchIDEXT = uvec3(x, y, 0);
+            sh::main();
+        }
+    return 0;
+}
+
+// ---- path-traced pipeline (Renderer::raytrace, src/renderer.cpp:465-501): raygen.rgen over
+//      W x H, miss 0 miss.rmiss, miss 1 shadow.rmiss, hit group closesthit.rchit; the image
+//      is the B8G8R8A8 _rtImage (src/renderer.cpp:1535), read and written in place ----
+int ref_pathtrace_pass(void* sp, uint32_t W, uint32_t H, const float* cam36, int samples, uint8_t* image_bgra8) {
+    RefScene& s = *(RefScene*)sp;
+    namespace sh = sh_raygen;
+    namespace ch = sh_closesthit;
+    const uint32_t L = (uint32_t)s.os.lights.size();
+    sh::image = image2D{image_bgra8, (int)W, (int)H, true, true};
+    sh::cam.viewInverse = mat_of(cam36);
+    sh::cam.projInverse = mat_of(cam36 + 16);
+    sh::cam.frame = vec4(cam36[32], cam36[33], cam36[34], cam36[35]);
+    // closest-hit resources (create_rt_descriptors, src/renderer.cpp:2092-2305)
+    std::vector<ch::Light> clights = make_lights<ch::Light>(s.os.lights);
+    std::vector<ch::Material> cmats = make_mats<ch::Material>(s.os.mats);
+    ch::lightsBuffer.lights = RuntimeArray<ch::Light>{clights.data(), (int)L};
+    ch::materials.mat = RuntimeArray<ch::Material>{cmats.data(), (int)cmats.size()};
+    bind_env(ch::environment_texture, s);
+    ch::textures.v.clear();
+    ch::samplesBuffer.samples = samples;
+    const size_t np = s.os.prims.size();
+    std::vector<vec4> ids(np);
+    std::vector<std::vector<ch::Vertex>> vbuf(np);
+    ch::vertices.v.assign(np, ch::Vertices());
+    ch::indices.v.assign(np, ch::Indices());
+    for (size_t p = 0; p < np; p++) {
+        const HyPrimitive& pr = s.os.prims[p];
+        ids[p] = vec4((float)p, (float)pr.material_id, (float)pr.transform_id, (float)pr.first_index);
+        const size_t nvx = s.os.verts.size() - pr.vertex_offset;
+        vbuf[p].resize(nvx);
+        for (size_t k = 0; k < nvx; k++) {
+            const HyVertex& v = s.os.verts[pr.vertex_offset + k];
+            vbuf[p][k].normal = vec4(v.normal[0], v.normal[1], v.normal[2], 1.f);
+            vbuf[p][k].color = vec4(v.color[0], v.color[1], v.color[2], 1.f);
+            vbuf[p][k].uv = vec4(v.uv[0], v.uv[1], 1.f, 1.f);
+        }
+        ch::vertices.v[p].v = RuntimeArray<ch::Vertex>{vbuf[p].data(), (int)nvx};
+        ch::indices.v[p].i = RuntimeArray<int>{s.indices.data(), (int)s.indices.size()};
+    }
+    ch::objIndices.idx = RuntimeArray<vec4>{ids.data(), (int)np};
+    std::vector<mat4> m4(s.os.xf.size() / 16);
+    for (size_t t = 0; t < m4.size(); t++) m4[t] = mat_of(&s.os.xf[t * 16]);
+    ch::matrices.m = RuntimeArray<mat4>{m4.data(), (int)m4.size()};
+    bind_env(sh_miss::skybox, s);
+    g_scene = &s;
+    g_pipeline = 2;
     g_trace = trace_hook;
     g_callers.assign(1, &sh::g_payloads);
     gl_LaunchSizeEXT = uvec3(W, H, 1);

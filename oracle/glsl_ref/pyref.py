@@ -54,6 +54,7 @@ def load():
         "ref_shadow_pass": (C.c_int, [P, U32, U32, P, P, C.c_int, P]),
         "ref_blur": (C.c_int, [U32, U32, C.c_int, P, P, P]),
         "ref_hybrid_pass": (C.c_int, [P, U32, U32, P, P, P, P]),
+        "ref_pathtrace_pass": (C.c_int, [P, U32, U32, P, C.c_int, P]),
     }
     for k, (r, a) in sig.items():
         f = getattr(lib, k)
@@ -139,6 +140,15 @@ class RefScene:
         sh = np.ascontiguousarray(shadow_u8, np.uint8)
         self.lib.ref_hybrid_pass(self.h, W, H, arr, _p(cam), _p(sh), _p(out))
         return out
+
+    def pathtrace_pass(self, cam36, width, height, samples, image_bgra8=None):
+        """raygen.rgen + closesthit.rchit + miss shaders; accumulates into the B8G8R8A8 image
+        (in place when given)."""
+        if image_bgra8 is None:
+            image_bgra8 = np.zeros((height, width, 4), np.uint8)
+        cam = np.ascontiguousarray(cam36, np.float32)
+        self.lib.ref_pathtrace_pass(self.h, width, height, _p(cam), samples, _p(image_bgra8))
+        return image_bgra8
 
 
 def blur(frame, motion_rg, shadow3_u8, hist3_u8):

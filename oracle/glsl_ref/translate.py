@@ -84,7 +84,8 @@ def main(src_dir: str, out_dir: str):
     src, out = Path(src_dir), Path(out_dir)
     out.mkdir(parents=True, exist_ok=True)
     stages = {"shadowRaygen.rgen": "shadowRaygen", "shadow.rmiss": "shadowMiss", "hybridRaygen.rgen": "hybridRaygen",
-              "hybridHit.rchit": "hybridHit", "miss.rmiss": "miss", "blur.comp": "blur"}
+              "hybridHit.rchit": "hybridHit", "miss.rmiss": "miss", "blur.comp": "blur", "raygen.rgen": "raygen",
+              "closesthit.rchit": "closesthit"}
     for name in ("random.glsl", "helpers.glsl", "raycommon.glsl"):
         (out / (name + ".hpp")).write_text(translate((src / name).read_text(), None))
     for name, stage in stages.items():

@@ -3,6 +3,7 @@
 // product's hy_scene_* calls so both sides are fed identical inputs.
 #include <cstring>
 
+#include "orc_grad.hpp"
 #include "orc_passes.hpp"
 
 using namespace orc;
@@ -162,6 +163,36 @@ int orc_shade(void* sp, const HyGBuffer* g, const HyCamera* cam, const HyPassCon
     PassStats p;
     shade(*(Scene*)sp, gb_of(g), *cam, *cfg, acc->format, acc->history, out_rgba32f, out_bgra8, mode, &p);
     stats_out(p, st);
+    return 0;
+}
+
+int orc_pathtrace(void* sp, const HyCamera* cam, uint32_t W, uint32_t H, const HyPassConfig* cfg,
+                  uint8_t* image_bgra8, float* out_rgba32f, int mode, HyStats* st) {
+    PassStats p;
+    pathtrace(*(Scene*)sp, *cam, W, H, *cfg, image_bgra8, out_rgba32f, mode, &p);
+    stats_out(p, st);
+    return 0;
+}
+
+// ---- FP64 shading as a function of the material / light parameters ----
+// The record's light count is the scene's (closest_hit shades with every
+// scene light); acc->num_lights must equal it.
+void* orc_grad_record(void* sp, const HyGBuffer* g, const HyCamera* cam, const HyPassConfig* cfg,
+                      const HyAccum* acc, int mode) {
+    Scene& s = *(Scene*)sp;
+    if (acc->num_lights != s.lights.size() || s.lights.size() > 64) return nullptr;
+    GradRecord* R = new GradRecord();
+    grad_record(s, gb_of(g), *cam, *cfg, acc->format, acc->history, acc->num_lights, mode, *R);
+    return R;
+}
+void orc_grad_free(void* r) { delete (GradRecord*)r; }
+int orc_grad_forward(void* sp, void* r, const double* mats, const double* lights, double* rgb) {
+    grad_forward64(*(Scene*)sp, *(GradRecord*)r, mats, lights, rgb);
+    return 0;
+}
+int orc_grad_adjoint(void* sp, void* r, const double* mats, const double* lights, const double* w, double* g_mats,
+                     double* g_lights) {
+    grad_adjoint64(*(Scene*)sp, *(GradRecord*)r, mats, lights, w, g_mats, g_lights);
     return 0;
 }
 

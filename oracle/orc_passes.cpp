@@ -24,16 +24,6 @@ int get_threads() {
     return h ? (int)h : 1;
 }
 
-template <class F> static void parallel_rows(uint32_t H, F&& f) {
-    int nt = std::min<int>(get_threads(), (int)std::max<uint32_t>(H, 1));
-    if (nt <= 1) { for (uint32_t y = 0; y < H; y++) f(y, 0); return; }
-    std::atomic<uint32_t> next{0};
-    std::vector<std::thread> th;
-    for (int t = 0; t < nt; t++)
-        th.emplace_back([&, t] { for (uint32_t y; (y = next.fetch_add(1)) < H;) f(y, t); });
-    for (auto& x : th) x.join();
-}
-
 // ---- texel access --------------------------------------------------------------
 static inline float half_to_float(uint16_t h) {
     uint32_t s = (uint32_t)(h >> 15) << 31, e = (h >> 10) & 0x1f, m = h & 0x3ff;
@@ -116,14 +106,14 @@ static V3<float> env_lookup(const Env& e, float u, float v) {
 }
 
 // hybridRaygen.rgen:59-60 / hybridHit.rchit:272-273
-static inline V3<float> irradiance_at(const Scene& s, V3<float> N) {
+V3<float> irradiance_at(const Scene& s, V3<float> N) {
     const float PI = K<float>::PI;
     float u = 0.5f + std::atan2(N.x, N.z) / (2.0f * PI);
     float v = 0.5f - std::asin(N.y) / PI;
     return env_lookup(s.env[1], u, v);
 }
 // miss.rmiss:13-18
-static inline V3<float> miss_color(const Scene& s, V3<float> d) {
+V3<float> miss_color(const Scene& s, V3<float> d) {
     const float PI = K<float>::PI_MISS;
     V3<float> dir = normalize(d);
     float u = 0.5f + std::atan2(dir.x, dir.z) / (2.0f * PI);
@@ -132,7 +122,7 @@ static inline V3<float> miss_color(const Scene& s, V3<float> d) {
 }
 
 // int(materialIdx) of a G-buffer texel; -1 when it names no material
-static inline int mat_index(float f, size_t n) {
+int mat_index(float f, size_t n) {
     if (!(f > -1.f && f < (float)n)) return -1;
     return (int)f;
 }
@@ -166,9 +156,7 @@ void primary_ray(const HyCamera& cam, uint32_t W, uint32_t H, uint32_t x, uint32
     d[0] = dir.x; d[1] = dir.y; d[2] = dir.z;
 }
 
-struct HitAttr { V3<float> N; float u, v; uint32_t prim; };
-
-static HitAttr hit_attributes(const Scene& s, const Hit& h) {
+HitAttr hit_attributes(const Scene& s, const Hit& h) {
     uint32_t p = s.tri_prim[h.id];
     const HyPrimitive& pr = s.prims[p];
     uint32_t local = h.id - s.prim_tri0[p];
@@ -343,10 +331,8 @@ void accumulate(const GBufHost& g, const HyPassConfig& cfg, uint32_t fmt, const 
 }
 
 // ---- hybrid shading (hybridRaygen.rgen, hybridHit.rchit, miss.rmiss) ----------------------
-struct Payload { V3<float> color; float t; V3<float> dir; float scattered; V3<float> origin; };
-
-static Payload closest_hit(const Scene& s, const Hit& h, V3<float> ro, V3<float> rd, uint32_t& seed,
-                           const HyPassConfig& cfg, int mode, PassStats& ls) {
+Payload closest_hit(const Scene& s, const Hit& h, V3<float> ro, V3<float> rd, uint32_t& seed,
+                    const HyPassConfig& cfg, int mode, PassStats& ls, uint64_t* vis) {
     const float PI = K<float>::PI;
     HitAttr a = hit_attributes(s, h);
     V3<float> N = a.N;
@@ -365,6 +351,7 @@ static Payload closest_hit(const Scene& s, const Hit& h, V3<float> ro, V3<float>
     float dirw = 0.f;
     V3<float> Lo = v3(0.f, 0.f, 0.f);
     float attenuation = 1.0f;
+    if (vis) *vis = 0;
     for (size_t i = 0; i < s.lights.size(); i++) {
         const HyLight& lt = s.lights[i];
         bool isDir = lt.pos[3] < 0.f;
@@ -398,7 +385,10 @@ static Payload closest_hit(const Scene& s, const Hit& h, V3<float> ro, V3<float>
                     ls.hit_shadow_rays++;
                     shadowed = sh.id != HY_NO_HIT;
                 }
-                if (!shadowed) shadowFactor += 1.0f;
+                if (!shadowed) {
+                    shadowFactor += 1.0f;
+                    if (vis && i < 64) *vis |= 1ull << i;
+                }
             }
             V3<float> radiance = I * lc * attenuation * shadowFactor;
             V3<float> F = FresnelSchlick(NdotH, F0);
@@ -567,6 +557,167 @@ void shade(const Scene& s, const GBufHost& g, const HyCamera& cam, const HyPassC
             if (out_bgra8) {
                 uint8_t* o = out_bgra8 + pix * 4;
                 o[0] = quant8(fc.z); o[1] = quant8(fc.y); o[2] = quant8(fc.x); o[3] = 255;
+            }
+        }
+    });
+    if (st) for (auto& l : loc) st->add(l);
+}
+
+// ---- path-traced mode (raygen.rgen:20-81, closesthit.rchit:26-186, miss.rmiss) ----------
+static Payload closest_hit_pt(const Scene& s, const Hit& h, V3<float> ro, V3<float> rd, uint32_t& seed,
+                              const HyPassConfig& cfg, int mode, PassStats& ls) {
+    const float PI = K<float>::PI;
+    HitAttr a = hit_attributes(s, h);
+    V3<float> N = a.N;
+    V3<float> V = normalize(-rd);
+    float NdotV = clampv(dot(N, V), 0.f, 1.f);
+    V3<float> worldPos = ro + rd * h.t;
+    const HyMaterial& mat = s.mats[s.prims[a.prim].material_id];
+    int smode = (int)mat.smr[0];
+    V3<float> albedo = pow3(v3(mat.diffuse[0], mat.diffuse[1], mat.diffuse[2]), 2.2f);
+    float roughness = mat.smr[2], metallic = mat.smr[1];
+    V3<float> F0 = mix3(splat(0.04f), albedo, metallic);
+    V3<float> irradiance = irradiance_at(s, N);
+    V3<float> direction = v3(1.f, 1.f, 1.f);
+    float dirw = 0.f;
+    V3<float> Lo = v3(0.f, 0.f, 0.f);
+    float attenuation = 1.0f;
+    const int samples = (int)cfg.shadow_spp;
+    for (size_t i = 0; i < s.lights.size(); i++) {
+        const HyLight& lt = s.lights[i];
+        bool isDir = lt.pos[3] < 0.f;
+        V3<float> L = isDir ? v3(lt.pos[0], lt.pos[1], lt.pos[2]) : v3(lt.pos[0], lt.pos[1], lt.pos[2]) - worldPos;
+        float maxd = lt.pos[3];
+        float dist = length(L);
+        L = normalize(L);
+        float I = isDir ? 1.0f : (lt.color[3] / (dist * dist));
+        V3<float> H = normalize(V + L);
+        float NdotL = clampv(dot(N, L), 0.f, 1.f);
+        float NdotH = clampv(dot(N, H), 0.f, 1.f);
+        float shadowFactor = 0.f;
+        // every shading model casts the shadow rays; sampleDisk's seed is by value,
+        // so in REFERENCE mode all samples are one ray
+        if (NdotL > 0.f) {
+            if (dist < maxd && cfg.rng_mode == HY_RNG_REFERENCE) {
+                uint32_t sd = seed;
+                V3<float> dir = sampleDisk<float>(lt.radius, worldPos, L, sd);
+                V3<float> o = worldPos + dir * 1e-2f;
+                float oo[3] = {o.x, o.y, o.z}, dd[3] = {dir.x, dir.y, dir.z};
+                Hit sh = trace(s, oo, dd, 0.001f, dist + 1.0f, true, mode, &ls.cnt);
+                ls.shadow_rays++;
+                shadowFactor = sh.id == HY_NO_HIT ? (float)samples : 0.f;
+            } else {
+                for (int k = 0; k < samples; k++) {
+                    bool shadowed = true;
+                    if (dist < maxd) {
+                        V3<float> dir = sampleDisk<float>(lt.radius, worldPos, L, seed);
+                        V3<float> o = worldPos + dir * 1e-2f;
+                        float oo[3] = {o.x, o.y, o.z}, dd[3] = {dir.x, dir.y, dir.z};
+                        Hit sh = trace(s, oo, dd, 0.001f, dist + 1.0f, true, mode, &ls.cnt);
+                        ls.shadow_rays++;
+                        shadowed = sh.id != HY_NO_HIT;
+                    }
+                    if (!shadowed) shadowFactor += 1.0f;
+                }
+            }
+            shadowFactor /= (float)samples;
+        }
+        // closesthit.rchit:109-117: no directional special case here
+        if (I == 0.f) attenuation = 0.f;
+        else {
+            attenuation = maxd - dist;
+            attenuation /= maxd;
+            attenuation = std::fmax(attenuation, 0.f);
+            attenuation = attenuation * attenuation;
+        }
+        V3<float> lc = v3(lt.color[0], lt.color[1], lt.color[2]);
+        if (smode == 0) {
+            V3<float> radiance = I * lc * attenuation * shadowFactor;
+            V3<float> F = FresnelSchlick(NdotH, F0);
+            float D = DistributionGGX(N, H, roughness);
+            float G = GeometrySmith(N, V, L, roughness);
+            V3<float> numerator = D * G * F;
+            float denominator = std::fmax(4.0f * clampv(dot(N, V), 0.f, 1.f) * NdotL, 0.000001f);
+            V3<float> specular = numerator / denominator;
+            V3<float> kD = (splat(1.0f) - F) * (1.0f - metallic);
+            Lo = Lo + (kD * albedo / PI + specular) * radiance * NdotL;
+            direction = v3(1.f, 1.f, 1.f);
+            dirw = 0.f;
+        } else if (smode == 3) {
+            V3<float> reflected = reflect(normalize(rd), N);
+            bool sc = dot(reflected, N) > 0.f;
+            Lo = Lo + ((NdotL > 0.f && I > 0.f) ? I * lc * attenuation * shadowFactor * metallic * albedo
+                                                : irradiance * albedo * metallic);
+            direction = reflected;
+            dirw = sc ? 1.f : 0.f;
+        } else if (smode == 4) {
+            float ior = mat.diffuse[3];
+            float NdV = dot(N, normalize(rd));
+            V3<float> refrN = NdV > 0.f ? -N : N;
+            float eta = NdV > 0.f ? 1.0f / ior : ior;
+            Lo = Lo + ((I > 0.f) ? I * lc * attenuation * albedo * metallic : irradiance * albedo * metallic);
+            float radicand = 1.0f + std::pow(eta, 2.0f) * (NdV * NdV - 1.0f);
+            direction = radicand < 0.f ? reflect(rd, N) : refract(rd, refrN, eta);
+            dirw = 1.f;
+        }
+    }
+    V3<float> F = FresnelSchlick(NdotV, F0);
+    V3<float> kD = (splat(1.0f) - F) * (1.0f - metallic);
+    Payload p;
+    p.color = Lo + kD * albedo * irradiance;
+    p.t = h.t;
+    p.dir = direction;
+    p.scattered = dirw;
+    p.origin = worldPos;
+    return p;
+}
+
+void pathtrace(const Scene& s, const HyCamera& cam, uint32_t W, uint32_t H, const HyPassConfig& cfg,
+               uint8_t* image_bgra8, float* out_rgba32f, int mode, PassStats* st) {
+    int nt = get_threads();
+    std::vector<PassStats> loc(nt);
+    const int frame = (int)cam.frame[0];
+    parallel_rows(H, [&](uint32_t y, int tid) {
+        PassStats& ls = loc[tid];
+        for (uint32_t x = 0; x < W; x++) {
+            const size_t pix = (size_t)y * W + x;
+            uint32_t seed = tea(y * W + x, (uint32_t)frame);
+            // NSAMPLES = 1 (helpers.glsl:6): the offset is the pixel centre, r1/r2 are still drawn
+            rnd(seed);
+            rnd(seed);
+            float o[3], d[3];
+            primary_ray(cam, W, H, x, y, o, d);  // the camera ray of raygen.rgen:35-44
+            V3<float> origin = mat_vec3(cam.inv_view, 0.f, 0.f, 0.f, 1.f);  // the loop adds the 1e-2 offset
+            V3<float> direction = v3(d[0], d[1], d[2]);
+            V3<float> rayColor = v3(1.f, 1.f, 1.f);
+            for (uint32_t depth = 0; depth < cfg.max_bounces; depth++) {
+                V3<float> ro = origin + direction * 1e-2f;
+                float oo[3] = {ro.x, ro.y, ro.z}, dd[3] = {direction.x, direction.y, direction.z};
+                Hit h = trace(s, oo, dd, 0.001f, 10000.0f, false, mode, &ls.cnt);
+                ls.reflection_rays++;
+                if (h.id == HY_NO_HIT) {
+                    rayColor = rayColor * miss_color(s, direction);
+                    break;
+                }
+                Payload p = closest_hit_pt(s, h, ro, direction, seed, cfg, mode, ls);
+                rayColor = rayColor * p.color;
+                if (!(p.scattered > 0.f)) break;
+                origin = p.origin;
+                direction = p.dir;
+            }
+            V3<float> fc = rayColor;  // finalColor / NSAMPLES with NSAMPLES = 1
+            if (out_rgba32f) {
+                float* q = out_rgba32f + pix * 4;
+                q[0] = fc.x; q[1] = fc.y; q[2] = fc.z; q[3] = 1.f;
+            }
+            if (image_bgra8) {
+                uint8_t* q = image_bgra8 + pix * 4;
+                if (frame >= 0) {
+                    const float a = 1.0f / (1.0f + (float)frame);
+                    V3<float> last = v3((float)q[2] / 255.0f, (float)q[1] / 255.0f, (float)q[0] / 255.0f);
+                    fc = mix3(last, fc, a);
+                }
+                q[0] = quant8(fc.z); q[1] = quant8(fc.y); q[2] = quant8(fc.x); q[3] = 255;
             }
         }
     });

@@ -57,6 +57,11 @@ def load():
         "orc_shadow_pass": (C.c_int, [P, P, P, P, U32, P, C.c_int, P]),
         "orc_accumulate": (C.c_int, [P, P, P, P, P]),
         "orc_shade": (C.c_int, [P, P, P, P, P, P, P, C.c_int, P]),
+        "orc_pathtrace": (C.c_int, [P, P, U32, U32, P, P, P, C.c_int, P]),
+        "orc_grad_record": (P, [P, P, P, P, P, C.c_int]),
+        "orc_grad_free": (None, [P]),
+        "orc_grad_forward": (C.c_int, [P, P, P, P, P]),
+        "orc_grad_adjoint": (C.c_int, [P, P, P, P, P, P, P]),
     }
     for k, (r, a) in sig.items():
         f = getattr(lib, k)
@@ -255,6 +260,19 @@ class OracleScene:
                            _p(out_f), _p(out_8), mode, C.byref(st))
         return out_f, out_8, st.as_dict()
 
+    def pathtrace(self, cam36, width: int, height: int, cfg: dict, image: np.ndarray | None = None,
+                  mode=TRACE_BVH8):
+        """Path-traced mode: returns (accumulated BGRA8 image (updated in place when given), the
+        frame's RGBA32F colour before accumulation, stats)."""
+        if image is None:
+            image = np.zeros((height, width, 4), np.uint8)
+        out_f = np.zeros((height, width, 4), np.float32)
+        st = _Stats()
+        cam = np.ascontiguousarray(cam36, np.float32)
+        self.lib.orc_pathtrace(self.h, _p(cam), width, height, C.byref(_Cfg(**cfg)), _p(image), _p(out_f), mode,
+                               C.byref(st))
+        return image, out_f, st.as_dict()
+
     def forward(self, planes, cam36, cfg: dict, hist: np.ndarray, fmt: int, mode=TRACE_BVH8,
                 formats=FP32_FORMATS):
         """shadow -> accumulate -> shade, the order of Renderer::rasterize_hybrid."""
@@ -269,6 +287,56 @@ class OracleScene:
         st = {k: st1[k] + st2[k] for k in st1 if k != "error_flags"}
         st["error_flags"] = st1["error_flags"] | st2["error_flags"]
         return out_f, out_8, shadow, st
+
+
+class GradOracle:
+    """FP64 shading as a function of the scene parameters, visibility fixed.
+
+    Records (in float, like the shading pass) the G-buffer geometry, bounce
+    hits, bounce-hit shadow outcomes and light sides of every pixel from the
+    scene as it is now, then evaluates the image in FP64 (`forward`) and the
+    gradient of sum(w * image) (`adjoint`) for any parameter vector:
+    mats (num_mats, 5) = diffuse rgb, roughness, metallic;
+    lights (num_lights, 4) = position xyz, intensity."""
+
+    def __init__(self, scene: "OracleScene", planes, cam36, cfg: dict, hist: np.ndarray, fmt: int,
+                 mode=TRACE_BVH8, formats=FP32_FORMATS):
+        self.scene = scene
+        self.lib = scene.lib
+        H, W = planes[0].shape[:2]
+        self.shape = (H, W)
+        self._hist = np.ascontiguousarray(hist)
+        acc = _Accum(fmt, self._hist.shape[0], self._hist.ctypes.data)
+        cam = np.ascontiguousarray(cam36, np.float32)
+        self.h = self.lib.orc_grad_record(scene.h, C.byref(scene._gb(planes, formats)), _p(cam),
+                                          C.byref(_Cfg(**cfg)), C.byref(acc), mode)
+        if not self.h:
+            raise ValueError("the record needs history planes for every scene light (<= 64)")
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.lib.orc_grad_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def forward(self, mats: np.ndarray, lights: np.ndarray) -> np.ndarray:
+        m = np.ascontiguousarray(mats, np.float64)
+        l = np.ascontiguousarray(lights, np.float64)
+        out = np.zeros(self.shape + (3,), np.float64)
+        self.lib.orc_grad_forward(self.scene.h, self.h, _p(m), _p(l), _p(out))
+        return out
+
+    def adjoint(self, mats: np.ndarray, lights: np.ndarray, w: np.ndarray):
+        m = np.ascontiguousarray(mats, np.float64)
+        l = np.ascontiguousarray(lights, np.float64)
+        w = np.ascontiguousarray(w, np.float64)
+        assert w.shape == self.shape + (3,)
+        gm = np.zeros_like(m)
+        gl = np.zeros_like(l)
+        self.lib.orc_grad_adjoint(self.scene.h, self.h, _p(m), _p(l), _p(w), _p(gm), _p(gl))
+        return gm, gl
 
 
 def cfg_dict(spp=1, max_bounces=8, rng_mode=0, accum_frame=0, flags=0):

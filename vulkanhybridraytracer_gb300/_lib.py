@@ -24,6 +24,10 @@ HY_ERR_NOT_READY = -8
 HY_ERR_UNSUPPORTED = -9
 HY_ERR_TOO_LARGE = -10
 HY_NOALLOC_SCRATCH_BYTES = 16 << 20
+HY_GRAD_MATERIAL_PARAMS = 5
+HY_GRAD_LIGHT_PARAMS = 4
+HY_GRAD_MAX_BOUNCES = 8
+HY_GRAD_MAX_LIGHTS = 64
 
 HY_FMT_RGBA32F, HY_FMT_RG32F, HY_FMT_RGBA16F, HY_FMT_RG16F, HY_FMT_RGBA8 = range(5)
 HY_ACCUM_U8, HY_ACCUM_F32 = 0, 1
@@ -88,6 +92,10 @@ class HyStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("_")}
 
 
+class HyKernelTime(C.Structure):
+    _fields_ = [("kernel", C.c_char * 40), ("launches", C.c_uint32), ("total_ms", C.c_float)]
+
+
 class HyView(C.Structure):
     _fields_ = [("scene", C.c_uint32), ("_pad", C.c_uint32), ("gbuffer", HyGBuffer), ("camera", HyCamera),
                 ("config", HyPassConfig), ("accum", HyAccum), ("out_rgba32f", C.c_void_p),
@@ -118,6 +126,8 @@ PROTOTYPES = {
     "hy_error_string": (C.c_char_p, [I32]),
     "hy_get_abi_version": (I32, []),
     "hy_synchronize": (I32, [P]),
+    "hy_profile_enable": (I32, [P, I32]),
+    "hy_profile_read": (I32, [P, C.POINTER(HyKernelTime), C.c_uint32, C.POINTER(C.c_uint32)]),
     "hy_debug_fail_alloc_after": (I32, [P, U32]),
     "hy_scene_set_geometry": (I32, [P, P, U32, P, U32, P, U32, P, U32]),
     "hy_scene_set_materials": (I32, [P, P, U32]),
@@ -137,6 +147,8 @@ PROTOTYPES = {
                                 C.POINTER(HyAccum), P, P, C.POINTER(HyStats)]),
     "hy_hybrid_forward_host": (I32, [P, C.POINTER(HyGBuffer), C.POINTER(HyCamera), C.POINTER(HyPassConfig),
                                      C.POINTER(HyAccum), P, P, C.POINTER(HyStats)]),
+    "hy_hybrid_backward": (I32, [P, C.POINTER(HyGBuffer), C.POINTER(HyCamera), C.POINTER(HyPassConfig),
+                                 C.POINTER(HyAccum), P, P, P, C.POINTER(HyStats)]),
     "hy_accumulate_pass_noalloc": (I32, [C.POINTER(HyGBuffer), C.POINTER(HyPassConfig), P, C.POINTER(HyAccum), P]),
     "hy_batch_forward": (I32, [P, C.POINTER(P), U32, C.POINTER(HyView), U32, U32, C.POINTER(HyPassConfig),
                                C.POINTER(HyStats)]),

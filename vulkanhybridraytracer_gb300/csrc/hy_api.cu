@@ -255,6 +255,42 @@ PassParams make_params(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const
     return P;
 }
 
+// ---- per-kernel timing ----
+// the first five are the MODE_* values of hy_pass.h
+enum { PK_ACCUM = MODE_SHADOW_ACCUM_G + 1, PK_GRAD, PK_COUNT };
+const char* const kProfNames[PK_COUNT] = {"k_shadow",       "k_pixels<shade>",       "k_shadow<accum>",
+                                          "k_shadow_group", "k_shadow_group<accum>", "k_accumulate",
+                                          "k_shade_grad"};
+static_assert(MODE_SHADOW == 0 && MODE_SHADE == 1 && MODE_SHADOW_ACCUM == 2 && MODE_SHADOW_G == 3 &&
+                  MODE_SHADOW_ACCUM_G == 4,
+              "profile names follow the pass modes");
+
+cudaEvent_t prof_event(HyCtx* c) {
+    if (c->prof_used == c->prof_pool.size()) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+        c->prof_pool.push_back(e);
+    }
+    return c->prof_pool[c->prof_used++];
+}
+
+// brackets the launches in its scope with events when profiling is on
+struct ProfScope {
+    HyCtx* c;
+    int kind;
+    cudaEvent_t a = nullptr;
+    ProfScope(HyCtx* ctx, int k) : c(ctx), kind(k) {
+        if (c->prof_on && c->prof_recs.size() < 4096 && (a = prof_event(c))) cudaEventRecord(a, c->stream);
+    }
+    ~ProfScope() {
+        if (!a) return;
+        cudaEvent_t b = prof_event(c);
+        if (!b) return;
+        cudaEventRecord(b, c->stream);
+        c->prof_recs.push_back(HyCtx::ProfRec{kind, a, b});
+    }
+};
+
 int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg, int queue_slot) {
     bool count = (cfg->flags & HY_FLAG_COUNT_TRAVERSAL) != 0;
     int block = cfg->block_size ? (int)cfg->block_size : 128;
@@ -273,6 +309,7 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
     int minb = cfg->min_blocks ? (int)cfg->min_blocks : 8;
     int grid = grid_for(c, mode, count, minb, block);
     grid = std::max(1, std::min<int>(grid, (int)((P.ntiles * 32ull + block - 1) / block)));
+    ProfScope prof(c, mode);
     HY_CUDA_TRY(launch_pixels(mode, count, minb, scene_dev(c), P, grid, block, c->stream));
     return HY_OK;
 }
@@ -342,9 +379,11 @@ void hy_destroy(HyCtx* c) {
                       &c->nt_scan, &c->scan_tmp, &c->hist, &c->total, &c->nodes, &c->tris, &c->node_ref,
                       &c->node_plan, &c->dstats,
                       &c->raw_shadow, &c->hist_prev, &c->host_in[0], &c->host_in[1], &c->host_in[2],
-                      &c->host_in[3], &c->host_in[4], &c->host_in[5], &c->host_out_f, &c->host_out_8};
+                      &c->host_in[3], &c->host_in[4], &c->host_in[5], &c->host_out_f, &c->host_out_8,
+                      &c->grad_partial};
     for (DevBuf* b : bufs) ctx_free(c, *b);
     if (c->h_stats) cudaFreeHost(c->h_stats);
+    for (cudaEvent_t e : c->prof_pool) cudaEventDestroy(e);
     if (c->batch_exec) cudaGraphExecDestroy(c->batch_exec);
     if (c->batch_done) cudaEventDestroy(c->batch_done);
     if (c->h_batch_tab) cudaFreeHost(c->h_batch_tab);
@@ -551,6 +590,7 @@ static int accumulate_impl(HyCtx* c, const HyGBuffer* gb, const HyPassConfig* cf
         HY_CUDA_TRY(cudaMemcpyAsync(c->hist_prev.p, acc->history, bytes, cudaMemcpyDeviceToDevice, c->stream));
         A.hist_prev = c->hist_prev.p;
     }
+    ProfScope prof(c, PK_ACCUM);
     HY_CUDA_TRY(launch_accumulate(A, c->stream));
     return HY_OK;
 }
@@ -611,6 +651,78 @@ int hy_hybrid_forward(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const 
     if ((rc = reset_counters(c))) return rc;
     if ((rc = forward_impl(c, gb, cam, cfg, acc, out_f, out_8))) return rc;
     return finish_call(c, st, !(cfg->flags & HY_FLAG_NO_STATUS_SYNC));
+}
+
+int hy_hybrid_backward(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const HyPassConfig* cfg,
+                       const HyAccum* acc, const float* d_grad, float* d_grad_mats, float* d_grad_lights,
+                       HyStats* st) {
+    if (!c || !cam || !acc || !acc->history || acc->format > HY_ACCUM_F32 || !d_grad) return HY_ERR_INVALID_ARG;
+    if (((uintptr_t)d_grad) % 16 != 0) return HY_ERR_INVALID_ARG;
+    int rc;
+    if ((rc = check_gbuffer(gb, true)) || (rc = check_cfg(cfg)) || (rc = check_scene_ready(c))) return rc;
+    if (acc->num_lights > c->nlights) return HY_ERR_INVALID_ARG;
+    if (cfg->max_bounces > HY_GRAD_MAX_BOUNCES || acc->num_lights > HY_GRAD_MAX_LIGHTS) return HY_ERR_UNSUPPORTED;
+    DeviceGuard g(c->device);
+    if ((rc = reset_counters(c))) return rc;
+    GradParams G;
+    G.P = make_params(c, gb, cam, cfg, acc->format, acc->history, acc->history, nullptr, nullptr);
+    G.P.num_lights = acc->num_lights;
+    G.P.queue = dev_queue(c, WQ_SHADE);
+    G.grad = reinterpret_cast<const float4*>(d_grad);
+    G.light_off = c->nmats * HY_GRAD_MATERIAL_PARAMS;
+    G.nparam = G.light_off + c->nlights * HY_GRAD_LIGHT_PARAMS;
+    int grid = 1;
+    bool smem = false;
+    size_t smem_bytes = 0;
+    HY_CUDA_TRY(grad_launch_shape(G.nparam, c->num_sms, G.P.ntiles, &grid, &smem, &smem_bytes));
+    const size_t rows = smem ? (size_t)grid : 1;
+    if ((rc = ensure_size(c, c->grad_partial, rows * G.nparam * 4))) return rc;
+    G.out = c->grad_partial.as<float>();
+    {
+        ProfScope prof(c, PK_GRAD);
+        HY_CUDA_TRY(launch_shade_grad(scene_dev(c), G, grid, smem, smem_bytes, d_grad_mats, d_grad_lights,
+                                      c->stream));
+    }
+    return finish_call(c, st, !(cfg->flags & HY_FLAG_NO_STATUS_SYNC));
+}
+
+int hy_profile_enable(HyCtx* c, int enable) {
+    if (!c) return HY_ERR_INVALID_ARG;
+    DeviceGuard g(c->device);
+    HY_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->prof_on = enable != 0;
+    c->prof_recs.clear();
+    c->prof_used = 0;
+    return HY_OK;
+}
+
+int hy_profile_read(HyCtx* c, HyKernelTime* out, uint32_t cap, uint32_t* count) {
+    if (!c || !count || (cap && !out)) return HY_ERR_INVALID_ARG;
+    DeviceGuard g(c->device);
+    HY_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    uint32_t launches[PK_COUNT] = {};
+    double ms[PK_COUNT] = {};
+    for (const HyCtx::ProfRec& r : c->prof_recs) {
+        float t = 0.f;
+        HY_CUDA_TRY(cudaEventElapsedTime(&t, r.a, r.b));
+        launches[r.kind]++;
+        ms[r.kind] += t;
+    }
+    c->prof_recs.clear();
+    c->prof_used = 0;
+    uint32_t n = 0;
+    for (int k = 0; k < PK_COUNT; k++) {
+        if (!launches[k]) continue;
+        if (n < cap) {
+            std::memset(&out[n], 0, sizeof(HyKernelTime));
+            std::strncpy(out[n].kernel, kProfNames[k], sizeof(out[n].kernel) - 1);
+            out[n].launches = launches[k];
+            out[n].total_ms = (float)ms[k];
+        }
+        n++;
+    }
+    *count = n;
+    return HY_OK;
 }
 
 int hy_hybrid_forward_host(HyCtx* c, const HyGBuffer* hgb, const HyCamera* cam, const HyPassConfig* cfg,

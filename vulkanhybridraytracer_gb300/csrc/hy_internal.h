@@ -66,6 +66,14 @@ struct HyCtx {
     hy::DevBuf raw_shadow;  // per-light raw shadow images (unfused path)
     hy::DevBuf hist_prev;   // history snapshot for the reprojection read
     hy::DevBuf host_in[6], host_out_f, host_out_8;  // device staging of hy_hybrid_forward_host
+    hy::DevBuf grad_partial;  // per-block partial gradient vectors of hy_hybrid_backward
+
+    // ---- per-kernel timing (hy_profile_*) ----
+    struct ProfRec { int kind; cudaEvent_t a, b; };
+    bool prof_on = false;
+    std::vector<cudaEvent_t> prof_pool;   // created on demand, reused after each read
+    size_t prof_used = 0;
+    std::vector<ProfRec> prof_recs;
     uint32_t* h_status = nullptr;   // pinned readback slot
     unsigned long long* h_stats = nullptr;
 

@@ -64,6 +64,23 @@ struct GbufParams {
     uint32_t* status;
 };
 
+// The adjoint of the shading pass: dLoss/dImage in, per-material (diffuse
+// rgb, roughness, metallic) and per-light (position xyz, intensity) gradients
+// out.  `out` holds one partial gradient vector per block (grid rows) when
+// the vector fits shared memory, else one vector the blocks add into.
+constexpr int kGradMaxBounces = HY_GRAD_MAX_BOUNCES;
+struct GradParams {
+    PassParams P;
+    const float4* grad;   // dLoss/dImage, RGBA32F (alpha ignored)
+    float* out;
+    uint32_t nparam;      // num_mats * 5 + num_lights * 4
+    uint32_t light_off;   // num_mats * 5
+};
+cudaError_t grad_launch_shape(uint32_t nparam, int num_sms, uint32_t ntiles, int* grid, bool* smem,
+                              size_t* smem_bytes);
+cudaError_t launch_shade_grad(const SceneDev& S, const GradParams& G, int grid, bool smem, size_t smem_bytes,
+                              float* out_mat, float* out_light, cudaStream_t s);
+
 cudaError_t launch_pixels(int mode, bool count, int minb, const SceneDev& S, const PassParams& P, int grid, int block,
                           cudaStream_t s);
 cudaError_t pixel_occupancy(int mode, bool count, int minb, int block, int* blocks_per_sm);

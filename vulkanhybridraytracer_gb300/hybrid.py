@@ -64,6 +64,7 @@ class HybridContext:
         L.check(self.lib.hy_create(C.byref(h), C.byref(info)), "hy_create")
         self.h = h
         self.num_lights = 0
+        self.num_mats = 0
         self.num_tris = 0
 
     def close(self):
@@ -95,6 +96,7 @@ class HybridContext:
             e = np.ascontiguousarray(e, np.uint8)
             L.check(self.lib.hy_scene_set_env(self.h, slot, _np_ptr(e), e.shape[1], e.shape[0]), "env")
         self.num_lights = len(lights)
+        self.num_mats = len(mats)
         self.num_tris = int(sum(int(p[1]) // 3 for p in prims))
 
     def set_scene(self, scene: Scene):
@@ -109,6 +111,7 @@ class HybridContext:
     def set_materials(self, mats: np.ndarray):
         mats = np.ascontiguousarray(mats, np.float32)
         L.check(self.lib.hy_scene_set_materials(self.h, _np_ptr(mats), len(mats)), "materials")
+        self.num_mats = len(mats)
 
     def build_bvh(self) -> dict:
         st = L.HyBvhStats()
@@ -221,6 +224,29 @@ class HybridContext:
                                        C.byref(st)), "shade_pass")
         return st.as_dict()
 
+    def backward(self, planes, cam36, cfg, hist, grad_img, fmt=L.HY_ACCUM_U8, grad_mats=None, grad_lights=None,
+                 formats=GBUF_FP32_FORMATS, stats: bool = True):
+        """hy_hybrid_backward: dLoss/dImage (device (H, W, 4) float32) -> gradients with respect to the
+        materials (num_mats, 5: diffuse rgb, roughness, metallic) and lights (num_lights, 4: position,
+        intensity), visibility held fixed.  Returns (grad_mats, grad_lights, stats)."""
+        import torch
+        h, w = planes[0].shape[0], planes[0].shape[1]
+        dev = grad_img.device
+        if grad_mats is None:
+            grad_mats = torch.empty((self.num_mats, L.HY_GRAD_MATERIAL_PARAMS), dtype=torch.float32, device=dev)
+        if grad_lights is None:
+            grad_lights = torch.empty((max(self.num_lights, 1), L.HY_GRAD_LIGHT_PARAMS), dtype=torch.float32,
+                                      device=dev)
+        gb = gbuffer_struct(planes, w, h, formats)
+        cam = camera_struct(cam36)
+        acc = self._accum(hist, fmt)
+        st = L.HyStats()
+        L.check(self.lib.hy_hybrid_backward(self.h, C.byref(gb), C.byref(cam), C.byref(cfg), C.byref(acc),
+                                            C.c_void_p(grad_img.data_ptr()), C.c_void_p(grad_mats.data_ptr()),
+                                            C.c_void_p(grad_lights.data_ptr()), C.byref(st) if stats else None),
+                "hybrid_backward")
+        return grad_mats, grad_lights[: self.num_lights], st.as_dict()
+
     def batch_forward(self, scenes, views, graph: bool = True, tuning: L.HyPassConfig | None = None,
                       sync: bool = True):
         """One batch of views over scene contexts (hy_batch_forward).
@@ -251,3 +277,19 @@ class HybridContext:
 
     def synchronize(self):
         L.check(self.lib.hy_synchronize(self.h), "synchronize")
+
+    # ---- per-kernel timing ----
+    def profile(self, enable: bool = True):
+        L.check(self.lib.hy_profile_enable(self.h, int(enable)), "profile_enable")
+
+    def profile_read(self) -> dict:
+        """{kernel: {"launches": n, "total_ms": t, "avg_ms": t / n}} since the last read / enable."""
+        buf = (L.HyKernelTime * 16)()
+        n = C.c_uint32()
+        L.check(self.lib.hy_profile_read(self.h, buf, 16, C.byref(n)), "profile_read")
+        out = {}
+        for i in range(min(n.value, 16)):
+            k = buf[i]
+            out[k.kernel.decode()] = {"launches": k.launches, "total_ms": k.total_ms,
+                                      "avg_ms": k.total_ms / max(k.launches, 1)}
+        return out
