@@ -46,9 +46,9 @@ def parse():
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--minb", type=int, default=0, help="shadow-kernel variant: resident blocks per SM")
-    ap.add_argument("--workload", default="hd", choices=["hd", "batch", "diff"],
+    ap.add_argument("--workload", default="hd", choices=["hd", "batch", "diff", "pathtrace"],
                     help="hd: the 1080p frame (headline); batch: 64 mixed views over 8 scenes, batched vs per "
-                         "view; diff: 512x512 forward + adjoint")
+                         "view; diff: 512x512 forward + adjoint; pathtrace: the path-traced mode at 1080p")
     ap.add_argument("--views", type=int, default=64)
     return ap.parse_args()
 
@@ -263,6 +263,58 @@ def run_diff(args):
     r.close()
 
 
+def run_pathtrace(args):
+    """Path-traced mode on the 1080p / 1.5M-triangle scene: camera rays, up to 8 mirror/glass
+    segments, args.spp decorrelated shadow rays per light at every hit, running mean into
+    the BGRA8 image."""
+    import torch
+
+    from vulkanhybridraytracer_gb300 import _lib as L
+    from vulkanhybridraytracer_gb300.hybrid import HybridContext, pass_config
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    wl = workload(args)
+    ctx = HybridContext(0, stream=stream.cuda_stream)
+    ctx.set_scene(wl.scene)
+    ctx.build_bvh()
+    img = torch.zeros((wl.height, wl.width, 4), dtype=torch.uint8, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    cfg = pass_config(spp=wl.spp, max_bounces=8, rng_mode=L.HY_RNG_DECORRELATED, flags=L.HY_FLAG_NO_STATUS_SYNC)
+    _, st = ctx.pathtrace(wl.camera(0.0), wl.width, wl.height, pass_config(wl.spp, 8, L.HY_RNG_DECORRELATED), img)
+    rays = st["shadow_rays"] + st["reflection_rays"]
+    for f in range(args.warmup):
+        ctx.pathtrace(wl.camera(float(f + 1)), wl.width, wl.height, cfg, img, stats=False)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = Clocks(0)
+    ctx.profile(True)
+    clocks.start()
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        ctx.pathtrace(wl.camera(float(args.warmup + k + 1)), wl.width, wl.height, cfg, img, stats=False)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    kernels = ctx.profile_read()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    line = {"metric": "pathtrace_mrays_per_s", "value": rays / (ms / 1e3) / 1e6, "unit": "Mrays/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": wl.name.replace("hd-", "pathtrace-"), "width": wl.width, "height": wl.height,
+                       "triangles": wl.scene.num_tris, "lights": len(wl.scene.lights), "shadow_spp": wl.spp,
+                       "rng": "decorrelated", "max_bounces": 8,
+                       "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)"},
+            "rays_per_frame": rays, "rays_breakdown": {"shadow_rays": st["shadow_rays"],
+                                                       "camera_and_bounce_rays": st["reflection_rays"]},
+            "per_kernel": kernels, "clocks": clk, "gpu_launches": args.steps}
+    print(json.dumps(line))
+    ctx.close()
+
+
 def run_batch(args):
     """64 views over 8 scenes (50k-2M triangles, 320x240..1920x1080, spp 1/4/16/64,
     1-8 lights): the views one by one through hy_hybrid_forward, then as one
@@ -365,6 +417,9 @@ def main():
         return
     if args.workload == "diff":
         run_diff(args)
+        return
+    if args.workload == "pathtrace":
+        run_pathtrace(args)
         return
     import torch
 

@@ -224,6 +224,15 @@ int hy_scene_set_materials(HyCtx* ctx, const HyMaterial* mats, uint32_t num_mats
 int hy_scene_set_lights(HyCtx* ctx, const HyLight* lights, uint32_t num_lights);
 /* slot 0 = sky (miss.rmiss, skybox[0]), slot 1 = irradiance (environmentTexture[1]) */
 int hy_scene_set_env(HyCtx* ctx, int slot, const uint8_t* rgba8, uint32_t width, uint32_t height);
+/* Material textures: Texture::_textures in load order (src/vk_textures.cpp, R8G8B8A8_UNORM,
+ * sampled NEAREST / REPEAT as by the sampler of src/renderer.cpp:3059); a material's
+ * textures[0] (diffuse), [2] (emissive) and [3] (metallic-roughness) index this list
+ * (-1: none), as hybridHit.rchit:63-65, closesthit.rchit:76-78 and
+ * geometry_shader.frag:56-59 read them.  Replaces the binding-7 texture array of
+ * create_hybrid_descriptors (src/renderer.cpp:3050-3069).  A pass whose materials name a
+ * texture past the list returns HY_ERR_INVALID_ARG. */
+int hy_scene_set_textures(HyCtx* ctx, const uint8_t* const* rgba8, const uint32_t* widths,
+                          const uint32_t* heights, uint32_t count);
 
 /* ---- acceleration structure (replaces buildBlas/buildTlas) ---- */
 int hy_bvh_build(HyCtx* ctx, HyBvhStats* stats);
@@ -272,6 +281,29 @@ int hy_hybrid_forward_host(HyCtx* ctx, const HyGBuffer* h_gb, const HyCamera* ca
                            const HyPassConfig* cfg, HyAccum* accum,
                            float* h_out_rgba32f, uint8_t* h_out_bgra8, HyStats* stats);
 
+/* ---- path-traced mode (replaces Renderer::raytrace, src/renderer.cpp:465-501:
+ *      raygen.rgen + closesthit.rchit + miss.rmiss + shadow.rmiss) ----
+ * A camera ray through the centre of every pixel of a width x height image,
+ * followed for up to cfg->max_bounces segments (MAX_RECURSION) through mirror
+ * and glass hits; at each hit every light with N.L > 0 gets cfg->shadow_spp
+ * shadow rays (samplesBuffer.samples; one ray in REFERENCE mode, where
+ * sampleDisk's by-value seed repeats it).  The frame's colour goes to
+ * d_out_rgba32f (W*H*4 floats, may be NULL) and into d_image_bgra8, the
+ * reference's B8G8R8A8 _rtImage (W*H*4 bytes, may be NULL): stored when
+ * cam->frame[0] < 0, else mixed with the image's 8-bit content with weight
+ * 1 / (1 + frame) (raygen.rgen:69-80).  cam->frame[0] also seeds the RNG. */
+int hy_pathtrace_pass(HyCtx* ctx, const HyCamera* cam, uint32_t width, uint32_t height, const HyPassConfig* cfg,
+                      uint8_t* d_image_bgra8, float* d_out_rgba32f, HyStats* stats);
+
+/* ---- post (replaces the post pass, postFragment.frag:9-20, drawn by
+ *      Renderer::build_post_command_buffers, src/renderer.cpp:2875) ----
+ * rgb = pow(max(rgb, 0.001), 1/2.2) per pixel, alpha kept, into the B8G8R8A8
+ * d_out_bgra8 (UNORM; a swapchain with an sRGB format would encode again on
+ * write).  The input is the pass's 8-bit image d_in_bgra8 (the reference's
+ * _rtImage) or, when that is NULL, the float image d_in_rgba32f. */
+int hy_post_resolve(HyCtx* ctx, uint32_t width, uint32_t height, const uint8_t* d_in_bgra8,
+                    const float* d_in_rgba32f, uint8_t* d_out_bgra8);
+
 /* ---- per-kernel timing (the reference's only timer is the frame rate it
  *      prints, src/renderer.cpp:614) ----
  * While enabled, every kernel launch of the context's passes is bracketed by
@@ -307,8 +339,10 @@ int hy_profile_read(HyCtx* ctx, HyKernelTime* out, uint32_t capacity, uint32_t* 
  * forward pass.  The G-buffer's albedo (plane 2) and roughness/metallic
  * (plane 4 .y/.z) are taken to be the material's own values at the texel's
  * material index (plane 0 .w), as hy_gbuffer_primary writes them; their
- * gradients go to that material.  Bounce rays and bounce-hit shadow rays are
- * re-traced (nothing is stored by the forward pass).
+ * gradients go to that material.  Values a texture supplies (textures[0] for
+ * the diffuse colour, textures[3] for roughness/metallic) are constants and
+ * get no gradient.  Bounce rays and bounce-hit shadow rays are re-traced
+ * (nothing is stored by the forward pass).
  *
  * d_grad_rgba32f: device, W*H*4 floats laid out like hy_shade_pass's
  * d_out_rgba32f (alpha ignored).  d_grad_materials (num_mats*5) and

@@ -115,6 +115,8 @@ struct Scene {
     std::vector<Material> _materials;
     std::vector<uint8_t> skybox_rgba8, irradiance_rgba8;  // equirect maps (miss.rmiss / irradiance)
     uint32_t skybox_w = 0, skybox_h = 0, irradiance_w = 0, irradiance_h = 0;
+    struct Texture { std::vector<uint8_t> rgba8; uint32_t width = 0, height = 0; };
+    std::vector<Texture> _textures;  // Texture::_textures in load order; Material::*Texture index it
 };
 
 class HybridRenderer {
@@ -181,6 +183,17 @@ public:
         if (!s.irradiance_rgba8.empty())
             check(hy_scene_set_env(ctx_, 1, s.irradiance_rgba8.data(), s.irradiance_w, s.irradiance_h),
                   "hy_scene_set_env");
+        if (!s._textures.empty()) {
+            std::vector<const uint8_t*> px;
+            std::vector<uint32_t> w, h;
+            for (const Scene::Texture& t : s._textures) {
+                px.push_back(t.rgba8.data());
+                w.push_back(t.width);
+                h.push_back(t.height);
+            }
+            check(hy_scene_set_textures(ctx_, px.data(), w.data(), h.data(), (uint32_t)px.size()),
+                  "hy_scene_set_textures");
+        }
         num_lights_ = (uint32_t)s._lights.size();
     }
 

@@ -149,6 +149,8 @@ inline ivec2::ivec2(const uvec2& u) : x((int)u.x), y((int)u.y) {}
     inline V normalize(const V& a) { return a / length(a); }                                                            \
     inline V min(const V& a, const V& b) { V r; for (int i = 0; i < N; i++) r.e[i] = b.e[i] < a.e[i] ? b.e[i] : a.e[i]; return r; } \
     inline V max(const V& a, const V& b) { V r; for (int i = 0; i < N; i++) r.e[i] = a.e[i] < b.e[i] ? b.e[i] : a.e[i]; return r; } \
+    inline V min(const V& a, float b) { V r; for (int i = 0; i < N; i++) r.e[i] = b < a.e[i] ? b : a.e[i]; return r; } \
+    inline V max(const V& a, float b) { V r; for (int i = 0; i < N; i++) r.e[i] = a.e[i] < b ? b : a.e[i]; return r; } \
     inline V mix(const V& a, const V& b, float t) { V r; for (int i = 0; i < N; i++) r.e[i] = a.e[i] * (1.0f - t) + b.e[i] * t; return r; } \
     inline V pow(const V& a, const V& b) { V r; for (int i = 0; i < N; i++) r.e[i] = std::pow(a.e[i], b.e[i]); return r; }
 

@@ -125,6 +125,7 @@ void traceRayEXT(const accelerationStructureEXT&, uint flags, uint, uint, uint, 
 #include "blur.comp.hpp"
 #include "raygen.rgen.hpp"
 #include "closesthit.rchit.hpp"
+#include "postFragment.frag.hpp"
 namespace sh_helpers {
 using namespace glsl;
 #include "helpers.glsl.hpp"
@@ -139,7 +140,21 @@ struct RefScene {
     std::vector<int> indices;
     std::vector<float> env[2];
     int env_w[2] = {0, 0}, env_h[2] = {0, 0};
+    std::vector<std::vector<float>> tex;   // Texture::_textures, RGBA8 UNORM as floats
+    std::vector<int> tex_w, tex_h;
 };
+
+// binding 7 / 9 of the hybrid / path-traced sets: the material textures with
+// the NEAREST + REPEAT sampler of src/renderer.cpp:3059
+void bind_textures(Array<sampler2D>& arr, RefScene& s) {
+    arr.v.assign(s.tex.size(), sampler2D());
+    for (size_t k = 0; k < s.tex.size(); k++) {
+        arr.v[k].texels = s.tex[k].data();
+        arr.v[k].w = s.tex_w[k];
+        arr.v[k].h = s.tex_h[k];
+        arr.v[k].repeat = true;
+    }
+}
 
 template <class LightT> std::vector<LightT> make_lights(const std::vector<HyLight>& in) {
     std::vector<LightT> v(in.size());
@@ -276,6 +291,16 @@ int ref_scene_set(void* sp, const HyVertex* verts, uint32_t nv, const uint32_t* 
     return 0;
 }
 
+int ref_scene_set_texture(void* sp, const uint8_t* px, uint32_t w, uint32_t h) {
+    RefScene& s = *(RefScene*)sp;
+    std::vector<float> t((size_t)w * h * 4);
+    for (size_t i = 0; i < t.size(); i++) t[i] = (float)px[i] / 255.0f;
+    s.tex.push_back(std::move(t));
+    s.tex_w.push_back((int)w);
+    s.tex_h.push_back((int)h);
+    return (int)s.tex.size() - 1;
+}
+
 int ref_scene_set_env(void* sp, int slot, const uint8_t* px, uint32_t w, uint32_t h) {
     RefScene& s = *(RefScene*)sp;
     s.env[slot].resize((size_t)w * h * 4);
@@ -403,7 +428,7 @@ int ref_hybrid_pass(void* sp, uint32_t W, uint32_t H, const float* const* planes
     hh::lightsBuffer.lights = RuntimeArray<hh::Light>{hlights.data(), (int)L};
     hh::materials.mat = RuntimeArray<hh::Material>{hmats.data(), (int)hmats.size()};
     bind_env(hh::environmentTexture, s);
-    hh::textures.v.clear();
+    bind_textures(hh::textures, s);
     const size_t np = s.os.prims.size();
     std::vector<vec4> ids(np);
     std::vector<std::vector<hh::Vertex>> vbuf(np);
@@ -442,6 +467,29 @@ int ref_hybrid_pass(void* sp, uint32_t W, uint32_t H, const float* const* planes
     return 0;
 }
 
+// ---- post pass: postFragment.frag at every pixel centre of a W x H target, sampling the
+//      B8G8R8A8 image with the NEAREST / CLAMP _offscreenSampler (src/renderer.cpp:822,
+//      2861); the colour attachment is written as UNORM bytes B, G, R, A ----
+int ref_post(uint32_t W, uint32_t H, const uint8_t* in_bgra8, uint8_t* out_bgra8) {
+    namespace sh = sh_post;
+    std::vector<float> tex((size_t)W * H * 4);
+    for (size_t i = 0; i < (size_t)W * H; i++) {
+        tex[i * 4 + 0] = (float)in_bgra8[i * 4 + 2] / 255.0f;
+        tex[i * 4 + 1] = (float)in_bgra8[i * 4 + 1] / 255.0f;
+        tex[i * 4 + 2] = (float)in_bgra8[i * 4 + 0] / 255.0f;
+        tex[i * 4 + 3] = (float)in_bgra8[i * 4 + 3] / 255.0f;
+    }
+    sh::finalTexture = plane_sampler(tex.data(), (int)W, (int)H);
+    image2D out{out_bgra8, (int)W, (int)H, true, true};
+    for (uint32_t y = 0; y < H; y++)
+        for (uint32_t x = 0; x < W; x++) {
+            sh::outUV = vec2(((float)x + 0.5f) / (float)W, ((float)y + 0.5f) / (float)H);
+            sh::main();
+            imageStore(out, ivec2((int)x, (int)y), sh::fragColor);
+        }
+    return 0;
+}
+
 // ---- path-traced pipeline (Renderer::raytrace, src/renderer.cpp:465-501): raygen.rgen over
 //      W x H, miss 0 miss.rmiss, miss 1 shadow.rmiss, hit group closesthit.rchit; the image
 //      is the B8G8R8A8 _rtImage (src/renderer.cpp:1535), read and written in place ----
@@ -460,7 +508,7 @@ int ref_pathtrace_pass(void* sp, uint32_t W, uint32_t H, const float* cam36, int
     ch::lightsBuffer.lights = RuntimeArray<ch::Light>{clights.data(), (int)L};
     ch::materials.mat = RuntimeArray<ch::Material>{cmats.data(), (int)cmats.size()};
     bind_env(ch::environment_texture, s);
-    ch::textures.v.clear();
+    bind_textures(ch::textures, s);
     ch::samplesBuffer.samples = samples;
     const size_t np = s.os.prims.size();
     std::vector<vec4> ids(np);

@@ -47,6 +47,7 @@ def load():
         "ref_scene_destroy": (None, [P]),
         "ref_scene_set": (C.c_int, [P, P, U32, P, U32, P, U32, P, U32, P, U32, P, U32]),
         "ref_scene_set_env": (C.c_int, [P, C.c_int, P, U32, U32]),
+        "ref_scene_set_texture": (C.c_int, [P, P, U32, U32]),
         "ref_tea": (U32, [U32, U32]),
         "ref_rnd_seq": (None, [U32, U32, P, P]),
         "ref_sample_disk": (None, [C.c_float, P, P, U32, P]),
@@ -55,6 +56,7 @@ def load():
         "ref_blur": (C.c_int, [U32, U32, C.c_int, P, P, P]),
         "ref_hybrid_pass": (C.c_int, [P, U32, U32, P, P, P, P]),
         "ref_pathtrace_pass": (C.c_int, [P, U32, U32, P, C.c_int, P]),
+        "ref_post": (C.c_int, [U32, U32, P, P]),
     }
     for k, (r, a) in sig.items():
         f = getattr(lib, k)
@@ -110,6 +112,9 @@ class RefScene:
         for slot, e in enumerate(env or []):
             e = np.ascontiguousarray(e, np.uint8)
             self.lib.ref_scene_set_env(self.h, slot, _p(e), e.shape[1], e.shape[0])
+        for t in (getattr(scene, "textures", None) or []) if scene is not None else []:
+            t = np.ascontiguousarray(t, np.uint8)
+            self.lib.ref_scene_set_texture(self.h, _p(t), t.shape[1], t.shape[0])
 
     def __del__(self):
         try:
@@ -149,6 +154,14 @@ class RefScene:
         cam = np.ascontiguousarray(cam36, np.float32)
         self.lib.ref_pathtrace_pass(self.h, width, height, _p(cam), samples, _p(image_bgra8))
         return image_bgra8
+
+
+def post(image_bgra8):
+    """postFragment.frag over a B8G8R8A8 image -> B8G8R8A8."""
+    img = np.ascontiguousarray(image_bgra8, np.uint8)
+    out = np.zeros_like(img)
+    load().ref_post(img.shape[1], img.shape[0], _p(img), _p(out))
+    return out
 
 
 def blur(frame, motion_rg, shadow3_u8, hist3_u8):

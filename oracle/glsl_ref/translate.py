@@ -66,6 +66,8 @@ def translate(src: str, stage: str | None) -> str:
     code = re.sub(r"\b(uniform|readonly|writeonly)\s+", "", code)
     # resource arrays `T[N] name;`
     code = re.sub(r"\b(\w+)\s*\[\s*(\w*)\s*\]\s+(\w+)\s*;", r"Array<\1> \3;", code)
+    # stage outputs (`out vec4 fragColor;` at file scope) are plain globals
+    code = re.sub(r"^(\s*)out\s+(\w+)\s+(\w+)\s*;", r"\1\2 \3;", code, flags=re.M)
     # parameter qualifiers
     code = re.sub(r"\binout\s+(\w+)\s+(\w+)", r"\1& \2", code)
     code = re.sub(r"\bout\s+(\w+)\s+(\w+)", r"\1& \2", code)
@@ -85,7 +87,7 @@ def main(src_dir: str, out_dir: str):
     out.mkdir(parents=True, exist_ok=True)
     stages = {"shadowRaygen.rgen": "shadowRaygen", "shadow.rmiss": "shadowMiss", "hybridRaygen.rgen": "hybridRaygen",
               "hybridHit.rchit": "hybridHit", "miss.rmiss": "miss", "blur.comp": "blur", "raygen.rgen": "raygen",
-              "closesthit.rchit": "closesthit"}
+              "closesthit.rchit": "closesthit", "postFragment.frag": "post"}
     for name in ("random.glsl", "helpers.glsl", "raycommon.glsl"):
         (out / (name + ".hpp")).write_text(translate((src / name).read_text(), None))
     for name, stage in stages.items():

@@ -39,6 +39,16 @@ int orc_scene_set_env(void* sp, int slot, const uint8_t* px, uint32_t w, uint32_
     e.px.assign(px, px + (size_t)w * h * 4);
     return 0;
 }
+int orc_scene_set_textures(void* sp, const uint8_t* const* px, const uint32_t* w, const uint32_t* h, uint32_t n) {
+    Scene& s = *(Scene*)sp;
+    s.tex.assign(n, Env());
+    for (uint32_t i = 0; i < n; i++) {
+        s.tex[i].w = w[i];
+        s.tex[i].h = h[i];
+        s.tex[i].px.assign(px[i], px[i] + (size_t)w[i] * h[i] * 4);
+    }
+    return 0;
+}
 uint32_t orc_num_tris(void* sp) { return ((Scene*)sp)->ntri; }
 void orc_world_tris(void* sp, float* out) {
     Scene& s = *(Scene*)sp;
@@ -164,6 +174,10 @@ int orc_shade(void* sp, const HyGBuffer* g, const HyCamera* cam, const HyPassCon
     shade(*(Scene*)sp, gb_of(g), *cam, *cfg, acc->format, acc->history, out_rgba32f, out_bgra8, mode, &p);
     stats_out(p, st);
     return 0;
+}
+
+void orc_post_resolve(uint32_t n, const uint8_t* in_bgra8, const float* in_rgba32f, uint8_t* out_bgra8) {
+    post_resolve(n, in_bgra8, in_rgba32f, out_bgra8);
 }
 
 int orc_pathtrace(void* sp, const HyCamera* cam, uint32_t W, uint32_t H, const HyPassConfig* cfg,

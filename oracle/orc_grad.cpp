@@ -147,8 +147,10 @@ template <class T, class MF, class LF>
 T3<T> eval_hit(const Scene& s, const BounceRec& b, uint32_t NL, MF&& mat, LF&& light) {
     const HyMaterial& M = s.mats[b.mat];
     const int smode = (int)M.smr[0];
-    const T3<T> albedo{gpow(mat(b.mat, 0), 2.2), gpow(mat(b.mat, 1), 2.2), gpow(mat(b.mat, 2), 2.2)};
-    const T rough = mat(b.mat, 3), metal = mat(b.mat, 4);
+    T dif[3];
+    for (int c = 0; c < 3; c++) dif[c] = b.var_alb ? mat(b.mat, c) : T((&b.ms.albedo.x)[c]);
+    const T3<T> albedo{gpow(dif[0], 2.2), gpow(dif[1], 2.2), gpow(dif[2], 2.2)};
+    const T rough = b.var_rm ? mat(b.mat, 3) : T(b.ms.rm.y), metal = b.var_rm ? mat(b.mat, 4) : T(b.ms.rm.z);
     const T keep = T(1.0) - metal;
     const T3<T> F0{T(0.04) * keep + albedo.x * metal, T(0.04) * keep + albedo.y * metal,
                    T(0.04) * keep + albedo.z * metal};
@@ -182,7 +184,7 @@ T3<T> eval_hit(const Scene& s, const BounceRec& b, uint32_t NL, MF&& mat, LF&& l
     }
     const T3<T> F = fresnel(NdotV, F0);
     const T3<T> kD = scale(one_minus(F), T(1.0) - metal);
-    return Lo + kD * albedo * irr;
+    return Lo + kD * albedo * irr + t3<T>(b.ms.emissive);
 }
 
 template <class T, class MF, class LF>
@@ -190,15 +192,9 @@ T3<T> eval_pixel(const Scene& s, const GradRecord& R, size_t pix, MF&& mat, LF&&
     const PixRec& p = R.px[pix];
     if (!p.active) return t3<T>(p.bg);
     T dif[3], rough, metal;
-    if (p.mi >= 0) {
-        for (int c = 0; c < 3; c++) dif[c] = mat(p.mi, c);
-        rough = mat(p.mi, 3);
-        metal = mat(p.mi, 4);
-    } else {
-        for (int c = 0; c < 3; c++) dif[c] = T(p.gb_mat[c]);
-        rough = T(p.gb_mat[3]);
-        metal = T(p.gb_mat[4]);
-    }
+    for (int c = 0; c < 3; c++) dif[c] = p.var_alb ? mat(p.mi, c) : T(p.gb_mat[c]);
+    rough = p.var_rm ? mat(p.mi, 3) : T(p.gb_mat[3]);
+    metal = p.var_rm ? mat(p.mi, 4) : T(p.gb_mat[4]);
     const T3<T> albedo{gpow(dif[0], 2.2), gpow(dif[1], 2.2), gpow(dif[2], 2.2)};
     const T keep = T(1.0) - metal;
     const T3<T> F0{T(0.04) * keep + albedo.x * metal, T(0.04) * keep + albedo.y * metal,
@@ -239,7 +235,7 @@ T3<T> eval_pixel(const Scene& s, const GradRecord& R, size_t pix, MF&& mat, LF&&
     }
     const T3<T> F = fresnel(NdotV, F0);
     const T3<T> kD = scale(one_minus(F), T(1.0) - metal);
-    return rc + kD * albedo * irr + t3<T>(p.emis);
+    return rc + (kD * albedo * irr + t3<T>(p.emis));
 }
 
 template <int KM>
@@ -325,6 +321,8 @@ void grad_record(const Scene& s, const GBufHost& g, const HyCamera& cam, const H
             p.emis = v3(g5[0], g5[1], g5[2]);
             p.gb_mat[0] = g2[0]; p.gb_mat[1] = g2[1]; p.gb_mat[2] = g2[2];
             p.gb_mat[3] = g4[1]; p.gb_mat[4] = g4[2];
+            p.var_alb = p.mi >= 0 && !(s.mats[p.mi].textures[0] > -1.f);
+            p.var_rm = p.mi >= 0 && !(s.mats[p.mi].textures[3] > -1.f);
             p.active = !(g0[3] == 0.f && g1[3] == 0.f);
             p.nb = 0;
             p.ndl = 0;
@@ -375,6 +373,9 @@ void grad_record(const Scene& s, const GBufHost& g, const HyCamera& cam, const H
                     Payload pl = closest_hit(s, h, ro, direction, seed, cfg, mode, ls, &b.vis);
                     const HitAttr a = hit_attributes(s, h);
                     b.mat = (int)s.prims[a.prim].material_id;
+                    b.ms = material_at(s, s.mats[b.mat], a.u, a.v);
+                    b.var_alb = !(s.mats[b.mat].textures[0] > -1.f);
+                    b.var_rm = !(s.mats[b.mat].textures[3] > -1.f);
                     b.N = a.N;
                     b.V = normalize(-direction);
                     b.wp = ro + direction * h.t;

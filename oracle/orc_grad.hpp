@@ -21,13 +21,16 @@ struct BounceRec {
     float NdotV;
     uint64_t vis;                   // bit i: light i's shadow factor was 2
     uint64_t ndl;                   // bit i: light i on the lit side of the hit
+    bool var_alb, var_rm;           // diffuse / roughness-metallic are parameters (no texture)
+    MatSample ms;                   // the material's inputs at the hit (textures sampled)
 };
 struct PixRec {
     bool active;                    // false: background, the colour is the G-buffer albedo
     int mi, smode;                  // material index (-1: none) and its shading model
     V3<float> pos, N, V, irr, emis, bg;
     float NdotV;
-    float gb_mat[5];                // G-buffer diffuse rgb, roughness, metallic (for mi < 0)
+    float gb_mat[5];                // G-buffer diffuse rgb, roughness, metallic (constants where not parameters)
+    bool var_alb, var_rm;           // the G-buffer values are the material's parameters
     uint64_t ndl;                   // bit i: light i on the lit side of the pixel
     int nb;
     BounceRec b[kGradMaxBounces];

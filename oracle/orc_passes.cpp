@@ -105,6 +105,22 @@ static V3<float> env_lookup(const Env& e, float u, float v) {
     return v3((float)p[0] / 255.0f, (float)p[1] / 255.0f, (float)p[2] / 255.0f);
 }
 
+V3<float> tex_lookup(const Scene& s, float id, float u, float v) {
+    const int i = (int)id;
+    if (i < 0 || (size_t)i >= s.tex.size()) return v3(0.f, 0.f, 0.f);
+    return env_lookup(s.tex[i], u, v);
+}
+
+// a material's inputs at a surface point: hybridHit.rchit:62-66 / closesthit.rchit:74-81
+// (textures ids in mat.textures: x diffuse, z emissive, w metallic-roughness)
+MatSample material_at(const Scene& s, const HyMaterial& m, float u, float v) {
+    MatSample r;
+    r.albedo = m.textures[0] > -1.f ? tex_lookup(s, m.textures[0], u, v) : v3(m.diffuse[0], m.diffuse[1], m.diffuse[2]);
+    r.emissive = m.textures[2] > -1.f ? tex_lookup(s, m.textures[2], u, v) : v3(0.f, 0.f, 0.f);
+    r.rm = m.textures[3] > -1.f ? tex_lookup(s, m.textures[3], u, v) : v3(0.f, m.smr[2], m.smr[1]);
+    return r;
+}
+
 // hybridRaygen.rgen:59-60 / hybridHit.rchit:272-273
 V3<float> irradiance_at(const Scene& s, V3<float> N) {
     const float PI = K<float>::PI;
@@ -161,7 +177,7 @@ HitAttr hit_attributes(const Scene& s, const Hit& h) {
     const HyPrimitive& pr = s.prims[p];
     uint32_t local = h.id - s.prim_tri0[p];
     float b0 = 1.0f - h.b1 - h.b2;
-    V3<float> n = v3(0.f, 0.f, 0.f);
+    V3<float> n = v3(0.f, 0.f, 0.f), col = v3(0.f, 0.f, 0.f);
     float u = 0.f, v = 0.f;
     float bw[3] = {b0, h.b1, h.b2};
     for (int k = 0; k < 3; k++) {
@@ -169,13 +185,14 @@ HitAttr hit_attributes(const Scene& s, const Hit& h) {
         n = n + v3(vx.normal[0], vx.normal[1], vx.normal[2]) * bw[k];
         u = u + vx.uv[0] * bw[k];
         v = v + vx.uv[1] * bw[k];
+        col = col + v3(vx.color[0], vx.color[1], vx.color[2]) * bw[k];
     }
     const float* nm = &s.nrm[(size_t)pr.transform_id * 9];
     V3<float> tn;
     tn.x = nm[0] * n.x + nm[3] * n.y + nm[6] * n.z;
     tn.y = nm[1] * n.x + nm[4] * n.y + nm[7] * n.z;
     tn.z = nm[2] * n.x + nm[5] * n.y + nm[8] * n.z;
-    return HitAttr{normalize(tn), u, v, p};
+    return HitAttr{normalize(tn), u, v, p, col};
 }
 
 void gbuffer_primary(const Scene& s, const HyCamera& cam, uint32_t W, uint32_t H, float* planes[6], int mode) {
@@ -197,10 +214,13 @@ void gbuffer_primary(const Scene& s, const HyCamera& cam, uint32_t W, uint32_t H
             V3<float> wp = v3(o[0], o[1], o[2]) + v3(d[0], d[1], d[2]) * h.t;
             p0[0] = wp.x; p0[1] = wp.y; p0[2] = wp.z; p0[3] = m.smr[3];
             p1[0] = a.N.x * 0.5f + 0.5f; p1[1] = a.N.y * 0.5f + 0.5f; p1[2] = a.N.z * 0.5f + 0.5f; p1[3] = 1.f;
-            p2[0] = m.diffuse[0]; p2[1] = m.diffuse[1]; p2[2] = m.diffuse[2]; p2[3] = 1.f;
+            // geometry_shader.frag:56-59: a diffuse texture is modulated by the vertex colour
+            const MatSample ms = material_at(s, m, a.u, a.v);
+            const V3<float> alb = m.textures[0] > -1.f ? ms.albedo * a.color : ms.albedo;
+            p2[0] = alb.x; p2[1] = alb.y; p2[2] = alb.z; p2[3] = 1.f;
             p3[0] = 0.5f; p3[1] = 0.5f;  // static camera: ndc - ndcPrev = 0
-            p4[0] = 0.f; p4[1] = m.smr[2]; p4[2] = m.smr[1]; p4[3] = 1.f;
-            p5[0] = 0.f; p5[1] = 0.f; p5[2] = 0.f; p5[3] = 1.f;
+            p4[0] = ms.rm.x; p4[1] = ms.rm.y; p4[2] = ms.rm.z; p4[3] = 1.f;
+            p5[0] = ms.emissive.x; p5[1] = ms.emissive.y; p5[2] = ms.emissive.z; p5[3] = 1.f;
         }
     });
 }
@@ -341,9 +361,10 @@ Payload closest_hit(const Scene& s, const Hit& h, V3<float> ro, V3<float> rd, ui
     V3<float> worldPos = ro + rd * h.t;
     const HyMaterial& mat = s.mats[s.prims[a.prim].material_id];
     int smode = (int)mat.smr[0];
-    V3<float> albedo = v3(mat.diffuse[0], mat.diffuse[1], mat.diffuse[2]);
-    V3<float> emissive = v3(0.f, 0.f, 0.f);
-    float roughness = mat.smr[2], metallic = mat.smr[1];
+    const MatSample ms = material_at(s, mat, a.u, a.v);  // hybridHit.rchit:62-66
+    V3<float> albedo = ms.albedo;
+    V3<float> emissive = ms.emissive;
+    float roughness = ms.rm.y, metallic = ms.rm.z;
     albedo = pow3(albedo, 2.2f);
     V3<float> F0 = mix3(splat(0.04f), albedo, metallic);
     V3<float> irradiance = irradiance_at(s, N);
@@ -548,7 +569,7 @@ void shade(const Scene& s, const GBufHost& g, const HyCamera& cam, const HyPassC
                 V3<float> F = FresnelSchlick(NdotV, F0);
                 V3<float> kD = (splat(1.0f) - F) * (1.0f - metallic);
                 V3<float> ambient = kD * albedo * irradiance;
-                fc = rayColor + ambient + emissive;
+                fc = rayColor + (ambient + emissive);  // finalColor += ambient + emissive (hybridRaygen.rgen:180)
             }
             if (out_rgba32f) {
                 float* o = out_rgba32f + pix * 4;
@@ -563,6 +584,25 @@ void shade(const Scene& s, const GBufHost& g, const HyCamera& cam, const HyPassC
     if (st) for (auto& l : loc) st->add(l);
 }
 
+// ---- post (postFragment.frag:9-20) ---------------------------------------------------
+void post_resolve(uint32_t n, const uint8_t* in_bgra8, const float* in_rgba32f, uint8_t* out_bgra8) {
+    const float gamma = 1.0f / 2.2f;
+    for (size_t i = 0; i < n; i++) {
+        float c[4];
+        if (in_bgra8) {
+            const uint8_t* q = in_bgra8 + i * 4;
+            c[0] = (float)q[2] / 255.0f; c[1] = (float)q[1] / 255.0f; c[2] = (float)q[0] / 255.0f;
+            c[3] = (float)q[3] / 255.0f;
+        } else {
+            for (int k = 0; k < 4; k++) c[k] = in_rgba32f[i * 4 + k];
+        }
+        float rgb[3];
+        for (int k = 0; k < 3; k++) rgb[k] = std::pow(std::fmax(c[k], 0.001f), gamma);
+        uint8_t* o = out_bgra8 + i * 4;
+        o[0] = quant8(rgb[2]); o[1] = quant8(rgb[1]); o[2] = quant8(rgb[0]); o[3] = quant8(c[3]);
+    }
+}
+
 // ---- path-traced mode (raygen.rgen:20-81, closesthit.rchit:26-186, miss.rmiss) ----------
 static Payload closest_hit_pt(const Scene& s, const Hit& h, V3<float> ro, V3<float> rd, uint32_t& seed,
                               const HyPassConfig& cfg, int mode, PassStats& ls) {
@@ -574,8 +614,9 @@ static Payload closest_hit_pt(const Scene& s, const Hit& h, V3<float> ro, V3<flo
     V3<float> worldPos = ro + rd * h.t;
     const HyMaterial& mat = s.mats[s.prims[a.prim].material_id];
     int smode = (int)mat.smr[0];
-    V3<float> albedo = pow3(v3(mat.diffuse[0], mat.diffuse[1], mat.diffuse[2]), 2.2f);
-    float roughness = mat.smr[2], metallic = mat.smr[1];
+    const MatSample ms = material_at(s, mat, a.u, a.v);  // closesthit.rchit:74-81
+    V3<float> albedo = pow3(ms.albedo, 2.2f);
+    float roughness = ms.rm.y, metallic = ms.rm.z;
     V3<float> F0 = mix3(splat(0.04f), albedo, metallic);
     V3<float> irradiance = irradiance_at(s, N);
     V3<float> direction = v3(1.f, 1.f, 1.f);
@@ -664,7 +705,7 @@ static Payload closest_hit_pt(const Scene& s, const Hit& h, V3<float> ro, V3<flo
     V3<float> F = FresnelSchlick(NdotV, F0);
     V3<float> kD = (splat(1.0f) - F) * (1.0f - metallic);
     Payload p;
-    p.color = Lo + kD * albedo * irradiance;
+    p.color = Lo + kD * albedo * irradiance + ms.emissive;
     p.t = h.t;
     p.dir = direction;
     p.scattered = dirw;

@@ -42,9 +42,12 @@ template <class F> void parallel_rows(uint32_t H, F&& f) {
     for (auto& x : th) x.join();
 }
 
-struct HitAttr { V3<float> N; float u, v; uint32_t prim; };
+struct HitAttr { V3<float> N; float u, v; uint32_t prim; V3<float> color; };
 struct Payload { V3<float> color; float t; V3<float> dir; float scattered; V3<float> origin; };
 
+struct MatSample { V3<float> albedo, emissive, rm; };  // albedo before pow(2.2); rm = (_, roughness, metallic)
+V3<float> tex_lookup(const Scene& s, float id, float u, float v);
+MatSample material_at(const Scene& s, const HyMaterial& m, float u, float v);
 V3<float> irradiance_at(const Scene& s, V3<float> N);
 V3<float> miss_color(const Scene& s, V3<float> d);
 int mat_index(float f, size_t n);
@@ -65,6 +68,8 @@ void accumulate(const GBufHost& g, const HyPassConfig& cfg, uint32_t fmt, const 
                 uint32_t num_lights);
 void shade(const Scene& s, const GBufHost& g, const HyCamera& cam, const HyPassConfig& cfg, uint32_t fmt,
            const void* hist, float* out_rgba32f, uint8_t* out_bgra8, int mode, PassStats* st);
+// post pass: pow(max(rgb, 0.001), 1/2.2) of n pixels into BGRA8
+void post_resolve(uint32_t n, const uint8_t* in_bgra8, const float* in_rgba32f, uint8_t* out_bgra8);
 // path-traced mode: camera rays, closesthit.rchit shading, running mean into the
 // BGRA8 image (frame >= 0) or a plain store (frame < 0); out_rgba32f gets the
 // frame's colour before the mean (either may be NULL)

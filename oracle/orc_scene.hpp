@@ -48,6 +48,7 @@ struct Scene {
     std::vector<HyMaterial> mats;
     std::vector<HyLight> lights;
     Env env[2];
+    std::vector<Env> tex;         // material textures (RGBA8, NEAREST / REPEAT), by texture id
     // derived geometry
     uint32_t ntri = 0;
     std::vector<float> world;        // 9 floats per triangle (v0, v1, v2) in world space

@@ -43,6 +43,7 @@ def load():
         "orc_scene_set_materials": (C.c_int, [P, P, U32]),
         "orc_scene_set_lights": (C.c_int, [P, P, U32]),
         "orc_scene_set_env": (C.c_int, [P, C.c_int, P, U32, U32]),
+        "orc_scene_set_textures": (C.c_int, [P, P, P, P, U32]),
         "orc_num_tris": (U32, [P]),
         "orc_world_tris": (None, [P, P]),
         "orc_bvh_build": (C.c_int, [P, P, P]),
@@ -58,6 +59,7 @@ def load():
         "orc_accumulate": (C.c_int, [P, P, P, P, P]),
         "orc_shade": (C.c_int, [P, P, P, P, P, P, P, C.c_int, P]),
         "orc_pathtrace": (C.c_int, [P, P, U32, U32, P, P, P, C.c_int, P]),
+        "orc_post_resolve": (None, [U32, P, P, P]),
         "orc_grad_record": (P, [P, P, P, P, P, C.c_int]),
         "orc_grad_free": (None, [P]),
         "orc_grad_forward": (C.c_int, [P, P, P, P, P]),
@@ -164,6 +166,18 @@ class OracleScene:
 
     def set_scene(self, scene):
         self.set_scene_arrays(*scene.pack(), scene.env)
+        if getattr(scene, "textures", None):
+            self.set_textures(scene.textures)
+
+    def set_textures(self, textures):
+        """textures: list of (H, W, 4) uint8 RGBA8 images, indexed by the materials' texture ids."""
+        texs = [np.ascontiguousarray(t, np.uint8) for t in textures]
+        self._tex = texs
+        n = len(texs)
+        ptrs = (C.c_void_p * max(n, 1))(*[t.ctypes.data for t in texs])
+        w = np.array([t.shape[1] for t in texs] or [0], np.uint32)
+        h = np.array([t.shape[0] for t in texs] or [0], np.uint32)
+        self.lib.orc_scene_set_textures(self.h, ptrs, _p(w), _p(h), n)
 
     def set_lights(self, lights):
         lights = np.ascontiguousarray(lights, np.float32)
@@ -287,6 +301,19 @@ class OracleScene:
         st = {k: st1[k] + st2[k] for k in st1 if k != "error_flags"}
         st["error_flags"] = st1["error_flags"] | st2["error_flags"]
         return out_f, out_8, shadow, st
+
+
+def post_resolve(image: np.ndarray) -> np.ndarray:
+    """postFragment.frag on a BGRA8 (uint8) or RGBA32F (float32) (H, W, 4) image -> BGRA8."""
+    img = np.ascontiguousarray(image)
+    out = np.zeros(img.shape[:2] + (4,), np.uint8)
+    n = img.shape[0] * img.shape[1]
+    if img.dtype == np.uint8:
+        load().orc_post_resolve(n, _p(img), None, _p(out))
+    else:
+        img = np.ascontiguousarray(img, np.float32)
+        load().orc_post_resolve(n, None, _p(img), _p(out))
+    return out
 
 
 class GradOracle:

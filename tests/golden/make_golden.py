@@ -11,6 +11,17 @@ ref_pass_small.npz
                   hybridRaygen.rgen + hybridHit.rchit + miss.rmiss +
                   shadow.rmiss run on the 48x48 small_glass workload (glass,
                   mirrors, 8 bounces), with its inputs (G-buffer, camera).
+ref_pathtrace_small.npz
+                  the reference's own path-traced pipeline (raygen.rgen +
+                  closesthit.rchit + miss.rmiss + shadow.rmiss) on the same
+                  workload: the B8G8R8A8 image after frames -1, 1 and 2.
+ref_textured_small.npz
+                  the reference's own shadowRaygen / hybrid shaders and
+                  path-traced shaders on the textured 48x40 workload, with
+                  its G-buffer input.
+ref_post_small.npz
+                  the reference's postFragment.frag (gamma 1/2.2) over a
+                  random B8G8R8A8 image.
 
 "The reference's own" = the reference checkout's shader sources rewritten
 into C++ and compiled by oracle/glsl_ref (Makefile, translate.py,
@@ -126,6 +137,48 @@ def ref_pass(ref):
                 blur_after_frame0=blur_f0, blur_after_frame3=blur_f3)
 
 
+def ref_pathtrace(ref):
+    """The reference's path-traced pipeline (raygen.rgen + closesthit.rchit + miss shaders) on
+    the 48x48 small_glass workload, 2 shadow samples: frame -1 stores, frames 1 and 2 mix
+    into the B8G8R8A8 image."""
+    from vulkanhybridraytracer_gb300 import scenes
+
+    wl = scenes.small_glass()
+    rs = ref.RefScene(wl.scene)
+    img = np.zeros((wl.height, wl.width, 4), np.uint8)
+    out = {}
+    for frame in (-1, 1, 2):
+        cam = wl.camera(float(frame))
+        img = rs.pathtrace_pass(cam, wl.width, wl.height, 2, img)
+        out[f"camera_f{frame + 1}"] = cam
+        out[f"image_f{frame + 1}"] = img.copy()
+    return out
+
+
+def ref_textured(ref):
+    """The reference's hybrid and path-traced shaders on the 48x40 small_textured workload
+    (checker / noise / emissive RGBA8 textures, NEAREST + REPEAT), with its G-buffer input."""
+    import pyoracle as po
+    from vulkanhybridraytracer_gb300 import scenes
+
+    wl = scenes.small_textured(48, 40)
+    cam = wl.camera(2.0)
+    orc = po.OracleScene()
+    orc.set_scene(wl.scene)
+    planes = orc.gbuffer(cam, wl.width, wl.height, po.TRACE_BRUTE)
+    rs = ref.RefScene(wl.scene)
+    shadow = rs.shadow_pass(planes, cam, 2)
+    hybrid = rs.hybrid_pass(planes, cam, shadow)
+    img = np.zeros((wl.height, wl.width, 4), np.uint8)
+    out = dict(camera=cam, **{f"plane{i}": planes[i] for i in range(6)}, shadow_spp2=shadow, hybrid_rgba=hybrid)
+    for frame in (-1, 1):
+        c = wl.camera(float(frame))
+        img = rs.pathtrace_pass(c, wl.width, wl.height, 2, img)
+        out[f"pt_camera_f{frame + 1}"] = c
+        out[f"pt_image_f{frame + 1}"] = img.copy()
+    return out
+
+
 def make():
     ref = None
     try:
@@ -142,7 +195,14 @@ def make():
         return
     (HERE / "ref_kat.json").write_text(json.dumps(ref_kat(ref)) + "\n")
     np.savez_compressed(HERE / "ref_pass_small.npz", **ref_pass(ref))
-    print("wrote rng_kat.json, ref_kat.json, ref_pass_small.npz from the reference's shader code")
+    np.savez_compressed(HERE / "ref_pathtrace_small.npz", **ref_pathtrace(ref))
+    np.savez_compressed(HERE / "ref_textured_small.npz", **ref_textured(ref))
+    g = np.random.default_rng(11)
+    post_in = g.integers(0, 256, (24, 40, 4)).astype(np.uint8)
+    post_in[0, :8, :3] = 0  # below the 0.001 floor
+    np.savez_compressed(HERE / "ref_post_small.npz", image=post_in, post=ref.post(post_in))
+    print("wrote rng_kat.json, ref_kat.json, ref_pass_small.npz, ref_pathtrace_small.npz, ref_textured_small.npz, "
+          "ref_post_small.npz from the reference's shader code")
 
 
 if __name__ == "__main__":

@@ -22,9 +22,17 @@ def _setup(oracle_lib, wl, spp=4):
     return sc, planes, cam, cfg, shadow, g, mp, lp
 
 
-@pytest.mark.parametrize("which", ["diff", "glass"])
+def _wl(which, w, h):
+    if which == "diff":
+        return scenes.diff(3, w, h)
+    if which == "glass":
+        return scenes.small_glass(w, h)
+    return scenes.small_textured(w, h)
+
+
+@pytest.mark.parametrize("which", ["diff", "glass", "textured"])
 def test_fp64_forward_matches_float_pass(oracle_lib, which):
-    wl = scenes.diff(3, 40, 40) if which == "diff" else scenes.small_glass(40, 40)
+    wl = _wl(which, 40, 40)
     sc, planes, cam, cfg, shadow, g, mp, lp = _setup(oracle_lib, wl)
     img64 = g.forward(mp, lp)
     out_f, _, _ = sc.shade(planes, cam, cfg, shadow, 1)
@@ -34,9 +42,9 @@ def test_fp64_forward_matches_float_pass(oracle_lib, which):
     assert err.max() <= 1e-3 * max(1.0, np.abs(ref).max())
 
 
-@pytest.mark.parametrize("which", ["diff", "glass"])
+@pytest.mark.parametrize("which", ["diff", "glass", "textured"])
 def test_fp64_adjoint_matches_central_differences(oracle_lib, which):
-    wl = scenes.diff(3, 32, 32) if which == "diff" else scenes.small_glass(32, 32)
+    wl = _wl(which, 32, 32)
     sc, planes, cam, cfg, shadow, g, mp, lp = _setup(oracle_lib, wl)
     rng = np.random.default_rng(7)
     w = rng.normal(size=(wl.height, wl.width, 3))

@@ -1,8 +1,9 @@
 """The oracle against the reference's own shader code.
 
-tests/golden/ref_kat.json and ref_pass_small.npz hold outputs of the
-reference's helpers.glsl / shadowRaygen.rgen / blur.comp / hybridRaygen.rgen
-+ hybridHit.rchit + miss.rmiss + shadow.rmiss, compiled as C++ from the
+tests/golden/ref_kat.json, ref_pass_small.npz and ref_pathtrace_small.npz
+hold outputs of the reference's helpers.glsl / shadowRaygen.rgen / blur.comp /
+hybridRaygen.rgen + hybridHit.rchit + miss.rmiss + shadow.rmiss and of its
+path-traced raygen.rgen + closesthit.rchit, compiled as C++ from the
 reference checkout (oracle/glsl_ref) and generated by
 tests/golden/make_golden.py.  The oracle must reproduce them bit for bit.
 Where the reference checkout is present the pin is also re-run live on
@@ -106,3 +107,87 @@ def test_live_pin_against_reference_shaders(oracle_lib):
             assert np.array_equal(sh, rs.shadow_pass(planes, cam, spp))
         out, _, _ = o.shade(planes, cam, po.cfg_dict(spp=3, max_bounces=8, rng_mode=0), sh, 0, po.TRACE_BRUTE)
         assert np.array_equal(out, rs.hybrid_pass(planes, cam, sh))
+
+
+@pytest.mark.parametrize("mode", [po.TRACE_BRUTE, po.TRACE_BVH8])
+def test_pathtrace_equals_reference(oracle_lib, mode):
+    """raygen.rgen + closesthit.rchit + miss shaders: the B8G8R8A8 image after frames -1, 1, 2."""
+    fx = dict(np.load(GOLD / "ref_pathtrace_small.npz"))
+    wl = scenes.small_glass()
+    o = po.OracleScene()
+    o.set_scene(wl.scene)
+    o.build_bvh()
+    img = np.zeros((wl.height, wl.width, 4), np.uint8)
+    for f in (0, 2, 3):
+        img, _, st = o.pathtrace(fx[f"camera_f{f}"], wl.width, wl.height,
+                                 po.cfg_dict(spp=2, max_bounces=8, rng_mode=0), img, mode)
+        ref = fx[f"image_f{f}"]
+        assert st["reflection_rays"] > 0 and st["shadow_rays"] > 0
+        if mode == po.TRACE_BRUTE:
+            assert np.array_equal(img, ref), f
+        else:  # BVH8: the same hits except exact ties/edges
+            assert np.mean(np.any(img != ref, -1)) <= 2e-3, f
+
+
+def test_live_pathtrace_pin(oracle_lib):
+    import sys
+    sys.path.insert(0, str(Path(po.__file__).resolve().parent / "glsl_ref"))
+    import pyref
+    if not pyref.available():
+        pytest.skip("reference checkout not present")
+    wl = scenes.small(0, 40, 32)
+    o = po.OracleScene()
+    o.set_scene(wl.scene)
+    rs = pyref.RefScene(wl.scene)
+    a = np.zeros((wl.height, wl.width, 4), np.uint8)
+    b = a.copy()
+    for frame in (0.0, 5.0):
+        cam = wl.camera(frame)
+        a, _, _ = o.pathtrace(cam, wl.width, wl.height, po.cfg_dict(spp=3, max_bounces=8, rng_mode=0), a,
+                              po.TRACE_BRUTE)
+        b = rs.pathtrace_pass(cam, wl.width, wl.height, 3, b)
+        assert np.array_equal(a, b)
+
+
+def test_post_equals_reference(oracle_lib):
+    """postFragment.frag: pow(max(rgb, 0.001), 1/2.2) on the 8-bit image."""
+    fx = dict(np.load(GOLD / "ref_post_small.npz"))
+    assert np.array_equal(po.post_resolve(fx["image"]), fx["post"])
+    # the float input form equals the 8-bit one on the same values
+    f = fx["image"][..., [2, 1, 0, 3]].astype(np.float32) / np.float32(255.0)
+    assert np.array_equal(po.post_resolve(f), fx["post"])
+
+
+@pytest.fixture(scope="module")
+def tex_fx(oracle_lib):
+    fx = dict(np.load(GOLD / "ref_textured_small.npz"))
+    wl = scenes.small_textured(48, 40)
+    o = po.OracleScene()
+    o.set_scene(wl.scene)
+    o.build_bvh()
+    return fx, wl, o
+
+
+def test_textured_gbuffer_input_is_the_oracle_producer(tex_fx):
+    fx, wl, o = tex_fx
+    planes = o.gbuffer(fx["camera"], wl.width, wl.height, po.TRACE_BRUTE)
+    for i in range(6):
+        assert np.array_equal(planes[i], fx[f"plane{i}"]), i
+    # the textures show up: albedo varies within one material, emissive texels exist
+    assert np.unique(planes[2][..., 0]).size > 8 and planes[5][..., :3].max() > 0
+
+
+def test_textured_passes_equal_reference(tex_fx):
+    """hybridHit.rchit / closesthit.rchit texture branches (hybridHit.rchit:63-65,
+    closesthit.rchit:76-78) and the emissive term, on the reference's own shader code."""
+    fx, wl, o = tex_fx
+    planes = [np.ascontiguousarray(fx[f"plane{i}"]) for i in range(6)]
+    sh, _ = o.shadow_pass(planes, fx["camera"], po.cfg_dict(spp=2, rng_mode=0), 0, po.TRACE_BRUTE)
+    assert np.array_equal(sh, fx["shadow_spp2"])
+    out, _, _ = o.shade(planes, fx["camera"], po.cfg_dict(spp=2, max_bounces=8, rng_mode=0), sh, 0, po.TRACE_BRUTE)
+    assert np.array_equal(out, fx["hybrid_rgba"])
+    img = np.zeros((wl.height, wl.width, 4), np.uint8)
+    for f in (0, 2):
+        img, _, _ = o.pathtrace(fx[f"pt_camera_f{f}"], wl.width, wl.height,
+                                po.cfg_dict(spp=2, max_bounces=8, rng_mode=0), img, po.TRACE_BRUTE)
+        assert np.array_equal(img, fx[f"pt_image_f{f}"]), f

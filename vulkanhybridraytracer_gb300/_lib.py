@@ -147,8 +147,13 @@ PROTOTYPES = {
                                 C.POINTER(HyAccum), P, P, C.POINTER(HyStats)]),
     "hy_hybrid_forward_host": (I32, [P, C.POINTER(HyGBuffer), C.POINTER(HyCamera), C.POINTER(HyPassConfig),
                                      C.POINTER(HyAccum), P, P, C.POINTER(HyStats)]),
+    "hy_scene_set_textures": (I32, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                    C.c_uint32]),
+    "hy_post_resolve": (I32, [P, C.c_uint32, C.c_uint32, P, P, P]),
     "hy_hybrid_backward": (I32, [P, C.POINTER(HyGBuffer), C.POINTER(HyCamera), C.POINTER(HyPassConfig),
                                  C.POINTER(HyAccum), P, P, P, C.POINTER(HyStats)]),
+    "hy_pathtrace_pass": (I32, [P, C.POINTER(HyCamera), C.c_uint32, C.c_uint32, C.POINTER(HyPassConfig), P, P,
+                                C.POINTER(HyStats)]),
     "hy_accumulate_pass_noalloc": (I32, [C.POINTER(HyGBuffer), C.POINTER(HyPassConfig), P, C.POINTER(HyAccum), P]),
     "hy_batch_forward": (I32, [P, C.POINTER(P), U32, C.POINTER(HyView), U32, U32, C.POINTER(HyPassConfig),
                                C.POINTER(HyStats)]),

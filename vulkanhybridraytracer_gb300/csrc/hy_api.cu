@@ -128,6 +128,9 @@ SceneDev scene_dev(HyCtx* c) {
     S.env1 = c->env[1].as<uchar4>();
     S.num_mats = c->nmats;
     S.num_lights = c->nlights;
+    S.tex_px = c->tex_px.as<uchar4>();
+    S.tex_tab = c->tex_tab.as<uint4>();
+    S.num_tex = c->ntex;
     S.num_nodes = c->bvh_ok ? c->n_bvh8 : 0;
     S.num_tris = c->bvh_ok ? c->ntri : 0;
     for (int i = 0; i < 2; i++) { S.env_w[i] = c->env_w[i]; S.env_h[i] = c->env_h[i]; }
@@ -207,6 +210,10 @@ int check_scene_ready(HyCtx* c) {
     if (!c->geometry_ok || !c->bvh_ok) return HY_ERR_NOT_READY;
     if (c->nmats == 0) return HY_ERR_NOT_READY;
     if (c->max_material_id >= c->nmats) return HY_ERR_INVALID_ARG;  // a primitive names a missing material
+    // the shaders sample textures x (diffuse), z (emissive), w (metallic-roughness) when > -1
+    for (const HyMaterial& m : c->h_mats)
+        for (int k : {0, 2, 3})
+            if (m.textures[k] > -1.f && !(m.textures[k] < (float)c->ntex)) return HY_ERR_INVALID_ARG;
     return HY_OK;
 }
 
@@ -257,10 +264,10 @@ PassParams make_params(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const
 
 // ---- per-kernel timing ----
 // the first five are the MODE_* values of hy_pass.h
-enum { PK_ACCUM = MODE_SHADOW_ACCUM_G + 1, PK_GRAD, PK_COUNT };
+enum { PK_ACCUM = MODE_SHADOW_ACCUM_G + 1, PK_GRAD, PK_PATHTRACE, PK_COUNT };
 const char* const kProfNames[PK_COUNT] = {"k_shadow",       "k_pixels<shade>",       "k_shadow<accum>",
                                           "k_shadow_group", "k_shadow_group<accum>", "k_accumulate",
-                                          "k_shade_grad"};
+                                          "k_shade_grad",   "k_pathtrace"};
 static_assert(MODE_SHADOW == 0 && MODE_SHADE == 1 && MODE_SHADOW_ACCUM == 2 && MODE_SHADOW_G == 3 &&
                   MODE_SHADOW_ACCUM_G == 4,
               "profile names follow the pass modes");
@@ -380,7 +387,7 @@ void hy_destroy(HyCtx* c) {
                       &c->node_plan, &c->dstats,
                       &c->raw_shadow, &c->hist_prev, &c->host_in[0], &c->host_in[1], &c->host_in[2],
                       &c->host_in[3], &c->host_in[4], &c->host_in[5], &c->host_out_f, &c->host_out_8,
-                      &c->grad_partial};
+                      &c->grad_partial, &c->tex_px, &c->tex_tab};
     for (DevBuf* b : bufs) ctx_free(c, *b);
     if (c->h_stats) cudaFreeHost(c->h_stats);
     for (cudaEvent_t e : c->prof_pool) cudaEventDestroy(e);
@@ -437,8 +444,11 @@ int hy_scene_set_geometry(HyCtx* c, const HyVertex* verts, uint32_t nv, const ui
         vattr[(size_t)v * 8 + 0] = verts[v].normal[0];
         vattr[(size_t)v * 8 + 1] = verts[v].normal[1];
         vattr[(size_t)v * 8 + 2] = verts[v].normal[2];
+        vattr[(size_t)v * 8 + 3] = verts[v].color[0];
         vattr[(size_t)v * 8 + 4] = verts[v].uv[0];
         vattr[(size_t)v * 8 + 5] = verts[v].uv[1];
+        vattr[(size_t)v * 8 + 6] = verts[v].color[1];
+        vattr[(size_t)v * 8 + 7] = verts[v].color[2];
     }
     std::vector<float> nrm = normal_matrices(xf, nx);
     int rc;
@@ -465,7 +475,32 @@ int hy_scene_set_materials(HyCtx* c, const HyMaterial* m, uint32_t n) {
     DeviceGuard g(c->device);
     int rc = upload(c, c->mats, m, n);
     if (rc) return rc;
+    c->h_mats.assign(m, m + n);
     c->nmats = n;
+    return HY_OK;
+}
+
+int hy_scene_set_textures(HyCtx* c, const uint8_t* const* rgba8, const uint32_t* widths, const uint32_t* heights,
+                          uint32_t n) {
+    if (!c || (n && (!rgba8 || !widths || !heights))) return HY_ERR_INVALID_ARG;
+    uint64_t total = 0;
+    std::vector<uint32_t> tab((size_t)std::max<uint32_t>(n, 1) * 4, 0u);
+    for (uint32_t i = 0; i < n; i++) {
+        if (!rgba8[i] || widths[i] == 0 || heights[i] == 0) return HY_ERR_INVALID_ARG;
+        tab[(size_t)i * 4 + 0] = (uint32_t)total;
+        tab[(size_t)i * 4 + 1] = widths[i];
+        tab[(size_t)i * 4 + 2] = heights[i];
+        total += (uint64_t)widths[i] * heights[i];
+        if (total >= (1ull << 32)) return HY_ERR_INVALID_ARG;
+    }
+    DeviceGuard g(c->device);
+    int rc;
+    if ((rc = ctx_alloc(c, c->tex_px, (size_t)std::max<uint64_t>(total, 1) * 4))) return rc;
+    for (uint32_t i = 0; i < n; i++)
+        HY_CUDA_TRY(cudaMemcpyAsync((uint8_t*)c->tex_px.p + (size_t)tab[(size_t)i * 4] * 4, rgba8[i],
+                                    (size_t)widths[i] * heights[i] * 4, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = upload(c, c->tex_tab, tab.data(), tab.size()))) return rc;  // synchronises the stream
+    c->ntex = n;
     return HY_OK;
 }
 
@@ -684,6 +719,55 @@ int hy_hybrid_backward(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const
                                       c->stream));
     }
     return finish_call(c, st, !(cfg->flags & HY_FLAG_NO_STATUS_SYNC));
+}
+
+int hy_pathtrace_pass(HyCtx* c, const HyCamera* cam, uint32_t W, uint32_t H, const HyPassConfig* cfg,
+                      uint8_t* d_image, float* d_out_f, HyStats* st) {
+    if (!c || !cam || W == 0 || H == 0 || (uint64_t)W * H >= (1ull << 31)) return HY_ERR_INVALID_ARG;
+    if (((uintptr_t)d_image) % 4 || ((uintptr_t)d_out_f) % 16) return HY_ERR_INVALID_ARG;
+    int rc;
+    if ((rc = check_cfg(cfg)) || (rc = check_scene_ready(c))) return rc;
+    DeviceGuard g(c->device);
+    if ((rc = reset_counters(c))) return rc;
+    PtParams T;
+    std::memset(&T, 0, sizeof(T));
+    PassParams& P = T.P;
+    P.W = W;
+    P.H = H;
+    P.spp = cfg->shadow_spp;
+    P.max_bounces = cfg->max_bounces;
+    P.rng_mode = cfg->rng_mode;
+    P.flags = cfg->flags;
+    P.out_f = d_out_f;
+    P.out_8 = d_image;
+    P.tiles_x = (W + 7) / 8;
+    P.ntiles = P.tiles_x * ((H + 3) / 4);
+    P.chunk = cfg->queue_chunk ? cfg->queue_chunk : 1;
+    P.stats = dev_stats(c);
+    P.status = dev_status(c);
+    P.queue = dev_queue(c, WQ_MISC);
+    P.num_lights = c->nlights;  // closesthit.rchit loops over every light of the scene
+    std::memcpy(T.inv_view, cam->inv_view, 64);
+    std::memcpy(T.inv_proj, cam->inv_proj, 64);
+    T.frame = (int32_t)cam->frame[0];
+    const bool count = (cfg->flags & HY_FLAG_COUNT_TRAVERSAL) != 0;
+    int per = 0;
+    if (pathtrace_occupancy(count, &per) != cudaSuccess || per <= 0) per = 1;
+    int grid = std::max(1, std::min<int>(per * c->num_sms, (int)((P.ntiles * 32ull + 127) / 128)));
+    {
+        ProfScope prof(c, PK_PATHTRACE);
+        HY_CUDA_TRY(launch_pathtrace(count, scene_dev(c), T, grid, c->stream));
+    }
+    return finish_call(c, st, !(cfg->flags & HY_FLAG_NO_STATUS_SYNC));
+}
+
+int hy_post_resolve(HyCtx* c, uint32_t W, uint32_t H, const uint8_t* in8, const float* inf, uint8_t* out) {
+    if (!c || !out || (!in8 && !inf) || (uint64_t)W * H >= (1ull << 31)) return HY_ERR_INVALID_ARG;
+    if (((uintptr_t)out) % 4 || ((uintptr_t)in8) % 4 || ((uintptr_t)inf) % 16) return HY_ERR_INVALID_ARG;
+    DeviceGuard g(c->device);
+    HY_CUDA_TRY(launch_post(in8, inf, W * H, out, c->stream));
+    HY_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return HY_OK;
 }
 
 int hy_profile_enable(HyCtx* c, int enable) {

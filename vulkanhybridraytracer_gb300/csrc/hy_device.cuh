@@ -186,7 +186,7 @@ constexpr uint32_t kMaxIters = 1u << 22;
 struct SceneDev {
     const Node8* nodes;
     const float4* tris;          // 3 per triangle
-    const float4* vattr;         // 2 per vertex: (normal.xyz, 0), (uv.xy, 0, 0)
+    const float4* vattr;         // 2 per vertex: (normal.xyz, color.r), (uv.xy, color.g, color.b)
     const uint32_t* idx;
     const HyPrimitive* prims;
     const uint32_t* tri_prim;    // global triangle -> primitive
@@ -199,6 +199,9 @@ struct SceneDev {
     uint32_t num_mats, num_lights;
     uint32_t num_nodes, num_tris;
     uint32_t env_w[2], env_h[2];
+    const uchar4* tex_px;        // material textures, concatenated RGBA8 texels
+    const uint4* tex_tab;        // per texture: first texel, width, height, 0
+    uint32_t num_tex;
 };
 
 struct Hit { float t; uint32_t id; float b1, b2; };

@@ -46,13 +46,16 @@ __device__ __forceinline__ Dg3 div3(const Dg3& a, const Dg& s) { return {a.x / s
 // material inputs: albedo = pow(diffuse, 2.2); F0 = mix(vec3(0.04), albedo, metallic)
 struct DMat { Dg3 albedo, F0; Dg rough, metal; };
 
-__device__ __forceinline__ DMat dmat(float dr, float dg, float db, float rough, float metal) {
+// var_alb / var_rm: the diffuse colour / roughness-metallic are the material's own
+// parameters (false where a texture supplies them: constants)
+__device__ __forceinline__ DMat dmat(float dr, float dg, float db, float rough, float metal, bool var_alb = true,
+                                     bool var_rm = true) {
     DMat m;
-    m.albedo.x = dpow(dvar<KG>(dr, S_ALB + 0), 2.2f);
-    m.albedo.y = dpow(dvar<KG>(dg, S_ALB + 1), 2.2f);
-    m.albedo.z = dpow(dvar<KG>(db, S_ALB + 2), 2.2f);
-    m.rough = dvar<KG>(rough, S_ROUGH);
-    m.metal = dvar<KG>(metal, S_METAL);
+    m.albedo.x = dpow(var_alb ? dvar<KG>(dr, S_ALB + 0) : dconst<KG>(dr), 2.2f);
+    m.albedo.y = dpow(var_alb ? dvar<KG>(dg, S_ALB + 1) : dconst<KG>(dg), 2.2f);
+    m.albedo.z = dpow(var_alb ? dvar<KG>(db, S_ALB + 2) : dconst<KG>(db), 2.2f);
+    m.rough = var_rm ? dvar<KG>(rough, S_ROUGH) : dconst<KG>(rough);
+    m.metal = var_rm ? dvar<KG>(metal, S_METAL) : dconst<KG>(metal);
     const Dg keep = 1.0f - m.metal;
     m.F0 = {0.04f * keep + m.albedo.x * m.metal, 0.04f * keep + m.albedo.y * m.metal,
             0.04f * keep + m.albedo.z * m.metal};
@@ -297,7 +300,10 @@ __device__ __forceinline__ void grad_pixel(const SceneDev& S, const GradParams& 
     for (int k = 0; k < nb; k++) chain = chain * pcs[k];
 
     // ---- 2. primary lights (hybridRaygen.rgen:73-149) ----
-    const DMat m = dmat(g2.x, g2.y, g2.z, g4.y, g4.z);
+    // a texel whose material samples a texture holds the texture's value, not a parameter
+    const bool var_alb = mi >= 0 && !(S.mats[mi].textures[0] > -1.f);
+    const bool var_rm = mi >= 0 && !(S.mats[mi].textures[3] > -1.f);
+    const DMat m = dmat(g2.x, g2.y, g2.z, g4.y, g4.z, var_alb, var_rm);
     const f3 w_rc = gup * chain;  // dLoss/d(rayColor before the bounces)
     f3 rc0 = mk(0.f, 0.f, 0.f);
     float macc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
@@ -376,7 +382,9 @@ __device__ __forceinline__ void grad_pixel(const SceneDev& S, const GradParams& 
             hmat = (int)S.prims[a.prim].material_id;
             const HyMaterial mat = S.mats[hmat];
             hsm = (int)mat.smr[0];
-            hm = dmat(mat.diffuse[0], mat.diffuse[1], mat.diffuse[2], mat.smr[2], mat.smr[1]);
+            const MatSample ms = material_at_hit(S, mat, hits[k]);
+            hm = dmat(ms.albedo.x, ms.albedo.y, ms.albedo.z, ms.rm.y, ms.rm.z, !(mat.textures[0] > -1.f),
+                      !(mat.textures[3] > -1.f));
             irr_h = irradiance_at(S, Nh);
             vb = vis[k];
         }

@@ -39,7 +39,9 @@ struct HyCtx {
 
     // ---- scene ----
     hy::DevBuf verts, vattr, idx, prims, xf, nrm, prim_tri0, tri_prim, mats, lights, env[2];
-    uint32_t nverts = 0, nidx = 0, nprims = 0, nxf = 0, ntri = 0, nmats = 0, nlights = 0;
+    hy::DevBuf tex_px, tex_tab;  // material textures: concatenated RGBA8 texels, (first, w, h, 0) per texture
+    uint32_t nverts = 0, nidx = 0, nprims = 0, nxf = 0, ntri = 0, nmats = 0, nlights = 0, ntex = 0;
+    std::vector<HyMaterial> h_mats;  // host copy for texture-id validation
     uint32_t max_material_id = 0;
     uint32_t env_w[2] = {0, 0}, env_h[2] = {0, 0};
     bool geometry_ok = false;

@@ -137,7 +137,7 @@ __device__ __forceinline__ void do_pixel(const SceneDev& S, const PassParams& P,
     }
     const f3 F = FresnelSchlick(NdotV, F0);
     const f3 kD = (splat(1.0f) - F) * (1.0f - metallic);
-    const f3 fc = rayColor + kD * albedo * irradiance + emissive;
+    const f3 fc = rayColor + (kD * albedo * irradiance + emissive);  // finalColor += ambient + emissive
     if (P.out_f) reinterpret_cast<float4*>(P.out_f)[pix] = make_float4(fc.x, fc.y, fc.z, 1.f);
     if (P.out_8) reinterpret_cast<uchar4*>(P.out_8)[pix] = make_uchar4(quant8(fc.z), quant8(fc.y), quant8(fc.x), 255);
 }
@@ -436,6 +436,33 @@ __global__ void __launch_bounds__(128) k_pixels(const SceneDev S, const PassPara
     flush_stats(ls, P.stats);
 }
 
+// postFragment.frag:9-20: rgb = pow(max(rgb, 0.001), 1/2.2) per pixel of the final
+// image (a full-screen quad sampling it NEAREST at texel centres), alpha kept
+__global__ void __launch_bounds__(256) k_post(const uint8_t* __restrict__ in8, const float4* __restrict__ inf,
+                                              uint32_t n, uchar4* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 c;
+    if (in8) {
+        const uchar4 q = reinterpret_cast<const uchar4*>(in8)[i];  // B, G, R, A bytes
+        c = make_float4(__fdiv_rn((float)q.z, 255.f), __fdiv_rn((float)q.y, 255.f), __fdiv_rn((float)q.x, 255.f),
+                        __fdiv_rn((float)q.w, 255.f));
+    } else {
+        c = inf[i];
+    }
+    const float gamma = 1.0f / 2.2f;
+    const float r = powf(fmaxf(c.x, 0.001f), gamma), g = powf(fmaxf(c.y, 0.001f), gamma),
+                b = powf(fmaxf(c.z, 0.001f), gamma);
+    out[i] = make_uchar4(quant8(b), quant8(g), quant8(r), quant8(c.w));
+}
+
+cudaError_t launch_post(const uint8_t* in8, const float* inf, uint32_t n, uint8_t* out, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_post<<<(n + 255) / 256, 256, 0, s>>>(in8, reinterpret_cast<const float4*>(inf), n,
+                                            reinterpret_cast<uchar4*>(out));
+    return cudaGetLastError();
+}
+
 // blur.comp:35-81, reset-frame branch and running mean, one texel per thread
 __global__ void k_accumulate(const AccumParams A) {
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -545,10 +572,23 @@ __global__ void __launch_bounds__(128) k_gbuffer(const SceneDev S, const GbufPar
     p0[i] = make_float4(wp.x, wp.y, wp.z, m.smr[3]);
     p1[i] = make_float4(__fadd_rn(__fmul_rn(a.N.x, 0.5f), 0.5f), __fadd_rn(__fmul_rn(a.N.y, 0.5f), 0.5f),
                         __fadd_rn(__fmul_rn(a.N.z, 0.5f), 0.5f), 1.f);
-    p2[i] = make_float4(m.diffuse[0], m.diffuse[1], m.diffuse[2], 1.f);
+    // geometry_shader.frag:56-59: textures, a diffuse texture modulated by the vertex colour
+    f3 alb = mk(m.diffuse[0], m.diffuse[1], m.diffuse[2]), emis = mk(0.f, 0.f, 0.f), rm = mk(0.f, m.smr[2], m.smr[1]);
+    if (has_textures(m)) {
+        float u, v;
+        f3 col;
+        hit_uv_color(S, h, u, v, col);
+        const MatSample ms = material_at(S, m, u, v);
+        alb = m.textures[0] > -1.f ? mk(__fmul_rn(ms.albedo.x, col.x), __fmul_rn(ms.albedo.y, col.y),
+                                        __fmul_rn(ms.albedo.z, col.z))
+                                   : ms.albedo;
+        emis = ms.emissive;
+        rm = ms.rm;
+    }
+    p2[i] = make_float4(alb.x, alb.y, alb.z, 1.f);
     p3[i] = make_float2(0.5f, 0.5f);
-    p4[i] = make_float4(0.f, m.smr[2], m.smr[1], 1.f);
-    p5[i] = make_float4(0.f, 0.f, 0.f, 1.f);
+    p4[i] = make_float4(rm.x, rm.y, rm.z, 1.f);
+    p5[i] = make_float4(emis.x, emis.y, emis.z, 1.f);
 }
 
 // ---------------------------------------------------------------------------------

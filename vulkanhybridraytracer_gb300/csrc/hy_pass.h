@@ -81,10 +81,22 @@ cudaError_t grad_launch_shape(uint32_t nparam, int num_sms, uint32_t ntiles, int
 cudaError_t launch_shade_grad(const SceneDev& S, const GradParams& G, int grid, bool smem, size_t smem_bytes,
                               float* out_mat, float* out_light, cudaStream_t s);
 
+// Path-traced mode: P.out_8 is the accumulated B8G8R8A8 image, P.out_f the
+// frame's colour; the camera matrices give the primary rays.
+struct PtParams {
+    PassParams P;
+    float inv_view[16], inv_proj[16];
+    int32_t frame;           // int(cam.frame.x): RNG frame and accumulation weight
+};
+cudaError_t pathtrace_occupancy(bool count, int* blocks_per_sm);
+cudaError_t launch_pathtrace(bool count, const SceneDev& S, const PtParams& T, int grid, cudaStream_t s);
+
 cudaError_t launch_pixels(int mode, bool count, int minb, const SceneDev& S, const PassParams& P, int grid, int block,
                           cudaStream_t s);
 cudaError_t pixel_occupancy(int mode, bool count, int minb, int block, int* blocks_per_sm);
 cudaError_t launch_accumulate(const AccumParams& A, cudaStream_t s);
+cudaError_t launch_post(const uint8_t* in_bgra8, const float* in_rgba32f, uint32_t n, uint8_t* out_bgra8,
+                        cudaStream_t s);
 cudaError_t launch_trace(const SceneDev& S, const HyRay* rays, uint32_t n, bool any, bool count, HyHit* hits,
                          unsigned long long* stats, uint32_t* status, int grid, cudaStream_t s);
 cudaError_t launch_gbuffer(const SceneDev& S, const GbufParams& G, cudaStream_t s);

@@ -60,6 +60,29 @@ __device__ __forceinline__ f3 miss_color(const SceneDev& S, f3 d) {
     return pow3(env_lookup(S.env0, S.env_w[0], S.env_h[0], u, v), 2.2f);
 }
 
+// material texture `id` at (u, v): RGBA8, NEAREST / REPEAT
+__device__ __forceinline__ f3 tex_lookup(const SceneDev& S, float id, float u, float v) {
+    const int i = (int)id;
+    if (i < 0 || (uint32_t)i >= S.num_tex) return mk(0.f, 0.f, 0.f);
+    const uint4 t = __ldg(S.tex_tab + i);
+    return env_lookup(S.tex_px + t.x, t.y, t.z, u, v);
+}
+
+__device__ __forceinline__ bool has_textures(const HyMaterial& m) {
+    return m.textures[0] > -1.f || m.textures[2] > -1.f || m.textures[3] > -1.f;
+}
+
+// a material's inputs at a surface point (hybridHit.rchit:62-66, closesthit.rchit:74-81):
+// albedo before pow(2.2), emissive, rm = (_, roughness, metallic)
+struct MatSample { f3 albedo, emissive, rm; };
+__device__ __forceinline__ MatSample material_at(const SceneDev& S, const HyMaterial& m, float u, float v) {
+    MatSample r;
+    r.albedo = m.textures[0] > -1.f ? tex_lookup(S, m.textures[0], u, v) : mk(m.diffuse[0], m.diffuse[1], m.diffuse[2]);
+    r.emissive = m.textures[2] > -1.f ? tex_lookup(S, m.textures[2], u, v) : mk(0.f, 0.f, 0.f);
+    r.rm = m.textures[3] > -1.f ? tex_lookup(S, m.textures[3], u, v) : mk(0.f, m.smr[2], m.smr[1]);
+    return r;
+}
+
 __device__ __forceinline__ int mat_index(float f, uint32_t n) {
     if (!(f > -1.f && f < (float)n)) return -1;
     return (int)f;
@@ -100,6 +123,36 @@ __device__ __forceinline__ HitAttr hit_attributes(const SceneDev& S, const Hit& 
     return HitAttr{normalize(tn), p};
 }
 
+// barycentric texture coordinates and vertex colour of a hit (uv = v0.uv*b0 + v1.uv*b1 + v2.uv*b2)
+__device__ __forceinline__ void hit_uv_color(const SceneDev& S, const Hit& h, float& u, float& v, f3& col) {
+    const uint32_t p = S.tri_prim[h.id];
+    const HyPrimitive pr = S.prims[p];
+    const uint32_t local = h.id - S.prim_tri0[p];
+    const float b0 = __fsub_rn(__fsub_rn(1.0f, h.b1), h.b2);
+    const float bw[3] = {b0, h.b1, h.b2};
+    u = 0.f;
+    v = 0.f;
+    col = mk(0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const uint32_t vi = S.idx[pr.first_index + 3 * local + k] + pr.vertex_offset;
+        const float4 a = __ldg(S.vattr + (size_t)vi * 2), t = __ldg(S.vattr + (size_t)vi * 2 + 1);
+        u = __fadd_rn(u, __fmul_rn(t.x, bw[k]));
+        v = __fadd_rn(v, __fmul_rn(t.y, bw[k]));
+        col = add_rn(col, scale_rn(mk(a.w, t.z, t.w), bw[k]));
+    }
+}
+
+// material inputs at a hit, sampling textures only for textured materials
+__device__ __forceinline__ MatSample material_at_hit(const SceneDev& S, const HyMaterial& m, const Hit& h) {
+    if (!has_textures(m)) return MatSample{mk(m.diffuse[0], m.diffuse[1], m.diffuse[2]), mk(0.f, 0.f, 0.f),
+                                           mk(0.f, m.smr[2], m.smr[1])};
+    float u, v;
+    f3 col;
+    hit_uv_color(S, h, u, v, col);
+    return material_at(S, m, u, v);
+}
+
 struct Payload { f3 color; float t; f3 dir; float scattered; f3 origin; };
 
 // hybridHit.rchit:24-183.  REC: also record, per light, whether the shadow
@@ -116,8 +169,9 @@ __device__ Payload closest_hit(const SceneDev& S, const PassParams& P, const Hit
     HyPrimitive pr = S.prims[a.prim];
     const HyMaterial mat = S.mats[pr.material_id];
     int smode = (int)mat.smr[0];
-    f3 albedo = pow3(mk(mat.diffuse[0], mat.diffuse[1], mat.diffuse[2]), 2.2f);
-    float roughness = mat.smr[2], metallic = mat.smr[1];
+    const MatSample ms = material_at_hit(S, mat, h);
+    f3 albedo = pow3(ms.albedo, 2.2f);
+    float roughness = ms.rm.y, metallic = ms.rm.z;
     f3 F0 = mix3(splat(0.04f), albedo, metallic);
     f3 irradiance = irradiance_at(S, N);
     f3 direction = mk(1.f, 1.f, 1.f);
@@ -196,7 +250,7 @@ __device__ Payload closest_hit(const SceneDev& S, const PassParams& P, const Hit
     f3 kD = (splat(1.0f) - F) * (1.0f - metallic);
     f3 ambient = kD * albedo * irradiance;
     Payload p;
-    p.color = Lo + ambient;  // emissive is vec3(0) without an emissive texture
+    p.color = Lo + ambient + ms.emissive;
     p.t = h.t;
     p.dir = direction;
     p.scattered = dirw;

@@ -102,6 +102,19 @@ class HybridContext:
     def set_scene(self, scene: Scene):
         verts, idx, prims, xf, mats, lights = scene.pack()
         self.set_scene_arrays(verts, idx, prims, xf, mats, lights, scene.env)
+        if scene.textures:
+            self.set_textures(scene.textures)
+
+    def set_textures(self, textures):
+        """Material textures (Texture::_textures): (H, W, 4) uint8 RGBA8 images, indexed by the
+        materials' texture ids."""
+        texs = [np.ascontiguousarray(t, np.uint8) for t in textures]
+        self._tex = texs
+        n = len(texs)
+        ptrs = (C.c_void_p * max(n, 1))(*[t.ctypes.data for t in texs])
+        w = (C.c_uint32 * max(n, 1))(*[t.shape[1] for t in texs])
+        h = (C.c_uint32 * max(n, 1))(*[t.shape[0] for t in texs])
+        L.check(self.lib.hy_scene_set_textures(self.h, ptrs, w, h, n), "textures")
 
     def set_lights(self, lights: np.ndarray):
         lights = np.ascontiguousarray(lights, np.float32)
@@ -223,6 +236,35 @@ class HybridContext:
                                        C.c_void_p(out_8.data_ptr()) if out_8 is not None else None,
                                        C.byref(st)), "shade_pass")
         return st.as_dict()
+
+    def pathtrace(self, cam36, width: int, height: int, cfg, image=None, out_f=None, stats: bool = True):
+        """hy_pathtrace_pass: the reference's path-traced mode into the BGRA8 image `image`
+        (device (H, W, 4) uint8, accumulated in place; allocated when None) and the frame's
+        colour into out_f (device (H, W, 4) float32, optional).  Returns (image, stats)."""
+        import torch
+        if image is None:
+            image = torch.zeros((height, width, 4), dtype=torch.uint8, device=torch.device("cuda", self.device))
+            torch.cuda.synchronize(self.device)  # the fill runs on torch's stream
+        cam = camera_struct(cam36)
+        st = L.HyStats()
+        L.check(self.lib.hy_pathtrace_pass(self.h, C.byref(cam), width, height, C.byref(cfg),
+                                           C.c_void_p(image.data_ptr()),
+                                           C.c_void_p(out_f.data_ptr()) if out_f is not None else None,
+                                           C.byref(st) if stats else None), "pathtrace_pass")
+        return image, st.as_dict()
+
+    def post(self, image, out=None):
+        """hy_post_resolve: gamma 1/2.2 of the pass's BGRA8 image (uint8 (H, W, 4)) or float image
+        (float32 (H, W, 4)) into a BGRA8 image."""
+        import torch
+        h, w = image.shape[0], image.shape[1]
+        if out is None:
+            out = torch.empty((h, w, 4), dtype=torch.uint8, device=image.device)
+        is8 = image.dtype == torch.uint8
+        L.check(self.lib.hy_post_resolve(self.h, w, h, C.c_void_p(image.data_ptr()) if is8 else None,
+                                         None if is8 else C.c_void_p(image.data_ptr()),
+                                         C.c_void_p(out.data_ptr())), "post_resolve")
+        return out
 
     def backward(self, planes, cam36, cfg, hist, grad_img, fmt=L.HY_ACCUM_U8, grad_mats=None, grad_lights=None,
                  formats=GBUF_FP32_FORMATS, stats: bool = True):

@@ -158,20 +158,27 @@ class Scene:
     materials: list = field(default_factory=list)
     camera: Camera = field(default_factory=Camera)
     env: list = field(default_factory=list)   # [sky, irradiance], each (h, w, 4) uint8
+    # Texture::_textures in load order: (h, w, 4) uint8 RGBA8 images; a material's
+    # *_texture field is an index into this list (-1: none)
+    textures: list = field(default_factory=list)
 
     def pack(self):
         """Arrays for the C ABI: verts (N,11) f32, idx u32, prims (P,6) u32,
         transforms (T,16) f32 column-major, materials (M,12) f32, lights (L,12) f32."""
         verts, idx, prims, xf = [], [], [], []
         vofs = iofs = 0
+        placed = {}  # a mesh shared by several entities is packed once (its Prefab's buffers)
         for e_i, ob in enumerate(self.entities):
             m = ob.mesh
-            verts.append(np.asarray(m.vertices, np.float32))
-            idx.append(np.asarray(m.indices, np.uint32))
-            prims.append([iofs, len(m.indices), vofs, ob.material_idx, e_i, e_i])
+            if id(m) not in placed:
+                placed[id(m)] = (iofs, vofs)
+                verts.append(np.asarray(m.vertices, np.float32))
+                idx.append(np.asarray(m.indices, np.uint32))
+                vofs += len(m.vertices)
+                iofs += len(m.indices)
+            fi, vo = placed[id(m)]
+            prims.append([fi, len(m.indices), vo, ob.material_idx, e_i, e_i])
             xf.append(np.asarray(ob.matrix, np.float64).astype(np.float32).reshape(-1))
-            vofs += len(m.vertices)
-            iofs += len(m.indices)
         mats = np.stack([mt.to_shader(i) for i, mt in enumerate(self.materials)])
         lights = (np.stack([l.to_ubo() for l in self.lights]) if self.lights
                   else np.zeros((0, 12), np.float32))

@@ -225,6 +225,43 @@ def small_glass(width: int = 48, height: int = 48) -> Workload:
     return wl
 
 
+def checker_texture(n: int, cells: int, a, b) -> np.ndarray:
+    y, x = np.mgrid[0:n, 0:n]
+    m = ((x * cells // n + y * cells // n) % 2).astype(bool)
+    img = np.where(m[..., None], np.array(a, np.float64), np.array(b, np.float64))
+    return np.round(np.concatenate([img, np.ones((n, n, 1))], -1) * 255).astype(np.uint8)
+
+
+def small_textured(width: int = 64, height: int = 48) -> Workload:
+    """The small scene with material textures (Texture::_textures, RGBA8 NEAREST/REPEAT):
+    a checker diffuse texture on the floor (UVs 0..4, so REPEAT wraps) and on spheres, a
+    metallic-roughness texture, an emissive texture, tinted vertex colours on the floor,
+    textured mirror and glass spheres; 4 bounces."""
+    rng = np.random.default_rng(5)
+    wl = small(0, width, height)
+    sc = wl.scene
+    sc.textures = [checker_texture(64, 8, (0.9, 0.8, 0.2), (0.1, 0.3, 0.8)),
+                   np.concatenate([rng.integers(0, 256, (32, 32, 3)), np.full((32, 32, 1), 255)], -1).astype(np.uint8),
+                   checker_texture(16, 4, (0.6, 0.1, 0.1), (0.0, 0.0, 0.0))]
+    floor = sc.entities[0].mesh
+    v = floor.vertices.copy()
+    v[:, 9:11] *= 4.0
+    v[:, 6:9] = [[1.0, 0.7, 0.7], [0.7, 1.0, 0.7], [0.7, 0.7, 1.0], [1.0, 1.0, 0.5]]
+    sc.entities[0].mesh = type(floor)(v, floor.indices)
+    m = sc.materials
+    m[0] = Material(0, (0.5, 0.5, 0.5, 1), 0.0, 0.6, 1.0, diffuse_texture=0)
+    m[1] = Material(0, (0.5, 0.5, 0.5, 1), 0.5, 0.5, 1.0, diffuse_texture=0, metallic_roughness_texture=1)
+    m[2] = Material(0, (0.8, 0.2, 0.2, 1), 0.0, 0.4, 1.0, emissive_texture=2)
+    m[3] = Material(3, (0.8, 0.8, 0.8, 1), 1.0, 0.05, 1.0, diffuse_texture=0)
+    m[4] = Material(4, (0.9, 0.95, 1.0, 1), 1.0, 0.0, 1.5, diffuse_texture=0, metallic_roughness_texture=1)
+    m[5] = Material(0, (0.3, 0.6, 0.3, 1), 0.0, 0.5, 1.0, diffuse_texture=0, emissive_texture=2,
+                    metallic_roughness_texture=1)
+    wl.max_bounces = 4
+    wl.width, wl.height = width, height
+    wl.name = f"small-textured-{width}x{height}"
+    return wl
+
+
 def diff(seed: int = 3, width: int = 512, height: int = 512) -> Workload:
     rng = np.random.default_rng(seed)
     sc = Scene()
