@@ -46,9 +46,12 @@ def parse():
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--minb", type=int, default=0, help="shadow-kernel variant: resident blocks per SM")
-    ap.add_argument("--workload", default="hd", choices=["hd", "batch", "diff", "pathtrace"],
+    ap.add_argument("--sched", default="groups", choices=["groups", "pool"],
+                    help="DECORRELATED shadow samples in fixed lane groups or from the per-warp ray pool")
+    ap.add_argument("--workload", default="hd", choices=["hd", "batch", "diff", "pathtrace", "large"],
                     help="hd: the 1080p frame (headline); batch: 64 mixed views over 8 scenes, batched vs per "
-                         "view; diff: 512x512 forward + adjoint; pathtrace: the path-traced mode at 1080p")
+                         "view; diff: 512x512 forward + adjoint; pathtrace: the path-traced mode at 1080p; "
+                         "large: 4K, 7.35M triangles, 64 lights, forward + adjoint + batch")
     ap.add_argument("--views", type=int, default=64)
     return ap.parse_args()
 
@@ -315,6 +318,144 @@ def run_pathtrace(args):
     ctx.close()
 
 
+def run_large(args):
+    """The large combined configuration: 3840x2160, 4096 instances of 8 base meshes + the
+    terrain (7.35M triangles in one BVH8), 64 area lights x 1 sample, 2 bounces; the frame,
+    its adjoint over 1024 materials and 64 lights, and the frame batched with 4 extra 1080p
+    views (hy_batch_forward) against the same 5 views one by one."""
+    import torch
+
+    from vulkanhybridraytracer_gb300 import _lib as L
+    from vulkanhybridraytracer_gb300 import scenes
+    from vulkanhybridraytracer_gb300.hybrid import HybridContext, pass_config
+    from vulkanhybridraytracer_gb300.scene import Camera
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    wl = scenes.large()
+    ctx = HybridContext(0, stream=stream.cuda_stream)
+    ctx.set_scene(wl.scene)
+    bvh = ctx.build_bvh()
+    W, H, NL = wl.width, wl.height, len(wl.scene.lights)
+    cam0 = wl.camera(1.0)
+    planes = ctx.gbuffer(cam0, W, H)
+    hist = torch.zeros((NL, H, W), dtype=torch.uint8, device=dev)
+    out8 = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
+    outf = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+
+    def cfg(frame, flags=L.HY_FLAG_NO_STATUS_SYNC):
+        return pass_config(spp=1, max_bounces=wl.max_bounces, rng_mode=L.HY_RNG_DECORRELATED, accum_frame=frame,
+                           flags=flags)
+
+    st = ctx.forward(planes, wl.camera(0.0), cfg(0, 0), hist, L.HY_ACCUM_U8, out_f=outf, out_8=out8)
+    rays = st["shadow_rays"] + st["reflection_rays"] + st["hit_shadow_rays"]
+    frame = 0
+    for _ in range(args.warmup):
+        frame += 1
+        ctx.forward(planes, wl.camera(float(frame)), cfg(frame), hist, L.HY_ACCUM_U8, out_f=outf, out_8=out8)
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    fw = []
+    for _ in range(args.steps):
+        flush.zero_()
+        frame += 1
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.forward(planes, wl.camera(float(frame)), cfg(frame), hist, L.HY_ACCUM_U8, out_f=outf, out_8=out8)
+        b.record(stream)
+        fw.append((a, b))
+    torch.cuda.synchronize()
+    f_ms = float(np.mean([a.elapsed_time(b) for a, b in fw]))
+
+    # adjoint of the frame's shading (dLoss/dImage: a fixed random image)
+    g = torch.randn((H, W, 4), generator=torch.Generator(device=dev).manual_seed(4), device=dev)
+    g[..., 3] = 0
+    bw = []
+    bcfg = cfg(frame, 0)
+    for k in range(args.warmup + args.steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        gm, gl, bst = ctx.backward(planes, wl.camera(float(frame)), bcfg, hist, g, L.HY_ACCUM_U8)
+        b.record(stream)
+        if k >= args.warmup:
+            bw.append((a, b))
+    torch.cuda.synchronize()
+    b_ms = float(np.mean([a.elapsed_time(b) for a, b in bw]))
+
+    # the frame batched with 4 extra 1080p views of the same scene
+    views = [dict(planes=planes, w=W, h=H, hist=hist, out_8=out8, cam=lambda f: wl.camera(f))]
+    for i in range(4):
+        ang = 2 * np.pi * (i + 0.5) / 4
+        c = Camera((50.0 * np.sin(ang), 20.0, 50.0 * np.cos(ang)), (0.0, 0.0, 0.0), 60.0)
+        p = ctx.gbuffer(c.rt_camera(1920, 1080, 1.0), 1920, 1080)
+        views.append(dict(planes=p, w=1920, h=1080, out_8=torch.empty((1080, 1920, 4), dtype=torch.uint8, device=dev),
+                          hist=torch.zeros((NL, 1080, 1920), dtype=torch.uint8, device=dev),
+                          cam=lambda f, c=c: c.rt_camera(1920, 1080, f)))
+    torch.cuda.synchronize()
+
+    def batch_views(f):
+        return [dict(scene=0, planes=v["planes"], camera=v["cam"](float(f)), config=cfg(f), hist=v["hist"],
+                     out_8=v["out_8"]) for v in views]
+
+    def time_it(fn, reps):
+        ts = []
+        for _ in range(reps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            ts.append((a, b))
+        torch.cuda.synchronize()
+        return float(np.mean([a.elapsed_time(b) for a, b in ts]))
+
+    bf = [frame]
+
+    def plain():
+        bf[0] += 1
+        for v in batch_views(bf[0]):
+            ctx.forward(v["planes"], v["camera"], v["config"], v["hist"], L.HY_ACCUM_U8, out_8=v["out_8"],
+                        stats=False)
+
+    def batched():
+        bf[0] += 1
+        ctx.batch_forward([ctx], batch_views(bf[0]), graph=True, sync=False)
+
+    for _ in range(2):
+        plain()
+        batched()
+    st_b = ctx.batch_forward([ctx], batch_views(bf[0] + 1), graph=True, sync=True)
+    bf[0] += 1
+    rays_b = st_b["shadow_rays"] + st_b["reflection_rays"] + st_b["hit_shadow_rays"]
+    mp = time_it(plain, args.steps)
+    mb = time_it(batched, args.steps)
+    clk = clocks.stop()
+    line = {"metric": "large_combined_mrays_per_s", "value": rays / (f_ms / 1e3) / 1e6, "unit": "Mrays/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": f_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": wl.name, "width": W, "height": H, "triangles": wl.scene.num_tris,
+                       "instances": len(wl.scene.entities) - 1, "materials": len(wl.scene.materials),
+                       "lights": NL, "shadow_spp_per_light": 1, "max_bounces": wl.max_bounces,
+                       "rng": "decorrelated", "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)"},
+            "bvh": {"build_ms": bvh["build_ms"], "bvh8_nodes": bvh["num_bvh8_nodes"], "depth": bvh["depth"]},
+            "rays_per_frame": rays,
+            "adjoint": {"backward_ms": b_ms, "backward_over_forward": b_ms / f_ms,
+                        "params": len(wl.scene.materials) * 5 + NL * 4,
+                        "rays_retraced": bst["reflection_rays"] + bst["hit_shadow_rays"]},
+            "batch_4k_plus_4x1080p": {"rays": rays_b, "batched_ms": mb, "per_view_ms": mp,
+                                      "batched_mrays_per_s": rays_b / (mb / 1e3) / 1e6,
+                                      "batched_over_per_view": mp / mb},
+            "clocks": clk, "gpu_launches": 2}
+    print(json.dumps(line))
+    ctx.close()
+
+
 def run_batch(args):
     """64 views over 8 scenes (50k-2M triangles, 320x240..1920x1080, spp 1/4/16/64,
     1-8 lights): the views one by one through hy_hybrid_forward, then as one
@@ -421,6 +562,9 @@ def main():
     if args.workload == "pathtrace":
         run_pathtrace(args)
         return
+    if args.workload == "large":
+        run_large(args)
+        return
     import torch
 
     from vulkanhybridraytracer_gb300 import replicas
@@ -446,9 +590,11 @@ def main():
     out_8 = torch.empty((wl.height, wl.width, 4), dtype=torch.uint8, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
+    sched = L.HY_FLAG_RAY_POOL if args.sched == "pool" else 0
+
     def cfg(frame, flags=L.HY_FLAG_NO_STATUS_SYNC):
         return pass_config(spp=wl.spp, max_bounces=wl.max_bounces, rng_mode=wl.rng_mode, accum_frame=frame,
-                           flags=flags, block_size=args.block, queue_chunk=args.chunk, min_blocks=args.minb)
+                           flags=flags | sched, block_size=args.block, queue_chunk=args.chunk, min_blocks=args.minb)
 
     # rays per frame and traversal counts (untimed counting launch, same frame as step 1)
     st_count = ctx.forward(planes, wl.camera(1.0), cfg(1, L.HY_FLAG_COUNT_TRAVERSAL), hist.clone(),
@@ -498,14 +644,16 @@ def main():
     L_ = len(wl.scene.lights)
     sh_rays = st_shadow["shadow_rays"]
     sh_nodes, sh_tris = st_shadow["nodes_visited"], st_shadow["tris_tested"]
+    shadow_bytes = sh_rays * 48 + 80 * sh_nodes + 48 * sh_tris + npx * (32 + 2 * L_)
     alg = {
         # G-buffer planes 0/1 (32 B/px), u8 history read + write per light
-        "k_shadow_group<accum>": sh_rays * 48 + 80 * sh_nodes + 48 * sh_tris + npx * (32 + 2 * L_),
+        "k_shadow_group<accum>": shadow_bytes,
+        "k_shadow_pool<accum>": shadow_bytes,
         # all six planes (88 B/px), RGBA32F + BGRA8 out, u8 history read per light
         "k_pixels<shade>": ((rays - sh_rays) * 48 + 80 * (st_count["nodes_visited"] - sh_nodes)
                             + 48 * (st_count["tris_tested"] - sh_tris) + npx * (88 + 16 + 4 + L_)),
     }
-    alg_frame = sum(alg.values())
+    alg_frame = shadow_bytes + alg["k_pixels<shade>"]
     peaks = {}
     try:
         peaks = json.load(open(ROOT / "MEASURED_PEAKS.json"))

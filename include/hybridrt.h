@@ -159,8 +159,11 @@ enum { HY_RNG_REFERENCE = 0, HY_RNG_DECORRELATED = 1 };
 #define HY_FLAG_NO_ACCUM           0x2u /* shade from the raw shadow images, no denoise pass */
 #define HY_FLAG_COUNT_TRAVERSAL    0x4u /* count BVH nodes visited / triangles tested into HyStats */
 #define HY_FLAG_NO_STATUS_SYNC     0x8u /* do not read back the status word (no host sync) */
-#define HY_FLAG_PIXEL_PARALLEL     0x10u /* one lane per pixel for DECORRELATED shadow rays (default: one lane
-                                            group per pixel-light, the samples on adjacent lanes) */
+#define HY_FLAG_PIXEL_PARALLEL     0x10u /* one lane per pixel for DECORRELATED shadow rays (default: the
+                                            samples of a pixel-light start together on adjacent lanes) */
+#define HY_FLAG_RAY_POOL           0x20u /* those samples from a per-warp ray pool that refills each lane as
+                                            soon as its ray ends (default: a fixed lane group per pixel-light,
+                                            which waits for its slowest sample but stays more coherent) */
 
 typedef struct HyPassConfig {
     uint32_t shadow_spp;    /* samplesBuffer.samples (1..64, src/renderer.cpp:656) */

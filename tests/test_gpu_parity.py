@@ -384,8 +384,9 @@ def test_hd_forward_parity(hd):
 
 @pytest.mark.parametrize("spp", [2, 3, 16, 40])
 def test_group_kernel_equals_pixel_kernel(small, spp):
-    """The sample-parallel shadow kernel (LCG jump-ahead per sample) writes the
-    same shadow images as the one-lane-per-pixel kernel, bit for bit."""
+    """The sample-parallel shadow kernels (lane groups, and the per-warp ray pool;
+    LCG jump-ahead per sample) write the same shadow images as the
+    one-lane-per-pixel kernel, bit for bit."""
     from vulkanhybridraytracer_gb300.hybrid import pass_config
     torch = _torch()
     wl = small.wl
@@ -394,7 +395,10 @@ def test_group_kernel_equals_pixel_kernel(small, spp):
     planes = [torch.from_numpy(x).cuda() for x in small.orc.gbuffer(cam, W, H)]
     a = torch.zeros((nl, H, W), dtype=torch.uint8, device="cuda")
     b = torch.zeros_like(a)
+    c = torch.zeros_like(a)
+    torch.cuda.synchronize()
     sa = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, 0), a)
     sb = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, L.HY_FLAG_PIXEL_PARALLEL), b)
-    assert torch.equal(a, b)
-    assert sa["shadow_rays"] == sb["shadow_rays"] > 0
+    sc = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, L.HY_FLAG_RAY_POOL), c)
+    assert torch.equal(a, b) and torch.equal(a, c)
+    assert sa["shadow_rays"] == sb["shadow_rays"] == sc["shadow_rays"] > 0

@@ -263,13 +263,14 @@ PassParams make_params(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const
 }
 
 // ---- per-kernel timing ----
-// the first five are the MODE_* values of hy_pass.h
-enum { PK_ACCUM = MODE_SHADOW_ACCUM_G + 1, PK_GRAD, PK_PATHTRACE, PK_COUNT };
+// the first seven are the MODE_* values of hy_pass.h
+enum { PK_ACCUM = MODE_SHADOW_ACCUM_P + 1, PK_GRAD, PK_PATHTRACE, PK_COUNT };
 const char* const kProfNames[PK_COUNT] = {"k_shadow",       "k_pixels<shade>",       "k_shadow<accum>",
-                                          "k_shadow_group", "k_shadow_group<accum>", "k_accumulate",
-                                          "k_shade_grad",   "k_pathtrace"};
+                                          "k_shadow_group", "k_shadow_group<accum>", "k_shadow_pool",
+                                          "k_shadow_pool<accum>", "k_accumulate", "k_shade_grad",
+                                          "k_pathtrace"};
 static_assert(MODE_SHADOW == 0 && MODE_SHADE == 1 && MODE_SHADOW_ACCUM == 2 && MODE_SHADOW_G == 3 &&
-                  MODE_SHADOW_ACCUM_G == 4,
+                  MODE_SHADOW_ACCUM_G == 4 && MODE_SHADOW_P == 5 && MODE_SHADOW_ACCUM_P == 6,
               "profile names follow the pass modes");
 
 cudaEvent_t prof_event(HyCtx* c) {
@@ -304,13 +305,19 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
     if (block % 32 || block > 128) return HY_ERR_INVALID_ARG;  // kernels are built for <= 128 threads
     PassParams P = P0;
     P.queue = dev_queue(c, queue_slot);
-    // DECORRELATED samples of one pixel-light go to one lane group
+    // DECORRELATED samples of one pixel-light start together on adjacent lanes:
+    // in fixed lane groups (measured fastest), or (HY_FLAG_RAY_POOL) from the
+    // per-warp ray pool
     if ((mode == MODE_SHADOW || mode == MODE_SHADOW_ACCUM) && P.rng_mode == HY_RNG_DECORRELATED && P.spp >= 2 &&
         !(cfg->flags & HY_FLAG_PIXEL_PARALLEL)) {
-        mode = mode == MODE_SHADOW ? MODE_SHADOW_G : MODE_SHADOW_ACCUM_G;
-        uint32_t G = 2;
-        while (G < P.spp && G < 32) G <<= 1;
-        P.group = G;
+        if (cfg->flags & HY_FLAG_RAY_POOL) {
+            mode = mode == MODE_SHADOW ? MODE_SHADOW_P : MODE_SHADOW_ACCUM_P;
+        } else {
+            mode = mode == MODE_SHADOW ? MODE_SHADOW_G : MODE_SHADOW_ACCUM_G;
+            uint32_t G = 2;
+            while (G < P.spp && G < 32) G <<= 1;
+            P.group = G;
+        }
     }
     // 8 resident blocks (64 registers) measured fastest on the 1080p workload
     int minb = cfg->min_blocks ? (int)cfg->min_blocks : 8;

@@ -768,6 +768,196 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_batch(const BatchParams B)
 }
 
 template <bool COUNT>
+__global__ void __launch_bounds__(128) k_pixels_batch(const BatchParams B);
+
+// ---------------------------------------------------------------------------------
+// DECORRELATED shadow rays as a per-warp ray pool.
+//
+// The warp expands its pixels, in order, into pixel-light entries (at most
+// kPoolEntries in flight, in shared memory) and each iteration hands every
+// idle lane the next sample of the oldest entry that still has samples to
+// start, opening entries as needed.  A lane whose ray ends takes new work in
+// the next iteration, whatever pixel-light it belongs to, so no lane waits for
+// the slowest sample of its group; the samples of one entry still start
+// together on adjacent lanes (nearly the same node path).  Unoccluded samples
+// are counted with shared-memory atomics and the lane that ends an entry's
+// last sample writes the light's factor.  Same rays, seeds and sums as
+// k_shadow_group: the unoccluded count is an integer, so the result does not
+// depend on the order the samples end in.
+// ---------------------------------------------------------------------------------
+constexpr int kPoolEntries = 8;
+struct PoolEntry {
+    float px, py, pz, Lx, Ly, Lz, dist, radius;
+    uint32_t pix, light, seed0, rays_before;
+    uint32_t issued;   // samples started (written by the issuing step only)
+    uint32_t in_blur;
+    int pending;       // started and not finished (shared atomics)
+    uint32_t unocc;    // unoccluded samples (shared atomics)
+};
+
+template <bool ACCUM>
+__device__ __forceinline__ void pool_finalize(const PassParams& P, uint32_t pix, uint32_t light, bool in_blur,
+                                              size_t plane, float v) {
+    ShadowLane s;
+    s.pix = pix;
+    s.light = light;
+    s.in_blur = in_blur;
+    shadow_finalize<ACCUM>(P, s, plane, v);
+}
+
+template <bool COUNT, bool ACCUM, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_shadow_pool(const SceneDev S, const PassParams P) {
+    __shared__ PoolEntry s_pool[4][kPoolEntries];
+    __shared__ uint32_t s_freed[4];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    PoolEntry* E = s_pool[warp];
+    if (lane == 0) s_freed[warp] = 0;
+    const size_t plane = (size_t)P.W * P.H;
+    const uint32_t spp = P.spp;
+    LaneStats ls;
+    uint2 stk[kStackMax];
+    Trav t;
+    RayPre r;
+    bool live = false;
+    uint32_t my_e = 0, nn = 0, nt = 0;
+    // warp-uniform state: entries in flight, the entry still starting samples,
+    // the pixel being expanded into entries, the warp's tile pool
+    uint32_t used = 0, head_issued = 0;
+    int head = -1;
+    bool cur_valid = false, cur_in_blur = false, queue_empty = false;
+    uint32_t cur_pix = 0, cur_light = 0, cur_rays = 0, cur_seed0 = 0, pool_cur = 0, pool_end = 0;
+    int cur_smode = 0;
+    f3 cur_pos = mk(0.f, 0.f, 0.f), cur_N = cur_pos;
+    for (;;) {
+        __syncwarp();
+        used &= ~s_freed[warp];
+        __syncwarp();
+        if (lane == 0) s_freed[warp] = 0;
+        // ---- hand the idle lanes their next samples ----
+        uint32_t idle = __ballot_sync(0xffffffffu, !live);
+        while (idle) {
+            if (head < 0) {
+                // open the next pixel-light that needs rays
+                bool opened = false;
+                while (!opened) {
+                    if (!cur_valid) {
+                        if (pool_cur == pool_end) {
+                            if (queue_empty) break;
+                            uint32_t t0 = 0;
+                            if (lane == 0) t0 = atomicAdd(P.queue, P.chunk);
+                            t0 = __shfl_sync(0xffffffffu, t0, 0);
+                            if (t0 >= P.ntiles) { queue_empty = true; break; }
+                            pool_cur = t0 * 32;
+                            pool_end = min(t0 + P.chunk, P.ntiles) * 32;
+                        }
+                        const uint32_t slot = pool_cur++;
+                        const uint32_t tile = slot >> 5, l = slot & 31;
+                        const uint32_t x = (tile % P.tiles_x) * 8 + (l & 7), y = (tile / P.tiles_x) * 4 + (l >> 3);
+                        if (x < P.W && y < P.H) {
+                            cur_valid = true;
+                            cur_pix = y * P.W + x;
+                            const float4 g0 = fetch_texel(P.plane[0], P.fmt[0], cur_pix);
+                            const float4 g1 = fetch_texel(P.plane[1], P.fmt[1], cur_pix);
+                            cur_pos = mk(g0.x, g0.y, g0.z);
+                            cur_N = normalize_rn(mk(__fsub_rn(__fmul_rn(g1.x, 2.0f), 1.0f),
+                                                    __fsub_rn(__fmul_rn(g1.y, 2.0f), 1.0f),
+                                                    __fsub_rn(__fmul_rn(g1.z, 2.0f), 1.0f)));
+                            const int mi = mat_index(g0.w, S.num_mats);
+                            cur_smode = mi >= 0 ? (int)S.mats[mi].smr[0] : 0;
+                            cur_seed0 = tea(cur_pix, P.frame_u);
+                            cur_light = 0;
+                            cur_rays = 0;
+                            cur_in_blur = x < P.blur_w && y < P.blur_h;
+                        }
+                        continue;
+                    }
+                    if (cur_light >= P.num_lights) { cur_valid = false; continue; }
+                    if (__popc(used) == kPoolEntries) break;  // wait for an entry to retire
+                    const HyLight lt = S.lights[cur_light];
+                    const LightGeo lg = light_geo(lt, cur_pos, cur_N);
+                    float v = -1.f;
+                    if (cur_smode == 4) v = 1.0f;
+                    else if (!(lg.NdotL > 0.f)) v = 0.0f;
+                    else if (!(lg.dist < lg.maxd)) v = 1.0f;
+                    if (v >= 0.f) {  // no rays: the factor is known
+                        if (lane == 0) pool_finalize<ACCUM>(P, cur_pix, cur_light, cur_in_blur, plane, v);
+                        cur_light++;
+                        continue;
+                    }
+                    const int e = __ffs(~used & ((1u << kPoolEntries) - 1u)) - 1;
+                    if (lane == 0) {
+                        PoolEntry& q = E[e];
+                        q.px = cur_pos.x; q.py = cur_pos.y; q.pz = cur_pos.z;
+                        q.Lx = lg.L.x; q.Ly = lg.L.y; q.Lz = lg.L.z;
+                        q.dist = lg.dist;
+                        q.radius = lt.radius;
+                        q.pix = cur_pix;
+                        q.light = cur_light;
+                        q.seed0 = cur_seed0;
+                        q.rays_before = cur_rays;
+                        q.issued = 0;
+                        q.in_blur = cur_in_blur ? 1u : 0u;
+                        q.pending = 0;
+                        q.unocc = 0;
+                    }
+                    used |= 1u << e;
+                    head = e;
+                    head_issued = 0;
+                    cur_rays += spp;
+                    cur_light++;
+                    opened = true;
+                }
+                if (!opened) break;
+                __syncwarp();
+            }
+            const uint32_t n = min((uint32_t)__popc(idle), spp - head_issued);
+            const uint32_t rank = __popc(idle & lt_mask);
+            if (!live && rank < n) {
+                const PoolEntry& q = E[head];
+                const uint32_t k = head_issued + rank;
+                uint32_t sd = lcg_jump(q.seed0, 2u * (q.rays_before + k));
+                const f3 pos = mk(q.px, q.py, q.pz);
+                const f3 dir = sampleDisk(q.radius, pos, mk(q.Lx, q.Ly, q.Lz), sd);
+                r = ray_pre(add_rn(pos, scale_rn(dir, 1e-1f)), dir);
+                trav_init(t, r, __fadd_rn(q.dist, 1.0f));
+                my_e = (uint32_t)head;
+                live = true;
+                ls.shadow++;
+            }
+            __syncwarp();
+            head_issued += n;
+            if (lane == 0) {
+                E[head].issued = head_issued;
+                E[head].pending += (int)n;
+            }
+            if (head_issued == spp) head = -1;
+            idle = __ballot_sync(0xffffffffu, !live);
+        }
+        if (queue_empty && !cur_valid && used == 0 && __ballot_sync(0xffffffffu, live) == 0) break;
+        __syncwarp();
+        // ---- one node visit ----
+        if (live) {
+            if (trav_step<true, COUNT>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
+                live = false;
+                PoolEntry& q = E[my_e];
+                if (t.h.id == HY_NO_HIT) atomicAdd(&q.unocc, 1u);
+                __threadfence_block();
+                if (atomicSub(&q.pending, 1) == 1 && q.issued == spp) {
+                    __threadfence_block();
+                    const uint32_t unocc = atomicAdd(&q.unocc, 0u);
+                    pool_finalize<ACCUM>(P, q.pix, q.light, q.in_blur != 0, plane,
+                                         __fdiv_rn((float)unocc, (float)spp));
+                    atomicOr(&s_freed[warp], 1u << my_e);
+                }
+            }
+        }
+    }
+    if (COUNT) { ls.nodes += nn; ls.tris += nt; }
+    flush_stats(ls, P.stats);
+}
+
+template <bool COUNT>
 __global__ void __launch_bounds__(128) k_pixels_batch(const BatchParams B) {
     __shared__ uint32_t s_begin[kMaxBatchViews + 1];
     for (uint32_t i = threadIdx.x; i <= B.nviews; i += blockDim.x)
@@ -804,12 +994,19 @@ static void* shadow_kernel(bool count, int minb) {
     return minb >= 8 ? shadow_kernel<GROUP, ACCUM, 8>(count) : shadow_kernel<GROUP, ACCUM, 5>(count);
 }
 // minb: resident blocks per SM the shadow kernel is compiled for (register cap)
+template <bool ACCUM, int MINB>
+static void* pool_kernel(bool count) {
+    return count ? (void*)k_shadow_pool<true, ACCUM, MINB> : (void*)k_shadow_pool<false, ACCUM, MINB>;
+}
+
 static void* pixel_kernel(int mode, bool count, int minb) {
     switch (mode) {
         case MODE_SHADOW: return shadow_kernel<false, false>(count, minb);
         case MODE_SHADOW_ACCUM: return shadow_kernel<false, true>(count, minb);
         case MODE_SHADOW_G: return shadow_kernel<true, false>(count, minb);
         case MODE_SHADOW_ACCUM_G: return shadow_kernel<true, true>(count, minb);
+        case MODE_SHADOW_P: return minb >= 8 ? pool_kernel<false, 8>(count) : pool_kernel<false, 5>(count);
+        case MODE_SHADOW_ACCUM_P: return minb >= 8 ? pool_kernel<true, 8>(count) : pool_kernel<true, 5>(count);
         default: return count ? (void*)k_pixels<MODE_SHADE, true> : (void*)k_pixels<MODE_SHADE, false>;
     }
 }

@@ -7,8 +7,12 @@
 
 namespace hy {
 
-// *_G: the sample-parallel shadow kernel (DECORRELATED rays, spp >= 2)
-enum { MODE_SHADOW = 0, MODE_SHADE = 1, MODE_SHADOW_ACCUM = 2, MODE_SHADOW_G = 3, MODE_SHADOW_ACCUM_G = 4 };
+// *_G: the sample-parallel shadow kernel (DECORRELATED rays, spp >= 2) with lane
+// groups per pixel-light; *_P: the same rays from a per-warp ray pool
+enum {
+    MODE_SHADOW = 0, MODE_SHADE = 1, MODE_SHADOW_ACCUM = 2, MODE_SHADOW_G = 3, MODE_SHADOW_ACCUM_G = 4,
+    MODE_SHADOW_P = 5, MODE_SHADOW_ACCUM_P = 6
+};
 
 struct PassParams {
     uint32_t W, H;

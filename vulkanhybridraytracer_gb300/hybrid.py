@@ -19,7 +19,14 @@ from .scene import Scene
 
 
 def _ptr(t) -> int:
-    return t.data_ptr() if hasattr(t, "data_ptr") else t.ctypes.data
+    """Address of a packed tensor / array (the C ABI takes row-major planes without strides)."""
+    if hasattr(t, "data_ptr"):
+        if not t.is_contiguous():
+            raise ValueError("the C ABI takes packed (contiguous) tensors")
+        return t.data_ptr()
+    if not t.flags["C_CONTIGUOUS"]:
+        raise ValueError("the C ABI takes packed (C-contiguous) arrays")
+    return t.ctypes.data
 
 
 def _np_ptr(a: np.ndarray):
@@ -156,8 +163,8 @@ class HybridContext:
         n = rays.shape[0]
         hits = torch.empty((n, 4), dtype=torch.float32, device=rays.device)
         st = L.HyStats()
-        L.check(self.lib.hy_trace_rays(self.h, C.c_void_p(rays.data_ptr()), n, int(any_hit),
-                                       C.c_void_p(hits.data_ptr()), C.byref(st) if count else None), "trace")
+        L.check(self.lib.hy_trace_rays(self.h, C.c_void_p(_ptr(rays)), n, int(any_hit),
+                                       C.c_void_p(_ptr(hits)), C.byref(st) if count else None), "trace")
         return hits, st.as_dict()
 
     def gbuffer(self, cam36, width: int, height: int):
@@ -165,7 +172,7 @@ class HybridContext:
         dev = torch.device("cuda", self.device)
         planes = [torch.empty((height, width, 4 if i != 3 else 2), dtype=torch.float32, device=dev)
                   for i in range(6)]
-        arr = (C.c_void_p * 6)(*[p.data_ptr() for p in planes])
+        arr = (C.c_void_p * 6)(*[_ptr(p) for p in planes])
         cam = camera_struct(cam36)
         L.check(self.lib.hy_gbuffer_primary(self.h, C.byref(cam), width, height, arr), "gbuffer")
         return planes
@@ -178,7 +185,7 @@ class HybridContext:
 
     @staticmethod
     def _accum(hist, fmt):
-        return L.HyAccum(fmt, hist.shape[0], hist.data_ptr())
+        return L.HyAccum(fmt, hist.shape[0], _ptr(hist))
 
     def forward(self, planes, cam36, cfg: L.HyPassConfig, hist, fmt=L.HY_ACCUM_U8, out_f=None, out_8=None,
                 formats=GBUF_FP32_FORMATS, stats: bool = True):
@@ -189,8 +196,8 @@ class HybridContext:
         acc = self._accum(hist, fmt)
         st = L.HyStats()
         L.check(self.lib.hy_hybrid_forward(self.h, C.byref(gb), C.byref(cam), C.byref(cfg), C.byref(acc),
-                                           C.c_void_p(out_f.data_ptr()) if out_f is not None else None,
-                                           C.c_void_p(out_8.data_ptr()) if out_8 is not None else None,
+                                           C.c_void_p(_ptr(out_f)) if out_f is not None else None,
+                                           C.c_void_p(_ptr(out_8)) if out_8 is not None else None,
                                            C.byref(st) if stats else None), "hybrid_forward")
         return st.as_dict()
 
@@ -214,14 +221,14 @@ class HybridContext:
         cam = camera_struct(cam36)
         st = L.HyStats()
         L.check(self.lib.hy_shadow_pass(self.h, C.byref(gb), C.byref(cam), C.byref(cfg), fmt,
-                                        C.c_void_p(shadow.data_ptr()), C.byref(st)), "shadow_pass")
+                                        C.c_void_p(_ptr(shadow)), C.byref(st)), "shadow_pass")
         return st.as_dict()
 
     def accumulate_pass(self, planes, cfg, shadow, hist, fmt=L.HY_ACCUM_U8, formats=GBUF_FP32_FORMATS):
         h, w = planes[0].shape[0], planes[0].shape[1]
         gb = gbuffer_struct(planes, w, h, formats)
         acc = self._accum(hist, fmt)
-        L.check(self.lib.hy_accumulate_pass(self.h, C.byref(gb), C.byref(cfg), C.c_void_p(shadow.data_ptr()),
+        L.check(self.lib.hy_accumulate_pass(self.h, C.byref(gb), C.byref(cfg), C.c_void_p(_ptr(shadow)),
                                             C.byref(acc)), "accumulate_pass")
 
     def shade_pass(self, planes, cam36, cfg, hist, fmt=L.HY_ACCUM_U8, out_f=None, out_8=None,
@@ -232,8 +239,8 @@ class HybridContext:
         acc = self._accum(hist, fmt)
         st = L.HyStats()
         L.check(self.lib.hy_shade_pass(self.h, C.byref(gb), C.byref(cam), C.byref(cfg), C.byref(acc),
-                                       C.c_void_p(out_f.data_ptr()) if out_f is not None else None,
-                                       C.c_void_p(out_8.data_ptr()) if out_8 is not None else None,
+                                       C.c_void_p(_ptr(out_f)) if out_f is not None else None,
+                                       C.c_void_p(_ptr(out_8)) if out_8 is not None else None,
                                        C.byref(st)), "shade_pass")
         return st.as_dict()
 
@@ -248,8 +255,8 @@ class HybridContext:
         cam = camera_struct(cam36)
         st = L.HyStats()
         L.check(self.lib.hy_pathtrace_pass(self.h, C.byref(cam), width, height, C.byref(cfg),
-                                           C.c_void_p(image.data_ptr()),
-                                           C.c_void_p(out_f.data_ptr()) if out_f is not None else None,
+                                           C.c_void_p(_ptr(image)),
+                                           C.c_void_p(_ptr(out_f)) if out_f is not None else None,
                                            C.byref(st) if stats else None), "pathtrace_pass")
         return image, st.as_dict()
 
@@ -261,9 +268,16 @@ class HybridContext:
         if out is None:
             out = torch.empty((h, w, 4), dtype=torch.uint8, device=image.device)
         is8 = image.dtype == torch.uint8
-        L.check(self.lib.hy_post_resolve(self.h, w, h, C.c_void_p(image.data_ptr()) if is8 else None,
-                                         None if is8 else C.c_void_p(image.data_ptr()),
-                                         C.c_void_p(out.data_ptr())), "post_resolve")
+        if not is8 and image.dtype != torch.float32:
+            raise TypeError("post expects a uint8 BGRA8 or float32 RGBA image")
+        if not image.is_contiguous():  # the kernel reads packed (H, W, 4) texels
+            image = image.contiguous()
+            torch.cuda.synchronize(image.device)  # the copy ran on torch's stream
+        if not out.is_contiguous():
+            raise ValueError("post writes a packed (H, W, 4) image")
+        L.check(self.lib.hy_post_resolve(self.h, w, h, C.c_void_p(_ptr(image)) if is8 else None,
+                                         None if is8 else C.c_void_p(_ptr(image)),
+                                         C.c_void_p(_ptr(out))), "post_resolve")
         return out
 
     def backward(self, planes, cam36, cfg, hist, grad_img, fmt=L.HY_ACCUM_U8, grad_mats=None, grad_lights=None,
@@ -284,8 +298,8 @@ class HybridContext:
         acc = self._accum(hist, fmt)
         st = L.HyStats()
         L.check(self.lib.hy_hybrid_backward(self.h, C.byref(gb), C.byref(cam), C.byref(cfg), C.byref(acc),
-                                            C.c_void_p(grad_img.data_ptr()), C.c_void_p(grad_mats.data_ptr()),
-                                            C.c_void_p(grad_lights.data_ptr()), C.byref(st) if stats else None),
+                                            C.c_void_p(_ptr(grad_img)), C.c_void_p(_ptr(grad_mats)),
+                                            C.c_void_p(_ptr(grad_lights)), C.byref(st) if stats else None),
                 "hybrid_backward")
         return grad_mats, grad_lights[: self.num_lights], st.as_dict()
 
@@ -307,8 +321,8 @@ class HybridContext:
             vs[i].camera = camera_struct(v["camera"])
             vs[i].config = v["config"]
             vs[i].accum = self._accum(v["hist"], v.get("fmt", L.HY_ACCUM_U8))
-            vs[i].out_rgba32f = v["out_f"].data_ptr() if v.get("out_f") is not None else None
-            vs[i].out_bgra8 = v["out_8"].data_ptr() if v.get("out_8") is not None else None
+            vs[i].out_rgba32f = _ptr(v["out_f"]) if v.get("out_f") is not None else None
+            vs[i].out_bgra8 = _ptr(v["out_8"]) if v.get("out_8") is not None else None
             keep.append(planes)
         flags = (0 if graph else L.HY_BATCH_NO_GRAPH) | (0 if sync else L.HY_BATCH_NO_STATUS_SYNC)
         st = L.HyStats()

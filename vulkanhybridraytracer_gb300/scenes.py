@@ -279,6 +279,66 @@ def diff(seed: int = 3, width: int = 512, height: int = 512) -> Workload:
     return Workload("diff-512x512-82k", sc, width, height, 16, 1, 1)
 
 
+# ---- the large combined configuration ----------------------------------------------------
+def torus(rng: np.random.Generator, nu: int = 32, nv: int = 32, R: float = 1.0, r: float = 0.35,
+          displacement: float = 0.06) -> Mesh:
+    """Torus of 2 nu nv triangles (2048 at 32 x 32) with a seeded radial displacement of the tube."""
+    u = np.arange(nu) * 2 * np.pi / nu
+    v = np.arange(nv) * 2 * np.pi / nv
+    U, V = np.meshgrid(u, v, indexing="ij")
+    bumps = 1.0 + displacement * (_value_noise(rng, max(nu, nv), 4)[:nu, :nv] - 0.5) * 2.0
+    rr = r * bumps
+    pos = np.stack([(R + rr * np.cos(V)) * np.cos(U), rr * np.sin(V), (R + rr * np.cos(V)) * np.sin(U)], -1)
+    nrm = np.stack([np.cos(V) * np.cos(U), np.sin(V), np.cos(V) * np.sin(U)], -1)
+    uv = np.stack([U / (2 * np.pi), V / (2 * np.pi)], -1)
+    i, j = np.meshgrid(np.arange(nu), np.arange(nv), indexing="ij")
+    a = i * nv + j
+    b = ((i + 1) % nu) * nv + j
+    c = i * nv + (j + 1) % nv
+    d = ((i + 1) % nu) * nv + (j + 1) % nv
+    idx = np.stack([a, c, b, b, c, d], -1).reshape(-1).astype(np.uint32)
+    return Mesh(_vertices(pos.reshape(-1, 3), nrm.reshape(-1, 3), uv.reshape(-1, 2)), idx)
+
+
+def _rotation(q: np.ndarray) -> np.ndarray:
+    w, x, y, z = q / np.linalg.norm(q)
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def large(seed: int = 4, width: int = 3840, height: int = 2160, n_instances: int = 4096, terrain_n: int = 512,
+          n_materials: int = 1024, n_lights: int = 64) -> Workload:
+    """3840x2160: 4096 instances of 8 base meshes (4 icospheres of subdivision 3, 1,280
+    triangles, and 4 displaced tori of 2,048) under random rotations, scale U[0.2, 4] and
+    positions over the terrain, flattened into one BVH (~6.8M triangles) plus the 1080p
+    configuration's 512x512 terrain; 1024 materials; 64 area lights (radius 0.5, intensity
+    U[10, 50]); 64 shadow samples per pixel spread over the lights (1 per light,
+    DECORRELATED); 2 reflection bounces."""
+    rng = np.random.default_rng(seed)
+    sc = Scene()
+    ter, hmap = terrain(rng, terrain_n)
+    sc.materials = random_materials(rng, n_materials)
+    sc.entities.append(Object(ter, int(rng.integers(n_materials)), trs()))
+    bases = [icosphere(3) for _ in range(4)] + [torus(rng) for _ in range(4)]
+    n = hmap.shape[0]
+    for _ in range(n_instances):
+        mesh = bases[int(rng.integers(len(bases)))]
+        s = float(rng.uniform(0.2, 4.0))
+        x, z = rng.uniform(-45, 45, 2)
+        gi = int(np.clip((x + 50) / 100 * (n - 1), 0, n - 1))
+        gj = int(np.clip((z + 50) / 100 * (n - 1), 0, n - 1))
+        m = np.eye(4)
+        m[:3, :3] = _rotation(rng.normal(size=4)) * s
+        m[:3, 3] = (x, hmap[gj, gi] + s, z)
+        sc.entities.append(Object(mesh, int(rng.integers(n_materials)), m.T.copy()))  # glm storage m[col][row]
+    sc.lights = [Light(POINT_LIGHT, (1, 1, 1), (rng.uniform(-40, 40), rng.uniform(10, 20), rng.uniform(-40, 40)),
+                       float(rng.uniform(10, 50)), 500.0, 0.5) for _ in range(n_lights)]
+    sc.camera = Camera((0.0, 22.0, 62.0), (0.0, 0.0, 0.0), 60.0)
+    sc.env = [env_map(rng), env_map(rng, sun=False)]
+    return Workload(f"large-{width}x{height}-{sc.num_tris // 1000}k", sc, width, height, 1, 2, 1)
+
+
 # ---- the mixed batch ------------------------------------------------------------------
 BATCH_RESOLUTIONS = ((320, 240), (640, 480), (1280, 720), (1920, 1080))
 BATCH_SPP = (1, 4, 16, 64)
