@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define HY_ABI_VERSION 1
+#define HY_ABI_VERSION 2
 
 /* ---- error codes (the reference aborts through VK_CHECK, src/vk_engine.h:15-24) ---- */
 enum {
@@ -174,6 +174,9 @@ typedef struct HyPassConfig {
     uint32_t block_size;    /* threads per block; 0 = default / autotuned */
     uint32_t queue_chunk;   /* work items fetched per warp from the ray queue; 0 = default */
     uint32_t stack_depth;   /* traversal stack entries; 0 = default (max 64) */
+    uint32_t group_lanes;   /* DECORRELATED shadow rays: lanes per pixel-light group (power of two,
+                               2..32, each lane traces spp / group_lanes samples in turn);
+                               0 = the next power of two >= spp */
     uint32_t min_blocks;    /* shadow-kernel variant: compiled for 5 (96 registers) or 8 (64 registers)
                                resident blocks per SM; 0 = 8 */
 } HyPassConfig;

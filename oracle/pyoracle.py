@@ -85,7 +85,8 @@ class _GBuf(C.Structure):
 
 class _Cfg(C.Structure):
     _fields_ = [("shadow_spp", U32), ("max_bounces", U32), ("rng_mode", U32), ("accum_frame", C.c_int32),
-                ("flags", U32), ("block_size", U32), ("queue_chunk", U32), ("stack_depth", U32), ("min_blocks", U32)]
+                ("flags", U32), ("block_size", U32), ("queue_chunk", U32), ("stack_depth", U32), ("group_lanes", U32),
+                ("min_blocks", U32)]
 
 
 class _Accum(C.Structure):
@@ -368,4 +369,4 @@ class GradOracle:
 
 def cfg_dict(spp=1, max_bounces=8, rng_mode=0, accum_frame=0, flags=0):
     return dict(shadow_spp=spp, max_bounces=max_bounces, rng_mode=rng_mode, accum_frame=accum_frame, flags=flags,
-                block_size=0, queue_chunk=0, stack_depth=0, min_blocks=0)
+                block_size=0, queue_chunk=0, stack_depth=0, group_lanes=0, min_blocks=0)

@@ -402,3 +402,9 @@ def test_group_kernel_equals_pixel_kernel(small, spp):
     sc = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, L.HY_FLAG_RAY_POOL), c)
     assert torch.equal(a, b) and torch.equal(a, c)
     assert sa["shadow_rays"] == sb["shadow_rays"] == sc["shadow_rays"] > 0
+    # smaller lane groups (several samples per lane in turn): the same images
+    for G in (2, 4, 8):
+        d = torch.zeros_like(a)
+        torch.cuda.synchronize()
+        small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, 0, group_lanes=G), d)
+        assert torch.equal(a, d), G

@@ -316,6 +316,10 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
             mode = mode == MODE_SHADOW ? MODE_SHADOW_G : MODE_SHADOW_ACCUM_G;
             uint32_t G = 2;
             while (G < P.spp && G < 32) G <<= 1;
+            if (cfg->group_lanes) {
+                G = cfg->group_lanes;
+                if (G < 2 || G > 32 || (G & (G - 1))) return HY_ERR_INVALID_ARG;
+            }
             P.group = G;
         }
     }
@@ -910,12 +914,24 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
         pv[i] = make_params(c, &v.gbuffer, &v.camera, &v.config, v.accum.format, nullptr, v.accum.history,
                             v.out_rgba32f, v.out_bgra8);
         pv[i].scene = v.scene;
-        pv[i].tile_begin = total;
         pv[i].num_lights = v.accum.num_lights;
         uint32_t G = 1;
         if (v.config.rng_mode == HY_RNG_DECORRELATED)
             while (G < v.config.shadow_spp && G < 32) G <<= 1;
         pv[i].group = G;
+    }
+    // the queue hands out the costliest views' tiles first (shadow rays per tile:
+    // lights x samples), so the launch ends on cheap tiles instead of waiting
+    // for the last warps of an expensive one
+    std::vector<uint32_t> order(nv);
+    for (uint32_t i = 0; i < nv; i++) order[i] = i;
+    auto tile_cost = [&](uint32_t i) {
+        const uint64_t spp = views[i].config.rng_mode == HY_RNG_DECORRELATED ? views[i].config.shadow_spp : 1;
+        return (uint64_t)pv[i].num_lights * spp + 1;
+    };
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return tile_cost(a) > tile_cost(b); });
+    for (uint32_t i : order) {
+        pv[i].tile_begin = total;
         total += pv[i].ntiles;
     }
     if ((rc = ensure_size(c, c->raw_shadow, raw_bytes ? raw_bytes : 16))) return rc;
@@ -938,7 +954,10 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
         c->h_batch_tab_bytes = tab_bytes;
         if (c->batch_exec) { cudaGraphExecDestroy(c->batch_exec); c->batch_exec = nullptr; c->batch_key.clear(); }
     }
-    std::memcpy(c->h_batch_tab, pv.data(), nv * sizeof(PassParams));
+    // the device table lists the views in queue order (increasing tile_begin, which
+    // the kernels' view lookup searches)
+    for (uint32_t k = 0; k < nv; k++)
+        std::memcpy((uint8_t*)c->h_batch_tab + k * sizeof(PassParams), &pv[order[k]], sizeof(PassParams));
     std::memcpy((uint8_t*)c->h_batch_tab + nv * sizeof(PassParams), sd.data(), ns * sizeof(SceneDev));
     BatchParams B;
     B.views = c->batch_tab.as<PassParams>();

@@ -277,6 +277,58 @@ __device__ __forceinline__ uint32_t byte_at(uint32_t lo4, uint32_t hi4, int slot
     return (w >> ((slot & 3) * 8)) & 0xffu;
 }
 
+// three-input max / min (one instruction on sm_100+); NaN inputs are ignored as by fmaxf / fminf
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// packed pairs of f32 (sm_100+ f32x2 arithmetic: two IEEE single-rounded ops per instruction)
+__device__ __forceinline__ unsigned long long f2_pack(float a, float b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2_pack_bits(uint32_t a, uint32_t b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "r"(a), "r"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(unsigned long long v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
+                                                     unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// bit k set when byte k of hi4:lo4 is nonzero
+__device__ __forceinline__ uint32_t nonzero_bytes(uint32_t lo4, uint32_t hi4) {
+    const uint32_t a = __vcmpne4(lo4, 0u) & 0x80808080u, b = __vcmpne4(hi4, 0u) & 0x80808080u;
+    return ((a * 0x00204081u) >> 28) | (((b * 0x00204081u) >> 28) << 4);
+}
+
+// bit s of an 8-bit slot mask moved to bit s ^ near (the slots' traversal ranks)
+__device__ __forceinline__ uint32_t slots_to_ranks(uint32_t m, uint32_t near) {
+    if (near & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (near & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (near & 4u) m = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
+    return m;
+}
+
 // Stack traversal of the 8-wide BVH.  ANY: TerminateOnFirstHit semantics.
 // COUNT: accumulate node visits / triangle tests.
 //
@@ -351,28 +403,42 @@ __device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& r, fl
             }
         }
     }
-    uint32_t hit_int = 0, hit_tri = 0;
+    // per axis, the (near, far) plane pair goes through one f32x2 add and one f32x2 fma
+    unsigned long long adj2[3], org2[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        adj2[a] = f2_pack(adj[a], adj[a]);
+        org2[a] = f2_pack(org[a], org[a]);
+    }
+    const unsigned long long kMinus2p23 = f2_pack(-8388608.0f, -8388608.0f);
+    uint32_t hitbits = 0;
 #pragma unroll
     for (int slot = 0; slot < 8; slot++) {
-        const uint32_t m = byte_at(q1.z, q1.w, slot);
         float tn[3], tf[3];
         // byte -> float without I2F: PRMT builds 0x4B0000qq (= 2^23 + q), the
-        // FADD removes 2^23 exactly
+        // add removes 2^23 exactly
         const uint32_t kSel = 0x7540u | (uint32_t)(slot & 3);  // an immediate once the loop unrolls
 #pragma unroll
         for (int a = 0; a < 3; a++) {
-            const float lo = __fsub_rn(__uint_as_float(__byte_perm(qn[a][slot >> 2], 0x4B000000u, kSel)), 8388608.0f);
-            const float hi = __fsub_rn(__uint_as_float(__byte_perm(qf[a][slot >> 2], 0x4B000000u, kSel)), 8388608.0f);
-            tn[a] = __fmaf_rn(lo, adj[a], org[a]);
-            tf[a] = __fmaf_rn(hi, adj[a], org[a]);
+            const unsigned long long q2 = f2_pack_bits(__byte_perm(qn[a][slot >> 2], 0x4B000000u, kSel),
+                                                       __byte_perm(qf[a][slot >> 2], 0x4B000000u, kSel));
+            f2_unpack(f2_fma(f2_add(q2, kMinus2p23), adj2[a], org2[a]), tn[a], tf[a]);
         }
-        const float tnear = fmaxf(fmaxf(tn[0], tn[1]), fmaxf(tn[2], tmin));
-        const float tfar = fminf(fminf(tf[0], tf[1]), fminf(tf[2], t.tmax));
-        const bool hit = m != 0 && tnear <= __fmul_rn(tfar, 1.0000003f);
-        if (hit) {
-            if (imask & (1u << slot)) hit_int |= 1u << (slot ^ r.near);
-            else hit_tri |= ((1u << (m >> 5)) - 1u) << (m & 31u);
-        }
+        // max(max(tn0, tn1), max(tn2, tmin)) and its min twin, as two instructions each
+        const float tnear = fmaxf(fmax3(tn[0], tn[1], tn[2]), tmin);
+        const float tfar = fminf(fmin3(tf[0], tf[1], tf[2]), t.tmax);
+        if (tnear <= __fmul_rn(tfar, 1.0000003f)) hitbits |= 1u << slot;
+    }
+    // empty slots (meta byte 0) never count; internal children go to the stack
+    // in rank order, leaf slots give their triangles
+    hitbits &= nonzero_bytes(q1.z, q1.w);
+    const uint32_t hit_int = slots_to_ranks(hitbits & imask, r.near);
+    uint32_t hit_leaf = hitbits & ~imask, hit_tri = 0;
+    while (hit_leaf) {
+        const uint32_t slot = __ffs(hit_leaf) - 1;
+        hit_leaf &= hit_leaf - 1u;
+        const uint32_t m = __byte_perm(q1.z, q1.w, slot) & 0xffu;
+        hit_tri |= ((1u << (m >> 5)) - 1u) << (m & 31u);
     }
     const uint32_t tri_base = q1.y;
     while (hit_tri) {
