@@ -489,7 +489,7 @@ def run_batch(args):
                           out_8=torch.empty((h, w, 4), dtype=torch.uint8, device=dev)))
     torch.cuda.synchronize()
 
-    def set_frame(frame, chunk=1, minb=8):
+    def set_frame(frame, chunk=1, minb=0):
         for v in views:
             v["camera"][32] = float(frame)
             v["config"] = pass_config(v["spp"], 1, L.HY_RNG_DECORRELATED, frame, L.HY_FLAG_NO_STATUS_SYNC,

@@ -178,7 +178,8 @@ typedef struct HyPassConfig {
                                2..32, each lane traces spp / group_lanes samples in turn);
                                0 = the next power of two >= spp */
     uint32_t min_blocks;    /* shadow-kernel variant: compiled for 5 (96 registers) or 8 (64 registers)
-                               resident blocks per SM; 0 = 8 */
+                               resident blocks per SM, the lane-group kernel also for 6 and 7;
+                               0 = 6 for the lane-group kernel, 8 otherwise */
 } HyPassConfig;
 
 typedef struct HyStats {

@@ -323,8 +323,10 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
             P.group = G;
         }
     }
-    // 8 resident blocks (64 registers) measured fastest on the 1080p workload
-    int minb = cfg->min_blocks ? (int)cfg->min_blocks : 8;
+    // measured fastest on the 1080p workload: 6 resident blocks (80 registers)
+    // for the lane-group kernel (1.4 % ahead of 8), 8 (64 registers) otherwise
+    const bool grouped = mode == MODE_SHADOW_G || mode == MODE_SHADOW_ACCUM_G;
+    int minb = cfg->min_blocks ? (int)cfg->min_blocks : (grouped ? 6 : 8);
     int grid = grid_for(c, mode, count, minb, block);
     grid = std::max(1, std::min<int>(grid, (int)((P.ntiles * 32ull + block - 1) / block)));
     ProfScope prof(c, mode);

@@ -991,7 +991,10 @@ static void* shadow_kernel(bool count) {
 }
 template <bool GROUP, bool ACCUM>
 static void* shadow_kernel(bool count, int minb) {
-    return minb >= 8 ? shadow_kernel<GROUP, ACCUM, 8>(count) : shadow_kernel<GROUP, ACCUM, 5>(count);
+    if (minb >= 8) return shadow_kernel<GROUP, ACCUM, 8>(count);
+    if (GROUP && minb == 7) return shadow_kernel<GROUP, ACCUM, 7>(count);
+    if (GROUP && minb == 6) return shadow_kernel<GROUP, ACCUM, 6>(count);
+    return shadow_kernel<GROUP, ACCUM, 5>(count);
 }
 // minb: resident blocks per SM the shadow kernel is compiled for (register cap)
 template <bool ACCUM, int MINB>
