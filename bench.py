@@ -436,6 +436,39 @@ def run_large(args):
     rays_b = st_b["shadow_rays"] + st_b["reflection_rays"] + st_b["hit_shadow_rays"]
     mp = time_it(plain, args.steps)
     mb = time_it(batched, args.steps)
+
+    # the same frame over the two-level structure (8 mesh BLASes + the terrain's
+    # under a TLAS of 4097 instances), and the per-frame structure update of both
+    xf = wl.scene.pack()[3]
+    ctx2 = HybridContext(0, stream=stream.cuda_stream)
+    ctx2.set_scene(wl.scene)
+    bvh2 = ctx2.build_bvh(instanced=True)
+    lay2 = ctx2.bvh_layout()
+    st2 = ctx2.forward(planes, wl.camera(0.0), cfg(0, 0), hist, L.HY_ACCUM_U8, out_f=outf, out_8=out8)
+    rays2 = st2["shadow_rays"] + st2["reflection_rays"] + st2["hit_shadow_rays"]
+    f2 = [frame]
+
+    def fwd2():
+        f2[0] += 1
+        ctx2.forward(planes, wl.camera(float(f2[0])), cfg(f2[0]), hist, L.HY_ACCUM_U8, out_f=outf, out_8=out8,
+                     stats=False)
+
+    for _ in range(args.warmup):
+        fwd2()
+    f2_ms = time_it(fwd2, args.steps)
+
+    def update_ms(c):
+        ts = []
+        for _ in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            c.refit_bvh(xf)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return 1e3 * float(np.median(ts[args.warmup:]))
+
+    upd_flat, upd_two = update_ms(ctx), update_ms(ctx2)
+    ctx2.close()
     clk = clocks.stop()
     line = {"metric": "large_combined_mrays_per_s", "value": rays / (f_ms / 1e3) / 1e6, "unit": "Mrays/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": f_ms, "higher_is_better": True,
@@ -452,6 +485,11 @@ def run_large(args):
             "batch_4k_plus_4x1080p": {"rays": rays_b, "batched_ms": mb, "per_view_ms": mp,
                                       "batched_mrays_per_s": rays_b / (mb / 1e3) / 1e6,
                                       "batched_over_per_view": mp / mb},
+            "two_level": {"build_ms": bvh2["build_ms"], "nodes": lay2["num_nodes"], "blas": lay2["num_blas"],
+                          "instances": lay2["num_instances"], "depth": lay2["depth"],
+                          "node_bytes": lay2["num_nodes"] * 80, "flat_node_bytes": bvh["num_bvh8_nodes"] * 80,
+                          "rays": rays2, "forward_ms": f2_ms, "mrays_per_s": rays2 / (f2_ms / 1e3) / 1e6,
+                          "update_ms": upd_two, "flat_refit_ms": upd_flat},
             "clocks": clk, "gpu_launches": 2}
     print(json.dumps(line))
     ctx.close()

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define HY_ABI_VERSION 2
+#define HY_ABI_VERSION 3
 
 /* ---- error codes (the reference aborts through VK_CHECK, src/vk_engine.h:15-24) ---- */
 enum {
@@ -250,9 +250,41 @@ int hy_bvh_refit(HyCtx* ctx, const float* transforms, uint32_t num_transforms);
  * NULL.  morton/order: num_tris each (sorted codes and triangle ids);
  * bvh2: 10 words per internal node (left, right, first, last, lo[3], hi[3];
  * a child with bit 31 set is leaf number child & 0x7fffffff); bvh8: 20 words
- * per node; tris: 12 words per triangle. */
+ * per node; tris: 12 words per triangle.  Two-level structure: bvh8 and tris
+ * only (HyBvhLayout.num_nodes / num_records entries); morton, order and bvh2
+ * must be NULL. */
 int hy_bvh_download(HyCtx* ctx, uint32_t* morton, uint32_t* order, uint32_t* bvh2,
                     uint32_t* bvh8, float* tris);
+
+/* Two-level structure, the driver's BLAS/TLAS split (one BLAS per primitive,
+ * src/vk_mesh.cpp:424-470 + buildBlas, src/renderer.cpp:1696-1753; one TLAS
+ * instance per primitive, src/vk_mesh.cpp:472-492 + buildTlas,
+ * src/renderer.cpp:1757-1865).  One BLAS per distinct mesh (primitives with
+ * equal first_index, index_count and vertex_offset share it), built over the
+ * mesh's object-space triangles; a TLAS over one instance per primitive with
+ * triangles, whose box is its mesh box through its transform.  Rays enter an
+ * instance through its world-to-object transform (t is the same in both
+ * frames; hit ids stay global triangle ids).  hy_bvh_refit then rebuilds the
+ * instance records and the TLAS only (the per-frame TLAS update of
+ * src/vk_engine.cpp:172-187).  The batch entry point and HY_FLAG_RAY_POOL
+ * return HY_ERR_UNSUPPORTED on it. */
+int hy_bvh_build_instanced(HyCtx* ctx, HyBvhStats* stats);
+
+typedef struct HyBvhLayout {
+    uint32_t two_level;      /* 0: one BVH8 over world-space triangles */
+    uint32_t num_nodes;      /* 80-byte nodes (two-level: TLAS region first, then each BLAS) */
+    uint32_t num_records;    /* 48-byte leaf records (two-level: TLAS instance entries first) */
+    uint32_t num_instances;  /* two-level: TLAS instances */
+    uint32_t num_blas;       /* two-level: distinct meshes */
+    uint32_t tlas_region;    /* two-level: nodes and records reserved for the TLAS (= instances) */
+    uint32_t tlas_nodes;     /* two-level: nodes the TLAS uses (the rest of its region is zero) */
+    uint32_t depth;          /* BVH8 levels (two-level: TLAS + deepest BLAS) */
+} HyBvhLayout;
+int hy_bvh_layout(HyCtx* ctx, HyBvhLayout* out);
+/* Two-level only.  records: 16 words per instance (world->object rows
+ * 3 x (m0, m1, m2, t), then BLAS root node, first global triangle, primitive,
+ * 0 as uint32 bits); boxes: 6 floats per instance (the TLAS box, lo then hi). */
+int hy_bvh_download_instances(HyCtx* ctx, float* records, float* boxes);
 
 /* ---- ray queries (any_hit: TerminateOnFirstHit semantics) ---- */
 int hy_trace_rays(HyCtx* ctx, const HyRay* d_rays, uint32_t num_rays, int any_hit,

@@ -197,9 +197,12 @@ public:
         num_lights_ = (uint32_t)s._lights.size();
     }
 
-    HyBvhStats create_acceleration_structures() {
+    // two_level: one BLAS per distinct mesh under a TLAS over the entities, as
+    // the reference's BLAS/TLAS pair; otherwise one BVH over the flattened scene
+    HyBvhStats create_acceleration_structures(bool two_level = false) {
         HyBvhStats st;
-        check(hy_bvh_build(ctx_, &st), "hy_bvh_build");
+        if (two_level) check(hy_bvh_build_instanced(ctx_, &st), "hy_bvh_build_instanced");
+        else check(hy_bvh_build(ctx_, &st), "hy_bvh_build");
         return st;
     }
 

@@ -235,17 +235,20 @@ static inline float surface(const Box& b) {
     return a;
 }
 
-void bvh_build(Scene& s) {
-    Bvh& B = s.bvh;
+// LBVH -> BVH8 over n items of three points each (9 floats: a triangle, or an
+// instance box as (lo, hi, hi)); an item's box is the min/max of its points.
+// Records hold the item's points and its index; node and record numbers in the
+// emitted nodes are offset by node_off / rec_off (BLASes and the TLAS of the
+// two-level structure share one node array and one record array).
+static void build_core(const float* items, uint32_t n, Bvh& B, uint32_t node_off, uint32_t rec_off) {
     B = Bvh();
-    const uint32_t n = s.ntri;
     B.n = n;
-    if (n == 0) { s.bvh_ok = false; return; }
+    if (n == 0) return;
     std::vector<Box> tb(n);
     std::vector<float> cen((size_t)n * 3);
     for (int a = 0; a < 3; a++) { B.slo[a] = INFINITY; B.shi[a] = -INFINITY; }
     for (uint32_t t = 0; t < n; t++) {
-        const float* w = &s.world[(size_t)t * 9];
+        const float* w = &items[(size_t)t * 9];
         for (int a = 0; a < 3; a++) {
             tb[t].lo[a] = fmin2(fmin2(w[a], w[3 + a]), w[6 + a]);
             tb[t].hi[a] = fmax2(fmax2(w[a], w[3 + a]), w[6 + a]);
@@ -413,7 +416,7 @@ void bvh_build(Scene& s) {
                 for (uint32_t j = 0; j < cnt; j++) {
                     uint32_t tid = B.order[f + j];
                     float* dst = &B.tris[(size_t)(tri_count + toff + j) * 12];
-                    const float* w = &s.world[(size_t)tid * 9];
+                    const float* w = &items[(size_t)tid * 9];
                     dst[0] = w[0]; dst[1] = w[1]; dst[2] = w[2]; dst[3] = bitsf(tid);
                     dst[4] = w[3]; dst[5] = w[4]; dst[6] = w[5]; dst[7] = 0.f;
                     dst[8] = w[6]; dst[9] = w[7]; dst[10] = w[8]; dst[11] = 0.f;
@@ -424,23 +427,32 @@ void bvh_build(Scene& s) {
         tri_count += toff;
         node.w[3] = imask << 24;
         quantize_node(B, tb, r, slots, node.w);
-        node.w[4] = child_base;
-        node.w[5] = tri_base;
+        node.w[4] = node_off + child_base;
+        node.w[5] = rec_off + tri_base;
         auto pack4 = [](const uint8_t* b) { return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24); };
         node.w[6] = pack4(meta); node.w[7] = pack4(meta + 4);
         B.bvh8.push_back(node);
     }
     (void)ref_box;
     B.depth = level.empty() ? 0 : level.back() + 1;
-    s.bvh_ok = true;
+}
+
+void bvh_build(Scene& s) {
+    s.two_level = false;
+    s.two = Bvh2L();
+    build_core(s.world.data(), s.ntri, s.bvh, 0, 0);
+    s.bvh_ok = s.ntri > 0;
 }
 
 // New transforms, same topology: re-transformed triangles, refitted binary
 // tree, every 8-wide node re-quantised with its stored slot plan, packed
 // triangles rewritten (the GPU refit computes exactly this).
+static void tlas_build(Scene& s);
+
 void bvh_refit(Scene& s) {
     Bvh& B = s.bvh;
     if (!s.bvh_ok) return;
+    if (s.two_level) { tlas_build(s); return; }
     std::vector<Box> tb = tri_boxes(s);
     refit_bvh2(B, tb);
     for (size_t k = 0; k < B.bvh8.size(); k++) quantize_node(B, tb, B.node_ref[k], &B.node_plan[k * 8], B.bvh8[k].w);
@@ -615,9 +627,312 @@ static Hit trace_bvh8(const Scene& s, const float o[3], const float d[3], float 
     return h;
 }
 
+// ---- two-level structure ------------------------------------------------------
+
+static inline float round_down_f(double x) {
+    float f = (float)x;
+    return ((double)f > x) ? std::nextafter(f, -INFINITY) : f;
+}
+static inline float round_up_f(double x) {
+    float f = (float)x;
+    return ((double)f < x) ? std::nextafter(f, INFINITY) : f;
+}
+
+// World box of an instance: the 8 corners of its mesh's object-space root box
+// through the object->world matrix M (column-major) in double, each corner
+// coordinate ((m0 x + m1 y) + m2 z) + m3, then padded by 2^-16 of the extent
+// plus 2^-20 of the largest magnitude per axis (room for the rounding of the
+// world->object ray transform) and rounded outwards to float.
+static void instance_box(const float* mesh_box, const float* M, float* out6) {
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int corner = 0; corner < 8; corner++) {
+        double p[3];
+        for (int a = 0; a < 3; a++) p[a] = (double)((corner >> a) & 1 ? mesh_box[3 + a] : mesh_box[a]);
+        for (int r = 0; r < 3; r++) {
+            double w = (double)M[0 * 4 + r] * p[0];
+            w = w + (double)M[1 * 4 + r] * p[1];
+            w = w + (double)M[2 * 4 + r] * p[2];
+            w = w + (double)M[3 * 4 + r];
+            lo[r] = std::fmin(lo[r], w);
+            hi[r] = std::fmax(hi[r], w);
+        }
+    }
+    for (int a = 0; a < 3; a++) {
+        const double mag = std::fmax(std::fabs(lo[a]), std::fabs(hi[a]));
+        const double pad = (hi[a] - lo[a]) * 0x1p-16 + mag * 0x1p-20;
+        out6[a] = round_down_f(lo[a] - pad);
+        out6[3 + a] = round_up_f(hi[a] + pad);
+    }
+}
+
+// world->object rows of every transform: rows of inverse(M) rounded to float
+static void derive_xinv(Scene& s) {
+    const size_t nx = s.xf.size() / 16;
+    s.two.xinv.assign(nx * 12, 0.f);
+    for (size_t t = 0; t < nx; t++) {
+        double m[16], inv[16];
+        for (int i = 0; i < 16; i++) m[i] = s.xf[t * 16 + i];
+        inverse4(m, inv);
+        for (int r = 0; r < 3; r++)
+            for (int k = 0; k < 4; k++) s.two.xinv[t * 12 + r * 4 + k] = (float)inv[k * 4 + r];
+    }
+}
+
+// instance records and TLAS (the per-frame part: transforms only)
+static void tlas_build(Scene& s) {
+    Bvh2L& T = s.two;
+    derive_xinv(s);
+    T.inst.assign((size_t)T.ninst * 16, 0.f);
+    T.inst_box.assign((size_t)T.ninst * 6, 0.f);
+    std::vector<float> items((size_t)T.ninst * 9);
+    for (uint32_t i = 0; i < T.ninst; i++) {
+        const uint32_t p = T.inst_prim[i], m = T.prim_mesh[p];
+        const uint32_t tf = s.prims[p].transform_id;
+        float* I = &T.inst[(size_t)i * 16];
+        for (int k = 0; k < 12; k++) I[k] = T.xinv[(size_t)tf * 12 + k];
+        I[12] = bitsf(T.blas_node0[m]);
+        I[13] = bitsf(s.prim_tri0[p]);
+        I[14] = bitsf(p);
+        float* b = &T.inst_box[(size_t)i * 6];
+        instance_box(&T.mesh_box[(size_t)m * 6], &s.xf[(size_t)tf * 16], b);
+        float* it = &items[(size_t)i * 9];
+        for (int a = 0; a < 3; a++) { it[a] = b[a]; it[3 + a] = b[3 + a]; it[6 + a] = b[3 + a]; }
+    }
+    Bvh tl;
+    build_core(items.data(), T.ninst, tl, 0, 0);
+    T.tlas_nodes = (uint32_t)tl.bvh8.size();
+    T.tlas_depth = tl.depth;
+    for (uint32_t k = 0; k < T.tlas_region; k++) std::memset(T.nodes[k].w, 0, 80);
+    for (uint32_t k = 0; k < T.tlas_nodes; k++) T.nodes[k] = tl.bvh8[k];
+    std::fill(T.tris.begin(), T.tris.begin() + (size_t)T.tlas_region * 12, 0.f);
+    std::copy(tl.tris.begin(), tl.tris.end(), T.tris.begin());
+}
+
+void bvh_build_instanced(Scene& s) {
+    s.bvh = Bvh();
+    s.bvh_ok = false;
+    s.two_level = false;
+    Bvh2L& T = s.two;
+    T = Bvh2L();
+    const uint32_t np = (uint32_t)s.prims.size();
+    T.prim_mesh.assign(np, 0xffffffffu);
+    for (uint32_t p = 0; p < np; p++) {
+        const HyPrimitive& pr = s.prims[p];
+        if (pr.index_count / 3 == 0) continue;
+        uint32_t m = 0;
+        for (; m < T.nblas; m++) {
+            const HyPrimitive& q = s.prims[T.mesh_prim[m]];
+            if (q.first_index == pr.first_index && q.index_count == pr.index_count &&
+                q.vertex_offset == pr.vertex_offset)
+                break;
+        }
+        if (m == T.nblas) { T.mesh_prim.push_back(p); T.nblas++; }
+        T.prim_mesh[p] = m;
+        T.inst_prim.push_back(p);
+    }
+    T.ninst = (uint32_t)T.inst_prim.size();
+    if (T.ninst == 0) return;
+    T.tlas_region = T.ninst;
+    T.nodes.assign(T.tlas_region, Bvh8Node{});
+    T.tris.assign((size_t)T.tlas_region * 12, 0.f);
+    T.mesh_box.assign((size_t)T.nblas * 6, 0.f);
+    uint32_t rec = T.tlas_region;
+    for (uint32_t m = 0; m < T.nblas; m++) {
+        const HyPrimitive& pr = s.prims[T.mesh_prim[m]];
+        const uint32_t nt = pr.index_count / 3;
+        std::vector<float> items((size_t)nt * 9);
+        for (uint32_t k = 0; k < nt; k++)
+            for (int v = 0; v < 3; v++) {
+                const float* P = s.verts[s.idx[pr.first_index + 3 * k + v] + pr.vertex_offset].pos;
+                for (int a = 0; a < 3; a++) items[(size_t)k * 9 + v * 3 + a] = P[a] + 0.0f;  // -0 -> +0
+            }
+        const uint32_t node0 = (uint32_t)T.nodes.size();
+        Bvh b;
+        build_core(items.data(), nt, b, node0, rec);
+        T.blas_node0.push_back(node0);
+        T.blas_rec0.push_back(rec);
+        T.blas_nodes.push_back((uint32_t)b.bvh8.size());
+        T.nodes.insert(T.nodes.end(), b.bvh8.begin(), b.bvh8.end());
+        T.tris.insert(T.tris.end(), b.tris.begin(), b.tris.end());
+        T.blas_depth = std::max(T.blas_depth, b.depth);
+        // root box: the binary tree's root, or the single triangle's box
+        float* mb = &T.mesh_box[(size_t)m * 6];
+        if (nt > 1) {
+            for (int a = 0; a < 3; a++) { mb[a] = b.bvh2[0].lo[a]; mb[3 + a] = b.bvh2[0].hi[a]; }
+        } else {
+            for (int a = 0; a < 3; a++) {
+                mb[a] = fmin2(fmin2(items[a], items[3 + a]), items[6 + a]);
+                mb[3 + a] = fmax2(fmax2(items[a], items[3 + a]), items[6 + a]);
+            }
+        }
+        rec += nt;
+    }
+    tlas_build(s);
+    s.two_level = true;
+    s.bvh_ok = true;
+}
+
+struct RayState {
+    RayPre p;
+    float invd[3];
+    uint32_t near;
+};
+
+static RayState ray_state(const float o[3], const float d[3]) {
+    RayState r;
+    r.p = ray_pre(o, d);
+    for (int a = 0; a < 3; a++) {
+        float dd = std::fabs(d[a]) > 1e-20f ? d[a] : std::copysign(1e-20f, d[a]);
+        r.invd[a] = 1.0f / dd;
+    }
+    r.near = (r.invd[0] < 0.f ? 1u : 0u) | (r.invd[1] < 0.f ? 2u : 0u) | (r.invd[2] < 0.f ? 4u : 0u);
+    return r;
+}
+
+// box tests of one node: internal children hit (rank order) and leaf records hit
+static void node_hits(const uint32_t* w, const RayState& r, float tmin, float tmax, uint32_t& hit_int,
+                      uint32_t& hit_tri) {
+    float adj[3], org[3];
+    for (int a = 0; a < 3; a++) {
+        uint32_t ea = (w[3] >> (8 * a)) & 0xffu;
+        adj[a] = bitsf(ea << 23) * r.invd[a];
+        org[a] = (bitsf(w[a]) - r.p.o[a]) * r.invd[a];
+    }
+    const uint32_t imask = w[3] >> 24;
+    hit_int = 0;
+    hit_tri = 0;
+    for (int slot = 0; slot < 8; slot++) {
+        uint8_t m = byte_of(w, 6, slot);
+        if (m == 0) continue;
+        float tn[3], tf[3];
+        for (int a = 0; a < 3; a++) {
+            float ql = (float)byte_of(w, 8 + 2 * a, slot);
+            float qh = (float)byte_of(w, 14 + 2 * a, slot);
+            float lo = r.invd[a] < 0.f ? qh : ql;
+            float hi = r.invd[a] < 0.f ? ql : qh;
+            tn[a] = std::fma(lo, adj[a], org[a]);
+            tf[a] = std::fma(hi, adj[a], org[a]);
+        }
+        float tnear = fmax2(fmax2(tn[0], tn[1]), fmax2(tn[2], tmin));
+        float tfar = fmin2(fmin2(tf[0], tf[1]), fmin2(tf[2], tmax));
+        if (!(tnear <= tfar * 1.0000003f)) continue;
+        if (imask & (1u << slot)) hit_int |= 1u << (slot ^ r.near);
+        else hit_tri |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+    }
+}
+
+// Two-level walk, step for step the product's: a TLAS leaf hands its hit
+// instance entries over one at a time; entering one saves the pending TLAS
+// group on the stack, moves the ray into object space
+// (((r0 x + r1 y) + r2 z) + t per row; the direction without t) and walks
+// the BLAS above the saved stack height; leaving it restores the world ray.
+// Hit ids are global triangle ids (the instance's first triangle + the
+// record's index in its mesh); t is shared by both levels (the direction is
+// not renormalised).
+static Hit trace_2l(const Scene& s, const float o[3], const float d[3], float tmin, float tmax, bool any_hit,
+                    Counters* c) {
+    const Bvh2L& T = s.two;
+    Hit h{tmax, HY_NO_HIT, 0.f, 0.f};
+    const RayState rw = ray_state(o, d);
+    RayState r = rw;
+    uint32_t stk_base[kStackMax], stk_bits[kStackMax];
+    int sp = 0, sp_base = 0;
+    bool level = false;
+    uint32_t inst_base = 0, inst_bits = 0, id_off = 0;
+    uint32_t g_base = 0, g_bits = (1u << 24) | (1u << r.near);
+    float cur_tmax = tmax;
+    const uint32_t nrec = (uint32_t)(T.tris.size() / 12), nnodes = (uint32_t)T.nodes.size();
+    for (uint32_t iter = 0;; iter++) {
+        if (iter >= kMaxIters) { if (c) c->status |= HY_STATUS_TIMEOUT; break; }
+        bool done = false;
+        for (;;) {
+            if (!level && inst_bits) {
+                if (g_bits & 0xff000000u) {
+                    if (sp >= kStackMax) { if (c) c->status |= HY_STATUS_STACK_OVERFLOW; done = true; break; }
+                    stk_base[sp] = g_base;
+                    stk_bits[sp] = g_bits;
+                    sp++;
+                }
+                const uint32_t b = (uint32_t)__builtin_ctz(inst_bits);
+                inst_bits &= inst_bits - 1u;
+                const uint32_t rec = inst_base + b;
+                if (rec >= nrec) { if (c) c->status |= HY_STATUS_BAD_INDEX; done = true; break; }
+                const uint32_t iid = fbits(T.tris[(size_t)rec * 12 + 3]);
+                if (iid >= T.ninst) { if (c) c->status |= HY_STATUS_BAD_INDEX; done = true; break; }
+                const float* I = &T.inst[(size_t)iid * 16];
+                float oo[3], dd[3];
+                for (int k = 0; k < 3; k++) {
+                    const float* R = I + 4 * k;
+                    float a = R[0] * rw.p.o[0];
+                    a = a + R[1] * rw.p.o[1];
+                    a = a + R[2] * rw.p.o[2];
+                    oo[k] = a + R[3];
+                    float e = R[0] * rw.p.d[0];
+                    e = e + R[1] * rw.p.d[1];
+                    dd[k] = e + R[2] * rw.p.d[2];
+                }
+                r = ray_state(oo, dd);
+                level = true;
+                sp_base = sp;
+                id_off = fbits(I[13]);
+                g_base = fbits(I[12]);
+                g_bits = (1u << 24) | (1u << r.near);
+                break;
+            }
+            if (g_bits & 0xff000000u) break;
+            if (level && sp == sp_base) { level = false; r = rw; continue; }
+            if (sp == 0) { done = true; break; }
+            --sp;
+            g_base = stk_base[sp];
+            g_bits = stk_bits[sp];
+        }
+        if (done) break;
+        const uint32_t rb = (uint32_t)__builtin_ctz(g_bits >> 24);
+        g_bits &= ~(1u << (24 + rb));
+        const uint32_t sl = rb ^ r.near;
+        const uint32_t idx = g_base + (uint32_t)__builtin_popcount(g_bits & 0xffu & ((1u << sl) - 1u));
+        if (g_bits & 0xff000000u) {
+            if (sp >= kStackMax) { if (c) c->status |= HY_STATUS_STACK_OVERFLOW; break; }
+            stk_base[sp] = g_base;
+            stk_bits[sp] = g_bits;
+            sp++;
+        }
+        if (idx >= nnodes) { if (c) c->status |= HY_STATUS_BAD_INDEX; break; }
+        const uint32_t* w = T.nodes[idx].w;
+        if (c) c->nodes++;
+        uint32_t hit_int, hit_tri;
+        node_hits(w, r, tmin, cur_tmax, hit_int, hit_tri);
+        const uint32_t tri_base = w[5];
+        if (!level) {
+            inst_base = tri_base;
+            inst_bits = hit_tri;
+        } else {
+            while (hit_tri) {
+                uint32_t b = (uint32_t)__builtin_ctz(hit_tri);
+                hit_tri &= hit_tri - 1u;
+                if (tri_base + b >= nrec) { if (c) c->status |= HY_STATUS_BAD_INDEX; return h; }
+                const float* tr = &T.tris[(size_t)(tri_base + b) * 12];
+                const uint32_t id = id_off + fbits(tr[3]);
+                if (c) c->tris++;
+                float tt, b1, b2;
+                if (tri_test(r.p, tr, tr + 4, tr + 8, tmin, cur_tmax, tt, b1, b2)) {
+                    if (h.id == HY_NO_HIT || better(tt, id, h)) { h = Hit{tt, id, b1, b2}; cur_tmax = tt; }
+                    if (any_hit) return h;
+                }
+            }
+        }
+        g_base = w[4];
+        g_bits = (hit_int << 24) | (w[3] >> 24);
+    }
+    return h;
+}
+
 Hit trace(const Scene& s, const float o[3], const float d[3], float tmin, float tmax, bool any_hit, int mode,
           Counters* c) {
-    if (mode == 1 && s.bvh_ok) return trace_bvh8(s, o, d, tmin, tmax, any_hit, c);
+    if (mode == 1 && s.bvh_ok) {
+        if (s.two_level) return trace_2l(s, o, d, tmin, tmax, any_hit, c);
+        return trace_bvh8(s, o, d, tmin, tmax, any_hit, c);
+    }
     return trace_brute(s, o, d, tmin, tmax, any_hit, c);
 }
 

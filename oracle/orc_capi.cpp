@@ -69,6 +69,35 @@ int orc_bvh_build(void* sp, uint32_t* info, float* bounds6) {
         for (int a = 0; a < 3; a++) { bounds6[a] = s.bvh.slo[a]; bounds6[3 + a] = s.bvh.shi[a]; }
     return s.bvh_ok ? 0 : -8;
 }
+// two-level build (hy_bvh_build_instanced's counterpart); layout = the 8 words
+// of HyBvhLayout
+static void layout_of(const Scene& s, uint32_t* L) {
+    const Bvh2L& T = s.two;
+    L[0] = s.two_level ? 1u : 0u;
+    L[1] = (uint32_t)T.nodes.size();
+    L[2] = (uint32_t)(T.tris.size() / 12);
+    L[3] = T.ninst;
+    L[4] = T.nblas;
+    L[5] = T.tlas_region;
+    L[6] = T.tlas_nodes;
+    L[7] = T.tlas_depth + T.blas_depth;
+}
+int orc_bvh_build_instanced(void* sp, uint32_t* layout) {
+    Scene& s = *(Scene*)sp;
+    bvh_build_instanced(s);
+    if (layout) layout_of(s, layout);
+    return s.bvh_ok ? 0 : -8;
+}
+void orc_bvh_download_instanced(void* sp, uint32_t* layout, uint32_t* bvh8, float* tris, float* inst,
+                                float* boxes) {
+    const Scene& s = *(const Scene*)sp;
+    const Bvh2L& T = s.two;
+    if (layout) layout_of(s, layout);
+    if (bvh8) std::memcpy(bvh8, T.nodes.data(), T.nodes.size() * 80);
+    if (tris) std::memcpy(tris, T.tris.data(), T.tris.size() * 4);
+    if (inst) std::memcpy(inst, T.inst.data(), T.inst.size() * 4);
+    if (boxes) std::memcpy(boxes, T.inst_box.data(), T.inst_box.size() * 4);
+}
 // new transforms, same topology (hy_bvh_refit's counterpart)
 int orc_bvh_refit(void* sp, const float* xf, uint32_t nx) {
     Scene& s = *(Scene*)sp;

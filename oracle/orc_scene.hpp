@@ -35,6 +35,28 @@ struct Bvh {
     std::vector<uint32_t> node_plan;       // its 8 slot children, 0xffffffff = empty (refits)
 };
 
+// Two-level structure (the driver's BLAS-per-primitive + TLAS split,
+// src/vk_mesh.cpp:424-492, src/renderer.cpp:1696-1865): one BLAS per distinct
+// mesh (primitives with equal first_index, index_count and vertex_offset share
+// it) over its object-space triangles, and a TLAS over the instance boxes.
+// Node array: the TLAS region (tlas_region nodes, root 0, unused tail zero),
+// then each BLAS.  Record array: tlas_region instance entries (box lo, hi, hi
+// and the instance index), then each BLAS's triangles (object-space vertices
+// and the triangle's index within its mesh).
+struct Bvh2L {
+    std::vector<Bvh8Node> nodes;
+    std::vector<float> tris;            // 12 floats per record
+    std::vector<float> inst;            // 16 per instance: world->object rows 3 x (m0 m1 m2 t), root, tri0, prim, 0
+    std::vector<float> inst_box;        // 6 per instance: TLAS item box (lo, hi)
+    std::vector<uint32_t> inst_prim;    // primitive of each instance (primitives with triangles, in order)
+    std::vector<uint32_t> prim_mesh;    // BLAS of each primitive, 0xffffffff when it has no triangles
+    std::vector<uint32_t> mesh_prim;    // first primitive of each BLAS (its index range)
+    std::vector<uint32_t> blas_node0, blas_rec0, blas_nodes;
+    std::vector<float> mesh_box;        // 6 per BLAS: root box in object space
+    std::vector<float> xinv;            // 12 per transform: world->object rows
+    uint32_t ninst = 0, nblas = 0, tlas_region = 0, tlas_nodes = 0, tlas_depth = 0, blas_depth = 0;
+};
+
 struct Counters { uint64_t nodes = 0, tris = 0; uint32_t status = 0; };
 
 struct Hit { float t; uint32_t id; float b1, b2; };
@@ -56,13 +78,16 @@ struct Scene {
     std::vector<uint32_t> prim_tri0; // first global triangle of each primitive
     Bvh bvh;
     bool bvh_ok = false;
+    Bvh2L two;                    // valid when two_level
+    bool two_level = false;
 };
 
 // geometry / BVH
 void scene_derive(Scene& s);
 void derive_world(Scene& s);   // normal matrices and world triangles from the current transforms
 void bvh_build(Scene& s);
-void bvh_refit(Scene& s);
+void bvh_build_instanced(Scene& s);   // two-level structure
+void bvh_refit(Scene& s);             // two-level: instance records and TLAS rebuilt, BLASes kept
 // traversal: mode 0 = brute force over all triangles, 1 = BVH8 (op-for-op the
 // product's traversal, so node/triangle counts are comparable)
 Hit trace(const Scene& s, const float o[3], const float d[3], float tmin, float tmax, bool any_hit,

@@ -49,6 +49,8 @@ def load():
         "orc_bvh_build": (C.c_int, [P, P, P]),
         "orc_bvh_download": (None, [P, P, P, P, P, P]),
         "orc_bvh_refit": (C.c_int, [P, P, U32]),
+        "orc_bvh_build_instanced": (C.c_int, [P, P]),
+        "orc_bvh_download_instanced": (None, [P, P, P, P, P, P]),
         "orc_trace": (None, [P, P, U32, C.c_int, C.c_int, P, P]),
         "orc_tea": (U32, [U32, U32]),
         "orc_rnd_seq": (None, [U32, U32, P, P]),
@@ -208,6 +210,29 @@ class OracleScene:
             raise RuntimeError("oracle bvh build failed")
         return {"num_tris": int(info[0]), "num_bvh2_nodes": int(info[1]), "num_bvh8_nodes": int(info[2]),
                 "depth": int(info[3]), "scene_lo": b[:3].tolist(), "scene_hi": b[3:].tolist()}
+
+    LAYOUT_FIELDS = ("two_level", "num_nodes", "num_records", "num_instances", "num_blas", "tlas_region",
+                     "tlas_nodes", "depth")
+
+    def build_bvh_instanced(self):
+        """Two-level structure: one BLAS per distinct mesh, a TLAS over the instances."""
+        lay = np.zeros(8, np.uint32)
+        if self.lib.orc_bvh_build_instanced(self.h, _p(lay)) != 0:
+            raise RuntimeError("oracle two-level build failed")
+        return dict(zip(self.LAYOUT_FIELDS, (int(v) for v in lay)))
+
+    def download_bvh_instanced(self):
+        """(layout, nodes [num_nodes, 20] u32, records [num_records, 12] f32,
+        instances [num_instances, 16] f32, instance boxes [num_instances, 6] f32)"""
+        lay = np.zeros(8, np.uint32)
+        self.lib.orc_bvh_download_instanced(self.h, _p(lay), None, None, None, None)
+        L = dict(zip(self.LAYOUT_FIELDS, (int(v) for v in lay)))
+        nodes = np.zeros((L["num_nodes"], 20), np.uint32)
+        recs = np.zeros((L["num_records"], 12), np.float32)
+        inst = np.zeros((L["num_instances"], 16), np.float32)
+        boxes = np.zeros((L["num_instances"], 6), np.float32)
+        self.lib.orc_bvh_download_instanced(self.h, None, _p(nodes), _p(recs), _p(inst), _p(boxes))
+        return L, nodes, recs, inst, boxes
 
     def refit_bvh(self, xf: np.ndarray):
         xf = np.ascontiguousarray(xf, np.float32)

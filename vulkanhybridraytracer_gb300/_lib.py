@@ -114,6 +114,12 @@ class HyBvhStats(C.Structure):
                 ("scene_hi", C.c_float * 3)]
 
 
+class HyBvhLayout(C.Structure):
+    _fields_ = [("two_level", C.c_uint32), ("num_nodes", C.c_uint32), ("num_records", C.c_uint32),
+                ("num_instances", C.c_uint32), ("num_blas", C.c_uint32), ("tlas_region", C.c_uint32),
+                ("tlas_nodes", C.c_uint32), ("depth", C.c_uint32)]
+
+
 assert C.sizeof(HyLight) == 48 and C.sizeof(HyMaterial) == 48 and C.sizeof(HyVertex) == 44
 assert C.sizeof(HyCamera) == 144
 
@@ -138,6 +144,9 @@ PROTOTYPES = {
     "hy_bvh_build": (I32, [P, C.POINTER(HyBvhStats)]),
     "hy_bvh_refit": (I32, [P, P, U32]),
     "hy_bvh_download": (I32, [P, P, P, P, P, P]),
+    "hy_bvh_build_instanced": (I32, [P, C.POINTER(HyBvhStats)]),
+    "hy_bvh_layout": (I32, [P, C.POINTER(HyBvhLayout)]),
+    "hy_bvh_download_instances": (I32, [P, P, P]),
     "hy_trace_rays": (I32, [P, P, U32, I32, P, C.POINTER(HyStats)]),
     "hy_gbuffer_primary": (I32, [P, C.POINTER(HyCamera), U32, U32, C.POINTER(C.c_void_p)]),
     "hy_shadow_pass": (I32, [P, C.POINTER(HyGBuffer), C.POINTER(HyCamera), C.POINTER(HyPassConfig), U32, P,

@@ -99,6 +99,19 @@ void inverse4(const double* a, double* inv) {
     for (int i = 0; i < 16; i++) inv[i] *= r;
 }
 
+// rows of inverse(M) (world -> object) of each transform, 3 x (m0 m1 m2 t)
+std::vector<float> world_to_object(const float* xf, uint32_t n) {
+    std::vector<float> out((size_t)n * 12);
+    for (uint32_t t = 0; t < n; t++) {
+        double m[16], inv[16];
+        for (int i = 0; i < 16; i++) m[i] = xf[(size_t)t * 16 + i];
+        inverse4(m, inv);
+        for (int r = 0; r < 3; r++)
+            for (int k = 0; k < 4; k++) out[(size_t)t * 12 + r * 4 + k] = (float)inv[k * 4 + r];
+    }
+    return out;
+}
+
 // mat3(transpose(inverse(M))) of each transform, column-major 3x3
 std::vector<float> normal_matrices(const float* xf, uint32_t n) {
     std::vector<float> out((size_t)n * 9);
@@ -132,7 +145,10 @@ SceneDev scene_dev(HyCtx* c) {
     S.tex_tab = c->tex_tab.as<uint4>();
     S.num_tex = c->ntex;
     S.num_nodes = c->bvh_ok ? c->n_bvh8 : 0;
-    S.num_tris = c->bvh_ok ? c->ntri : 0;
+    S.num_tris = c->bvh_ok ? c->n_records : 0;
+    S.inst = c->inst.as<float4>();
+    S.num_inst = c->bvh_ok && c->two_level ? c->ninst : 0;
+    S.two_level = c->bvh_ok && c->two_level ? 1u : 0u;
     for (int i = 0; i < 2; i++) { S.env_w[i] = c->env_w[i]; S.env_h[i] = c->env_h[i]; }
     return S;
 }
@@ -219,7 +235,7 @@ int check_scene_ready(HyCtx* c) {
 
 int grid_for(HyCtx* c, int mode, bool count, int minb, int block) {
     int per = 0;
-    if (pixel_occupancy(mode, count, minb, block, &per) != cudaSuccess || per <= 0) per = 1;
+    if (pixel_occupancy(mode, count, minb, c->two_level, block, &per) != cudaSuccess || per <= 0) per = 1;
     return per * c->num_sms;
 }
 
@@ -303,6 +319,7 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
     bool count = (cfg->flags & HY_FLAG_COUNT_TRAVERSAL) != 0;
     int block = cfg->block_size ? (int)cfg->block_size : 128;
     if (block % 32 || block > 128) return HY_ERR_INVALID_ARG;  // kernels are built for <= 128 threads
+    if (c->two_level && (cfg->flags & HY_FLAG_RAY_POOL)) return HY_ERR_UNSUPPORTED;
     PassParams P = P0;
     P.queue = dev_queue(c, queue_slot);
     // DECORRELATED samples of one pixel-light start together on adjacent lanes:
@@ -464,15 +481,19 @@ int hy_scene_set_geometry(HyCtx* c, const HyVertex* verts, uint32_t nv, const ui
         vattr[(size_t)v * 8 + 7] = verts[v].color[2];
     }
     std::vector<float> nrm = normal_matrices(xf, nx);
+    std::vector<float> xinv = world_to_object(xf, nx);
     int rc;
     c->geometry_ok = false;
     c->bvh_ok = false;
-    if ((rc = upload(c, c->verts, verts, nv)) || (rc = upload(c, c->vattr, vattr.data(), vattr.size())) ||
+    c->two_level = false;
+    if ((rc = upload(c, c->xinv, xinv.data(), xinv.size())) ||
+        (rc = upload(c, c->verts, verts, nv)) || (rc = upload(c, c->vattr, vattr.data(), vattr.size())) ||
         (rc = upload(c, c->idx, indices, ni)) || (rc = upload(c, c->prims, prims, np)) ||
         (rc = upload(c, c->xf, xf, (size_t)nx * 16)) || (rc = upload(c, c->nrm, nrm.data(), nrm.size())) ||
         (rc = upload(c, c->prim_tri0, prim_tri0.data(), np)) ||
         (rc = upload(c, c->tri_prim, tri_prim.data(), tri_prim.size())))
         return rc;
+    c->h_prims.assign(prims, prims + np);
     c->nverts = nv;
     c->nidx = ni;
     c->nprims = np;
@@ -546,14 +567,53 @@ int hy_bvh_build(HyCtx* c, HyBvhStats* st) {
     return bvh_build_impl(c, st);
 }
 
+int hy_bvh_build_instanced(HyCtx* c, HyBvhStats* st) {
+    if (!c) return HY_ERR_INVALID_ARG;
+    if (!c->geometry_ok) return HY_ERR_NOT_READY;
+    DeviceGuard g(c->device);
+    c->bvh_ok = false;
+    return bvh_build_instanced_impl(c, st);
+}
+
+int hy_bvh_layout(HyCtx* c, HyBvhLayout* out) {
+    if (!c || !out) return HY_ERR_INVALID_ARG;
+    if (!c->bvh_ok) return HY_ERR_NOT_READY;
+    HyBvhLayout L{};
+    L.two_level = c->two_level ? 1u : 0u;
+    L.num_nodes = c->n_bvh8;
+    L.num_records = c->n_records;
+    L.num_instances = c->two_level ? c->ninst : 0;
+    L.num_blas = c->two_level ? c->nblas : 0;
+    L.tlas_region = c->two_level ? c->tlas_region : 0;
+    L.tlas_nodes = c->two_level ? c->tlas_nodes : 0;
+    L.depth = c->depth;
+    *out = L;
+    return HY_OK;
+}
+
+int hy_bvh_download_instances(HyCtx* c, float* records, float* boxes) {
+    if (!c) return HY_ERR_INVALID_ARG;
+    if (!c->bvh_ok || !c->two_level) return HY_ERR_NOT_READY;
+    DeviceGuard g(c->device);
+    HY_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (records) HY_CUDA_TRY(cudaMemcpy(records, c->inst.p, (size_t)c->ninst * 64, cudaMemcpyDeviceToHost));
+    if (boxes) HY_CUDA_TRY(cudaMemcpy(boxes, c->inst_box.p, (size_t)c->ninst * 24, cudaMemcpyDeviceToHost));
+    return HY_OK;
+}
+
 int hy_bvh_refit(HyCtx* c, const float* xf, uint32_t nx) {
     if (!c || !xf || nx != c->nxf) return HY_ERR_INVALID_ARG;
     if (!c->bvh_ok) return HY_ERR_NOT_READY;
     if (!finite_all(xf, (size_t)nx * 16)) return HY_ERR_NAN_INPUT;
     DeviceGuard g(c->device);
     std::vector<float> nrm = normal_matrices(xf, nx);
+    std::vector<float> xinv = world_to_object(xf, nx);
     int rc;
-    if ((rc = upload(c, c->xf, xf, (size_t)nx * 16)) || (rc = upload(c, c->nrm, nrm.data(), nrm.size()))) return rc;
+    if ((rc = upload(c, c->xf, xf, (size_t)nx * 16)) || (rc = upload(c, c->nrm, nrm.data(), nrm.size())) ||
+        (rc = upload(c, c->xinv, xinv.data(), xinv.size())))
+        return rc;
+    // two-level: the BLASes stay, the instance records and the TLAS follow the transforms
+    if (c->two_level) return tlas_build_impl(c);
     return bvh_refit_impl(c);
 }
 
@@ -562,7 +622,13 @@ int hy_bvh_download(HyCtx* c, uint32_t* morton, uint32_t* order, uint32_t* bvh2,
     if (!c->bvh_ok) return HY_ERR_NOT_READY;
     DeviceGuard g(c->device);
     const size_t n = c->ntri;
+    if (c->two_level && (morton || order || bvh2)) return HY_ERR_INVALID_ARG;  // nodes and records only
     HY_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (c->two_level) {
+        if (bvh8) HY_CUDA_TRY(cudaMemcpy(bvh8, c->nodes.p, (size_t)c->n_bvh8 * 80, cudaMemcpyDeviceToHost));
+        if (tris) HY_CUDA_TRY(cudaMemcpy(tris, c->tris.p, (size_t)c->n_records * 48, cudaMemcpyDeviceToHost));
+        return HY_OK;
+    }
     if (morton) HY_CUDA_TRY(cudaMemcpy(morton, c->keys[0].p, n * 4, cudaMemcpyDeviceToHost));
     if (order) HY_CUDA_TRY(cudaMemcpy(order, c->vals[0].p, n * 4, cudaMemcpyDeviceToHost));
     if (bvh2 && n > 1) HY_CUDA_TRY(cudaMemcpy(bvh2, c->bvh2.p, (n - 1) * 40, cudaMemcpyDeviceToHost));
@@ -884,6 +950,7 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
         if (!scenes[i]) return HY_ERR_INVALID_ARG;
         if (scenes[i]->device != c->device) return HY_ERR_INVALID_ARG;
         if ((rc = check_scene_ready(scenes[i]))) return rc;
+        if (scenes[i]->two_level) return HY_ERR_UNSUPPORTED;  // the batch kernels walk one-level structures
     }
     DeviceGuard g(c->device);
     const bool count = tuning && (tuning->flags & HY_FLAG_COUNT_TRAVERSAL);

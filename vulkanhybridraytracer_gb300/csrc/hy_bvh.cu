@@ -469,7 +469,8 @@ __device__ __forceinline__ void quantize_node(const Ref& nb, const uint32_t* slo
     }
 }
 
-__global__ void k_collapse_emit(uint32_t m, uint32_t level_start, uint32_t tri_start,
+__global__ void k_collapse_emit(uint32_t m, uint32_t level_start, uint32_t tri_start, uint32_t node_off,
+                                uint32_t rec_off,
                                 const uint32_t* __restrict__ lvl, const uint32_t* __restrict__ plan,
                                 const uint32_t* __restrict__ ni_scan, const uint32_t* __restrict__ nt_scan,
                                 const uint32_t* __restrict__ bvh2, const uint32_t* __restrict__ order,
@@ -479,8 +480,8 @@ __global__ void k_collapse_emit(uint32_t m, uint32_t level_start, uint32_t tri_s
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m) return;
     Ref nb = load_ref(lvl[k], bvh2, order, tribox);
-    uint32_t child_base = level_start + m + ni_scan[k];
-    uint32_t tri_base = tri_start + nt_scan[k];
+    uint32_t child_base = node_off + level_start + m + ni_scan[k];
+    uint32_t tri_base = rec_off + tri_start + nt_scan[k];
     const uint32_t* slots = plan + (size_t)k * 8;
     // kept for refits: the node's BVH2 subtree and its children in slot order
     node_ref[level_start + k] = lvl[k];
@@ -520,7 +521,7 @@ __global__ void k_collapse_emit(uint32_t m, uint32_t level_start, uint32_t tri_s
     nd.q[2] = make_uint4(qlo[0][0], qlo[0][1], qlo[1][0], qlo[1][1]);
     nd.q[3] = make_uint4(qlo[2][0], qlo[2][1], qhi[0][0], qhi[0][1]);
     nd.q[4] = make_uint4(qhi[1][0], qhi[1][1], qhi[2][0], qhi[2][1]);
-    nodes[level_start + k] = nd;
+    nodes[node_off + level_start + k] = nd;
 }
 
 // Refit: the same topology, slot order and child/triangle bases; only the
@@ -574,15 +575,16 @@ int world_tris_impl(HyCtx* c) {
     return HY_OK;
 }
 
-int bvh_build_impl(HyCtx* c, HyBvhStats* st) {
-    const uint32_t n = c->ntri;
+// LBVH -> BVH8 over the n items in c->world / c->tribox / c->centroid (three
+// points per item: a triangle, or an instance box as (lo, hi, hi)).  Nodes go
+// to nodes[node_off ...], leaf records to records rec_off ...; the emitted
+// child and record indices include the offsets.  Records carry the item's
+// index.  Leaves the sorted keys / ids in keys[0] / vals[0] and the binary tree
+// in bvh2 (the refit of a one-level structure reuses them).
+static int build_core(HyCtx* c, uint32_t n, uint32_t node_off, uint32_t rec_off, uint32_t* n_nodes,
+                      uint32_t* depth_out) {
     if (n == 0) return HY_ERR_NOT_READY;
     int rc;
-    cudaEvent_t e0, e1;
-    HY_CUDA_TRY(cudaEventCreate(&e0));
-    HY_CUDA_TRY(cudaEventCreate(&e1));
-    HY_CUDA_TRY(cudaEventRecord(e0, c->stream));
-    if ((rc = world_tris_impl(c))) return rc;
     const uint32_t nb_rs = cdiv(n, RS_TILE);
     if ((rc = ctx_alloc(c, c->keys[0], (size_t)n * 4)) || (rc = ctx_alloc(c, c->keys[1], (size_t)n * 4)) ||
         (rc = ctx_alloc(c, c->vals[0], (size_t)n * 4)) || (rc = ctx_alloc(c, c->vals[1], (size_t)n * 4)) ||
@@ -591,8 +593,6 @@ int bvh_build_impl(HyCtx* c, HyBvhStats* st) {
         (rc = ctx_alloc(c, c->bvh2, (size_t)std::max<uint32_t>(n - 1, 1) * 40)) ||
         (rc = ctx_alloc(c, c->parent, (size_t)(2 * n) * 4)) ||
         (rc = ctx_alloc(c, c->flags, (size_t)std::max<uint32_t>(n, 1) * 4)) ||
-        (rc = ctx_alloc(c, c->nodes, (size_t)std::max<uint32_t>(n, 1) * sizeof(Node8))) ||
-        (rc = ctx_alloc(c, c->tris, (size_t)n * 48)) ||
         (rc = ctx_alloc(c, c->lvl_ref[0], (size_t)n * 4)) || (rc = ctx_alloc(c, c->lvl_ref[1], (size_t)n * 4)) ||
         (rc = ctx_alloc(c, c->plan, (size_t)n * 32)) || (rc = ctx_alloc(c, c->ni, (size_t)n * 4)) ||
         (rc = ctx_alloc(c, c->nt, (size_t)n * 4)) || (rc = ctx_alloc(c, c->ni_scan, (size_t)n * 4)) ||
@@ -642,7 +642,8 @@ int bvh_build_impl(HyCtx* c, HyBvhStats* st) {
                                                      c->ni.as<uint32_t>(), c->nt.as<uint32_t>());
         if ((rc = scan_exclusive(c, c->ni.as<uint32_t>(), c->ni_scan.as<uint32_t>(), m, tot))) return rc;
         if ((rc = scan_exclusive(c, c->nt.as<uint32_t>(), c->nt_scan.as<uint32_t>(), m, tot + 1))) return rc;
-        k_collapse_emit<<<cdiv(m, 128), 128, 0, s>>>(m, level_start, tri_start, lvl, c->plan.as<uint32_t>(),
+        k_collapse_emit<<<cdiv(m, 128), 128, 0, s>>>(m, level_start, tri_start, node_off, rec_off, lvl,
+                                                     c->plan.as<uint32_t>(),
                                                      c->ni_scan.as<uint32_t>(), c->nt_scan.as<uint32_t>(), bvh2, ord,
                                                      c->tribox.as<float>(), c->world.as<float4>(),
                                                      c->nodes.as<Node8>(), c->tris.as<float4>(),
@@ -659,22 +660,44 @@ int bvh_build_impl(HyCtx* c, HyBvhStats* st) {
         depth++;
         if (depth > 256) return HY_ERR_TIMEOUT;
     }
-    HY_CUDA_TRY(cudaEventRecord(e1, s));
+    if (tri_start != n) return HY_ERR_CUDA;
+    *n_nodes = level_start;
+    *depth_out = depth;
+    return HY_OK;
+}
+
+int bvh_build_impl(HyCtx* c, HyBvhStats* st) {
+    const uint32_t n = c->ntri;
+    if (n == 0) return HY_ERR_NOT_READY;
+    int rc;
+    c->bvh_ok = false;
+    c->two_level = false;
+    cudaEvent_t e0, e1;
+    HY_CUDA_TRY(cudaEventCreate(&e0));
+    HY_CUDA_TRY(cudaEventCreate(&e1));
+    HY_CUDA_TRY(cudaEventRecord(e0, c->stream));
+    if ((rc = world_tris_impl(c))) return rc;
+    if ((rc = ctx_alloc(c, c->nodes, (size_t)std::max<uint32_t>(n, 1) * sizeof(Node8))) ||
+        (rc = ctx_alloc(c, c->tris, (size_t)n * 48)))
+        return rc;
+    uint32_t n_nodes = 0, depth = 0;
+    if ((rc = build_core(c, n, 0, 0, &n_nodes, &depth))) return rc;
+    HY_CUDA_TRY(cudaEventRecord(e1, c->stream));
     HY_CUDA_TRY(cudaEventSynchronize(e1));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (tri_start != n) return HY_ERR_CUDA;
-    c->n_bvh8 = level_start;
+    c->n_bvh8 = n_nodes;
+    c->n_records = n;
     c->depth = depth;
     c->bvh_ok = true;
     int hb[6];
-    HY_CUDA_TRY(cudaMemcpy(hb, bnd, 24, cudaMemcpyDeviceToHost));
+    HY_CUDA_TRY(cudaMemcpy(hb, c->bounds.p, 24, cudaMemcpyDeviceToHost));
     HyBvhStats out{};
     out.num_tris = n;
     out.num_bvh2_nodes = n > 1 ? n - 1 : 0;
-    out.num_bvh8_nodes = level_start;
+    out.num_bvh8_nodes = n_nodes;
     out.depth = depth;
     out.build_ms = ms;
     for (int a = 0; a < 3; a++) {
@@ -710,6 +733,240 @@ int bvh_refit_impl(HyCtx* c) {
     k_repack_tris<<<cdiv(n, 256), 256, 0, s>>>(n, c->world.as<float4>(), c->tris.as<float4>());
     HY_CUDA_TRY(cudaGetLastError());
     HY_CUDA_TRY(cudaStreamSynchronize(s));
+    return HY_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Two-level structure: one BLAS per distinct mesh over its object-space
+// triangles, a TLAS over the instance boxes (the driver's BLAS-per-primitive
+// and TLAS builds of src/vk_mesh.cpp:424-492 and src/renderer.cpp:1696-1865).
+// ---------------------------------------------------------------------------------
+
+// object-space triangles of one mesh; x + 0 folds -0 into +0 so box bits do
+// not depend on the sign of zero
+__global__ void k_mesh_tris(const HyVertex* __restrict__ verts, const uint32_t* __restrict__ idx,
+                            uint32_t first_index, uint32_t vertex_offset, uint32_t n, float4* __restrict__ world,
+                            float* __restrict__ tribox, float4* __restrict__ cen) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int v = 0; v < 3; v++) {
+        const float* P = verts[idx[first_index + 3 * t + v] + vertex_offset].pos;
+        float w[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            w[a] = __fadd_rn(P[a], 0.0f);
+            lo[a] = fminf(lo[a], w[a]);
+            hi[a] = fmaxf(hi[a], w[a]);
+        }
+        world[(size_t)t * 3 + v] = make_float4(w[0], w[1], w[2], 0.f);
+    }
+    float* b = tribox + (size_t)t * 6;
+    for (int a = 0; a < 3; a++) { b[a] = lo[a]; b[3 + a] = hi[a]; }
+    cen[t] = make_float4(__fmul_rn(__fadd_rn(lo[0], hi[0]), 0.5f), __fmul_rn(__fadd_rn(lo[1], hi[1]), 0.5f),
+                         __fmul_rn(__fadd_rn(lo[2], hi[2]), 0.5f), 0.f);
+}
+
+// root box of a BLAS just built: the binary tree's root, or its only triangle
+__global__ void k_mesh_box(uint32_t n, const uint32_t* __restrict__ bvh2, const float* __restrict__ tribox,
+                           float* __restrict__ out) {
+    if (threadIdx.x != 0) return;
+    for (int a = 0; a < 6; a++) out[a] = n > 1 ? __uint_as_float(bvh2[4 + a]) : tribox[a];
+}
+
+// Instance records and TLAS items.  Record: the world->object rows of the
+// instance's transform, then (BLAS root node, first global triangle,
+// primitive, 0).  Box: the 8 corners of the mesh box through the
+// object->world matrix in double, ((m0 x + m1 y) + m2 z) + m3, padded by
+// 2^-16 of the extent plus 2^-20 of the largest magnitude per axis (room for
+// the rounding of the world->object ray transform) and rounded outwards.
+__global__ void k_inst_setup(uint32_t ninst, const uint32_t* __restrict__ inst_prim,
+                             const HyPrimitive* __restrict__ prims, const uint32_t* __restrict__ prim_mesh,
+                             const uint32_t* __restrict__ blas_node0, const uint32_t* __restrict__ prim_tri0,
+                             const float* __restrict__ xinv, const float* __restrict__ xf,
+                             const float* __restrict__ mesh_box, float4* __restrict__ inst,
+                             float* __restrict__ inst_box, float4* __restrict__ world, float* __restrict__ tribox,
+                             float4* __restrict__ cen) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    const uint32_t p = inst_prim[i], m = prim_mesh[p], tf = prims[p].transform_id;
+    const float* R = xinv + (size_t)tf * 12;
+    for (int k = 0; k < 3; k++) inst[(size_t)i * 4 + k] = make_float4(R[4 * k], R[4 * k + 1], R[4 * k + 2], R[4 * k + 3]);
+    inst[(size_t)i * 4 + 3] = make_float4(__uint_as_float(blas_node0[m]), __uint_as_float(prim_tri0[p]),
+                                          __uint_as_float(p), 0.f);
+    const float* M = xf + (size_t)tf * 16;
+    const float* mb = mesh_box + (size_t)m * 6;
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int corner = 0; corner < 8; corner++) {
+        double q[3];
+        for (int a = 0; a < 3; a++) q[a] = (double)((corner >> a) & 1 ? mb[3 + a] : mb[a]);
+        for (int r = 0; r < 3; r++) {
+            double w = __dmul_rn((double)M[0 * 4 + r], q[0]);
+            w = __dadd_rn(w, __dmul_rn((double)M[1 * 4 + r], q[1]));
+            w = __dadd_rn(w, __dmul_rn((double)M[2 * 4 + r], q[2]));
+            w = __dadd_rn(w, (double)M[3 * 4 + r]);
+            lo[r] = fmin(lo[r], w);
+            hi[r] = fmax(hi[r], w);
+        }
+    }
+    float bl[3], bh[3];
+    for (int a = 0; a < 3; a++) {
+        const double mag = fmax(fabs(lo[a]), fabs(hi[a]));
+        const double pad = __dadd_rn(__dmul_rn(__dsub_rn(hi[a], lo[a]), 0x1p-16), __dmul_rn(mag, 0x1p-20));
+        bl[a] = __double2float_rd(__dsub_rn(lo[a], pad));
+        bh[a] = __double2float_ru(__dadd_rn(hi[a], pad));
+        inst_box[(size_t)i * 6 + a] = bl[a];
+        inst_box[(size_t)i * 6 + 3 + a] = bh[a];
+        tribox[(size_t)i * 6 + a] = bl[a];
+        tribox[(size_t)i * 6 + 3 + a] = bh[a];
+    }
+    world[(size_t)i * 3 + 0] = make_float4(bl[0], bl[1], bl[2], 0.f);
+    world[(size_t)i * 3 + 1] = make_float4(bh[0], bh[1], bh[2], 0.f);
+    world[(size_t)i * 3 + 2] = make_float4(bh[0], bh[1], bh[2], 0.f);
+    cen[i] = make_float4(__fmul_rn(__fadd_rn(bl[0], bh[0]), 0.5f), __fmul_rn(__fadd_rn(bl[1], bh[1]), 0.5f),
+                         __fmul_rn(__fadd_rn(bl[2], bh[2]), 0.5f), 0.f);
+}
+
+int tlas_build_impl(HyCtx* c) {
+    const uint32_t ni = c->ninst;
+    int rc;
+    cudaStream_t s = c->stream;
+    if ((rc = ctx_alloc(c, c->inst, (size_t)ni * 64)) || (rc = ctx_alloc(c, c->inst_box, (size_t)ni * 24)) ||
+        (rc = ctx_alloc(c, c->world, (size_t)ni * 48)) || (rc = ctx_alloc(c, c->tribox, (size_t)ni * 24)) ||
+        (rc = ctx_alloc(c, c->centroid, (size_t)ni * 16)))
+        return rc;
+    k_inst_setup<<<cdiv(ni, 128), 128, 0, s>>>(
+        ni, c->inst_prim.as<uint32_t>(), c->prims.as<HyPrimitive>(), c->prim_mesh.as<uint32_t>(),
+        c->blas_node0.as<uint32_t>(), c->prim_tri0.as<uint32_t>(), c->xinv.as<float>(), c->xf.as<float>(),
+        c->mesh_box.as<float>(), c->inst.as<float4>(), c->inst_box.as<float>(), c->world.as<float4>(),
+        c->tribox.as<float>(), c->centroid.as<float4>());
+    HY_CUDA_TRY(cudaGetLastError());
+    HY_CUDA_TRY(cudaMemsetAsync(c->nodes.p, 0, (size_t)c->tlas_region * sizeof(Node8), s));
+    HY_CUDA_TRY(cudaMemsetAsync(c->tris.p, 0, (size_t)c->tlas_region * 48, s));
+    uint32_t nn = 0, depth = 0;
+    if ((rc = build_core(c, ni, 0, 0, &nn, &depth))) return rc;
+    HY_CUDA_TRY(cudaStreamSynchronize(s));
+    c->tlas_nodes = nn;
+    c->tlas_depth = depth;
+    c->depth = c->tlas_depth + c->blas_depth;
+    return HY_OK;
+}
+
+int bvh_build_instanced_impl(HyCtx* c, HyBvhStats* st) {
+    c->bvh_ok = false;
+    c->two_level = false;
+    const uint32_t np = c->nprims;
+    if (c->h_prims.size() != np) return HY_ERR_NOT_READY;
+    // distinct meshes in order of first use; one instance per primitive with triangles
+    c->h_prim_mesh.assign(np, 0xffffffffu);
+    c->h_mesh_prim.clear();
+    c->h_inst_prim.clear();
+    {
+        // (first_index, index_count, vertex_offset) -> mesh, through 1024 hash buckets
+        std::vector<std::vector<uint32_t>> bucket(1024);
+        for (uint32_t p = 0; p < np; p++) {
+            const HyPrimitive& pr = c->h_prims[p];
+            if (pr.index_count / 3 == 0) continue;
+            const uint64_t h = ((uint64_t)pr.first_index * 0x9E3779B97F4A7C15ull) ^
+                               ((uint64_t)pr.index_count * 0xC2B2AE3D27D4EB4Full) ^ (uint64_t)pr.vertex_offset;
+            std::vector<uint32_t>& b = bucket[(h >> 20) & 1023u];
+            uint32_t m = 0xffffffffu;
+            for (uint32_t cand : b) {
+                const HyPrimitive& q = c->h_prims[c->h_mesh_prim[cand]];
+                if (q.first_index == pr.first_index && q.index_count == pr.index_count &&
+                    q.vertex_offset == pr.vertex_offset) { m = cand; break; }
+            }
+            if (m == 0xffffffffu) {
+                m = (uint32_t)c->h_mesh_prim.size();
+                c->h_mesh_prim.push_back(p);
+                b.push_back(m);
+            }
+            c->h_prim_mesh[p] = m;
+            c->h_inst_prim.push_back(p);
+        }
+    }
+    c->ninst = (uint32_t)c->h_inst_prim.size();
+    c->nblas = (uint32_t)c->h_mesh_prim.size();
+    if (c->ninst == 0) return HY_ERR_NOT_READY;
+    c->tlas_region = c->ninst;
+    uint64_t node_cap = c->tlas_region, rec_cap = c->tlas_region;
+    uint32_t max_nt = c->ninst;
+    for (uint32_t m = 0; m < c->nblas; m++) {
+        const uint32_t nt = c->h_prims[c->h_mesh_prim[m]].index_count / 3;
+        node_cap += std::max<uint32_t>(nt, 1);
+        rec_cap += nt;
+        max_nt = std::max(max_nt, nt);
+    }
+    if (node_cap >= (1ull << 31) || rec_cap >= (1ull << 31)) return HY_ERR_TOO_LARGE;
+    int rc;
+    cudaStream_t s = c->stream;
+    if ((rc = ctx_alloc(c, c->nodes, (size_t)node_cap * sizeof(Node8))) ||
+        (rc = ctx_alloc(c, c->tris, (size_t)rec_cap * 48)) ||
+        (rc = ctx_alloc(c, c->world, (size_t)max_nt * 48)) || (rc = ctx_alloc(c, c->tribox, (size_t)max_nt * 24)) ||
+        (rc = ctx_alloc(c, c->centroid, (size_t)max_nt * 16)) ||
+        (rc = ctx_alloc(c, c->mesh_box, (size_t)c->nblas * 24)) ||
+        (rc = ctx_alloc(c, c->prim_mesh, (size_t)np * 4)) || (rc = ctx_alloc(c, c->inst_prim, (size_t)c->ninst * 4)) ||
+        (rc = ctx_alloc(c, c->blas_node0, (size_t)c->nblas * 4)))
+        return rc;
+    cudaEvent_t e0, e1;
+    HY_CUDA_TRY(cudaEventCreate(&e0));
+    HY_CUDA_TRY(cudaEventCreate(&e1));
+    HY_CUDA_TRY(cudaEventRecord(e0, s));
+    HY_CUDA_TRY(cudaMemsetAsync(c->nodes.p, 0, (size_t)node_cap * sizeof(Node8), s));
+    HY_CUDA_TRY(cudaMemsetAsync(c->tris.p, 0, (size_t)rec_cap * 48, s));
+    HY_CUDA_TRY(cudaMemcpyAsync(c->prim_mesh.p, c->h_prim_mesh.data(), (size_t)np * 4, cudaMemcpyHostToDevice, s));
+    HY_CUDA_TRY(cudaMemcpyAsync(c->inst_prim.p, c->h_inst_prim.data(), (size_t)c->ninst * 4, cudaMemcpyHostToDevice,
+                                s));
+    uint32_t node_off = c->tlas_region, rec_off = c->tlas_region;
+    c->h_blas_node0.assign(c->nblas, 0);
+    c->blas_depth = 0;
+    for (uint32_t m = 0; m < c->nblas; m++) {
+        const HyPrimitive& pr = c->h_prims[c->h_mesh_prim[m]];
+        const uint32_t nt = pr.index_count / 3;
+        k_mesh_tris<<<cdiv(nt, 256), 256, 0, s>>>(c->verts.as<HyVertex>(), c->idx.as<uint32_t>(), pr.first_index,
+                                                  pr.vertex_offset, nt, c->world.as<float4>(), c->tribox.as<float>(),
+                                                  c->centroid.as<float4>());
+        HY_CUDA_TRY(cudaGetLastError());
+        uint32_t nn = 0, depth = 0;
+        if ((rc = build_core(c, nt, node_off, rec_off, &nn, &depth))) return rc;
+        k_mesh_box<<<1, 32, 0, s>>>(nt, c->bvh2.as<uint32_t>(), c->tribox.as<float>(),
+                                    c->mesh_box.as<float>() + (size_t)m * 6);
+        HY_CUDA_TRY(cudaGetLastError());
+        c->h_blas_node0[m] = node_off;
+        node_off += nn;
+        rec_off += nt;
+        c->blas_depth = std::max(c->blas_depth, depth);
+    }
+    HY_CUDA_TRY(cudaMemcpyAsync(c->blas_node0.p, c->h_blas_node0.data(), (size_t)c->nblas * 4,
+                                cudaMemcpyHostToDevice, s));
+    c->n_bvh8 = node_off;
+    c->n_records = rec_off;
+    if ((rc = tlas_build_impl(c))) return rc;
+    HY_CUDA_TRY(cudaEventRecord(e1, s));
+    HY_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->two_level = true;
+    c->bvh_ok = true;
+    HyBvhStats out{};
+    out.num_tris = c->ntri;
+    out.num_bvh2_nodes = 0;
+    out.num_bvh8_nodes = c->n_bvh8;
+    out.depth = c->depth;
+    out.build_ms = ms;
+    // scene bounds: the union of the instance boxes
+    std::vector<float> boxes((size_t)c->ninst * 6);
+    HY_CUDA_TRY(cudaMemcpy(boxes.data(), c->inst_box.p, boxes.size() * 4, cudaMemcpyDeviceToHost));
+    for (int a = 0; a < 3; a++) { out.scene_lo[a] = INFINITY; out.scene_hi[a] = -INFINITY; }
+    for (uint32_t i = 0; i < c->ninst; i++)
+        for (int a = 0; a < 3; a++) {
+            out.scene_lo[a] = std::min(out.scene_lo[a], boxes[(size_t)i * 6 + a]);
+            out.scene_hi[a] = std::max(out.scene_hi[a], boxes[(size_t)i * 6 + 3 + a]);
+        }
+    c->last_build = out;
+    if (st) *st = out;
     return HY_OK;
 }
 

@@ -202,6 +202,11 @@ struct SceneDev {
     const uchar4* tex_px;        // material textures, concatenated RGBA8 texels
     const uint4* tex_tab;        // per texture: first texel, width, height, 0
     uint32_t num_tex;
+    // two-level structure: nodes / tris start with the TLAS (instance entries
+    // as leaf records), each BLAS follows; 4 x float4 per instance
+    const float4* inst;
+    uint32_t num_inst;
+    uint32_t two_level;
 };
 
 struct Hit { float t; uint32_t id; float b1, b2; };
@@ -341,6 +346,12 @@ struct Trav {
     uint32_t iters;
     float tmax;
     Hit h;
+    // two-level walk only (dead, and dropped by the compiler, in one-level code)
+    RayPre cur;                  // the ray in the frame of the level being walked
+    uint32_t inst_base, inst_bits;  // hit instance entries of the last TLAS leaf set
+    uint32_t id_off;             // first global triangle of the instance being walked
+    int sp_base;                 // stack height when the instance was entered
+    bool level;                  // inside a BLAS
 };
 
 __device__ __forceinline__ void trav_init(Trav& t, const RayPre& r, float tmax) {
@@ -350,20 +361,93 @@ __device__ __forceinline__ void trav_init(Trav& t, const RayPre& r, float tmax) 
     t.iters = 0;
     t.tmax = tmax;
     t.h = Hit{tmax, HY_NO_HIT, 0.f, 0.f};
+    t.cur = r;
+    t.inst_base = 0;
+    t.inst_bits = 0;
+    t.id_off = 0;
+    t.sp_base = 0;
+    t.level = false;
+}
+
+// world -> object: ((r.x o.x + r.y o.y) + r.z o.z) + r.w per row; the
+// direction without r.w (not renormalised, so t is the same in both frames)
+__device__ __forceinline__ f3 xform_point(float4 r0, float4 r1, float4 r2, f3 o) {
+    const float4 R[3] = {r0, r1, r2};
+    float v[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        v[k] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(R[k].x, o.x), __fmul_rn(R[k].y, o.y)), __fmul_rn(R[k].z, o.z)),
+                         R[k].w);
+    return mk(v[0], v[1], v[2]);
+}
+__device__ __forceinline__ f3 xform_dir(float4 r0, float4 r1, float4 r2, const float* d) {
+    const float4 R[3] = {r0, r1, r2};
+    float v[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        v[k] = __fadd_rn(__fadd_rn(__fmul_rn(R[k].x, d[0]), __fmul_rn(R[k].y, d[1])), __fmul_rn(R[k].z, d[2]));
+    return mk(v[0], v[1], v[2]);
+}
+
+// Two-level walk: brings t to a non-empty node group.  A TLAS leaf hands its
+// hit instance entries over one at a time; entering one saves the pending
+// TLAS group on the stack, moves the ray into object space and walks the
+// BLAS above the saved stack height; once that part of the stack is empty
+// the world ray is restored.  Returns false when the walk is over.
+__device__ __forceinline__ bool two_level_settle(const SceneDev& S, const RayPre& rw, Trav& t, uint2* stk,
+                                                 uint32_t* status) {
+    for (;;) {
+        if (!t.level && t.inst_bits) {
+            if (t.g_bits & 0xff000000u) {
+                if (t.sp >= kStackMax) { atomicOr(status, HY_STATUS_STACK_OVERFLOW); return false; }
+                stk[t.sp] = make_uint2(t.g_base, t.g_bits);
+                t.sp++;
+            }
+            const uint32_t b = __ffs(t.inst_bits) - 1;
+            t.inst_bits &= t.inst_bits - 1u;
+            const uint32_t rec = t.inst_base + b;
+            if (rec >= S.num_tris) { atomicOr(status, HY_STATUS_BAD_INDEX); return false; }
+            const uint32_t iid = __float_as_uint(__ldg(&S.tris[(size_t)rec * 3].w));
+            if (iid >= S.num_inst) { atomicOr(status, HY_STATUS_BAD_INDEX); return false; }
+            const float4* I = S.inst + (size_t)iid * 4;
+            const float4 r0 = __ldg(I), r1 = __ldg(I + 1), r2 = __ldg(I + 2), m = __ldg(I + 3);
+            t.cur = ray_pre(xform_point(r0, r1, r2, rw.o), xform_dir(r0, r1, r2, rw.d));
+            t.level = true;
+            t.sp_base = t.sp;
+            t.id_off = __float_as_uint(m.y);
+            t.g_base = __float_as_uint(m.x);
+            t.g_bits = (1u << 24) | (1u << t.cur.near);  // virtual group holding the BLAS root
+            return true;
+        }
+        if (t.g_bits & 0xff000000u) return true;
+        if (t.level && t.sp == t.sp_base) {
+            t.level = false;
+            t.cur = rw;
+            continue;
+        }
+        if (t.sp == 0) return false;
+        --t.sp;
+        t.g_base = stk[t.sp].x;
+        t.g_bits = stk[t.sp].y;
+    }
 }
 
 // One node visit (its box tests and the triangles of its leaf slots).
 // Returns true when the ray is finished: t.h holds the hit, or id HY_NO_HIT.
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& r, float tmin, Trav& t, uint2* stk,
+// TWO: the two-level structure (r is the world ray; t.cur the current one).
+template <bool ANY, bool COUNT, bool TWO = false>
+__device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& rw, float tmin, Trav& t, uint2* stk,
                                           uint32_t& nodes_ctr, uint32_t& tris_ctr, uint32_t* status) {
     if (++t.iters > kMaxIters) { atomicOr(status, HY_STATUS_TIMEOUT); return true; }
-    if ((t.g_bits & 0xff000000u) == 0) {
+    if (TWO) {
+        if (!two_level_settle(S, rw, t, stk, status)) return true;
+    } else if ((t.g_bits & 0xff000000u) == 0) {
         if (t.sp == 0) return true;
         --t.sp;
         t.g_base = stk[t.sp].x;
         t.g_bits = stk[t.sp].y;
     }
+    const RayPre& r = TWO ? t.cur : rw;
     const uint32_t rb = __ffs(t.g_bits >> 24) - 1;
     t.g_bits &= ~(1u << (24 + rb));
     const uint32_t sl = rb ^ r.near;
@@ -441,13 +525,18 @@ __device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& r, fl
         hit_tri |= ((1u << (m >> 5)) - 1u) << (m & 31u);
     }
     const uint32_t tri_base = q1.y;
+    if (TWO && !t.level) {  // TLAS leaves: instance entries, walked by two_level_settle
+        t.inst_base = tri_base;
+        t.inst_bits = hit_tri;
+        hit_tri = 0;
+    }
     while (hit_tri) {
         const uint32_t b = __ffs(hit_tri) - 1;
         hit_tri &= hit_tri - 1u;
         if (tri_base + b >= S.num_tris) { atomicOr(status, HY_STATUS_BAD_INDEX); return true; }
         const float4* tp = S.tris + (size_t)(tri_base + b) * 3;
         const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
-        const uint32_t id = __float_as_uint(v0.w);
+        const uint32_t id = TWO ? t.id_off + __float_as_uint(v0.w) : __float_as_uint(v0.w);
         if (COUNT) tris_ctr++;
         float tt, b1, b2;
         if (tri_test(r, v0, v1, v2, tmin, t.tmax, tt, b1, b2)) {
@@ -463,14 +552,14 @@ __device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& r, fl
     return false;
 }
 
-template <bool ANY, bool COUNT>
+template <bool ANY, bool COUNT, bool TWO = false>
 __device__ __forceinline__ Hit traverse(const SceneDev& S, const RayPre& r, float tmin, float tmax,
                                         uint32_t* nodes_ctr, uint32_t* tris_ctr, uint32_t* status) {
     uint2 stk[kStackMax];
     Trav t;
     trav_init(t, r, tmax);
     uint32_t nn = 0, nt = 0;
-    while (!trav_step<ANY, COUNT>(S, r, tmin, t, stk, nn, nt, status)) {
+    while (!trav_step<ANY, COUNT, TWO>(S, r, tmin, t, stk, nn, nt, status)) {
     }
     if (COUNT) { *nodes_ctr += nn; *tris_ctr += nt; }
     return t.h;

@@ -61,6 +61,19 @@ struct HyCtx {
     hy::DevBuf node_ref, node_plan;  // per BVH8 node: its BVH2 subtree, its 8 slot children (refits)
     uint32_t n_bvh8 = 0, depth = 0;
     bool bvh_ok = false;
+
+    // ---- two-level structure (hy_bvh_build_instanced) ----
+    // nodes / tris then hold the TLAS region (tlas_region nodes and records)
+    // followed by one BLAS per distinct mesh
+    bool two_level = false;
+    hy::DevBuf xinv;                 // 12 floats per transform: world->object rows (always kept current)
+    hy::DevBuf inst;                 // 64 B per instance: 3 rows + (BLAS root, first triangle, primitive, 0)
+    hy::DevBuf inst_box;             // 6 floats per instance: its TLAS box
+    hy::DevBuf inst_prim, prim_mesh, blas_node0, mesh_box;
+    std::vector<HyPrimitive> h_prims;
+    std::vector<uint32_t> h_inst_prim, h_prim_mesh, h_mesh_prim, h_blas_node0;
+    uint32_t ninst = 0, nblas = 0, tlas_region = 0, tlas_nodes = 0, tlas_depth = 0, blas_depth = 0;
+    uint32_t n_records = 0;          // leaf records in tris
     HyBvhStats last_build{};
 
     // ---- pass scratch ----
@@ -91,6 +104,8 @@ struct HyCtx {
 namespace hy {
 int bvh_build_impl(HyCtx* c, HyBvhStats* st);
 int bvh_refit_impl(HyCtx* c);
+int bvh_build_instanced_impl(HyCtx* c, HyBvhStats* st);
+int tlas_build_impl(HyCtx* c);   // instance records + TLAS from the current transforms
 int world_tris_impl(HyCtx* c);
 int scan_exclusive(HyCtx* c, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* d_total);
 }  // namespace hy

@@ -176,7 +176,7 @@ __device__ __forceinline__ void shadow_finalize(const PassParams& P, const Shado
     }
 }
 
-template <bool COUNT, bool ACCUM, int MINB>
+template <bool COUNT, bool ACCUM, int MINB, bool TWO = false>
 __global__ void __launch_bounds__(128, MINB) k_shadow(const SceneDev S, const PassParams P) {
     LaneStats ls;
     const uint32_t lane = threadIdx.x & 31;
@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(128, MINB) k_shadow(const SceneDev S, const Pa
 
         // ---- one node visit ----
         if (live) {
-            if (trav_step<true, COUNT>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
+            if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
                 live = false;
                 if (t.h.id == HY_NO_HIT) s.sf = __fadd_rn(s.sf, 1.0f);
             }
@@ -303,7 +303,7 @@ __device__ __forceinline__ uint32_t lcg_jump(uint32_t s, uint32_t n) {
     return s;
 }
 
-template <bool COUNT, bool ACCUM, int MINB>
+template <bool COUNT, bool ACCUM, int MINB, bool TWO = false>
 __global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, const PassParams P) {
     LaneStats ls;
     const uint32_t lane = threadIdx.x & 31;
@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, co
         }
         // ---- one node visit ----
         if (live) {
-            if (trav_step<true, COUNT>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
+            if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
                 live = false;
                 if (t.h.id == HY_NO_HIT) s.sf = __fadd_rn(s.sf, 1.0f);
             }
@@ -1002,7 +1002,29 @@ static void* pool_kernel(bool count) {
     return count ? (void*)k_shadow_pool<true, ACCUM, MINB> : (void*)k_shadow_pool<false, ACCUM, MINB>;
 }
 
-static void* pixel_kernel(int mode, bool count, int minb) {
+// two-level structure: the lane-group shadow kernel (register cap of 5 or 6
+// resident blocks), the pixel-parallel one (5) and the shade kernel; nullptr
+// for the ray pool
+template <bool ACCUM>
+static void* shadow_kernel_two(bool count, int minb) {
+    if (minb >= 6)
+        return count ? (void*)k_shadow_group<true, ACCUM, 6, true> : (void*)k_shadow_group<false, ACCUM, 6, true>;
+    return count ? (void*)k_shadow_group<true, ACCUM, 5, true> : (void*)k_shadow_group<false, ACCUM, 5, true>;
+}
+
+static void* pixel_kernel(int mode, bool count, int minb, bool two) {
+    if (two) {
+        switch (mode) {
+            case MODE_SHADOW_G: return shadow_kernel_two<false>(count, minb);
+            case MODE_SHADOW_ACCUM_G: return shadow_kernel_two<true>(count, minb);
+            case MODE_SHADOW:
+                return count ? (void*)k_shadow<true, false, 5, true> : (void*)k_shadow<false, false, 5, true>;
+            case MODE_SHADOW_ACCUM:
+                return count ? (void*)k_shadow<true, true, 5, true> : (void*)k_shadow<false, true, 5, true>;
+            case MODE_SHADE: return count ? (void*)k_pixels<MODE_SHADE, true> : (void*)k_pixels<MODE_SHADE, false>;
+            default: return nullptr;
+        }
+    }
     switch (mode) {
         case MODE_SHADOW: return shadow_kernel<false, false>(count, minb);
         case MODE_SHADOW_ACCUM: return shadow_kernel<false, true>(count, minb);
@@ -1017,11 +1039,15 @@ static void* pixel_kernel(int mode, bool count, int minb) {
 cudaError_t launch_pixels(int mode, bool count, int minb, const SceneDev& S, const PassParams& P, int grid, int block,
                           cudaStream_t s) {
     void* args[] = {(void*)&S, (void*)&P};
-    return cudaLaunchKernel(pixel_kernel(mode, count, minb), dim3(grid), dim3(block), args, 0, s);
+    void* k = pixel_kernel(mode, count, minb, S.two_level != 0);
+    if (!k) return cudaErrorNotSupported;
+    return cudaLaunchKernel(k, dim3(grid), dim3(block), args, 0, s);
 }
 
-cudaError_t pixel_occupancy(int mode, bool count, int minb, int block, int* blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pixel_kernel(mode, count, minb), block, 0);
+cudaError_t pixel_occupancy(int mode, bool count, int minb, bool two, int block, int* blocks_per_sm) {
+    void* k = pixel_kernel(mode, count, minb, two);
+    if (!k) return cudaErrorNotSupported;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, block, 0);
 }
 
 cudaError_t launch_accumulate(const AccumParams& A, cudaStream_t s) {

@@ -97,7 +97,7 @@ cudaError_t launch_pathtrace(bool count, const SceneDev& S, const PtParams& T, i
 
 cudaError_t launch_pixels(int mode, bool count, int minb, const SceneDev& S, const PassParams& P, int grid, int block,
                           cudaStream_t s);
-cudaError_t pixel_occupancy(int mode, bool count, int minb, int block, int* blocks_per_sm);
+cudaError_t pixel_occupancy(int mode, bool count, int minb, bool two, int block, int* blocks_per_sm);
 cudaError_t launch_accumulate(const AccumParams& A, cudaStream_t s);
 cudaError_t launch_post(const uint8_t* in_bgra8, const float* in_rgba32f, uint32_t n, uint8_t* out_bgra8,
                         cudaStream_t s);

@@ -29,7 +29,8 @@ __device__ __forceinline__ Hit trace(const SceneDev& S, f3 o, f3 d, float tmin, 
                                      uint32_t* status) {
     RayPre r = ray_pre(o, d);
     uint32_t nn = 0, nt = 0;
-    Hit h = traverse<ANY, COUNT>(S, r, tmin, tmax, &nn, &nt, status);
+    Hit h = S.two_level ? traverse<ANY, COUNT, true>(S, r, tmin, tmax, &nn, &nt, status)
+                        : traverse<ANY, COUNT, false>(S, r, tmin, tmax, &nn, &nt, status);
     if (COUNT) { ls.nodes += nn; ls.tris += nt; }
     return h;
 }

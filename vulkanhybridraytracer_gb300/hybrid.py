@@ -133,12 +133,32 @@ class HybridContext:
         L.check(self.lib.hy_scene_set_materials(self.h, _np_ptr(mats), len(mats)), "materials")
         self.num_mats = len(mats)
 
-    def build_bvh(self) -> dict:
+    def build_bvh(self, instanced: bool = False) -> dict:
+        """One BVH8 over the world-space triangles, or (instanced) one BLAS per
+        distinct mesh under a TLAS over the primitives."""
         st = L.HyBvhStats()
-        L.check(self.lib.hy_bvh_build(self.h, C.byref(st)), "bvh_build")
+        fn = self.lib.hy_bvh_build_instanced if instanced else self.lib.hy_bvh_build
+        L.check(fn(self.h, C.byref(st)), "bvh_build")
         return {"num_tris": st.num_tris, "num_bvh2_nodes": st.num_bvh2_nodes, "num_bvh8_nodes": st.num_bvh8_nodes,
                 "depth": st.depth, "build_ms": st.build_ms, "scene_lo": list(st.scene_lo),
                 "scene_hi": list(st.scene_hi)}
+
+    def bvh_layout(self) -> dict:
+        lay = L.HyBvhLayout()
+        L.check(self.lib.hy_bvh_layout(self.h, C.byref(lay)), "bvh_layout")
+        return {k: int(getattr(lay, k)) for k, _ in L.HyBvhLayout._fields_}
+
+    def download_bvh_instanced(self):
+        """(layout, nodes [num_nodes, 20] u32, records [num_records, 12] f32,
+        instances [num_instances, 16] f32, instance boxes [num_instances, 6] f32)"""
+        lay = self.bvh_layout()
+        nodes = np.zeros((lay["num_nodes"], 20), np.uint32)
+        recs = np.zeros((lay["num_records"], 12), np.float32)
+        inst = np.zeros((lay["num_instances"], 16), np.float32)
+        boxes = np.zeros((lay["num_instances"], 6), np.float32)
+        L.check(self.lib.hy_bvh_download(self.h, None, None, None, _np_ptr(nodes), _np_ptr(recs)), "bvh_download")
+        L.check(self.lib.hy_bvh_download_instances(self.h, _np_ptr(inst), _np_ptr(boxes)), "bvh_download_instances")
+        return lay, nodes, recs, inst, boxes
 
     def refit_bvh(self, transforms: np.ndarray):
         """New column-major transforms, same topology (the per-frame TLAS update)."""
