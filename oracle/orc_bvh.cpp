@@ -638,20 +638,21 @@ static inline float round_up_f(double x) {
     return ((double)f < x) ? std::nextafter(f, INFINITY) : f;
 }
 
-// World box of an instance: the 8 corners of its mesh's object-space root box
-// through the object->world matrix M (column-major) in double, each corner
-// coordinate ((m0 x + m1 y) + m2 z) + m3, then padded by 2^-16 of the extent
-// plus 2^-20 of the largest magnitude per axis (room for the rounding of the
-// world->object ray transform) and rounded outwards to float.
-static void instance_box(const float* mesh_box, const float* M, float* out6) {
+// World box of an instance: the vertices of its mesh's vertex range (from the
+// smallest to the largest vertex its triangles use) through the
+// object->world matrix M (column-major) in double, each coordinate
+// ((m0 x + m1 y) + m2 z) + m3; min / max, then padded by 2^-16 of the extent
+// plus 2^-20 of the largest magnitude plus 2^-60 per axis (room for the
+// rounding of the world->object ray transform; the last term also makes the
+// result independent of the sign of a zero) and rounded outwards to float.
+static void instance_box(const Scene& s, uint32_t v0, uint32_t v1, const float* M, float* out6) {
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int corner = 0; corner < 8; corner++) {
-        double p[3];
-        for (int a = 0; a < 3; a++) p[a] = (double)((corner >> a) & 1 ? mesh_box[3 + a] : mesh_box[a]);
+    for (uint32_t v = v0; v < v1; v++) {
+        const float* P = s.verts[v].pos;
         for (int r = 0; r < 3; r++) {
-            double w = (double)M[0 * 4 + r] * p[0];
-            w = w + (double)M[1 * 4 + r] * p[1];
-            w = w + (double)M[2 * 4 + r] * p[2];
+            double w = (double)M[0 * 4 + r] * (double)P[0];
+            w = w + (double)M[1 * 4 + r] * (double)P[1];
+            w = w + (double)M[2 * 4 + r] * (double)P[2];
             w = w + (double)M[3 * 4 + r];
             lo[r] = std::fmin(lo[r], w);
             hi[r] = std::fmax(hi[r], w);
@@ -659,7 +660,7 @@ static void instance_box(const float* mesh_box, const float* M, float* out6) {
     }
     for (int a = 0; a < 3; a++) {
         const double mag = std::fmax(std::fabs(lo[a]), std::fabs(hi[a]));
-        const double pad = (hi[a] - lo[a]) * 0x1p-16 + mag * 0x1p-20;
+        const double pad = ((hi[a] - lo[a]) * 0x1p-16 + mag * 0x1p-20) + 0x1p-60;
         out6[a] = round_down_f(lo[a] - pad);
         out6[3 + a] = round_up_f(hi[a] + pad);
     }
@@ -694,7 +695,7 @@ static void tlas_build(Scene& s) {
         I[13] = bitsf(s.prim_tri0[p]);
         I[14] = bitsf(p);
         float* b = &T.inst_box[(size_t)i * 6];
-        instance_box(&T.mesh_box[(size_t)m * 6], &s.xf[(size_t)tf * 16], b);
+        instance_box(s, T.mesh_vrange[2 * m], T.mesh_vrange[2 * m + 1], &s.xf[(size_t)tf * 16], b);
         float* it = &items[(size_t)i * 9];
         for (int a = 0; a < 3; a++) { it[a] = b[a]; it[3 + a] = b[3 + a]; it[6 + a] = b[3 + a]; }
     }
@@ -735,7 +736,7 @@ void bvh_build_instanced(Scene& s) {
     T.tlas_region = T.ninst;
     T.nodes.assign(T.tlas_region, Bvh8Node{});
     T.tris.assign((size_t)T.tlas_region * 12, 0.f);
-    T.mesh_box.assign((size_t)T.nblas * 6, 0.f);
+    T.mesh_vrange.assign((size_t)T.nblas * 2, 0u);
     uint32_t rec = T.tlas_region;
     for (uint32_t m = 0; m < T.nblas; m++) {
         const HyPrimitive& pr = s.prims[T.mesh_prim[m]];
@@ -755,16 +756,14 @@ void bvh_build_instanced(Scene& s) {
         T.nodes.insert(T.nodes.end(), b.bvh8.begin(), b.bvh8.end());
         T.tris.insert(T.tris.end(), b.tris.begin(), b.tris.end());
         T.blas_depth = std::max(T.blas_depth, b.depth);
-        // root box: the binary tree's root, or the single triangle's box
-        float* mb = &T.mesh_box[(size_t)m * 6];
-        if (nt > 1) {
-            for (int a = 0; a < 3; a++) { mb[a] = b.bvh2[0].lo[a]; mb[3 + a] = b.bvh2[0].hi[a]; }
-        } else {
-            for (int a = 0; a < 3; a++) {
-                mb[a] = fmin2(fmin2(items[a], items[3 + a]), items[6 + a]);
-                mb[3 + a] = fmax2(fmax2(items[a], items[3 + a]), items[6 + a]);
-            }
+        // vertex range the mesh's triangles use
+        uint32_t vmin = 0xffffffffu, vmax = 0;
+        for (uint32_t k = 0; k < nt * 3; k++) {
+            vmin = std::min(vmin, s.idx[pr.first_index + k]);
+            vmax = std::max(vmax, s.idx[pr.first_index + k]);
         }
+        T.mesh_vrange[2 * m] = pr.vertex_offset + vmin;
+        T.mesh_vrange[2 * m + 1] = pr.vertex_offset + vmax + 1;
         rec += nt;
     }
     tlas_build(s);

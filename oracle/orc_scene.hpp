@@ -52,7 +52,7 @@ struct Bvh2L {
     std::vector<uint32_t> prim_mesh;    // BLAS of each primitive, 0xffffffff when it has no triangles
     std::vector<uint32_t> mesh_prim;    // first primitive of each BLAS (its index range)
     std::vector<uint32_t> blas_node0, blas_rec0, blas_nodes;
-    std::vector<float> mesh_box;        // 6 per BLAS: root box in object space
+    std::vector<uint32_t> mesh_vrange;  // 2 per BLAS: first vertex, one past the last vertex its triangles use
     std::vector<float> xinv;            // 12 per transform: world->object rows
     uint32_t ninst = 0, nblas = 0, tlas_region = 0, tlas_nodes = 0, tlas_depth = 0, blas_depth = 0;
 };

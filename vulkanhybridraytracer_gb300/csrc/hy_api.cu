@@ -417,7 +417,9 @@ void hy_destroy(HyCtx* c) {
                       &c->node_plan, &c->dstats,
                       &c->raw_shadow, &c->hist_prev, &c->host_in[0], &c->host_in[1], &c->host_in[2],
                       &c->host_in[3], &c->host_in[4], &c->host_in[5], &c->host_out_f, &c->host_out_8,
-                      &c->grad_partial, &c->tex_px, &c->tex_tab};
+                      &c->grad_partial, &c->tex_px, &c->tex_tab, &c->xinv, &c->inst, &c->inst_box,
+                      &c->inst_prim, &c->prim_mesh, &c->blas_node0, &c->mesh_vrange, &c->inst_chunks,
+                      &c->inst_keys};
     for (DevBuf* b : bufs) ctx_free(c, *b);
     if (c->h_stats) cudaFreeHost(c->h_stats);
     for (cudaEvent_t e : c->prof_pool) cudaEventDestroy(e);

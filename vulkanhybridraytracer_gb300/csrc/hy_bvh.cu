@@ -767,26 +767,90 @@ __global__ void k_mesh_tris(const HyVertex* __restrict__ verts, const uint32_t* 
                          __fmul_rn(__fadd_rn(lo[2], hi[2]), 0.5f), 0.f);
 }
 
-// root box of a BLAS just built: the binary tree's root, or its only triangle
-__global__ void k_mesh_box(uint32_t n, const uint32_t* __restrict__ bvh2, const float* __restrict__ tribox,
-                           float* __restrict__ out) {
-    if (threadIdx.x != 0) return;
-    for (int a = 0; a < 6; a++) out[a] = n > 1 ? __uint_as_float(bvh2[4 + a]) : tribox[a];
+// smallest / largest vertex index a mesh's triangles use (out: min, max)
+__global__ void k_mesh_vrange(const uint32_t* __restrict__ idx, uint32_t n, uint32_t* __restrict__ out) {
+    uint32_t lo = 0xffffffffu, hi = 0;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const uint32_t v = idx[k];
+        lo = min(lo, v);
+        hi = max(hi, v);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) { atomicMin(out, lo); atomicMax(out + 1, hi); }
+}
+
+// doubles as order-preserving signed 64-bit keys (-0 below +0)
+__device__ __forceinline__ long long d2ord(double x) {
+    const long long b = __double_as_longlong(x);
+    return b >= 0 ? b : b ^ 0x7fffffffffffffffll;
+}
+__device__ __forceinline__ double ord2d(long long k) {
+    return __longlong_as_double(k >= 0 ? k : k ^ 0x7fffffffffffffffll);
+}
+
+__global__ void k_inst_box_init(uint32_t ninst, long long* __restrict__ keys) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    for (int a = 0; a < 3; a++) {
+        keys[(size_t)i * 6 + a] = d2ord(INFINITY);
+        keys[(size_t)i * 6 + 3 + a] = d2ord(-INFINITY);
+    }
+}
+
+// World box of an instance, one chunk (instance, first vertex, end vertex) of
+// its mesh's vertex range per block: each vertex through the object->world
+// matrix in double, ((m0 x + m1 y) + m2 z) + m3, min / max folded into the
+// instance's keys (min and max are exact, so the order does not matter)
+__global__ void __launch_bounds__(128) k_inst_box(const uint4* __restrict__ chunks,
+                                                  const uint32_t* __restrict__ inst_prim,
+                                                  const HyPrimitive* __restrict__ prims,
+                                                  const HyVertex* __restrict__ verts, const float* __restrict__ xf,
+                                                  long long* __restrict__ keys) {
+    const uint4 ch = chunks[blockIdx.x];
+    const float* M = xf + (size_t)prims[inst_prim[ch.x]].transform_id * 16;
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t v = ch.y + threadIdx.x; v < ch.z; v += blockDim.x) {
+        const float* P = verts[v].pos;
+#pragma unroll
+        for (int r = 0; r < 3; r++) {
+            double w = __dmul_rn((double)M[0 * 4 + r], (double)P[0]);
+            w = __dadd_rn(w, __dmul_rn((double)M[1 * 4 + r], (double)P[1]));
+            w = __dadd_rn(w, __dmul_rn((double)M[2 * 4 + r], (double)P[2]));
+            w = __dadd_rn(w, (double)M[3 * 4 + r]);
+            lo[r] = fmin(lo[r], w);
+            hi[r] = fmax(hi[r], w);
+        }
+    }
+    long long* k = keys + (size_t)ch.x * 6;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        long long kl = d2ord(lo[a]), kh = d2ord(hi[a]);
+        for (int o = 16; o > 0; o >>= 1) {
+            kl = min(kl, __shfl_xor_sync(0xffffffffu, kl, o));
+            kh = max(kh, __shfl_xor_sync(0xffffffffu, kh, o));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicMin(k + a, kl);
+            atomicMax(k + 3 + a, kh);
+        }
+    }
 }
 
 // Instance records and TLAS items.  Record: the world->object rows of the
 // instance's transform, then (BLAS root node, first global triangle,
-// primitive, 0).  Box: the 8 corners of the mesh box through the
-// object->world matrix in double, ((m0 x + m1 y) + m2 z) + m3, padded by
-// 2^-16 of the extent plus 2^-20 of the largest magnitude per axis (room for
-// the rounding of the world->object ray transform) and rounded outwards.
+// primitive, 0).  Box: the vertex-range box, padded by 2^-16 of the extent
+// plus 2^-20 of the largest magnitude plus 2^-60 per axis (room for the
+// rounding of the world->object ray transform; the last term also makes the
+// result independent of the sign of a zero) and rounded outwards to float.
 __global__ void k_inst_setup(uint32_t ninst, const uint32_t* __restrict__ inst_prim,
                              const HyPrimitive* __restrict__ prims, const uint32_t* __restrict__ prim_mesh,
                              const uint32_t* __restrict__ blas_node0, const uint32_t* __restrict__ prim_tri0,
-                             const float* __restrict__ xinv, const float* __restrict__ xf,
-                             const float* __restrict__ mesh_box, float4* __restrict__ inst,
-                             float* __restrict__ inst_box, float4* __restrict__ world, float* __restrict__ tribox,
-                             float4* __restrict__ cen) {
+                             const float* __restrict__ xinv, const long long* __restrict__ keys,
+                             float4* __restrict__ inst, float* __restrict__ inst_box, float4* __restrict__ world,
+                             float* __restrict__ tribox, float4* __restrict__ cen) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ninst) return;
     const uint32_t p = inst_prim[i], m = prim_mesh[p], tf = prims[p].transform_id;
@@ -794,27 +858,14 @@ __global__ void k_inst_setup(uint32_t ninst, const uint32_t* __restrict__ inst_p
     for (int k = 0; k < 3; k++) inst[(size_t)i * 4 + k] = make_float4(R[4 * k], R[4 * k + 1], R[4 * k + 2], R[4 * k + 3]);
     inst[(size_t)i * 4 + 3] = make_float4(__uint_as_float(blas_node0[m]), __uint_as_float(prim_tri0[p]),
                                           __uint_as_float(p), 0.f);
-    const float* M = xf + (size_t)tf * 16;
-    const float* mb = mesh_box + (size_t)m * 6;
-    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int corner = 0; corner < 8; corner++) {
-        double q[3];
-        for (int a = 0; a < 3; a++) q[a] = (double)((corner >> a) & 1 ? mb[3 + a] : mb[a]);
-        for (int r = 0; r < 3; r++) {
-            double w = __dmul_rn((double)M[0 * 4 + r], q[0]);
-            w = __dadd_rn(w, __dmul_rn((double)M[1 * 4 + r], q[1]));
-            w = __dadd_rn(w, __dmul_rn((double)M[2 * 4 + r], q[2]));
-            w = __dadd_rn(w, (double)M[3 * 4 + r]);
-            lo[r] = fmin(lo[r], w);
-            hi[r] = fmax(hi[r], w);
-        }
-    }
     float bl[3], bh[3];
     for (int a = 0; a < 3; a++) {
-        const double mag = fmax(fabs(lo[a]), fabs(hi[a]));
-        const double pad = __dadd_rn(__dmul_rn(__dsub_rn(hi[a], lo[a]), 0x1p-16), __dmul_rn(mag, 0x1p-20));
-        bl[a] = __double2float_rd(__dsub_rn(lo[a], pad));
-        bh[a] = __double2float_ru(__dadd_rn(hi[a], pad));
+        const double lo = ord2d(keys[(size_t)i * 6 + a]), hi = ord2d(keys[(size_t)i * 6 + 3 + a]);
+        const double mag = fmax(fabs(lo), fabs(hi));
+        const double pad =
+            __dadd_rn(__dadd_rn(__dmul_rn(__dsub_rn(hi, lo), 0x1p-16), __dmul_rn(mag, 0x1p-20)), 0x1p-60);
+        bl[a] = __double2float_rd(__dsub_rn(lo, pad));
+        bh[a] = __double2float_ru(__dadd_rn(hi, pad));
         inst_box[(size_t)i * 6 + a] = bl[a];
         inst_box[(size_t)i * 6 + 3 + a] = bh[a];
         tribox[(size_t)i * 6 + a] = bl[a];
@@ -832,14 +883,19 @@ int tlas_build_impl(HyCtx* c) {
     int rc;
     cudaStream_t s = c->stream;
     if ((rc = ctx_alloc(c, c->inst, (size_t)ni * 64)) || (rc = ctx_alloc(c, c->inst_box, (size_t)ni * 24)) ||
+        (rc = ctx_alloc(c, c->inst_keys, (size_t)ni * 48)) ||
         (rc = ctx_alloc(c, c->world, (size_t)ni * 48)) || (rc = ctx_alloc(c, c->tribox, (size_t)ni * 24)) ||
         (rc = ctx_alloc(c, c->centroid, (size_t)ni * 16)))
         return rc;
+    long long* keys = c->inst_keys.as<long long>();
+    k_inst_box_init<<<cdiv(ni, 128), 128, 0, s>>>(ni, keys);
+    k_inst_box<<<c->n_chunks, 128, 0, s>>>(c->inst_chunks.as<uint4>(), c->inst_prim.as<uint32_t>(),
+                                           c->prims.as<HyPrimitive>(), c->verts.as<HyVertex>(), c->xf.as<float>(),
+                                           keys);
     k_inst_setup<<<cdiv(ni, 128), 128, 0, s>>>(
         ni, c->inst_prim.as<uint32_t>(), c->prims.as<HyPrimitive>(), c->prim_mesh.as<uint32_t>(),
-        c->blas_node0.as<uint32_t>(), c->prim_tri0.as<uint32_t>(), c->xinv.as<float>(), c->xf.as<float>(),
-        c->mesh_box.as<float>(), c->inst.as<float4>(), c->inst_box.as<float>(), c->world.as<float4>(),
-        c->tribox.as<float>(), c->centroid.as<float4>());
+        c->blas_node0.as<uint32_t>(), c->prim_tri0.as<uint32_t>(), c->xinv.as<float>(), keys, c->inst.as<float4>(),
+        c->inst_box.as<float>(), c->world.as<float4>(), c->tribox.as<float>(), c->centroid.as<float4>());
     HY_CUDA_TRY(cudaGetLastError());
     HY_CUDA_TRY(cudaMemsetAsync(c->nodes.p, 0, (size_t)c->tlas_region * sizeof(Node8), s));
     HY_CUDA_TRY(cudaMemsetAsync(c->tris.p, 0, (size_t)c->tlas_region * 48, s));
@@ -904,7 +960,7 @@ int bvh_build_instanced_impl(HyCtx* c, HyBvhStats* st) {
         (rc = ctx_alloc(c, c->tris, (size_t)rec_cap * 48)) ||
         (rc = ctx_alloc(c, c->world, (size_t)max_nt * 48)) || (rc = ctx_alloc(c, c->tribox, (size_t)max_nt * 24)) ||
         (rc = ctx_alloc(c, c->centroid, (size_t)max_nt * 16)) ||
-        (rc = ctx_alloc(c, c->mesh_box, (size_t)c->nblas * 24)) ||
+        (rc = ctx_alloc(c, c->mesh_vrange, (size_t)c->nblas * 8)) ||
         (rc = ctx_alloc(c, c->prim_mesh, (size_t)np * 4)) || (rc = ctx_alloc(c, c->inst_prim, (size_t)c->ninst * 4)) ||
         (rc = ctx_alloc(c, c->blas_node0, (size_t)c->nblas * 4)))
         return rc;
@@ -915,6 +971,9 @@ int bvh_build_instanced_impl(HyCtx* c, HyBvhStats* st) {
     HY_CUDA_TRY(cudaMemsetAsync(c->nodes.p, 0, (size_t)node_cap * sizeof(Node8), s));
     HY_CUDA_TRY(cudaMemsetAsync(c->tris.p, 0, (size_t)rec_cap * 48, s));
     HY_CUDA_TRY(cudaMemcpyAsync(c->prim_mesh.p, c->h_prim_mesh.data(), (size_t)np * 4, cudaMemcpyHostToDevice, s));
+    std::vector<uint32_t> vr_init((size_t)c->nblas * 2);
+    for (uint32_t m = 0; m < c->nblas; m++) { vr_init[2 * m] = 0xffffffffu; vr_init[2 * m + 1] = 0; }
+    HY_CUDA_TRY(cudaMemcpyAsync(c->mesh_vrange.p, vr_init.data(), vr_init.size() * 4, cudaMemcpyHostToDevice, s));
     HY_CUDA_TRY(cudaMemcpyAsync(c->inst_prim.p, c->h_inst_prim.data(), (size_t)c->ninst * 4, cudaMemcpyHostToDevice,
                                 s));
     uint32_t node_off = c->tlas_region, rec_off = c->tlas_region;
@@ -929,8 +988,8 @@ int bvh_build_instanced_impl(HyCtx* c, HyBvhStats* st) {
         HY_CUDA_TRY(cudaGetLastError());
         uint32_t nn = 0, depth = 0;
         if ((rc = build_core(c, nt, node_off, rec_off, &nn, &depth))) return rc;
-        k_mesh_box<<<1, 32, 0, s>>>(nt, c->bvh2.as<uint32_t>(), c->tribox.as<float>(),
-                                    c->mesh_box.as<float>() + (size_t)m * 6);
+        k_mesh_vrange<<<std::min<uint32_t>(cdiv(nt * 3, 256), 4 * (uint32_t)c->num_sms), 256, 0, s>>>(
+            c->idx.as<uint32_t>() + pr.first_index, nt * 3, c->mesh_vrange.as<uint32_t>() + (size_t)m * 2);
         HY_CUDA_TRY(cudaGetLastError());
         c->h_blas_node0[m] = node_off;
         node_off += nn;
@@ -938,6 +997,20 @@ int bvh_build_instanced_impl(HyCtx* c, HyBvhStats* st) {
         c->blas_depth = std::max(c->blas_depth, depth);
     }
     HY_CUDA_TRY(cudaMemcpyAsync(c->blas_node0.p, c->h_blas_node0.data(), (size_t)c->nblas * 4,
+                                cudaMemcpyHostToDevice, s));
+    // per-frame box work: each instance's vertex range in chunks of 1024 vertices
+    std::vector<uint32_t> vr((size_t)c->nblas * 2);
+    HY_CUDA_TRY(cudaMemcpyAsync(vr.data(), c->mesh_vrange.p, vr.size() * 4, cudaMemcpyDeviceToHost, s));
+    HY_CUDA_TRY(cudaStreamSynchronize(s));
+    std::vector<uint4> chunks;
+    for (uint32_t i = 0; i < c->ninst; i++) {
+        const uint32_t p = c->h_inst_prim[i], m = c->h_prim_mesh[p];
+        const uint32_t v0 = c->h_prims[p].vertex_offset + vr[2 * m], v1 = c->h_prims[p].vertex_offset + vr[2 * m + 1] + 1;
+        for (uint32_t v = v0; v < v1; v += 1024) chunks.push_back(make_uint4(i, v, std::min(v1, v + 1024), 0));
+    }
+    c->n_chunks = (uint32_t)chunks.size();
+    if ((rc = ctx_alloc(c, c->inst_chunks, chunks.size() * sizeof(uint4)))) return rc;
+    HY_CUDA_TRY(cudaMemcpyAsync(c->inst_chunks.p, chunks.data(), chunks.size() * sizeof(uint4),
                                 cudaMemcpyHostToDevice, s));
     c->n_bvh8 = node_off;
     c->n_records = rec_off;

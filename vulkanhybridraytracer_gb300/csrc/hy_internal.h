@@ -69,7 +69,11 @@ struct HyCtx {
     hy::DevBuf xinv;                 // 12 floats per transform: world->object rows (always kept current)
     hy::DevBuf inst;                 // 64 B per instance: 3 rows + (BLAS root, first triangle, primitive, 0)
     hy::DevBuf inst_box;             // 6 floats per instance: its TLAS box
-    hy::DevBuf inst_prim, prim_mesh, blas_node0, mesh_box;
+    hy::DevBuf inst_prim, prim_mesh, blas_node0;
+    hy::DevBuf mesh_vrange;          // per mesh: smallest, largest vertex index its triangles use
+    hy::DevBuf inst_chunks;          // (instance, first vertex, end vertex, 0): the box work of a TLAS update
+    hy::DevBuf inst_keys;            // 6 order-preserving 64-bit keys per instance (box min / max)
+    uint32_t n_chunks = 0;
     std::vector<HyPrimitive> h_prims;
     std::vector<uint32_t> h_inst_prim, h_prim_mesh, h_mesh_prim, h_blas_node0;
     uint32_t ninst = 0, nblas = 0, tlas_region = 0, tlas_nodes = 0, tlas_depth = 0, blas_depth = 0;
