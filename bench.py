@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--minb", type=int, default=0, help="shadow-kernel variant: resident blocks per SM")
     ap.add_argument("--group", type=int, default=0, help="lanes per pixel-light group (0: next power of 2 >= spp)")
+    ap.add_argument("--visits", type=int, default=0, help="node visits per scheduling round of the shadow kernel")
     ap.add_argument("--sched", default="groups", choices=["groups", "pool"],
                     help="DECORRELATED shadow samples in fixed lane groups or from the per-warp ray pool")
     ap.add_argument("--workload", default="hd", choices=["hd", "batch", "diff", "pathtrace", "large"],
@@ -634,7 +635,7 @@ def main():
     def cfg(frame, flags=L.HY_FLAG_NO_STATUS_SYNC):
         return pass_config(spp=wl.spp, max_bounces=wl.max_bounces, rng_mode=wl.rng_mode, accum_frame=frame,
                            flags=flags | sched, block_size=args.block, queue_chunk=args.chunk, min_blocks=args.minb,
-                           group_lanes=args.group)
+                           group_lanes=args.group, visits_per_round=args.visits)
 
     # rays per frame and traversal counts (untimed counting launch, same frame as step 1)
     st_count = ctx.forward(planes, wl.camera(1.0), cfg(1, L.HY_FLAG_COUNT_TRAVERSAL), hist.clone(),

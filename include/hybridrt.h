@@ -180,6 +180,9 @@ typedef struct HyPassConfig {
     uint32_t min_blocks;    /* shadow-kernel variant: compiled for 5 (96 registers) or 8 (64 registers)
                                resident blocks per SM, the lane-group kernel also for 6 and 7;
                                0 = 6 for the lane-group kernel, 8 otherwise */
+    uint32_t visits_per_round; /* BVH node visits a shadow lane makes between two scheduling rounds
+                                  of the persistent shadow kernels (1..16; a lane whose ray ends
+                                  early waits for the round); 0 = 4 */
 } HyPassConfig;
 
 typedef struct HyStats {

@@ -88,7 +88,7 @@ class _GBuf(C.Structure):
 class _Cfg(C.Structure):
     _fields_ = [("shadow_spp", U32), ("max_bounces", U32), ("rng_mode", U32), ("accum_frame", C.c_int32),
                 ("flags", U32), ("block_size", U32), ("queue_chunk", U32), ("stack_depth", U32), ("group_lanes", U32),
-                ("min_blocks", U32)]
+                ("min_blocks", U32), ("visits_per_round", U32)]
 
 
 class _Accum(C.Structure):

@@ -204,6 +204,48 @@ int main() {
         r.rasterize_hybrid(gb, cam, hist_a, nullptr, out_a);
         r.synchronize();
 
+        // the two-level structure (BLAS per mesh, TLAS over the entities) renders the
+        // same frame through the adapter and through the C ABI, before and after a
+        // TLAS update
+        {
+            r.load_data_to_gpu(s);
+            HyBvhStats b2 = r.create_acceleration_structures(true);
+            HyBvhLayout lay;
+            check(hy_bvh_layout(r.handle(), &lay), "layout");
+            if (!lay.two_level || lay.num_instances != 4 || lay.num_blas != 2 || b2.num_tris != 2 + 3 * 20) {
+                std::fprintf(stderr, "two-level layout %u %u %u\n", lay.two_level, lay.num_instances, lay.num_blas);
+                fails++;
+            }
+            std::vector<float> xf;
+            for (const Object& o : s._entities) xf.insert(xf.end(), o.m_matrix, o.m_matrix + 16);
+            check(hy_bvh_refit(raw, xf.data(), (uint32_t)s._entities.size()), "raw refit");
+            check(hy_bvh_build_instanced(raw, nullptr), "raw two-level build");
+            for (int step = 0; step < 2; step++) {
+                if (step == 1) {
+                    translate_scale(s._entities[3].m_matrix, 1.f, 2.f, 0.f, 0.6f);
+                    r.update_tlas(s);
+                    xf.clear();
+                    for (const Object& o : s._entities) xf.insert(xf.end(), o.m_matrix, o.m_matrix + 16);
+                    check(hy_bvh_refit(raw, xf.data(), (uint32_t)s._entities.size()), "raw TLAS update");
+                }
+                HyCamera c2 = camera(eye, 60.f, (float)W / H, 1.f);
+                check(hy_gbuffer_primary(r.handle(), &c2, W, H, planes), "gbuffer two-level");
+                CK(cudaMemset(hist_a, 0, npx * 2));
+                CK(cudaMemset(hist_b, 0, npx * 2));
+                r.rasterize_hybrid(gb, c2, hist_a, nullptr, out_a);
+                HyPassConfig cfg = r.pass_config();
+                HyAccum acc{HY_ACCUM_U8, 2, hist_b};
+                check(hy_hybrid_forward(raw, &gb, &c2, &cfg, &acc, nullptr, out_b, nullptr), "forward two-level");
+                CK(cudaDeviceSynchronize());
+                CK(cudaMemcpy(ha.data(), out_a, npx * 4, cudaMemcpyDeviceToHost));
+                CK(cudaMemcpy(hb.data(), out_b, npx * 4, cudaMemcpyDeviceToHost));
+                if (std::memcmp(ha.data(), hb.data(), npx * 4) != 0) {
+                    std::fprintf(stderr, "two-level frame %d differs from the C ABI result\n", step);
+                    fails++;
+                }
+            }
+        }
+
         // errors come back as exceptions with the C code
         try {
             Scene bad = s;

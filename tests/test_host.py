@@ -67,6 +67,8 @@ def test_struct_layouts():
     assert C.sizeof(L.HyCamera) == 144        # RTCameraData
     assert C.sizeof(L.HyPrimitive) == 24
     assert C.sizeof(L.HyStats) == 48
+    assert C.sizeof(L.HyPassConfig) == 44
+    assert C.sizeof(L.HyBvhLayout) == 32
     assert L.HyGBuffer.plane.offset == 8
 
 

@@ -255,3 +255,34 @@ def test_gpu_instanced_unsupported_paths(gpu_lib, oracle_lib):
     ctx.build_bvh()
     assert ctx.bvh_layout()["two_level"] == 0
     ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_instanced_pathtrace_parity(gpu_lib, oracle_lib):
+    """The path-traced mode (camera rays, closesthit shading, shadow rays at every
+    hit) over the two-level structure against the oracle's over the same one."""
+    import torch
+    from vulkanhybridraytracer_gb300.hybrid import pass_config
+    wl = scenes.small_glass(64, 48)
+    ctx, gi, o = _gpu_pair(wl)
+    try:
+        img = torch.zeros((wl.height, wl.width, 4), dtype=torch.uint8, device="cuda")
+        out = torch.zeros((wl.height, wl.width, 4), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        img_o = np.zeros((wl.height, wl.width, 4), np.uint8)
+        for frame in (-1.0, 1.0):
+            cam = wl.camera(frame)
+            img, st = ctx.pathtrace(cam, wl.width, wl.height, pass_config(4, 8, L.HY_RNG_DECORRELATED), img,
+                                    out_f=out)
+            img_o, out_o, st_o = o.pathtrace(cam, wl.width, wl.height,
+                                             po.cfg_dict(spp=4, max_bounces=8, rng_mode=L.HY_RNG_DECORRELATED), img_o)
+            got = out.cpu().numpy()[..., :3].astype(np.float64)
+            ref = out_o[..., :3].astype(np.float64)
+            err = np.abs(got - ref)
+            rms = np.sqrt((err ** 2).sum() / max((ref ** 2).sum(), 1e-30))
+            assert rms <= 1e-3, (frame, rms)
+            assert np.mean(err.max(-1) > 1e-2) <= 2e-3
+            assert st["error_flags"] == 0
+            assert abs(st["shadow_rays"] - st_o["shadow_rays"]) <= 1e-3 * st_o["shadow_rays"] + 4
+    finally:
+        ctx.close()

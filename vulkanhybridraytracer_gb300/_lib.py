@@ -82,7 +82,7 @@ class HyPassConfig(C.Structure):
     _fields_ = [("shadow_spp", C.c_uint32), ("max_bounces", C.c_uint32), ("rng_mode", C.c_uint32),
                 ("accum_frame", C.c_int32), ("flags", C.c_uint32), ("block_size", C.c_uint32),
                 ("queue_chunk", C.c_uint32), ("stack_depth", C.c_uint32), ("group_lanes", C.c_uint32),
-                ("min_blocks", C.c_uint32)]
+                ("min_blocks", C.c_uint32), ("visits_per_round", C.c_uint32)]
 
 
 class HyStats(C.Structure):

@@ -270,11 +270,14 @@ __global__ void __launch_bounds__(128, MINB) k_shadow(const SceneDev S, const Pa
             }
         }
 
-        // ---- one node visit ----
+        // ---- up to P.inner node visits ----
         if (live) {
-            if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
-                live = false;
-                if (t.h.id == HY_NO_HIT) s.sf = __fadd_rn(s.sf, 1.0f);
+            for (uint32_t it = 0, ni = max(P.inner, 1u); it < ni; it++) {
+                if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
+                    live = false;
+                    if (t.h.id == HY_NO_HIT) s.sf = __fadd_rn(s.sf, 1.0f);
+                    break;
+                }
             }
         }
     }
@@ -395,11 +398,14 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, co
             live = true;
             ls.shadow++;
         }
-        // ---- one node visit ----
+        // ---- up to P.inner node visits ----
         if (live) {
-            if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
-                live = false;
-                if (t.h.id == HY_NO_HIT) s.sf = __fadd_rn(s.sf, 1.0f);
+            for (uint32_t it = 0, ni = max(P.inner, 1u); it < ni; it++) {
+                if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
+                    live = false;
+                    if (t.h.id == HY_NO_HIT) s.sf = __fadd_rn(s.sf, 1.0f);
+                    break;
+                }
             }
         }
         // ---- a group whose samples are all in folds them into the light's factor ----
@@ -745,11 +751,14 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_batch(const BatchParams B)
             live = true;
             ls.shadow++;
         }
-        // ---- one node visit ----
+        // ---- up to P->inner node visits ----
         if (live) {
-            if (trav_step<true, COUNT>(*S, r, 0.001f, t, stk, nn, nt, P->status)) {
-                live = false;
-                if (t.h.id == HY_NO_HIT) s.sf = __fadd_rn(s.sf, 1.0f);
+            for (uint32_t it = 0, ni = max(P->inner, 1u); it < ni; it++) {
+                if (trav_step<true, COUNT>(*S, r, 0.001f, t, stk, nn, nt, P->status)) {
+                    live = false;
+                    if (t.h.id == HY_NO_HIT) s.sf = __fadd_rn(s.sf, 1.0f);
+                    break;
+                }
             }
         }
         // ---- groups whose samples are all in fold them into the light's factor ----

@@ -42,9 +42,9 @@ def camera_struct(cam36) -> L.HyCamera:
 
 
 def pass_config(spp=1, max_bounces=8, rng_mode=L.HY_RNG_REFERENCE, accum_frame=0, flags=0, block_size=0,
-                queue_chunk=0, stack_depth=0, min_blocks=0, group_lanes=0) -> L.HyPassConfig:
+                queue_chunk=0, stack_depth=0, min_blocks=0, group_lanes=0, visits_per_round=0) -> L.HyPassConfig:
     return L.HyPassConfig(spp, max_bounces, rng_mode, accum_frame, flags, block_size, queue_chunk, stack_depth,
-                          group_lanes, min_blocks)
+                          group_lanes, min_blocks, visits_per_round)
 
 
 GBUF_FP32_FORMATS = (L.HY_FMT_RGBA32F, L.HY_FMT_RGBA32F, L.HY_FMT_RGBA32F, L.HY_FMT_RG32F, L.HY_FMT_RGBA32F,
