@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--minb", type=int, default=0, help="shadow-kernel variant: resident blocks per SM")
     ap.add_argument("--group", type=int, default=0, help="lanes per pixel-light group (0: next power of 2 >= spp)")
     ap.add_argument("--visits", type=int, default=0, help="node visits per scheduling round of the shadow kernel")
-    ap.add_argument("--sched", default="groups", choices=["groups", "pool"],
+    ap.add_argument("--sched", default="groups", choices=["groups", "pool", "stream"],
                     help="DECORRELATED shadow samples in fixed lane groups or from the per-warp ray pool")
     ap.add_argument("--workload", default="hd", choices=["hd", "batch", "diff", "pathtrace", "large"],
                     help="hd: the 1080p frame (headline); batch: 64 mixed views over 8 scenes, batched vs per "
@@ -630,7 +630,7 @@ def main():
     out_8 = torch.empty((wl.height, wl.width, 4), dtype=torch.uint8, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
-    sched = L.HY_FLAG_RAY_POOL if args.sched == "pool" else 0
+    sched = {"pool": L.HY_FLAG_RAY_POOL, "stream": L.HY_FLAG_TILE_STREAM}.get(args.sched, 0)
 
     def cfg(frame, flags=L.HY_FLAG_NO_STATUS_SYNC):
         return pass_config(spp=wl.spp, max_bounces=wl.max_bounces, rng_mode=wl.rng_mode, accum_frame=frame,

@@ -164,6 +164,8 @@ enum { HY_RNG_REFERENCE = 0, HY_RNG_DECORRELATED = 1 };
 #define HY_FLAG_RAY_POOL           0x20u /* those samples from a per-warp ray pool that refills each lane as
                                             soon as its ray ends (default: a fixed lane group per pixel-light,
                                             which waits for its slowest sample but stays more coherent) */
+#define HY_FLAG_TILE_STREAM        0x40u /* those samples light by light over a warp's 8x4 tile, each lane
+                                            walking its share without waiting per pixel-light */
 
 typedef struct HyPassConfig {
     uint32_t shadow_spp;    /* samplesBuffer.samples (1..64, src/renderer.cpp:656) */

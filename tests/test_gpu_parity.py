@@ -400,11 +400,45 @@ def test_group_kernel_equals_pixel_kernel(small, spp):
     sa = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, 0), a)
     sb = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, L.HY_FLAG_PIXEL_PARALLEL), b)
     sc = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, L.HY_FLAG_RAY_POOL), c)
-    assert torch.equal(a, b) and torch.equal(a, c)
-    assert sa["shadow_rays"] == sb["shadow_rays"] == sc["shadow_rays"] > 0
+    e = torch.zeros_like(a)
+    torch.cuda.synchronize()
+    se = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, L.HY_FLAG_TILE_STREAM), e)
+    assert torch.equal(a, b) and torch.equal(a, c) and torch.equal(a, e)
+    assert sa["shadow_rays"] == sb["shadow_rays"] == sc["shadow_rays"] == se["shadow_rays"] > 0
+    # the same schedules with one node visit per round, and the tile streams at each register cap
+    for flags, minb, visits in ((0, 0, 1), (L.HY_FLAG_TILE_STREAM, 5, 1), (L.HY_FLAG_TILE_STREAM, 8, 3)):
+        f = torch.zeros_like(a)
+        torch.cuda.synchronize()
+        small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, flags, min_blocks=minb,
+                                                       visits_per_round=visits), f)
+        assert torch.equal(a, f), (flags, minb, visits)
     # smaller lane groups (several samples per lane in turn): the same images
     for G in (2, 4, 8):
         d = torch.zeros_like(a)
         torch.cuda.synchronize()
         small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, 0, group_lanes=G), d)
         assert torch.equal(a, d), G
+
+
+@pytest.mark.parametrize("frame", [0, 3])
+def test_tile_stream_forward_equals_groups(small, frame):
+    """The light-major tile schedule (HY_FLAG_TILE_STREAM), raw images and the
+    fused running-mean variant alike, gives the same history and image as the
+    lane groups, bit for bit."""
+    from vulkanhybridraytracer_gb300.hybrid import pass_config
+    torch = _torch()
+    wl = small.wl
+    W, H, nl = wl.width, wl.height, len(wl.scene.lights)
+    cam = wl.camera(float(frame))
+    planes = [torch.from_numpy(x).cuda() for x in small.orc.gbuffer(cam, W, H)]
+    h0 = torch.randint(0, 256, (nl, H, W), dtype=torch.uint8, generator=torch.Generator().manual_seed(frame)).cuda()
+    outs = []
+    for flags in (0, L.HY_FLAG_TILE_STREAM):
+        h = h0.clone()
+        o = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        st = small.ctx.forward(planes, cam, pass_config(8, 2, L.HY_RNG_DECORRELATED, frame, flags), h, out_8=o)
+        outs.append((h, o, st))
+    (ha, oa, sa), (hb, ob, sb) = outs
+    assert torch.equal(ha, hb) and torch.equal(oa, ob)
+    assert sa["shadow_rays"] == sb["shadow_rays"] > 0 and sb["error_flags"] == 0

@@ -283,13 +283,14 @@ PassParams make_params(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const
 
 // ---- per-kernel timing ----
 // the first seven are the MODE_* values of hy_pass.h
-enum { PK_ACCUM = MODE_SHADOW_ACCUM_P + 1, PK_GRAD, PK_PATHTRACE, PK_COUNT };
+enum { PK_ACCUM = MODE_SHADOW_ACCUM_S + 1, PK_GRAD, PK_PATHTRACE, PK_COUNT };
 const char* const kProfNames[PK_COUNT] = {"k_shadow",       "k_pixels<shade>",       "k_shadow<accum>",
                                           "k_shadow_group", "k_shadow_group<accum>", "k_shadow_pool",
-                                          "k_shadow_pool<accum>", "k_accumulate", "k_shade_grad",
-                                          "k_pathtrace"};
+                                          "k_shadow_pool<accum>", "k_shadow_stream", "k_shadow_stream<accum>",
+                                          "k_accumulate", "k_shade_grad", "k_pathtrace"};
 static_assert(MODE_SHADOW == 0 && MODE_SHADE == 1 && MODE_SHADOW_ACCUM == 2 && MODE_SHADOW_G == 3 &&
-                  MODE_SHADOW_ACCUM_G == 4 && MODE_SHADOW_P == 5 && MODE_SHADOW_ACCUM_P == 6,
+                  MODE_SHADOW_ACCUM_G == 4 && MODE_SHADOW_P == 5 && MODE_SHADOW_ACCUM_P == 6 &&
+                  MODE_SHADOW_S == 7 && MODE_SHADOW_ACCUM_S == 8,
               "profile names follow the pass modes");
 
 cudaEvent_t prof_event(HyCtx* c) {
@@ -332,6 +333,8 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
         !(cfg->flags & HY_FLAG_PIXEL_PARALLEL)) {
         if (cfg->flags & HY_FLAG_RAY_POOL) {
             mode = mode == MODE_SHADOW ? MODE_SHADOW_P : MODE_SHADOW_ACCUM_P;
+        } else if (cfg->flags & HY_FLAG_TILE_STREAM) {
+            mode = mode == MODE_SHADOW ? MODE_SHADOW_S : MODE_SHADOW_ACCUM_S;
         } else {
             mode = mode == MODE_SHADOW ? MODE_SHADOW_G : MODE_SHADOW_ACCUM_G;
             uint32_t G = 2;
@@ -345,7 +348,8 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
     }
     // measured fastest on the 1080p workload: 6 resident blocks (80 registers)
     // for the lane-group kernel (1.4 % ahead of 8), 8 (64 registers) otherwise
-    const bool grouped = mode == MODE_SHADOW_G || mode == MODE_SHADOW_ACCUM_G;
+    const bool grouped = mode == MODE_SHADOW_G || mode == MODE_SHADOW_ACCUM_G || mode == MODE_SHADOW_S ||
+                         mode == MODE_SHADOW_ACCUM_S;
     int minb = cfg->min_blocks ? (int)cfg->min_blocks : (grouped ? 6 : 8);
     int grid = grid_for(c, mode, count, minb, block);
     grid = std::max(1, std::min<int>(grid, (int)((P.ntiles * 32ull + block - 1) / block)));

@@ -422,6 +422,128 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, co
     flush_stats(ls, P.stats);
 }
 
+// ---------------------------------------------------------------------------------
+// DECORRELATED shadow rays, light-major over a tile: a warp takes an 8x4 tile
+// and, light by light, traces all 32 x spp samples of its pixels, item
+// q = lane + 32 n (n < spp) being sample q % spp of pixel q / spp.  Lane i sets
+// up light l for pixel i (its G-buffer texel, the skip tests of
+// shadowRaygen.rgen:43-63) and publishes origin, direction, distance and RNG
+// state in shared memory; every lane then walks its spp items without waiting
+// for the others, counting unoccluded samples per pixel with shared-memory
+// atomics; once the warp's items for light l are all traced, lane i folds
+// pixel i's count into its factor.  A lane waits only at the end of a light
+// (for the slowest sum of spp rays) instead of after every pixel-light (for
+// the slowest single ray), and the samples in flight stay within a few
+// adjacent pixels of one light.  Seeds as in k_shadow_group (LCG jump-ahead),
+// so the rays equal those of k_shadow.
+// ---------------------------------------------------------------------------------
+template <bool COUNT, bool ACCUM, int MINB, bool TWO = false>
+__global__ void __launch_bounds__(128, MINB) k_shadow_stream(const SceneDev S, const PassParams P) {
+    __shared__ float4 sm_pos[128];   // per pixel of the warp's tile: position
+    __shared__ float4 sm_L[128];     // direction to the current light, distance
+    __shared__ uint2 sm_seed[128];   // TEA seed, rays traced before this light (0xffffffff: not traced)
+    __shared__ uint32_t sm_cnt[128]; // unoccluded samples of the current light
+    LaneStats ls;
+    const uint32_t lane = threadIdx.x & 31, wb = threadIdx.x & ~31u;
+    const size_t plane = (size_t)P.W * P.H;
+    const uint32_t spp = P.spp;
+    uint2 stk[kStackMax];
+    ShadowLane s;
+    Trav t;
+    RayPre r;
+    uint32_t chunk_cur = 0, chunk_end = 0, nn = 0, nt = 0;
+    for (;;) {
+        // ---- the warp's next tile ----
+        if (chunk_cur == chunk_end) {
+            uint32_t t0 = 0;
+            if (lane == 0) t0 = atomicAdd(P.queue, P.chunk);
+            t0 = __shfl_sync(0xffffffffu, t0, 0);
+            if (t0 >= P.ntiles) break;
+            chunk_cur = t0;
+            chunk_end = min(t0 + P.chunk, P.ntiles);
+        }
+        const uint32_t tile = chunk_cur++;
+        const uint32_t x = (tile % P.tiles_x) * 8 + (lane & 7), y = (tile / P.tiles_x) * 4 + (lane >> 3);
+        const bool present = x < P.W && y < P.H;
+        uint32_t seed0 = 0, rays_before = 0;
+        if (present) {
+            s.pix = y * P.W + x;
+            const float4 g0 = fetch_texel(P.plane[0], P.fmt[0], s.pix);
+            const float4 g1 = fetch_texel(P.plane[1], P.fmt[1], s.pix);
+            s.position = mk(g0.x, g0.y, g0.z);
+            s.N = normalize_rn(mk(__fsub_rn(__fmul_rn(g1.x, 2.0f), 1.0f), __fsub_rn(__fmul_rn(g1.y, 2.0f), 1.0f),
+                                  __fsub_rn(__fmul_rn(g1.z, 2.0f), 1.0f)));
+            const int mi = mat_index(g0.w, S.num_mats);
+            s.smode = mi >= 0 ? (int)S.mats[mi].smr[0] : 0;
+            s.in_blur = x < P.blur_w && y < P.blur_h;
+            seed0 = tea(s.pix, P.frame_u);
+            sm_pos[wb + lane] = make_float4(s.position.x, s.position.y, s.position.z, 0.f);
+        }
+        for (uint32_t l = 0; l < P.num_lights; l++) {
+            // ---- light l for this lane's pixel ----
+            bool traced = false;
+            s.light = l;
+            if (present) {
+                const LightGeo lg = light_geo(S.lights[l], s.position, s.N);
+                float v = -1.f;
+                if (s.smode == 4) v = 1.0f;
+                else if (!(lg.NdotL > 0.f)) v = 0.0f;
+                else if (!(lg.dist < lg.maxd)) v = 1.0f;
+                if (v >= 0.f) {
+                    shadow_finalize<ACCUM>(P, s, plane, v);
+                } else {
+                    traced = true;
+                    sm_L[wb + lane] = make_float4(lg.L.x, lg.L.y, lg.L.z, lg.dist);
+                }
+            }
+            sm_seed[wb + lane] = make_uint2(seed0, traced ? rays_before : 0xffffffffu);
+            sm_cnt[wb + lane] = 0;
+            const bool any = __ballot_sync(0xffffffffu, traced) != 0;
+            __syncwarp();
+            if (any) {
+                const float radius = S.lights[l].radius;
+                bool live = false;
+                uint32_t n = 0, cur = 0;
+                for (;;) {
+                    // ---- this lane's next item of a traced pixel ----
+                    while (!live && n < spp) {
+                        const uint32_t q = lane + 32u * n++;
+                        const uint32_t pi = q / spp, k = q - pi * spp;
+                        const uint2 sd = sm_seed[wb + pi];
+                        if (sd.y == 0xffffffffu) continue;
+                        const float4 pp = sm_pos[wb + pi], lp = sm_L[wb + pi];
+                        const f3 pos = mk(pp.x, pp.y, pp.z);
+                        uint32_t st = lcg_jump(sd.x, 2u * (sd.y + k));
+                        const f3 dir = sampleDisk(radius, pos, mk(lp.x, lp.y, lp.z), st);
+                        r = ray_pre(add_rn(pos, scale_rn(dir, 1e-1f)), dir);
+                        trav_init(t, r, __fadd_rn(lp.w, 1.0f));
+                        cur = pi;
+                        live = true;
+                        ls.shadow++;
+                    }
+                    // ---- up to P.inner node visits ----
+                    if (live) {
+                        for (uint32_t it = 0, ni = max(P.inner, 1u); it < ni; it++) {
+                            if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
+                                live = false;
+                                if (t.h.id == HY_NO_HIT) atomicAdd(&sm_cnt[wb + cur], 1u);
+                                break;
+                            }
+                        }
+                    }
+                    if (__ballot_sync(0xffffffffu, live || n < spp) == 0) break;
+                }
+                __syncwarp();
+                if (traced) shadow_finalize<ACCUM>(P, s, plane, __fdiv_rn((float)sm_cnt[wb + lane], (float)spp));
+            }
+            if (traced) rays_before += spp;
+            __syncwarp();  // the slots are rewritten by the next light's set-up
+        }
+    }
+    if (COUNT) { ls.nodes += nn; ls.tris += nt; }
+    flush_stats(ls, P.stats);
+}
+
 template <int MODE, bool COUNT>
 __global__ void __launch_bounds__(128) k_pixels(const SceneDev S, const PassParams P) {
     LaneStats ls;
@@ -1021,7 +1143,17 @@ static void* shadow_kernel_two(bool count, int minb) {
     return count ? (void*)k_shadow_group<true, ACCUM, 5, true> : (void*)k_shadow_group<false, ACCUM, 5, true>;
 }
 
+template <bool ACCUM>
+static void* stream_kernel(bool count, int minb, bool two) {
+    if (two) return count ? (void*)k_shadow_stream<true, ACCUM, 6, true> : (void*)k_shadow_stream<false, ACCUM, 6, true>;
+    if (minb >= 8) return count ? (void*)k_shadow_stream<true, ACCUM, 8> : (void*)k_shadow_stream<false, ACCUM, 8>;
+    if (minb >= 6) return count ? (void*)k_shadow_stream<true, ACCUM, 6> : (void*)k_shadow_stream<false, ACCUM, 6>;
+    return count ? (void*)k_shadow_stream<true, ACCUM, 5> : (void*)k_shadow_stream<false, ACCUM, 5>;
+}
+
 static void* pixel_kernel(int mode, bool count, int minb, bool two) {
+    if (mode == MODE_SHADOW_S) return stream_kernel<false>(count, minb, two);
+    if (mode == MODE_SHADOW_ACCUM_S) return stream_kernel<true>(count, minb, two);
     if (two) {
         switch (mode) {
             case MODE_SHADOW_G: return shadow_kernel_two<false>(count, minb);

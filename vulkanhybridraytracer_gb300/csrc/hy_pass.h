@@ -11,7 +11,7 @@ namespace hy {
 // groups per pixel-light; *_P: the same rays from a per-warp ray pool
 enum {
     MODE_SHADOW = 0, MODE_SHADE = 1, MODE_SHADOW_ACCUM = 2, MODE_SHADOW_G = 3, MODE_SHADOW_ACCUM_G = 4,
-    MODE_SHADOW_P = 5, MODE_SHADOW_ACCUM_P = 6
+    MODE_SHADOW_P = 5, MODE_SHADOW_ACCUM_P = 6, MODE_SHADOW_S = 7, MODE_SHADOW_ACCUM_S = 8
 };
 
 struct PassParams {
