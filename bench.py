@@ -48,8 +48,8 @@ def parse():
     ap.add_argument("--minb", type=int, default=0, help="shadow-kernel variant: resident blocks per SM")
     ap.add_argument("--group", type=int, default=0, help="lanes per pixel-light group (0: next power of 2 >= spp)")
     ap.add_argument("--visits", type=int, default=0, help="node visits per scheduling round of the shadow kernel")
-    ap.add_argument("--sched", default="groups", choices=["groups", "pool", "stream"],
-                    help="DECORRELATED shadow samples in fixed lane groups or from the per-warp ray pool")
+    ap.add_argument("--sched", default="stream", choices=["stream", "groups", "pool"],
+                    help="DECORRELATED shadow samples: tile streams, fixed lane groups or the per-warp ray pool")
     ap.add_argument("--workload", default="hd", choices=["hd", "batch", "diff", "pathtrace", "large"],
                     help="hd: the 1080p frame (headline); batch: 64 mixed views over 8 scenes, batched vs per "
                          "view; diff: 512x512 forward + adjoint; pathtrace: the path-traced mode at 1080p; "
@@ -630,7 +630,7 @@ def main():
     out_8 = torch.empty((wl.height, wl.width, 4), dtype=torch.uint8, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
-    sched = {"pool": L.HY_FLAG_RAY_POOL, "stream": L.HY_FLAG_TILE_STREAM}.get(args.sched, 0)
+    sched = {"pool": L.HY_FLAG_RAY_POOL, "groups": L.HY_FLAG_LANE_GROUPS}.get(args.sched, 0)
 
     def cfg(frame, flags=L.HY_FLAG_NO_STATUS_SYNC):
         return pass_config(spp=wl.spp, max_bounces=wl.max_bounces, rng_mode=wl.rng_mode, accum_frame=frame,
@@ -688,6 +688,7 @@ def main():
     shadow_bytes = sh_rays * 48 + 80 * sh_nodes + 48 * sh_tris + npx * (32 + 2 * L_)
     alg = {
         # G-buffer planes 0/1 (32 B/px), u8 history read + write per light
+        "k_shadow_stream<accum>": shadow_bytes,
         "k_shadow_group<accum>": shadow_bytes,
         "k_shadow_pool<accum>": shadow_bytes,
         # all six planes (88 B/px), RGBA32F + BGRA8 out, u8 history read per light

@@ -159,13 +159,15 @@ enum { HY_RNG_REFERENCE = 0, HY_RNG_DECORRELATED = 1 };
 #define HY_FLAG_NO_ACCUM           0x2u /* shade from the raw shadow images, no denoise pass */
 #define HY_FLAG_COUNT_TRAVERSAL    0x4u /* count BVH nodes visited / triangles tested into HyStats */
 #define HY_FLAG_NO_STATUS_SYNC     0x8u /* do not read back the status word (no host sync) */
-#define HY_FLAG_PIXEL_PARALLEL     0x10u /* one lane per pixel for DECORRELATED shadow rays (default: the
-                                            samples of a pixel-light start together on adjacent lanes) */
-#define HY_FLAG_RAY_POOL           0x20u /* those samples from a per-warp ray pool that refills each lane as
-                                            soon as its ray ends (default: a fixed lane group per pixel-light,
-                                            which waits for its slowest sample but stays more coherent) */
-#define HY_FLAG_TILE_STREAM        0x40u /* those samples light by light over a warp's 8x4 tile, each lane
-                                            walking its share without waiting per pixel-light */
+/* Schedules of DECORRELATED shadow rays with spp >= 2.  Default: tile streams — a
+ * warp takes an 8x4 tile and, light by light, its lanes walk the tile's 32 x spp
+ * samples (adjacent lanes on samples of the same or a neighbouring pixel), each
+ * lane without waiting for the others until the light is done. */
+#define HY_FLAG_PIXEL_PARALLEL     0x10u /* one lane per pixel, lights and samples in turn */
+#define HY_FLAG_RAY_POOL           0x20u /* the samples of a pixel-light from a per-warp ray pool that refills
+                                            each lane as soon as its ray ends */
+#define HY_FLAG_LANE_GROUPS        0x40u /* the samples of a pixel-light on a fixed group of adjacent lanes,
+                                            which waits for its slowest sample before the next pixel-light */
 
 typedef struct HyPassConfig {
     uint32_t shadow_spp;    /* samplesBuffer.samples (1..64, src/renderer.cpp:656) */

@@ -51,10 +51,13 @@ def _views(ctxs, frame0, seed=0):
     return views
 
 
-@pytest.mark.parametrize("graph", [False, True])
-def test_batch_equals_per_view(two_scenes, graph):
+@pytest.mark.parametrize("graph,sched", [(False, 0), (True, 0), (False, L.HY_FLAG_LANE_GROUPS),
+                                         (True, L.HY_FLAG_LANE_GROUPS)])
+def test_batch_equals_per_view(two_scenes, graph, sched):
     import torch
+    from vulkanhybridraytracer_gb300.hybrid import pass_config
     runner, ctxs = two_scenes
+    tuning = pass_config(1, flags=sched)
     scene_ctx = [c for c, _ in ctxs]
     for rep in range(3):   # the graph is captured once, then replayed with new frames
         views = _views(ctxs, 3 + 5 * rep, seed=rep)
@@ -66,7 +69,7 @@ def test_batch_equals_per_view(two_scenes, graph):
             st = scene_ctx[v["scene"]].forward(v["planes"], v["camera"], v["config"], h, out_f=of, out_8=o8)
             ref.append((h, of, o8, st))
         torch.cuda.synchronize()
-        st = runner.batch_forward(scene_ctx, views, graph=graph)
+        st = runner.batch_forward(scene_ctx, views, graph=graph, tuning=tuning)
         torch.cuda.synchronize()
         assert st["error_flags"] == 0
         for v, (h, of, o8, st1) in zip(views, ref):

@@ -402,11 +402,11 @@ def test_group_kernel_equals_pixel_kernel(small, spp):
     sc = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, L.HY_FLAG_RAY_POOL), c)
     e = torch.zeros_like(a)
     torch.cuda.synchronize()
-    se = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, L.HY_FLAG_TILE_STREAM), e)
+    se = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, L.HY_FLAG_LANE_GROUPS), e)
     assert torch.equal(a, b) and torch.equal(a, c) and torch.equal(a, e)
     assert sa["shadow_rays"] == sb["shadow_rays"] == sc["shadow_rays"] == se["shadow_rays"] > 0
     # the same schedules with one node visit per round, and the tile streams at each register cap
-    for flags, minb, visits in ((0, 0, 1), (L.HY_FLAG_TILE_STREAM, 5, 1), (L.HY_FLAG_TILE_STREAM, 8, 3)):
+    for flags, minb, visits in ((L.HY_FLAG_LANE_GROUPS, 0, 1), (0, 5, 1), (0, 6, 3), (0, 8, 16)):
         f = torch.zeros_like(a)
         torch.cuda.synchronize()
         small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, flags, min_blocks=minb,
@@ -422,9 +422,9 @@ def test_group_kernel_equals_pixel_kernel(small, spp):
 
 @pytest.mark.parametrize("frame", [0, 3])
 def test_tile_stream_forward_equals_groups(small, frame):
-    """The light-major tile schedule (HY_FLAG_TILE_STREAM), raw images and the
-    fused running-mean variant alike, gives the same history and image as the
-    lane groups, bit for bit."""
+    """The light-major tile schedule (the default), raw images and the fused
+    running-mean variant alike, gives the same history and image as the lane
+    groups (HY_FLAG_LANE_GROUPS), bit for bit."""
     from vulkanhybridraytracer_gb300.hybrid import pass_config
     torch = _torch()
     wl = small.wl
@@ -433,7 +433,7 @@ def test_tile_stream_forward_equals_groups(small, frame):
     planes = [torch.from_numpy(x).cuda() for x in small.orc.gbuffer(cam, W, H)]
     h0 = torch.randint(0, 256, (nl, H, W), dtype=torch.uint8, generator=torch.Generator().manual_seed(frame)).cuda()
     outs = []
-    for flags in (0, L.HY_FLAG_TILE_STREAM):
+    for flags in (L.HY_FLAG_LANE_GROUPS, 0):
         h = h0.clone()
         o = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
         torch.cuda.synchronize()

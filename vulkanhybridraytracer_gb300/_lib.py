@@ -38,7 +38,7 @@ HY_FLAG_COUNT_TRAVERSAL = 0x4
 HY_FLAG_NO_STATUS_SYNC = 0x8
 HY_FLAG_PIXEL_PARALLEL = 0x10
 HY_FLAG_RAY_POOL = 0x20
-HY_FLAG_TILE_STREAM = 0x40
+HY_FLAG_LANE_GROUPS = 0x40
 HY_NO_HIT = 0xFFFFFFFF
 
 HY_STATUS_STACK_OVERFLOW = 0x1

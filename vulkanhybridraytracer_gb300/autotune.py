@@ -2,7 +2,8 @@
 
 Times a workload under each candidate launch shape — queue chunk (8x4 tiles
 a warp pulls per atomic: 32..1024 pixels) and register cap of the shadow
-kernel (5 or 8 resident 128-thread blocks per SM, i.e. 96 or 64 registers)
+kernel (5, 6 or 8 resident 128-thread blocks per SM, i.e. 96, 80 or 64
+registers)
 — and keeps the fastest.  Results are cached on disk per GPU name and
 workload signature, so a workload is tuned once per machine.
 """
@@ -14,7 +15,7 @@ import time
 from pathlib import Path
 
 CHUNKS = (1, 2, 4, 8, 16, 32)       # tiles per queue pull: 32 .. 1024 pixels
-MIN_BLOCKS = (5, 8)
+MIN_BLOCKS = (5, 6, 8)
 
 DEFAULT_CACHE = Path(os.environ.get("HY_AUTOTUNE_CACHE", Path.home() / ".cache" / "hybridrt_autotune.json"))
 

@@ -271,7 +271,9 @@ PassParams make_params(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const
     P.ntiles = P.tiles_x * ((P.H + 3) / 4);
     P.chunk = cfg->queue_chunk ? cfg->queue_chunk : 1;
     // node visits per scheduling round of the persistent shadow kernels: 4
-    // measured 9.5 % ahead of 1 on the 1080p workload (2: 6.8 %, 3: 8.8 %, 8: 8.9 %)
+    // measured 9.5 % ahead of 1 for the lane groups on the 1080p workload
+    // (2: 6.8 %, 3: 8.8 %, 8: 8.9 %); the tile streams default to 8 (at 8
+    // resident blocks: 4: -3.9 %, 6: -1.7 %, 12: -3.6 %, 16: -2.7 %)
     P.inner = cfg->visits_per_round ? std::min(cfg->visits_per_round, 16u) : 4u;
     if (cfg->flags & HY_FLAG_FULL_BLUR_DISPATCH) { P.blur_w = P.W; P.blur_h = P.H; }
     else { P.blur_w = (P.W / 16) * 16; P.blur_h = (P.H / 16) * 16; }
@@ -333,7 +335,7 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
         !(cfg->flags & HY_FLAG_PIXEL_PARALLEL)) {
         if (cfg->flags & HY_FLAG_RAY_POOL) {
             mode = mode == MODE_SHADOW ? MODE_SHADOW_P : MODE_SHADOW_ACCUM_P;
-        } else if (cfg->flags & HY_FLAG_TILE_STREAM) {
+        } else if (!(cfg->flags & HY_FLAG_LANE_GROUPS)) {
             mode = mode == MODE_SHADOW ? MODE_SHADOW_S : MODE_SHADOW_ACCUM_S;
         } else {
             mode = mode == MODE_SHADOW ? MODE_SHADOW_G : MODE_SHADOW_ACCUM_G;
@@ -347,10 +349,12 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
         }
     }
     // measured fastest on the 1080p workload: 6 resident blocks (80 registers)
-    // for the lane-group kernel (1.4 % ahead of 8), 8 (64 registers) otherwise
-    const bool grouped = mode == MODE_SHADOW_G || mode == MODE_SHADOW_ACCUM_G || mode == MODE_SHADOW_S ||
-                         mode == MODE_SHADOW_ACCUM_S;
+    // for the lane-group kernel (1.4 % ahead of 8), 8 (64 registers) otherwise;
+    // 8 node visits per round for the tile streams (4 for the others)
+    const bool grouped = mode == MODE_SHADOW_G || mode == MODE_SHADOW_ACCUM_G;
+    const bool streams = mode == MODE_SHADOW_S || mode == MODE_SHADOW_ACCUM_S;
     int minb = cfg->min_blocks ? (int)cfg->min_blocks : (grouped ? 6 : 8);
+    if (streams && !cfg->visits_per_round) P.inner = 8;
     int grid = grid_for(c, mode, count, minb, block);
     grid = std::max(1, std::min<int>(grid, (int)((P.ntiles * 32ull + block - 1) / block)));
     ProfScope prof(c, mode);
@@ -926,27 +930,27 @@ int hy_hybrid_forward_host(HyCtx* c, const HyGBuffer* hgb, const HyCamera* cam, 
 // ---- batches -------------------------------------------------------------------
 static int batch_enqueue(HyCtx* c, const std::vector<PassParams>& pv, const std::vector<SceneDev>& sd,
                          const HyView* views, const std::vector<uint32_t>& reset_views, const BatchParams& B,
-                         bool count, int minb, size_t tab_bytes) {
+                         bool count, int minb, bool stream, size_t tab_bytes) {
     cudaStream_t s = c->stream;
     HY_CUDA_TRY(cudaMemcpyAsync(c->batch_tab.p, c->h_batch_tab, tab_bytes, cudaMemcpyHostToDevice, s));
     HY_CUDA_TRY(cudaMemsetAsync(c->dstats.p, 0, c->dstats.bytes, s));
     int per = 0;
-    if (batch_occupancy(false, count, minb, &per) != cudaSuccess || per <= 0) per = 1;
+    if (batch_occupancy(false, count, minb, stream, &per) != cudaSuccess || per <= 0) per = 1;
     int grid = std::max(1, std::min<int>(per * c->num_sms, (int)((B.total_tiles * 32ull + 127) / 128)));
     BatchParams Bs = B;
     Bs.queue = dev_queue(c, WQ_SHADOW);
-    HY_CUDA_TRY(launch_batch(false, count, minb, Bs, grid, s));
+    HY_CUDA_TRY(launch_batch(false, count, minb, stream, Bs, grid, s));
     for (uint32_t v : reset_views) {
         const HyView& vw = views[v];
         HyAccum acc = vw.accum;
         int rc = accumulate_impl(c, &vw.gbuffer, &vw.config, pv[v].shadow, &acc);
         if (rc) return rc;
     }
-    if (batch_occupancy(true, count, minb, &per) != cudaSuccess || per <= 0) per = 1;
+    if (batch_occupancy(true, count, minb, false, &per) != cudaSuccess || per <= 0) per = 1;
     grid = std::max(1, std::min<int>(per * c->num_sms, (int)((B.total_tiles * 32ull + 127) / 128)));
     BatchParams Bh = B;
     Bh.queue = dev_queue(c, WQ_SHADE);
-    HY_CUDA_TRY(launch_batch(true, count, minb, Bh, grid, s));
+    HY_CUDA_TRY(launch_batch(true, count, minb, false, Bh, grid, s));
     (void)sd;
     return HY_OK;
 }
@@ -965,6 +969,7 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
     const bool count = tuning && (tuning->flags & HY_FLAG_COUNT_TRAVERSAL);
     const uint32_t chunk = tuning && tuning->queue_chunk ? tuning->queue_chunk : 1;
     const int minb = tuning && tuning->min_blocks ? (int)tuning->min_blocks : 8;
+    const bool stream = !(tuning && (tuning->flags & HY_FLAG_LANE_GROUPS));
     // per-view parameters
     std::vector<PassParams> pv(nv);
     std::vector<uint32_t> reset_views;
@@ -993,6 +998,7 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
                             v.out_rgba32f, v.out_bgra8);
         pv[i].scene = v.scene;
         pv[i].num_lights = v.accum.num_lights;
+        if (stream && !v.config.visits_per_round) pv[i].inner = 8;
         uint32_t G = 1;
         if (v.config.rng_mode == HY_RNG_DECORRELATED)
             while (G < v.config.shadow_spp && G < 32) G <<= 1;
@@ -1047,10 +1053,11 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
     B.status = dev_status(c);
     B.queue = nullptr;
     if (bflags & HY_BATCH_NO_GRAPH) {
-        if ((rc = batch_enqueue(c, pv, sd, views, reset_views, B, count, minb, tab_bytes))) return rc;
+        if ((rc = batch_enqueue(c, pv, sd, views, reset_views, B, count, minb, stream, tab_bytes))) return rc;
     } else {
         // the graph bakes pointers of the tables, scratch and reset-view launches
-        std::vector<uint64_t> key = {nv, ns, total, chunk, (uint64_t)minb, (uint64_t)count, (uint64_t)(uintptr_t)c->batch_tab.p,
+        std::vector<uint64_t> key = {nv, ns, total, chunk, (uint64_t)minb, (uint64_t)count, (uint64_t)stream,
+                                     (uint64_t)(uintptr_t)c->batch_tab.p,
                                      (uint64_t)(uintptr_t)c->h_batch_tab, (uint64_t)(uintptr_t)c->raw_shadow.p,
                                      (uint64_t)(uintptr_t)c->hist_prev.p, (uint64_t)(uintptr_t)c->stream};
         for (uint32_t v : reset_views) {
@@ -1067,7 +1074,7 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
             c->batch_key.clear();
             cudaGraph_t graph = nullptr;
             HY_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            rc = batch_enqueue(c, pv, sd, views, reset_views, B, count, minb, tab_bytes);
+            rc = batch_enqueue(c, pv, sd, views, reset_views, B, count, minb, stream, tab_bytes);
             cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
             if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
             if (e != cudaSuccess) { cudaGetLastError(); return HY_ERR_CUDA; }

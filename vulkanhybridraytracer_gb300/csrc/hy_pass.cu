@@ -437,23 +437,138 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, co
 // adjacent pixels of one light.  Seeds as in k_shadow_group (LCG jump-ahead),
 // so the rays equal those of k_shadow.
 // ---------------------------------------------------------------------------------
-template <bool COUNT, bool ACCUM, int MINB, bool TWO = false>
-__global__ void __launch_bounds__(128, MINB) k_shadow_stream(const SceneDev S, const PassParams P) {
-    __shared__ float4 sm_pos[128];   // per pixel of the warp's tile: position
-    __shared__ float4 sm_L[128];     // direction to the current light, distance
-    __shared__ uint2 sm_seed[128];   // TEA seed, rays traced before this light (0xffffffff: not traced)
-    __shared__ uint32_t sm_cnt[128]; // unoccluded samples of the current light
-    LaneStats ls;
+// Per-warp shared state of the tile streams: per pixel of the warp's tile its
+// position, the direction to the current light and distance, the TEA seed and
+// rays traced before this light (0xffffffff: not traced), the unoccluded count.
+struct StreamSlots {
+    float4 pos[128];
+    float4 L[128];
+    uint2 seed[128];
+    uint32_t cnt[128];
+};
+
+// One 8x4 tile of a view, light by light.  ACC: 0 raw shadow images, 1 the
+// running mean into the history, 2 either (accum) at run time.  reference:
+// REFERENCE RNG (one ray per pixel-light from the pixel's seed, by value).
+template <bool COUNT, bool TWO, int ACC>
+__device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams& P, uint32_t tile, bool reference,
+                                            bool accum, StreamSlots& sm, uint2* stk, Trav& t, RayPre& r,
+                                            ShadowLane& s, LaneStats& ls, uint32_t& nn, uint32_t& nt) {
     const uint32_t lane = threadIdx.x & 31, wb = threadIdx.x & ~31u;
     const size_t plane = (size_t)P.W * P.H;
-    const uint32_t spp = P.spp;
+    const uint32_t spp = P.spp, nrays = reference ? 1u : spp;
+    const uint32_t x = (tile % P.tiles_x) * 8 + (lane & 7), y = (tile / P.tiles_x) * 4 + (lane >> 3);
+    const bool present = x < P.W && y < P.H;
+    auto finalize = [&](float v) {
+        if (ACC == 0 || (ACC == 2 && !accum)) shadow_finalize<false>(P, s, plane, v);
+        else shadow_finalize<true>(P, s, plane, v);
+    };
+    uint32_t seed0 = 0, rays_before = 0;
+    if (present) {
+        s.pix = y * P.W + x;
+        const float4 g0 = fetch_texel(P.plane[0], P.fmt[0], s.pix);
+        const float4 g1 = fetch_texel(P.plane[1], P.fmt[1], s.pix);
+        s.position = mk(g0.x, g0.y, g0.z);
+        s.N = normalize_rn(mk(__fsub_rn(__fmul_rn(g1.x, 2.0f), 1.0f), __fsub_rn(__fmul_rn(g1.y, 2.0f), 1.0f),
+                              __fsub_rn(__fmul_rn(g1.z, 2.0f), 1.0f)));
+        const int mi = mat_index(g0.w, S.num_mats);
+        s.smode = mi >= 0 ? (int)S.mats[mi].smr[0] : 0;
+        s.in_blur = x < P.blur_w && y < P.blur_h;
+        seed0 = tea(s.pix, P.frame_u);
+        sm.pos[wb + lane] = make_float4(s.position.x, s.position.y, s.position.z, 0.f);
+    }
+    for (uint32_t l = 0; l < P.num_lights; l++) {
+        // ---- light l for this lane's pixel ----
+        bool traced = false;
+        s.light = l;
+        if (present) {
+            const LightGeo lg = light_geo(S.lights[l], s.position, s.N);
+            float v = -1.f;
+            if (s.smode == 4) v = 1.0f;
+            else if (!(lg.NdotL > 0.f)) v = 0.0f;
+            else if (!(lg.dist < lg.maxd)) v = 1.0f;
+            if (v >= 0.f) {
+                finalize(v);
+            } else {
+                traced = true;
+                sm.L[wb + lane] = make_float4(lg.L.x, lg.L.y, lg.L.z, lg.dist);
+            }
+        }
+        sm.seed[wb + lane] = make_uint2(seed0, traced ? rays_before : 0xffffffffu);
+        sm.cnt[wb + lane] = 0;
+        const bool any = __ballot_sync(0xffffffffu, traced) != 0;
+        __syncwarp();
+        if (any) {
+            const float radius = S.lights[l].radius;
+            bool live = false;
+            uint32_t n = 0, cur = 0;
+            for (;;) {
+                // ---- this lane's next item of a traced pixel: q = lane + 32 n is
+                //      sample q % nrays of pixel q / nrays ----
+                while (!live && n < nrays) {
+                    const uint32_t q = lane + 32u * n++;
+                    const uint32_t pi = q / nrays, k = q - pi * nrays;
+                    const uint2 sd = sm.seed[wb + pi];
+                    if (sd.y == 0xffffffffu) continue;
+                    const float4 pp = sm.pos[wb + pi], lp = sm.L[wb + pi];
+                    const f3 pos = mk(pp.x, pp.y, pp.z);
+                    uint32_t st = reference ? sd.x : lcg_jump(sd.x, 2u * (sd.y + k));
+                    const f3 dir = sampleDisk(radius, pos, mk(lp.x, lp.y, lp.z), st);
+                    r = ray_pre(add_rn(pos, scale_rn(dir, 1e-1f)), dir);
+                    trav_init(t, r, __fadd_rn(lp.w, 1.0f));
+                    cur = pi;
+                    live = true;
+                    ls.shadow++;
+                }
+                // ---- up to P.inner node visits ----
+                if (live) {
+                    for (uint32_t it = 0, ni = max(P.inner, 1u); it < ni; it++) {
+                        if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
+                            live = false;
+                            if (t.h.id == HY_NO_HIT) atomicAdd(&sm.cnt[wb + cur], 1u);
+                            break;
+                        }
+                    }
+                }
+                if (__ballot_sync(0xffffffffu, live || n < nrays) == 0) break;
+            }
+            __syncwarp();
+            if (traced) {
+                const uint32_t unocc = sm.cnt[wb + lane];
+                finalize(reference ? (float)unocc : __fdiv_rn((float)unocc, (float)spp));
+            }
+        }
+        if (traced) rays_before += spp;
+        __syncwarp();  // the slots are rewritten by the next light's set-up
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// DECORRELATED shadow rays, light-major over a tile: a warp takes an 8x4 tile
+// and, light by light, traces all 32 x spp samples of its pixels, item
+// q = lane + 32 n (n < spp) being sample q % spp of pixel q / spp.  Lane i sets
+// up light l for pixel i (its G-buffer texel, the skip tests of
+// shadowRaygen.rgen:43-63) and publishes origin, direction, distance and RNG
+// state in shared memory; every lane then walks its spp items without waiting
+// for the others, counting unoccluded samples per pixel with shared-memory
+// atomics; once the warp's items for light l are all traced, lane i folds
+// pixel i's count into its factor.  A lane waits only at the end of a light
+// (for the slowest sum of spp rays) instead of after every pixel-light (for
+// the slowest single ray), and the samples in flight stay within a few
+// adjacent pixels of one light.  Seeds as in k_shadow_group (LCG jump-ahead),
+// so the rays equal those of k_shadow.
+// ---------------------------------------------------------------------------------
+template <bool COUNT, bool ACCUM, int MINB, bool TWO = false>
+__global__ void __launch_bounds__(128, MINB) k_shadow_stream(const SceneDev S, const PassParams P) {
+    __shared__ StreamSlots sm;
+    LaneStats ls;
+    const uint32_t lane = threadIdx.x & 31;
     uint2 stk[kStackMax];
     ShadowLane s;
     Trav t;
     RayPre r;
     uint32_t chunk_cur = 0, chunk_end = 0, nn = 0, nt = 0;
     for (;;) {
-        // ---- the warp's next tile ----
         if (chunk_cur == chunk_end) {
             uint32_t t0 = 0;
             if (lane == 0) t0 = atomicAdd(P.queue, P.chunk);
@@ -462,83 +577,7 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_stream(const SceneDev S, c
             chunk_cur = t0;
             chunk_end = min(t0 + P.chunk, P.ntiles);
         }
-        const uint32_t tile = chunk_cur++;
-        const uint32_t x = (tile % P.tiles_x) * 8 + (lane & 7), y = (tile / P.tiles_x) * 4 + (lane >> 3);
-        const bool present = x < P.W && y < P.H;
-        uint32_t seed0 = 0, rays_before = 0;
-        if (present) {
-            s.pix = y * P.W + x;
-            const float4 g0 = fetch_texel(P.plane[0], P.fmt[0], s.pix);
-            const float4 g1 = fetch_texel(P.plane[1], P.fmt[1], s.pix);
-            s.position = mk(g0.x, g0.y, g0.z);
-            s.N = normalize_rn(mk(__fsub_rn(__fmul_rn(g1.x, 2.0f), 1.0f), __fsub_rn(__fmul_rn(g1.y, 2.0f), 1.0f),
-                                  __fsub_rn(__fmul_rn(g1.z, 2.0f), 1.0f)));
-            const int mi = mat_index(g0.w, S.num_mats);
-            s.smode = mi >= 0 ? (int)S.mats[mi].smr[0] : 0;
-            s.in_blur = x < P.blur_w && y < P.blur_h;
-            seed0 = tea(s.pix, P.frame_u);
-            sm_pos[wb + lane] = make_float4(s.position.x, s.position.y, s.position.z, 0.f);
-        }
-        for (uint32_t l = 0; l < P.num_lights; l++) {
-            // ---- light l for this lane's pixel ----
-            bool traced = false;
-            s.light = l;
-            if (present) {
-                const LightGeo lg = light_geo(S.lights[l], s.position, s.N);
-                float v = -1.f;
-                if (s.smode == 4) v = 1.0f;
-                else if (!(lg.NdotL > 0.f)) v = 0.0f;
-                else if (!(lg.dist < lg.maxd)) v = 1.0f;
-                if (v >= 0.f) {
-                    shadow_finalize<ACCUM>(P, s, plane, v);
-                } else {
-                    traced = true;
-                    sm_L[wb + lane] = make_float4(lg.L.x, lg.L.y, lg.L.z, lg.dist);
-                }
-            }
-            sm_seed[wb + lane] = make_uint2(seed0, traced ? rays_before : 0xffffffffu);
-            sm_cnt[wb + lane] = 0;
-            const bool any = __ballot_sync(0xffffffffu, traced) != 0;
-            __syncwarp();
-            if (any) {
-                const float radius = S.lights[l].radius;
-                bool live = false;
-                uint32_t n = 0, cur = 0;
-                for (;;) {
-                    // ---- this lane's next item of a traced pixel ----
-                    while (!live && n < spp) {
-                        const uint32_t q = lane + 32u * n++;
-                        const uint32_t pi = q / spp, k = q - pi * spp;
-                        const uint2 sd = sm_seed[wb + pi];
-                        if (sd.y == 0xffffffffu) continue;
-                        const float4 pp = sm_pos[wb + pi], lp = sm_L[wb + pi];
-                        const f3 pos = mk(pp.x, pp.y, pp.z);
-                        uint32_t st = lcg_jump(sd.x, 2u * (sd.y + k));
-                        const f3 dir = sampleDisk(radius, pos, mk(lp.x, lp.y, lp.z), st);
-                        r = ray_pre(add_rn(pos, scale_rn(dir, 1e-1f)), dir);
-                        trav_init(t, r, __fadd_rn(lp.w, 1.0f));
-                        cur = pi;
-                        live = true;
-                        ls.shadow++;
-                    }
-                    // ---- up to P.inner node visits ----
-                    if (live) {
-                        for (uint32_t it = 0, ni = max(P.inner, 1u); it < ni; it++) {
-                            if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
-                                live = false;
-                                if (t.h.id == HY_NO_HIT) atomicAdd(&sm_cnt[wb + cur], 1u);
-                                break;
-                            }
-                        }
-                    }
-                    if (__ballot_sync(0xffffffffu, live || n < spp) == 0) break;
-                }
-                __syncwarp();
-                if (traced) shadow_finalize<ACCUM>(P, s, plane, __fdiv_rn((float)sm_cnt[wb + lane], (float)spp));
-            }
-            if (traced) rays_before += spp;
-            __syncwarp();  // the slots are rewritten by the next light's set-up
-        }
+        stream_tile<COUNT, TWO, ACCUM ? 1 : 0>(S, P, chunk_cur++, false, ACCUM, sm, stk, t, r, s, ls, nn, nt);
     }
     if (COUNT) { ls.nodes += nn; ls.tris += nt; }
     flush_stats(ls, P.stats);
@@ -898,6 +937,42 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_batch(const BatchParams B)
     flush_stats(ls, B.stats);
 }
 
+// The batch over tile streams: a warp pulls (view, tile) units from the
+// batch's queue and walks each tile light by light (stream_tile) with that
+// view's parameters; REFERENCE-RNG views trace one ray per pixel-light.
+template <bool COUNT, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_shadow_batch_stream(const BatchParams B) {
+    __shared__ uint32_t s_begin[kMaxBatchViews + 1];
+    __shared__ StreamSlots sm;
+    for (uint32_t i = threadIdx.x; i <= B.nviews; i += blockDim.x)
+        s_begin[i] = i < B.nviews ? B.views[i].tile_begin : B.total_tiles;
+    __syncthreads();
+    LaneStats ls;
+    const uint32_t lane = threadIdx.x & 31;
+    uint2 stk[kStackMax];
+    ShadowLane s;
+    Trav t;
+    RayPre r;
+    uint32_t chunk_cur = 0, chunk_end = 0, nn = 0, nt = 0;
+    for (;;) {
+        if (chunk_cur == chunk_end) {
+            uint32_t t0 = 0;
+            if (lane == 0) t0 = atomicAdd(B.queue, B.chunk);
+            t0 = __shfl_sync(0xffffffffu, t0, 0);
+            if (t0 >= B.total_tiles) break;
+            chunk_cur = t0;
+            chunk_end = min(t0 + B.chunk, B.total_tiles);
+        }
+        const uint32_t unit = chunk_cur++;
+        const PassParams& P = B.views[view_of_tile(s_begin, B.nviews, unit)];
+        const bool accum = !(P.flags & HY_FLAG_NO_ACCUM) && P.accum_frame > 0;
+        stream_tile<COUNT, false, 2>(B.scenes[P.scene], P, unit - P.tile_begin, P.rng_mode == HY_RNG_REFERENCE, accum,
+                                     sm, stk, t, r, s, ls, nn, nt);
+    }
+    if (COUNT) { ls.nodes += nn; ls.tris += nt; }
+    flush_stats(ls, B.stats);
+}
+
 template <bool COUNT>
 __global__ void __launch_bounds__(128) k_pixels_batch(const BatchParams B);
 
@@ -1217,19 +1292,26 @@ cudaError_t launch_gbuffer(const SceneDev& S, const GbufParams& G, cudaStream_t 
     return cudaGetLastError();
 }
 
-static void* batch_kernel(bool shade, bool count, int minb) {
+static void* batch_kernel(bool shade, bool count, int minb, bool stream) {
     if (shade) return count ? (void*)k_pixels_batch<true> : (void*)k_pixels_batch<false>;
+    if (stream) {
+        if (minb >= 8) return count ? (void*)k_shadow_batch_stream<true, 8> : (void*)k_shadow_batch_stream<false, 8>;
+        if (minb >= 6) return count ? (void*)k_shadow_batch_stream<true, 6> : (void*)k_shadow_batch_stream<false, 6>;
+        return count ? (void*)k_shadow_batch_stream<true, 5> : (void*)k_shadow_batch_stream<false, 5>;
+    }
     if (minb >= 8) return count ? (void*)k_shadow_batch<true, 8> : (void*)k_shadow_batch<false, 8>;
     return count ? (void*)k_shadow_batch<true, 5> : (void*)k_shadow_batch<false, 5>;
 }
 
-cudaError_t launch_batch(bool shade, bool count, int minb, const BatchParams& B, int grid, cudaStream_t s) {
+cudaError_t launch_batch(bool shade, bool count, int minb, bool stream, const BatchParams& B, int grid,
+                         cudaStream_t s) {
     void* args[] = {(void*)&B};
-    return cudaLaunchKernel(batch_kernel(shade, count, minb), dim3(grid), dim3(128), args, 0, s);
+    return cudaLaunchKernel(batch_kernel(shade, count, minb, stream), dim3(grid), dim3(128), args, 0, s);
 }
 
-cudaError_t batch_occupancy(bool shade, bool count, int minb, int* blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, batch_kernel(shade, count, minb), 128, 0);
+cudaError_t batch_occupancy(bool shade, bool count, int minb, bool stream, int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, batch_kernel(shade, count, minb, stream), 128,
+                                                         0);
 }
 
 }  // namespace hy
