@@ -351,7 +351,7 @@ def run_large(args):
 
     def cfg(frame, flags=L.HY_FLAG_NO_STATUS_SYNC):
         return pass_config(spp=1, max_bounces=wl.max_bounces, rng_mode=L.HY_RNG_DECORRELATED, accum_frame=frame,
-                           flags=flags, min_blocks=args.minb)
+                           flags=flags, min_blocks=args.minb, visits_per_round=args.visits)
 
     st = ctx.forward(planes, wl.camera(0.0), cfg(0, 0), hist, L.HY_ACCUM_U8, out_f=outf, out_8=out8)
     rays = st["shadow_rays"] + st["reflection_rays"] + st["hit_shadow_rays"]
