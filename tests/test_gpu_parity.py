@@ -442,3 +442,23 @@ def test_tile_stream_forward_equals_groups(small, frame):
     (ha, oa, sa), (hb, ob, sb) = outs
     assert torch.equal(ha, hb) and torch.equal(oa, ob)
     assert sa["shadow_rays"] == sb["shadow_rays"] > 0 and sb["error_flags"] == 0
+
+
+@pytest.mark.parametrize("rng_mode,spp", [(L.HY_RNG_REFERENCE, 1), (L.HY_RNG_REFERENCE, 8),
+                                          (L.HY_RNG_DECORRELATED, 1)])
+def test_tile_stream_one_ray_per_pixel_light(small, rng_mode, spp):
+    """REFERENCE RNG (all samples one ray) and spp = 1 also go through the tile
+    streams by default: the same images as one lane per pixel."""
+    from vulkanhybridraytracer_gb300.hybrid import pass_config
+    torch = _torch()
+    wl = small.wl
+    W, H, nl = wl.width, wl.height, len(wl.scene.lights)
+    cam = wl.camera(2.0)
+    planes = [torch.from_numpy(x).cuda() for x in small.orc.gbuffer(cam, W, H)]
+    a = torch.zeros((nl, H, W), dtype=torch.uint8, device="cuda")
+    b = torch.zeros_like(a)
+    torch.cuda.synchronize()
+    sa = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, rng_mode, 2, 0), a)
+    sb = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, rng_mode, 2, L.HY_FLAG_PIXEL_PARALLEL), b)
+    assert torch.equal(a, b)
+    assert sa["shadow_rays"] == sb["shadow_rays"] > 0

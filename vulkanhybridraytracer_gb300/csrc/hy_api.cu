@@ -328,14 +328,14 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
     if (c->two_level && (cfg->flags & HY_FLAG_RAY_POOL)) return HY_ERR_UNSUPPORTED;
     PassParams P = P0;
     P.queue = dev_queue(c, queue_slot);
-    // DECORRELATED samples of one pixel-light start together on adjacent lanes:
-    // in fixed lane groups (measured fastest), or (HY_FLAG_RAY_POOL) from the
-    // per-warp ray pool
-    if ((mode == MODE_SHADOW || mode == MODE_SHADOW_ACCUM) && P.rng_mode == HY_RNG_DECORRELATED && P.spp >= 2 &&
-        !(cfg->flags & HY_FLAG_PIXEL_PARALLEL)) {
-        if (cfg->flags & HY_FLAG_RAY_POOL) {
+    // shadow schedules: tile streams (the default, any RNG mode and spp), or for
+    // DECORRELATED spp >= 2 the lane groups / the per-warp ray pool on request,
+    // or one lane per pixel (HY_FLAG_PIXEL_PARALLEL)
+    const bool sampled = P.rng_mode == HY_RNG_DECORRELATED && P.spp >= 2;
+    if ((mode == MODE_SHADOW || mode == MODE_SHADOW_ACCUM) && !(cfg->flags & HY_FLAG_PIXEL_PARALLEL)) {
+        if (sampled && (cfg->flags & HY_FLAG_RAY_POOL)) {
             mode = mode == MODE_SHADOW ? MODE_SHADOW_P : MODE_SHADOW_ACCUM_P;
-        } else if (!(cfg->flags & HY_FLAG_LANE_GROUPS)) {
+        } else if (!sampled || !(cfg->flags & HY_FLAG_LANE_GROUPS)) {
             mode = mode == MODE_SHADOW ? MODE_SHADOW_S : MODE_SHADOW_ACCUM_S;
         } else {
             mode = mode == MODE_SHADOW ? MODE_SHADOW_G : MODE_SHADOW_ACCUM_G;

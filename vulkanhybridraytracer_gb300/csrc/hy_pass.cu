@@ -423,20 +423,6 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, co
 }
 
 // ---------------------------------------------------------------------------------
-// DECORRELATED shadow rays, light-major over a tile: a warp takes an 8x4 tile
-// and, light by light, traces all 32 x spp samples of its pixels, item
-// q = lane + 32 n (n < spp) being sample q % spp of pixel q / spp.  Lane i sets
-// up light l for pixel i (its G-buffer texel, the skip tests of
-// shadowRaygen.rgen:43-63) and publishes origin, direction, distance and RNG
-// state in shared memory; every lane then walks its spp items without waiting
-// for the others, counting unoccluded samples per pixel with shared-memory
-// atomics; once the warp's items for light l are all traced, lane i folds
-// pixel i's count into its factor.  A lane waits only at the end of a light
-// (for the slowest sum of spp rays) instead of after every pixel-light (for
-// the slowest single ray), and the samples in flight stay within a few
-// adjacent pixels of one light.  Seeds as in k_shadow_group (LCG jump-ahead),
-// so the rays equal those of k_shadow.
-// ---------------------------------------------------------------------------------
 // Per-warp shared state of the tile streams: per pixel of the warp's tile its
 // position, the direction to the current light and distance, the TEA seed and
 // rays traced before this light (0xffffffff: not traced), the unoccluded count.
@@ -520,7 +506,9 @@ __device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams&
                     live = true;
                     ls.shadow++;
                 }
-                // ---- up to P.inner node visits ----
+                // ---- up to P.inner node visits (ending the round early once enough
+                //      lanes wait for an item measured slower: the extra votes per
+                //      visit cost more than the waits they save) ----
                 if (live) {
                     for (uint32_t it = 0, ni = max(P.inner, 1u); it < ni; it++) {
                         if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status)) {
@@ -544,9 +532,10 @@ __device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams&
 }
 
 // ---------------------------------------------------------------------------------
-// DECORRELATED shadow rays, light-major over a tile: a warp takes an 8x4 tile
-// and, light by light, traces all 32 x spp samples of its pixels, item
-// q = lane + 32 n (n < spp) being sample q % spp of pixel q / spp.  Lane i sets
+// Shadow rays, light-major over a tile: a warp takes an 8x4 tile and, light
+// by light, traces all 32 x n_rays samples of its pixels (n_rays = spp for
+// DECORRELATED; 1 for REFERENCE, whose samples are one ray), item
+// q = lane + 32 n (n < n_rays) being sample q % n_rays of pixel q / n_rays.  Lane i sets
 // up light l for pixel i (its G-buffer texel, the skip tests of
 // shadowRaygen.rgen:43-63) and publishes origin, direction, distance and RNG
 // state in shared memory; every lane then walks its spp items without waiting
@@ -577,7 +566,8 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_stream(const SceneDev S, c
             chunk_cur = t0;
             chunk_end = min(t0 + P.chunk, P.ntiles);
         }
-        stream_tile<COUNT, TWO, ACCUM ? 1 : 0>(S, P, chunk_cur++, false, ACCUM, sm, stk, t, r, s, ls, nn, nt);
+        stream_tile<COUNT, TWO, ACCUM ? 1 : 0>(S, P, chunk_cur++, P.rng_mode == HY_RNG_REFERENCE, ACCUM, sm, stk, t, r,
+                                               s, ls, nn, nt);
     }
     if (COUNT) { ls.nodes += nn; ls.tris += nt; }
     flush_stats(ls, P.stats);
