@@ -87,7 +87,8 @@ __device__ __forceinline__ uint32_t lcg(uint32_t& prev) {
     prev = 1664525u * prev + 1013904223u;
     return prev & 0x00FFFFFFu;
 }
-__device__ __forceinline__ float rnd(uint32_t& prev) { return __fdiv_rn((float)lcg(prev), 16777216.0f); }
+// float(lcg) / 16777216: the division by 2^24 is the exact product with 2^-24
+__device__ __forceinline__ float rnd(uint32_t& prev) { return __fmul_rn((float)lcg(prev), 0x1p-24f); }
 
 // ------------------------------------------------------------------------------
 // shading helpers (helpers.glsl:33-93)
@@ -234,11 +235,11 @@ __device__ __forceinline__ RayPre ray_pre(f3 o, f3 d) {
     float dz = comp(d, r.kz);
     r.Sx = __fdiv_rn(comp(d, r.kx), dz);
     r.Sy = __fdiv_rn(comp(d, r.ky), dz);
-    r.Sz = __fdiv_rn(1.0f, dz);
+    r.Sz = __frcp_rn(dz);  // the correctly rounded reciprocal: 1 / dz, bit for bit
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         float dd = fabsf(r.d[a]) > 1e-20f ? r.d[a] : copysignf(1e-20f, r.d[a]);
-        r.invd[a] = __fdiv_rn(1.0f, dd);
+        r.invd[a] = __frcp_rn(dd);
     }
     r.near = (r.invd[0] < 0.f ? 1u : 0u) | (r.invd[1] < 0.f ? 2u : 0u) | (r.invd[2] < 0.f ? 4u : 0u);
     return r;
