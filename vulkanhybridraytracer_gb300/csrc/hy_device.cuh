@@ -117,18 +117,29 @@ __device__ __forceinline__ f3 FresnelSchlick(float cosTheta, f3 F0) {
     return F0 + (splat(1.0f) - F0) * p;
 }
 // sampleDisk (helpers.glsl:82-93); `seed` advances (the caller passes a copy
-// for the reference's by-value semantics).
-__device__ __forceinline__ f3 sampleDisk(float light_radius, f3 position, f3 L, uint32_t& seed) {
+// for the reference's by-value semantics).  Split in two: the disk's frame
+// (tangent, bitangent, position + L) depends only on the pixel and the light,
+// so a caller drawing many samples of one pixel-light computes it once.
+struct DiskFrame { f3 T, B, PL; };
+__device__ __forceinline__ DiskFrame disk_frame(f3 position, f3 L) {
+    DiskFrame d;
+    d.T = normalize_rn(cross_rn(L, mk(0.f, 1.f, 0.f)));
+    if (L.x == 0.f && L.y == 1.f && L.z == 0.f) d.T = mk(0.f, 0.f, 1.f);
+    d.B = normalize_rn(cross_rn(d.T, L));
+    d.PL = add_rn(position, L);
+    return d;
+}
+__device__ __forceinline__ f3 sampleDisk(float light_radius, f3 position, const DiskFrame& d, uint32_t& seed) {
     float r1 = rnd(seed);
     float radius = __fmul_rn(light_radius, __fsqrt_rn(r1));
     float r2 = rnd(seed);
     float angle = __fmul_rn(__fmul_rn(r2, 2.0f), PI);
     float px = __fmul_rn(radius, cosf(angle)), py = __fmul_rn(radius, sinf(angle));
-    f3 tangent = normalize_rn(cross_rn(L, mk(0.f, 1.f, 0.f)));
-    if (L.x == 0.f && L.y == 1.f && L.z == 0.f) tangent = mk(0.f, 0.f, 1.f);
-    f3 bitangent = normalize_rn(cross_rn(tangent, L));
-    f3 target = add_rn(add_rn(add_rn(position, L), scale_rn(tangent, px)), scale_rn(bitangent, py));
+    f3 target = add_rn(add_rn(d.PL, scale_rn(d.T, px)), scale_rn(d.B, py));
     return normalize_rn(sub_rn(target, position));
+}
+__device__ __forceinline__ f3 sampleDisk(float light_radius, f3 position, f3 L, uint32_t& seed) {
+    return sampleDisk(light_radius, position, disk_frame(position, L), seed);
 }
 
 // ------------------------------------------------------------------------------

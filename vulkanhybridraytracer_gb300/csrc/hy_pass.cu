@@ -423,13 +423,16 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, co
 }
 
 // ---------------------------------------------------------------------------------
-// Per-warp shared state of the tile streams: per pixel of the warp's tile its
-// position, the direction to the current light and distance, the TEA seed and
-// rays traced before this light (0xffffffff: not traced), the unoccluded count.
+// Per-warp shared state of the tile streams, per pixel of the warp's tile and
+// the current light: position and distance to the light; the disk frame of
+// sampleDisk (position + L, tangent, bitangent); the RNG state of the
+// pixel-light's first sample (w of PL, as bits); a not-traced mark (w of T,
+// 0xffffffff); the unoccluded count.
 struct StreamSlots {
     float4 pos[128];
-    float4 L[128];
-    uint2 seed[128];
+    float4 PL[128];
+    float4 T[128];
+    float4 B[128];
     uint32_t cnt[128];
 };
 
@@ -461,7 +464,6 @@ __device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams&
         s.smode = mi >= 0 ? (int)S.mats[mi].smr[0] : 0;
         s.in_blur = x < P.blur_w && y < P.blur_h;
         seed0 = tea(s.pix, P.frame_u);
-        sm.pos[wb + lane] = make_float4(s.position.x, s.position.y, s.position.z, 0.f);
     }
     for (uint32_t l = 0; l < P.num_lights; l++) {
         // ---- light l for this lane's pixel ----
@@ -477,10 +479,15 @@ __device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams&
                 finalize(v);
             } else {
                 traced = true;
-                sm.L[wb + lane] = make_float4(lg.L.x, lg.L.y, lg.L.z, lg.dist);
+                const DiskFrame d = disk_frame(s.position, lg.L);
+                const uint32_t st = reference ? seed0 : lcg_jump(seed0, 2u * rays_before);
+                sm.pos[wb + lane] = make_float4(s.position.x, s.position.y, s.position.z, lg.dist);
+                sm.PL[wb + lane] = make_float4(d.PL.x, d.PL.y, d.PL.z, __uint_as_float(st));
+                sm.T[wb + lane] = make_float4(d.T.x, d.T.y, d.T.z, 0.f);
+                sm.B[wb + lane] = make_float4(d.B.x, d.B.y, d.B.z, 0.f);
             }
         }
-        sm.seed[wb + lane] = make_uint2(seed0, traced ? rays_before : 0xffffffffu);
+        if (!traced) sm.T[wb + lane].w = __uint_as_float(0xffffffffu);
         sm.cnt[wb + lane] = 0;
         const bool any = __ballot_sync(0xffffffffu, traced) != 0;
         __syncwarp();
@@ -494,14 +501,16 @@ __device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams&
                 while (!live && n < nrays) {
                     const uint32_t q = lane + 32u * n++;
                     const uint32_t pi = q / nrays, k = q - pi * nrays;
-                    const uint2 sd = sm.seed[wb + pi];
-                    if (sd.y == 0xffffffffu) continue;
-                    const float4 pp = sm.pos[wb + pi], lp = sm.L[wb + pi];
+                    const float4 tp = sm.T[wb + pi];
+                    if (__float_as_uint(tp.w) == 0xffffffffu) continue;
+                    const float4 pp = sm.pos[wb + pi], pl = sm.PL[wb + pi], bp = sm.B[wb + pi];
                     const f3 pos = mk(pp.x, pp.y, pp.z);
-                    uint32_t st = reference ? sd.x : lcg_jump(sd.x, 2u * (sd.y + k));
-                    const f3 dir = sampleDisk(radius, pos, mk(lp.x, lp.y, lp.z), st);
+                    const DiskFrame d{mk(tp.x, tp.y, tp.z), mk(bp.x, bp.y, bp.z), mk(pl.x, pl.y, pl.z)};
+                    // sample k: the pixel-light's first state advanced 2k LCG steps
+                    uint32_t st = lcg_jump(__float_as_uint(pl.w), 2u * k);
+                    const f3 dir = sampleDisk(radius, pos, d, st);
                     r = ray_pre(add_rn(pos, scale_rn(dir, 1e-1f)), dir);
-                    trav_init(t, r, __fadd_rn(lp.w, 1.0f));
+                    trav_init(t, r, __fadd_rn(pp.w, 1.0f));
                     cur = pi;
                     live = true;
                     ls.shadow++;
@@ -537,8 +546,10 @@ __device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams&
 // DECORRELATED; 1 for REFERENCE, whose samples are one ray), item
 // q = lane + 32 n (n < n_rays) being sample q % n_rays of pixel q / n_rays.  Lane i sets
 // up light l for pixel i (its G-buffer texel, the skip tests of
-// shadowRaygen.rgen:43-63) and publishes origin, direction, distance and RNG
-// state in shared memory; every lane then walks its spp items without waiting
+// shadowRaygen.rgen:43-63) and publishes position, distance, sampleDisk's frame
+// (tangent, bitangent, position + L: the same for every sample of the
+// pixel-light) and the RNG state of its first sample in shared memory; every
+// lane then walks its n_rays items without waiting
 // for the others, counting unoccluded samples per pixel with shared-memory
 // atomics; once the warp's items for light l are all traced, lane i folds
 // pixel i's count into its factor.  A lane waits only at the end of a light
@@ -1214,6 +1225,7 @@ static void* stream_kernel(bool count, int minb, bool two) {
     // instanced frame 1.5x slower)
     if (two) return count ? (void*)k_shadow_stream<true, ACCUM, 5, true> : (void*)k_shadow_stream<false, ACCUM, 5, true>;
     if (minb >= 8) return count ? (void*)k_shadow_stream<true, ACCUM, 8> : (void*)k_shadow_stream<false, ACCUM, 8>;
+    if (minb == 7) return count ? (void*)k_shadow_stream<true, ACCUM, 7> : (void*)k_shadow_stream<false, ACCUM, 7>;
     if (minb >= 6) return count ? (void*)k_shadow_stream<true, ACCUM, 6> : (void*)k_shadow_stream<false, ACCUM, 6>;
     return count ? (void*)k_shadow_stream<true, ACCUM, 5> : (void*)k_shadow_stream<false, ACCUM, 5>;
 }
