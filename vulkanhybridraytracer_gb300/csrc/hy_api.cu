@@ -355,6 +355,7 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
     const bool streams = mode == MODE_SHADOW_S || mode == MODE_SHADOW_ACCUM_S;
     int minb = cfg->min_blocks ? (int)cfg->min_blocks : (grouped ? 6 : 8);
     if (streams && !cfg->visits_per_round) P.inner = 8;
+    P.top_nodes = 73;  // levels 0-2 of the 8-wide tree (measured neutral against 0, 9 and 128)
     int grid = grid_for(c, mode, count, minb, block);
     grid = std::max(1, std::min<int>(grid, (int)((P.ntiles * 32ull + block - 1) / block)));
     ProfScope prof(c, mode);

@@ -447,9 +447,12 @@ __device__ __forceinline__ bool two_level_settle(const SceneDev& S, const RayPre
 // One node visit (its box tests and the triangles of its leaf slots).
 // Returns true when the ray is finished: t.h holds the hit, or id HY_NO_HIT.
 // TWO: the two-level structure (r is the world ray; t.cur the current one).
+// top / ntop: the structure's first ntop nodes (its top levels, BFS order)
+// staged in shared memory by the caller's block.
 template <bool ANY, bool COUNT, bool TWO = false>
 __device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& rw, float tmin, Trav& t, uint2* stk,
-                                          uint32_t& nodes_ctr, uint32_t& tris_ctr, uint32_t* status) {
+                                          uint32_t& nodes_ctr, uint32_t& tris_ctr, uint32_t* status,
+                                          const uint4* top = nullptr, uint32_t ntop = 0) {
     if (++t.iters > kMaxIters) { atomicOr(status, HY_STATUS_TIMEOUT); return true; }
     if (TWO) {
         if (!two_level_settle(S, rw, t, stk, status)) return true;
@@ -470,8 +473,14 @@ __device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& rw, f
         t.sp++;
     }
     if (idx >= S.num_nodes) { atomicOr(status, HY_STATUS_BAD_INDEX); return true; }
-    const uint4* np = S.nodes[idx].q;
-    const uint4 q0 = __ldg(np + 0), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3), q4 = __ldg(np + 4);
+    uint4 q0, q1, q2, q3, q4;
+    if (idx < ntop) {
+        const uint4* np = top + (size_t)idx * 5;
+        q0 = np[0]; q1 = np[1]; q2 = np[2]; q3 = np[3]; q4 = np[4];
+    } else {
+        const uint4* np = S.nodes[idx].q;
+        q0 = __ldg(np + 0); q1 = __ldg(np + 1); q2 = __ldg(np + 2); q3 = __ldg(np + 3); q4 = __ldg(np + 4);
+    }
     if (COUNT) nodes_ctr++;
     float adj[3], org[3];
     const float p[3] = {__uint_as_float(q0.x), __uint_as_float(q0.y), __uint_as_float(q0.z)};

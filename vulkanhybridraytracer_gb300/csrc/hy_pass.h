@@ -31,6 +31,7 @@ struct PassParams {
     uint32_t blur_w, blur_h; // texels the blur dispatch covers
     uint32_t group;          // lanes per pixel-light in the sample-parallel shadow kernel
     uint32_t inner;          // node visits per scheduling round of that kernel (>= 1)
+    uint32_t top_nodes;      // tile streams: top nodes staged in shared memory (<= kTopNodes)
     unsigned long long* stats;
     uint32_t* status;
     uint32_t* queue;
