@@ -140,3 +140,32 @@ def test_pathtrace_argument_errors(gpu_lib):
         assert e.value.code == L.HY_ERR_INVALID_ARG
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("rng", [L.HY_RNG_REFERENCE, L.HY_RNG_DECORRELATED])
+def test_pathtrace_tile_streams_equal_per_lane(gpu_lib, rng):
+    """The warp-cooperative kernel (each hit's shadow rays as tile streams, the
+    default) traces the same rays as one lane per pixel (HY_FLAG_PIXEL_PARALLEL):
+    equal ray counts and, up to the rounding of fused multiply-adds the compiler
+    places differently in the two kernels, the same colours."""
+    import torch
+    from vulkanhybridraytracer_gb300.hybrid import pass_config
+    wl = scenes.small_glass(64, 48)
+    ctx = _ctx(wl)
+    try:
+        outs = []
+        for flags in (0, L.HY_FLAG_PIXEL_PARALLEL):
+            img = torch.zeros((wl.height, wl.width, 4), dtype=torch.uint8, device="cuda")
+            out = torch.zeros((wl.height, wl.width, 4), dtype=torch.float32, device="cuda")
+            torch.cuda.synchronize()
+            img, st = ctx.pathtrace(wl.camera(-1.0), wl.width, wl.height, pass_config(4, 8, rng, flags=flags), img,
+                                    out_f=out)
+            outs.append((img.cpu().numpy(), out.cpu().numpy(), st))
+        (ia, fa, sa), (ib, fb, sb) = outs
+        assert sa["shadow_rays"] == sb["shadow_rays"] > 0
+        assert sa["reflection_rays"] == sb["reflection_rays"]
+        assert sa["error_flags"] == 0
+        np.testing.assert_allclose(fa, fb, rtol=1e-5, atol=1e-6)
+        assert np.abs(ia.astype(int) - ib.astype(int)).max() <= 1
+    finally:
+        ctx.close()

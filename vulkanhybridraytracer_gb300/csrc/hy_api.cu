@@ -844,12 +844,15 @@ int hy_pathtrace_pass(HyCtx* c, const HyCamera* cam, uint32_t W, uint32_t H, con
     std::memcpy(T.inv_proj, cam->inv_proj, 64);
     T.frame = (int32_t)cam->frame[0];
     const bool count = (cfg->flags & HY_FLAG_COUNT_TRAVERSAL) != 0;
+    // shadow rays of each hit as tile streams (default), or on the hit's own lane
+    const bool stream = !(cfg->flags & HY_FLAG_PIXEL_PARALLEL);
+    P.inner = cfg->visits_per_round ? std::min(cfg->visits_per_round, 16u) : 8u;
     int per = 0;
-    if (pathtrace_occupancy(count, &per) != cudaSuccess || per <= 0) per = 1;
+    if (pathtrace_occupancy(count, stream, c->two_level, &per) != cudaSuccess || per <= 0) per = 1;
     int grid = std::max(1, std::min<int>(per * c->num_sms, (int)((P.ntiles * 32ull + 127) / 128)));
     {
         ProfScope prof(c, PK_PATHTRACE);
-        HY_CUDA_TRY(launch_pathtrace(count, scene_dev(c), T, grid, c->stream));
+        HY_CUDA_TRY(launch_pathtrace(count, stream, scene_dev(c), T, grid, c->stream));
     }
     return finish_call(c, st, !(cfg->flags & HY_FLAG_NO_STATUS_SYNC));
 }

@@ -87,6 +87,18 @@ __device__ __forceinline__ uint32_t lcg(uint32_t& prev) {
     prev = 1664525u * prev + 1013904223u;
     return prev & 0x00FFFFFFu;
 }
+// n steps of the LCG at once: x -> A x + C composed with itself by squaring
+// (jump-ahead), exactly the state n calls of lcg() reach
+__device__ __forceinline__ uint32_t lcg_jump(uint32_t s, uint32_t n) {
+    uint32_t A = 1664525u, C = 1013904223u;  // one step of random.glsl:21-27
+    while (n) {
+        if (n & 1u) s = A * s + C;
+        C = (A + 1u) * C;                    // the map composed with itself
+        A = A * A;
+        n >>= 1;
+    }
+    return s;
+}
 // float(lcg) / 16777216: the division by 2^24 is the exact product with 2^-24
 __device__ __forceinline__ float rnd(uint32_t& prev) { return __fmul_rn((float)lcg(prev), 0x1p-24f); }
 

@@ -18,6 +18,7 @@
 #include "hy_device.cuh"
 #include "hy_pass.h"
 #include "hy_shade.cuh"
+#include "hy_stream.cuh"
 
 namespace hy {
 
@@ -295,16 +296,6 @@ __global__ void __launch_bounds__(128, MINB) k_shadow(const SceneDev S, const Pa
 // jump-ahead), which is exactly the state the sequential per-pixel loop
 // reaches, so the rays equal those of k_shadow.
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t lcg_jump(uint32_t s, uint32_t n) {
-    uint32_t A = 1664525u, C = 1013904223u;  // x -> A x + C, one step of random.glsl:21-27
-    while (n) {
-        if (n & 1u) s = A * s + C;
-        C = (A + 1u) * C;                    // the map composed with itself
-        A = A * A;
-        n >>= 1;
-    }
-    return s;
-}
 
 template <bool COUNT, bool ACCUM, int MINB, bool TWO = false>
 __global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, const PassParams P) {
@@ -423,31 +414,6 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, co
 }
 
 // ---------------------------------------------------------------------------------
-// The top levels of the node array (BFS order: levels 0-2 of an 8-wide tree
-// are its first 73 nodes) staged in shared memory once per block.  Measured
-// neutral at 1080p (0 / 9 / 73 / 128 staged nodes: 2,551 / 2,547 / 2,560 /
-// 2,553 Mrays/s): those nodes are L1-resident anyway.
-constexpr uint32_t kTopNodes = 73;
-__device__ __forceinline__ uint32_t stage_top(const SceneDev& S, uint4* top, uint32_t limit) {
-    const uint32_t ntop = min(min(S.num_nodes, kTopNodes), limit);
-    for (uint32_t i = threadIdx.x; i < ntop * 5; i += blockDim.x) top[i] = __ldg(&S.nodes[i / 5].q[i % 5]);
-    __syncthreads();
-    return ntop;
-}
-
-// Per-warp shared state of the tile streams, per pixel of the warp's tile and
-// the current light: position and distance to the light; the disk frame of
-// sampleDisk (position + L, tangent, bitangent); the RNG state of the
-// pixel-light's first sample (w of PL, as bits); a not-traced mark (w of T,
-// 0xffffffff); the unoccluded count.
-struct StreamSlots {
-    float4 pos[128];
-    float4 PL[128];
-    float4 T[128];
-    float4 B[128];
-    uint32_t cnt[128];
-};
-
 // One 8x4 tile of a view, light by light.  ACC: 0 raw shadow images, 1 the
 // running mean into the history, 2 either (accum) at run time.  reference:
 // REFERENCE RNG (one ray per pixel-light from the pixel's seed, by value).
@@ -488,61 +454,16 @@ __device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams&
             if (s.smode == 4) v = 1.0f;
             else if (!(lg.NdotL > 0.f)) v = 0.0f;
             else if (!(lg.dist < lg.maxd)) v = 1.0f;
-            if (v >= 0.f) {
-                finalize(v);
-            } else {
-                traced = true;
-                const DiskFrame d = disk_frame(s.position, lg.L);
-                const uint32_t st = reference ? seed0 : lcg_jump(seed0, 2u * rays_before);
-                sm.pos[wb + lane] = make_float4(s.position.x, s.position.y, s.position.z, lg.dist);
-                sm.PL[wb + lane] = make_float4(d.PL.x, d.PL.y, d.PL.z, __uint_as_float(st));
-                sm.T[wb + lane] = make_float4(d.T.x, d.T.y, d.T.z, 0.f);
-                sm.B[wb + lane] = make_float4(d.B.x, d.B.y, d.B.z, 0.f);
-            }
+            if (v >= 0.f) finalize(v);
+            else traced = true;
+            stream_publish(sm, traced, s.position, lg.L, lg.dist,
+                           !traced || reference ? seed0 : lcg_jump(seed0, 2u * rays_before));
+        } else {
+            stream_publish(sm, false, s.position, s.position, 0.f, 0u);
         }
-        if (!traced) sm.T[wb + lane].w = __uint_as_float(0xffffffffu);
-        sm.cnt[wb + lane] = 0;
-        const bool any = __ballot_sync(0xffffffffu, traced) != 0;
-        __syncwarp();
-        if (any) {
-            const float radius = S.lights[l].radius;
-            bool live = false;
-            uint32_t n = 0, cur = 0;
-            for (;;) {
-                // ---- this lane's next item of a traced pixel: q = lane + 32 n is
-                //      sample q % nrays of pixel q / nrays ----
-                while (!live && n < nrays) {
-                    const uint32_t q = lane + 32u * n++;
-                    const uint32_t pi = q / nrays, k = q - pi * nrays;
-                    const float4 tp = sm.T[wb + pi];
-                    if (__float_as_uint(tp.w) == 0xffffffffu) continue;
-                    const float4 pp = sm.pos[wb + pi], pl = sm.PL[wb + pi], bp = sm.B[wb + pi];
-                    const f3 pos = mk(pp.x, pp.y, pp.z);
-                    const DiskFrame d{mk(tp.x, tp.y, tp.z), mk(bp.x, bp.y, bp.z), mk(pl.x, pl.y, pl.z)};
-                    // sample k: the pixel-light's first state advanced 2k LCG steps
-                    uint32_t st = lcg_jump(__float_as_uint(pl.w), 2u * k);
-                    const f3 dir = sampleDisk(radius, pos, d, st);
-                    r = ray_pre(add_rn(pos, scale_rn(dir, 1e-1f)), dir);
-                    trav_init(t, r, __fadd_rn(pp.w, 1.0f));
-                    cur = pi;
-                    live = true;
-                    ls.shadow++;
-                }
-                // ---- up to P.inner node visits (ending the round early once enough
-                //      lanes wait for an item measured slower: the extra votes per
-                //      visit cost more than the waits they save) ----
-                if (live) {
-                    for (uint32_t it = 0, ni = max(P.inner, 1u); it < ni; it++) {
-                        if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status, top, ntop)) {
-                            live = false;
-                            if (t.h.id == HY_NO_HIT) atomicAdd(&sm.cnt[wb + cur], 1u);
-                            break;
-                        }
-                    }
-                }
-                if (__ballot_sync(0xffffffffu, live || n < nrays) == 0) break;
-            }
-            __syncwarp();
+        if (__ballot_sync(0xffffffffu, traced) != 0) {
+            // shadowRaygen.rgen:78: origin position + 0.1 dir, tmax distance + 1
+            stream_light<COUNT, TWO>(S, P, sm, nrays, S.lights[l].radius, 1e-1f, stk, t, r, ls, nn, nt, top, ntop);
             if (traced) {
                 const uint32_t unocc = sm.cnt[wb + lane];
                 finalize(reference ? (float)unocc : __fdiv_rn((float)unocc, (float)spp));

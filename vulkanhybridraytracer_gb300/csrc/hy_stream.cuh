@@ -1,0 +1,110 @@
+// Tile streams: the warp-cooperative shadow-ray schedule shared by the hybrid
+// pass (hy_pass.cu) and the path-traced mode (hy_pt.cu).  Per light, each lane
+// publishes one pixel's shadow-ray inputs (position, distance, sampleDisk's
+// frame, the RNG state of the pixel-light's first sample) in shared memory;
+// the warp then traces the 32 x n_rays samples as items q = lane + 32 n
+// (sample q % n_rays of pixel q / n_rays), each lane walking its items with
+// several node visits per scheduling round and without waiting for the
+// others; unoccluded samples are counted per pixel with shared-memory atomics.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "hy_device.cuh"
+#include "hy_pass.h"
+#include "hy_shade.cuh"
+
+namespace hy {
+
+// The top levels of the node array (BFS order: levels 0-2 of an 8-wide tree
+// are its first 73 nodes) staged in shared memory once per block.  Measured
+// neutral at 1080p (0 / 9 / 73 / 128 staged nodes: 2,551 / 2,547 / 2,560 /
+// 2,553 Mrays/s): those nodes are L1-resident anyway.
+constexpr uint32_t kTopNodes = 73;
+__device__ __forceinline__ uint32_t stage_top(const SceneDev& S, uint4* top, uint32_t limit) {
+    const uint32_t ntop = min(min(S.num_nodes, kTopNodes), limit);
+    for (uint32_t i = threadIdx.x; i < ntop * 5; i += blockDim.x) top[i] = __ldg(&S.nodes[i / 5].q[i % 5]);
+    __syncthreads();
+    return ntop;
+}
+
+// Per-warp shared state of the tile streams, per pixel of the warp's tile and
+// the current light: position and distance to the light; the disk frame of
+// sampleDisk (position + L, tangent, bitangent); the RNG state of the
+// pixel-light's first sample (w of PL, as bits); a not-traced mark (w of T,
+// 0xffffffff); the unoccluded count.
+struct StreamSlots {
+    float4 pos[128];
+    float4 PL[128];
+    float4 T[128];
+    float4 B[128];
+    uint32_t cnt[128];
+};
+
+constexpr uint32_t kNotTraced = 0xffffffffu;
+
+// lane's slot for the current light; first_state: the RNG state of sample 0
+__device__ __forceinline__ void stream_publish(StreamSlots& sm, bool traced, f3 position, f3 L, float dist,
+                                               uint32_t first_state) {
+    const uint32_t i = threadIdx.x;
+    if (traced) {
+        const DiskFrame d = disk_frame(position, L);
+        sm.pos[i] = make_float4(position.x, position.y, position.z, dist);
+        sm.PL[i] = make_float4(d.PL.x, d.PL.y, d.PL.z, __uint_as_float(first_state));
+        sm.T[i] = make_float4(d.T.x, d.T.y, d.T.z, 0.f);
+        sm.B[i] = make_float4(d.B.x, d.B.y, d.B.z, 0.f);
+    } else {
+        sm.T[i].w = __uint_as_float(kNotTraced);
+    }
+    sm.cnt[i] = 0;
+}
+
+// The warp's items of one light (every lane calls it, after all lanes have
+// published): sample k of a pixel starts from its first state advanced 2k LCG
+// steps (sampleDisk's two draws per sample), its ray from position +
+// offset * dir to distance + 1.  On return sm.cnt holds each pixel's
+// unoccluded samples.
+template <bool COUNT, bool TWO>
+__device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams& P, StreamSlots& sm, uint32_t nrays,
+                                             float radius, float offset, uint2* stk, Trav& t, RayPre& r,
+                                             LaneStats& ls, uint32_t& nn, uint32_t& nt, const uint4* top,
+                                             uint32_t ntop) {
+    const uint32_t lane = threadIdx.x & 31, wb = threadIdx.x & ~31u;
+    __syncwarp();
+    bool live = false;
+    uint32_t n = 0, cur = 0;
+    for (;;) {
+        // ---- this lane's next item of a traced pixel ----
+        while (!live && n < nrays) {
+            const uint32_t q = lane + 32u * n++;
+            const uint32_t pi = q / nrays, k = q - pi * nrays;
+            const float4 tp = sm.T[wb + pi];
+            if (__float_as_uint(tp.w) == kNotTraced) continue;
+            const float4 pp = sm.pos[wb + pi], pl = sm.PL[wb + pi], bp = sm.B[wb + pi];
+            const f3 pos = mk(pp.x, pp.y, pp.z);
+            const DiskFrame d{mk(tp.x, tp.y, tp.z), mk(bp.x, bp.y, bp.z), mk(pl.x, pl.y, pl.z)};
+            uint32_t st = lcg_jump(__float_as_uint(pl.w), 2u * k);
+            const f3 dir = sampleDisk(radius, pos, d, st);
+            r = ray_pre(add_rn(pos, scale_rn(dir, offset)), dir);
+            trav_init(t, r, __fadd_rn(pp.w, 1.0f));
+            cur = pi;
+            live = true;
+            ls.shadow++;
+        }
+        // ---- up to P.inner node visits (ending the round early once enough
+        //      lanes wait for an item measured slower: the extra votes per
+        //      visit cost more than the waits they save) ----
+        if (live) {
+            for (uint32_t it = 0, ni = max(P.inner, 1u); it < ni; it++) {
+                if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status, top, ntop)) {
+                    live = false;
+                    if (t.h.id == HY_NO_HIT) atomicAdd(&sm.cnt[wb + cur], 1u);
+                    break;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, live || n < nrays) == 0) break;
+    }
+    __syncwarp();
+}
+
+}  // namespace hy
