@@ -287,7 +287,8 @@ def run_pathtrace(args):
     ctx.build_bvh()
     img = torch.zeros((wl.height, wl.width, 4), dtype=torch.uint8, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
-    cfg = pass_config(spp=wl.spp, max_bounces=8, rng_mode=L.HY_RNG_DECORRELATED, flags=L.HY_FLAG_NO_STATUS_SYNC)
+    cfg = pass_config(spp=wl.spp, max_bounces=8, rng_mode=L.HY_RNG_DECORRELATED, flags=L.HY_FLAG_NO_STATUS_SYNC,
+                      min_blocks=args.minb, visits_per_round=args.visits)
     _, st = ctx.pathtrace(wl.camera(0.0), wl.width, wl.height, pass_config(wl.spp, 8, L.HY_RNG_DECORRELATED), img)
     rays = st["shadow_rays"] + st["reflection_rays"]
     for f in range(args.warmup):

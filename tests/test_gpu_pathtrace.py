@@ -142,8 +142,9 @@ def test_pathtrace_argument_errors(gpu_lib):
         ctx.close()
 
 
-@pytest.mark.parametrize("rng", [L.HY_RNG_REFERENCE, L.HY_RNG_DECORRELATED])
-def test_pathtrace_tile_streams_equal_per_lane(gpu_lib, rng):
+@pytest.mark.parametrize("rng,minb", [(L.HY_RNG_REFERENCE, 0), (L.HY_RNG_DECORRELATED, 0),
+                                      (L.HY_RNG_DECORRELATED, 4), (L.HY_RNG_DECORRELATED, 5)])
+def test_pathtrace_tile_streams_equal_per_lane(gpu_lib, rng, minb):
     """The warp-cooperative kernel (each hit's shadow rays as tile streams, the
     default) traces the same rays as one lane per pixel (HY_FLAG_PIXEL_PARALLEL):
     equal ray counts and, up to the rounding of fused multiply-adds the compiler
@@ -158,8 +159,8 @@ def test_pathtrace_tile_streams_equal_per_lane(gpu_lib, rng):
             img = torch.zeros((wl.height, wl.width, 4), dtype=torch.uint8, device="cuda")
             out = torch.zeros((wl.height, wl.width, 4), dtype=torch.float32, device="cuda")
             torch.cuda.synchronize()
-            img, st = ctx.pathtrace(wl.camera(-1.0), wl.width, wl.height, pass_config(4, 8, rng, flags=flags), img,
-                                    out_f=out)
+            img, st = ctx.pathtrace(wl.camera(-1.0), wl.width, wl.height,
+                                    pass_config(4, 8, rng, flags=flags, min_blocks=minb), img, out_f=out)
             outs.append((img.cpu().numpy(), out.cpu().numpy(), st))
         (ia, fa, sa), (ib, fb, sb) = outs
         assert sa["shadow_rays"] == sb["shadow_rays"] > 0

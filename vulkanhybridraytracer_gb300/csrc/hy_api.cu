@@ -847,12 +847,16 @@ int hy_pathtrace_pass(HyCtx* c, const HyCamera* cam, uint32_t W, uint32_t H, con
     // shadow rays of each hit as tile streams (default), or on the hit's own lane
     const bool stream = !(cfg->flags & HY_FLAG_PIXEL_PARALLEL);
     P.inner = cfg->visits_per_round ? std::min(cfg->visits_per_round, 16u) : 8u;
+    // resident blocks the tile-stream kernel is compiled for: 6 (80 registers)
+    // measured fastest at 1080p (uncapped 195 registers: 1,015; 3: 1,351; 4: 1,536;
+    // 5: 1,697; 6: 1,769; 8: 1,774 Mrays/s) — occupancy beats the spills
+    const int minb = cfg->min_blocks ? (int)cfg->min_blocks : 6;
     int per = 0;
-    if (pathtrace_occupancy(count, stream, c->two_level, &per) != cudaSuccess || per <= 0) per = 1;
+    if (pathtrace_occupancy(count, stream, c->two_level, minb, &per) != cudaSuccess || per <= 0) per = 1;
     int grid = std::max(1, std::min<int>(per * c->num_sms, (int)((P.ntiles * 32ull + 127) / 128)));
     {
         ProfScope prof(c, PK_PATHTRACE);
-        HY_CUDA_TRY(launch_pathtrace(count, stream, scene_dev(c), T, grid, c->stream));
+        HY_CUDA_TRY(launch_pathtrace(count, stream, minb, scene_dev(c), T, grid, c->stream));
     }
     return finish_call(c, st, !(cfg->flags & HY_FLAG_NO_STATUS_SYNC));
 }

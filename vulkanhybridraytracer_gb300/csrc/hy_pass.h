@@ -94,8 +94,9 @@ struct PtParams {
     float inv_view[16], inv_proj[16];
     int32_t frame;           // int(cam.frame.x): RNG frame and accumulation weight
 };
-cudaError_t pathtrace_occupancy(bool count, bool stream, bool two, int* blocks_per_sm);
-cudaError_t launch_pathtrace(bool count, bool stream, const SceneDev& S, const PtParams& T, int grid, cudaStream_t s);
+cudaError_t pathtrace_occupancy(bool count, bool stream, bool two, int minb, int* blocks_per_sm);
+cudaError_t launch_pathtrace(bool count, bool stream, int minb, const SceneDev& S, const PtParams& T, int grid,
+                             cudaStream_t s);
 
 cudaError_t launch_pixels(int mode, bool count, int minb, const SceneDev& S, const PassParams& P, int grid, int block,
                           cudaStream_t s);

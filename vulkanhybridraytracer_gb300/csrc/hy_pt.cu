@@ -268,8 +268,8 @@ __global__ void __launch_bounds__(128) k_pathtrace(const SceneDev S, const PtPar
 // hit starts from the hit's RNG state advanced 2 (rays_before + k) LCG steps,
 // exactly the state the per-lane loop reaches, and the per-light shading runs
 // in the same order, so the image equals k_pathtrace's.
-template <bool COUNT, bool TWO>
-__global__ void __launch_bounds__(128) k_pathtrace_stream(const SceneDev S, const PtParams T) {
+template <bool COUNT, bool TWO, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_pathtrace_stream(const SceneDev S, const PtParams T) {
     __shared__ StreamSlots sm;
     const PassParams& P = T.P;
     LaneStats ls;
@@ -354,21 +354,31 @@ __global__ void __launch_bounds__(128) k_pathtrace_stream(const SceneDev S, cons
     flush_stats(ls, P.stats);
 }
 
+template <bool COUNT, int MINB>
+static void* pt_stream_kernel(bool two) {
+    return two ? (void*)k_pathtrace_stream<COUNT, true, MINB> : (void*)k_pathtrace_stream<COUNT, false, MINB>;
+}
 template <bool COUNT>
-static void* pt_kernel(bool stream, bool two) {
+static void* pt_kernel(bool stream, bool two, int minb) {
     if (!stream) return (void*)k_pathtrace<COUNT>;
-    return two ? (void*)k_pathtrace_stream<COUNT, true> : (void*)k_pathtrace_stream<COUNT, false>;
+    if (minb >= 8) return pt_stream_kernel<COUNT, 8>(two);
+    if (minb >= 6) return pt_stream_kernel<COUNT, 6>(two);
+    if (minb == 5) return pt_stream_kernel<COUNT, 5>(two);
+    if (minb == 4) return pt_stream_kernel<COUNT, 4>(two);
+    if (minb == 3) return pt_stream_kernel<COUNT, 3>(two);
+    return pt_stream_kernel<COUNT, 1>(two);
 }
 
 }  // namespace
 
-cudaError_t pathtrace_occupancy(bool count, bool stream, bool two, int* blocks_per_sm) {
-    void* k = count ? pt_kernel<true>(stream, two) : pt_kernel<false>(stream, two);
+cudaError_t pathtrace_occupancy(bool count, bool stream, bool two, int minb, int* blocks_per_sm) {
+    void* k = count ? pt_kernel<true>(stream, two, minb) : pt_kernel<false>(stream, two, minb);
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, 128, 0);
 }
 
-cudaError_t launch_pathtrace(bool count, bool stream, const SceneDev& S, const PtParams& T, int grid, cudaStream_t s) {
-    void* k = count ? pt_kernel<true>(stream, S.two_level != 0) : pt_kernel<false>(stream, S.two_level != 0);
+cudaError_t launch_pathtrace(bool count, bool stream, int minb, const SceneDev& S, const PtParams& T, int grid,
+                             cudaStream_t s) {
+    void* k = count ? pt_kernel<true>(stream, S.two_level != 0, minb) : pt_kernel<false>(stream, S.two_level != 0, minb);
     void* args[] = {(void*)&S, (void*)&T};
     return cudaLaunchKernel(k, dim3(grid), dim3(128), args, 0, s);
 }
