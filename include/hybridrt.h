@@ -273,8 +273,8 @@ int hy_bvh_download(HyCtx* ctx, uint32_t* morton, uint32_t* order, uint32_t* bvh
  * instance through its world-to-object transform (t is the same in both
  * frames; hit ids stay global triangle ids).  hy_bvh_refit then rebuilds the
  * instance records and the TLAS only (the per-frame TLAS update of
- * src/vk_engine.cpp:172-187).  The batch entry point and HY_FLAG_RAY_POOL
- * return HY_ERR_UNSUPPORTED on it. */
+ * src/vk_engine.cpp:172-187).  HY_FLAG_RAY_POOL, and HY_FLAG_LANE_GROUPS in a
+ * batch's tuning, return HY_ERR_UNSUPPORTED on it. */
 int hy_bvh_build_instanced(HyCtx* ctx, HyBvhStats* stats);
 
 typedef struct HyBvhLayout {

@@ -286,3 +286,49 @@ def test_gpu_instanced_pathtrace_parity(gpu_lib, oracle_lib):
             assert abs(st["shadow_rays"] - st_o["shadow_rays"]) <= 1e-3 * st_o["shadow_rays"] + 4
     finally:
         ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_instanced_batch_equals_per_view(gpu_lib, oracle_lib):
+    """A batch mixing a two-level scene and a one-level one (tile streams, graph
+    replay) equals the views rendered one by one, bit for bit."""
+    import torch
+    from vulkanhybridraytracer_gb300.hybrid import HybridContext, pass_config
+    wa, wb = scenes.small(0, 48, 40), scenes.small_glass(40, 32)
+    ca, cb = HybridContext(0), HybridContext(0)
+    ca.set_scene(wa.scene)
+    ca.build_bvh(instanced=True)
+    cb.set_scene(wb.scene)
+    cb.build_bvh()
+    runner = HybridContext(0)
+    try:
+        views = []
+        for si, (c, wl, spp, rng_mode) in enumerate(((ca, wa, 4, L.HY_RNG_DECORRELATED), (cb, wb, 1, L.HY_RNG_REFERENCE),
+                                                      (ca, wa, 1, L.HY_RNG_REFERENCE))):
+            cam = wl.scene.camera.rt_camera(wl.width, wl.height, 3.0)
+            planes = c.gbuffer(cam, wl.width, wl.height)
+            hist = torch.full((len(wl.scene.lights), wl.height, wl.width), 90, dtype=torch.uint8, device="cuda")
+            views.append(dict(scene=0 if c is ca else 1, planes=planes, camera=cam,
+                              config=pass_config(spp, 4, rng_mode, 3, 0), hist=hist,
+                              out_8=torch.zeros((wl.height, wl.width, 4), dtype=torch.uint8, device="cuda")))
+        torch.cuda.synchronize()
+        ref = []
+        for v in views:
+            h = v["hist"].clone()
+            o = torch.zeros_like(v["out_8"])
+            torch.cuda.synchronize()
+            (ca if v["scene"] == 0 else cb).forward(v["planes"], v["camera"], v["config"], h, out_8=o)
+            ref.append((h, o))
+        torch.cuda.synchronize()
+        st = runner.batch_forward([ca, cb], views, graph=True)
+        torch.cuda.synchronize()
+        assert st["error_flags"] == 0
+        for v, (h, o) in zip(views, ref):
+            assert torch.equal(v["hist"], h) and torch.equal(v["out_8"], o)
+        with pytest.raises(L.HyError) as e:
+            runner.batch_forward([ca, cb], views, tuning=pass_config(1, flags=L.HY_FLAG_LANE_GROUPS))
+        assert e.value.code == L.HY_ERR_UNSUPPORTED
+    finally:
+        runner.close()
+        ca.close()
+        cb.close()

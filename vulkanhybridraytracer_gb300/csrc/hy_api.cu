@@ -938,27 +938,27 @@ int hy_hybrid_forward_host(HyCtx* c, const HyGBuffer* hgb, const HyCamera* cam, 
 // ---- batches -------------------------------------------------------------------
 static int batch_enqueue(HyCtx* c, const std::vector<PassParams>& pv, const std::vector<SceneDev>& sd,
                          const HyView* views, const std::vector<uint32_t>& reset_views, const BatchParams& B,
-                         bool count, int minb, bool stream, size_t tab_bytes) {
+                         bool count, int minb, bool stream, bool two, size_t tab_bytes) {
     cudaStream_t s = c->stream;
     HY_CUDA_TRY(cudaMemcpyAsync(c->batch_tab.p, c->h_batch_tab, tab_bytes, cudaMemcpyHostToDevice, s));
     HY_CUDA_TRY(cudaMemsetAsync(c->dstats.p, 0, c->dstats.bytes, s));
     int per = 0;
-    if (batch_occupancy(false, count, minb, stream, &per) != cudaSuccess || per <= 0) per = 1;
+    if (batch_occupancy(false, count, minb, stream, two, &per) != cudaSuccess || per <= 0) per = 1;
     int grid = std::max(1, std::min<int>(per * c->num_sms, (int)((B.total_tiles * 32ull + 127) / 128)));
     BatchParams Bs = B;
     Bs.queue = dev_queue(c, WQ_SHADOW);
-    HY_CUDA_TRY(launch_batch(false, count, minb, stream, Bs, grid, s));
+    HY_CUDA_TRY(launch_batch(false, count, minb, stream, two, Bs, grid, s));
     for (uint32_t v : reset_views) {
         const HyView& vw = views[v];
         HyAccum acc = vw.accum;
         int rc = accumulate_impl(c, &vw.gbuffer, &vw.config, pv[v].shadow, &acc);
         if (rc) return rc;
     }
-    if (batch_occupancy(true, count, minb, false, &per) != cudaSuccess || per <= 0) per = 1;
+    if (batch_occupancy(true, count, minb, false, false, &per) != cudaSuccess || per <= 0) per = 1;
     grid = std::max(1, std::min<int>(per * c->num_sms, (int)((B.total_tiles * 32ull + 127) / 128)));
     BatchParams Bh = B;
     Bh.queue = dev_queue(c, WQ_SHADE);
-    HY_CUDA_TRY(launch_batch(true, count, minb, false, Bh, grid, s));
+    HY_CUDA_TRY(launch_batch(true, count, minb, false, false, Bh, grid, s));
     (void)sd;
     return HY_OK;
 }
@@ -971,13 +971,16 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
         if (!scenes[i]) return HY_ERR_INVALID_ARG;
         if (scenes[i]->device != c->device) return HY_ERR_INVALID_ARG;
         if ((rc = check_scene_ready(scenes[i]))) return rc;
-        if (scenes[i]->two_level) return HY_ERR_UNSUPPORTED;  // the batch kernels walk one-level structures
+        // the lane-group batch kernel walks one-level structures only
+        if (scenes[i]->two_level && tuning && (tuning->flags & HY_FLAG_LANE_GROUPS)) return HY_ERR_UNSUPPORTED;
     }
     DeviceGuard g(c->device);
     const bool count = tuning && (tuning->flags & HY_FLAG_COUNT_TRAVERSAL);
     const uint32_t chunk = tuning && tuning->queue_chunk ? tuning->queue_chunk : 1;
     const int minb = tuning && tuning->min_blocks ? (int)tuning->min_blocks : 8;
     const bool stream = !(tuning && (tuning->flags & HY_FLAG_LANE_GROUPS));
+    bool any_two = false;
+    for (uint32_t i = 0; i < ns; i++) any_two = any_two || scenes[i]->two_level;
     // per-view parameters
     std::vector<PassParams> pv(nv);
     std::vector<uint32_t> reset_views;
@@ -1061,10 +1064,11 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
     B.status = dev_status(c);
     B.queue = nullptr;
     if (bflags & HY_BATCH_NO_GRAPH) {
-        if ((rc = batch_enqueue(c, pv, sd, views, reset_views, B, count, minb, stream, tab_bytes))) return rc;
+        if ((rc = batch_enqueue(c, pv, sd, views, reset_views, B, count, minb, stream, any_two, tab_bytes))) return rc;
     } else {
         // the graph bakes pointers of the tables, scratch and reset-view launches
         std::vector<uint64_t> key = {nv, ns, total, chunk, (uint64_t)minb, (uint64_t)count, (uint64_t)stream,
+                                     (uint64_t)any_two,
                                      (uint64_t)(uintptr_t)c->batch_tab.p,
                                      (uint64_t)(uintptr_t)c->h_batch_tab, (uint64_t)(uintptr_t)c->raw_shadow.p,
                                      (uint64_t)(uintptr_t)c->hist_prev.p, (uint64_t)(uintptr_t)c->stream};
@@ -1082,7 +1086,7 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
             c->batch_key.clear();
             cudaGraph_t graph = nullptr;
             HY_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            rc = batch_enqueue(c, pv, sd, views, reset_views, B, count, minb, stream, tab_bytes);
+            rc = batch_enqueue(c, pv, sd, views, reset_views, B, count, minb, stream, any_two, tab_bytes);
             cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
             if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
             if (e != cudaSuccess) { cudaGetLastError(); return HY_ERR_CUDA; }

@@ -877,7 +877,9 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_batch(const BatchParams B)
 // The batch over tile streams: a warp pulls (view, tile) units from the
 // batch's queue and walks each tile light by light (stream_tile) with that
 // view's parameters; REFERENCE-RNG views trace one ray per pixel-light.
-template <bool COUNT, int MINB>
+// ANY_TWO: the batch holds a two-level scene (compiled separately: the second
+// traversal raises the register pressure of the one-level case)
+template <bool COUNT, int MINB, bool ANY_TWO>
 __global__ void __launch_bounds__(128, MINB) k_shadow_batch_stream(const BatchParams B) {
     __shared__ uint32_t s_begin[kMaxBatchViews + 1];
     __shared__ StreamSlots sm;
@@ -902,9 +904,15 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_batch_stream(const BatchPa
         }
         const uint32_t unit = chunk_cur++;
         const PassParams& P = B.views[view_of_tile(s_begin, B.nviews, unit)];
+        const SceneDev& S = B.scenes[P.scene];
         const bool accum = !(P.flags & HY_FLAG_NO_ACCUM) && P.accum_frame > 0;
-        stream_tile<COUNT, false, 2>(B.scenes[P.scene], P, unit - P.tile_begin, P.rng_mode == HY_RNG_REFERENCE, accum,
-                                     sm, stk, t, r, s, ls, nn, nt, nullptr, 0);
+        const bool reference = P.rng_mode == HY_RNG_REFERENCE;
+        if (ANY_TWO && S.two_level)  // a two-level scene: the same tile with the instance walk
+            stream_tile<COUNT, true, 2>(S, P, unit - P.tile_begin, reference, accum, sm, stk, t, r, s, ls, nn, nt,
+                                        nullptr, 0);
+        else
+            stream_tile<COUNT, false, 2>(S, P, unit - P.tile_begin, reference, accum, sm, stk, t, r, s, ls, nn, nt,
+                                         nullptr, 0);
     }
     if (COUNT) { ls.nodes += nn; ls.tris += nt; }
     flush_stats(ls, B.stats);
@@ -1232,26 +1240,34 @@ cudaError_t launch_gbuffer(const SceneDev& S, const GbufParams& G, cudaStream_t 
     return cudaGetLastError();
 }
 
-static void* batch_kernel(bool shade, bool count, int minb, bool stream) {
+template <int MINB>
+static void* batch_stream_kernel(bool count, bool two) {
+    if (two)
+        return count ? (void*)k_shadow_batch_stream<true, MINB, true> : (void*)k_shadow_batch_stream<false, MINB, true>;
+    return count ? (void*)k_shadow_batch_stream<true, MINB, false> : (void*)k_shadow_batch_stream<false, MINB, false>;
+}
+
+static void* batch_kernel(bool shade, bool count, int minb, bool stream, bool two) {
     if (shade) return count ? (void*)k_pixels_batch<true> : (void*)k_pixels_batch<false>;
     if (stream) {
-        if (minb >= 8) return count ? (void*)k_shadow_batch_stream<true, 8> : (void*)k_shadow_batch_stream<false, 8>;
-        if (minb >= 6) return count ? (void*)k_shadow_batch_stream<true, 6> : (void*)k_shadow_batch_stream<false, 6>;
-        return count ? (void*)k_shadow_batch_stream<true, 5> : (void*)k_shadow_batch_stream<false, 5>;
+        if (two) return batch_stream_kernel<5>(count, true);
+        if (minb >= 8) return batch_stream_kernel<8>(count, false);
+        if (minb >= 6) return batch_stream_kernel<6>(count, false);
+        return batch_stream_kernel<5>(count, false);
     }
     if (minb >= 8) return count ? (void*)k_shadow_batch<true, 8> : (void*)k_shadow_batch<false, 8>;
     return count ? (void*)k_shadow_batch<true, 5> : (void*)k_shadow_batch<false, 5>;
 }
 
-cudaError_t launch_batch(bool shade, bool count, int minb, bool stream, const BatchParams& B, int grid,
+cudaError_t launch_batch(bool shade, bool count, int minb, bool stream, bool two, const BatchParams& B, int grid,
                          cudaStream_t s) {
     void* args[] = {(void*)&B};
-    return cudaLaunchKernel(batch_kernel(shade, count, minb, stream), dim3(grid), dim3(128), args, 0, s);
+    return cudaLaunchKernel(batch_kernel(shade, count, minb, stream, two), dim3(grid), dim3(128), args, 0, s);
 }
 
-cudaError_t batch_occupancy(bool shade, bool count, int minb, bool stream, int* blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, batch_kernel(shade, count, minb, stream), 128,
-                                                         0);
+cudaError_t batch_occupancy(bool shade, bool count, int minb, bool stream, bool two, int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, batch_kernel(shade, count, minb, stream, two),
+                                                         128, 0);
 }
 
 }  // namespace hy

@@ -107,8 +107,8 @@ cudaError_t launch_post(const uint8_t* in_bgra8, const float* in_rgba32f, uint32
 cudaError_t launch_trace(const SceneDev& S, const HyRay* rays, uint32_t n, bool any, bool count, HyHit* hits,
                          unsigned long long* stats, uint32_t* status, int grid, cudaStream_t s);
 cudaError_t launch_gbuffer(const SceneDev& S, const GbufParams& G, cudaStream_t s);
-cudaError_t launch_batch(bool shade, bool count, int minb, bool stream, const BatchParams& B, int grid,
+cudaError_t launch_batch(bool shade, bool count, int minb, bool stream, bool two, const BatchParams& B, int grid,
                          cudaStream_t s);
-cudaError_t batch_occupancy(bool shade, bool count, int minb, bool stream, int* blocks_per_sm);
+cudaError_t batch_occupancy(bool shade, bool count, int minb, bool stream, bool two, int* blocks_per_sm);
 
 }  // namespace hy
