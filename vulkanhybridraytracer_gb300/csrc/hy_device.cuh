@@ -358,6 +358,25 @@ __device__ __forceinline__ uint32_t slots_to_ranks(uint32_t m, uint32_t near) {
     return m;
 }
 
+// Traversal stacks: a per-lane array (local memory), or a short stack whose
+// first kShortStack entries sit in shared memory (entry i of lane t at
+// sh[i * 128 + t]: conflict-free) and whose deeper entries spill to the
+// lane's local array.
+constexpr int kShortStack = 8;
+struct SplitStack {
+    uint2* sh;    // &smem[threadIdx.x], entries 128 apart
+    uint2* deep;  // local array of kStackMax - kShortStack entries
+};
+__device__ __forceinline__ void stack_put(uint2* s, int i, uint2 v) { s[i] = v; }
+__device__ __forceinline__ uint2 stack_get(const uint2* s, int i) { return s[i]; }
+__device__ __forceinline__ void stack_put(const SplitStack& s, int i, uint2 v) {
+    if (i < kShortStack) s.sh[i * 128] = v;
+    else s.deep[i - kShortStack] = v;
+}
+__device__ __forceinline__ uint2 stack_get(const SplitStack& s, int i) {
+    return i < kShortStack ? s.sh[i * 128] : s.deep[i - kShortStack];
+}
+
 // Stack traversal of the 8-wide BVH.  ANY: TerminateOnFirstHit semantics.
 // COUNT: accumulate node visits / triangle tests.
 //
@@ -418,13 +437,14 @@ __device__ __forceinline__ f3 xform_dir(float4 r0, float4 r1, float4 r2, const f
 // TLAS group on the stack, moves the ray into object space and walks the
 // BLAS above the saved stack height; once that part of the stack is empty
 // the world ray is restored.  Returns false when the walk is over.
-__device__ __forceinline__ bool two_level_settle(const SceneDev& S, const RayPre& rw, Trav& t, uint2* stk,
+template <class Stack>
+__device__ __forceinline__ bool two_level_settle(const SceneDev& S, const RayPre& rw, Trav& t, Stack stk,
                                                  uint32_t* status) {
     for (;;) {
         if (!t.level && t.inst_bits) {
             if (t.g_bits & 0xff000000u) {
                 if (t.sp >= kStackMax) { atomicOr(status, HY_STATUS_STACK_OVERFLOW); return false; }
-                stk[t.sp] = make_uint2(t.g_base, t.g_bits);
+                stack_put(stk, t.sp, make_uint2(t.g_base, t.g_bits));
                 t.sp++;
             }
             const uint32_t b = __ffs(t.inst_bits) - 1;
@@ -451,8 +471,9 @@ __device__ __forceinline__ bool two_level_settle(const SceneDev& S, const RayPre
         }
         if (t.sp == 0) return false;
         --t.sp;
-        t.g_base = stk[t.sp].x;
-        t.g_bits = stk[t.sp].y;
+        const uint2 e = stack_get(stk, t.sp);
+        t.g_base = e.x;
+        t.g_bits = e.y;
     }
 }
 
@@ -461,8 +482,8 @@ __device__ __forceinline__ bool two_level_settle(const SceneDev& S, const RayPre
 // TWO: the two-level structure (r is the world ray; t.cur the current one).
 // top / ntop: the structure's first ntop nodes (its top levels, BFS order)
 // staged in shared memory by the caller's block.
-template <bool ANY, bool COUNT, bool TWO = false>
-__device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& rw, float tmin, Trav& t, uint2* stk,
+template <bool ANY, bool COUNT, bool TWO = false, class Stack = uint2*>
+__device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& rw, float tmin, Trav& t, Stack stk,
                                           uint32_t& nodes_ctr, uint32_t& tris_ctr, uint32_t* status,
                                           const uint4* top = nullptr, uint32_t ntop = 0) {
     if (++t.iters > kMaxIters) { atomicOr(status, HY_STATUS_TIMEOUT); return true; }
@@ -471,8 +492,9 @@ __device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& rw, f
     } else if ((t.g_bits & 0xff000000u) == 0) {
         if (t.sp == 0) return true;
         --t.sp;
-        t.g_base = stk[t.sp].x;
-        t.g_bits = stk[t.sp].y;
+        const uint2 e = stack_get(stk, t.sp);
+        t.g_base = e.x;
+        t.g_bits = e.y;
     }
     const RayPre& r = TWO ? t.cur : rw;
     const uint32_t rb = __ffs(t.g_bits >> 24) - 1;
@@ -481,7 +503,7 @@ __device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& rw, f
     const uint32_t idx = t.g_base + __popc(t.g_bits & 0xffu & ((1u << sl) - 1u));
     if (t.g_bits & 0xff000000u) {
         if (t.sp >= kStackMax) { atomicOr(status, HY_STATUS_STACK_OVERFLOW); return true; }
-        stk[t.sp] = make_uint2(t.g_base, t.g_bits);
+        stack_put(stk, t.sp, make_uint2(t.g_base, t.g_bits));
         t.sp++;
     }
     if (idx >= S.num_nodes) { atomicOr(status, HY_STATUS_BAD_INDEX); return true; }

@@ -417,9 +417,9 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, co
 // One 8x4 tile of a view, light by light.  ACC: 0 raw shadow images, 1 the
 // running mean into the history, 2 either (accum) at run time.  reference:
 // REFERENCE RNG (one ray per pixel-light from the pixel's seed, by value).
-template <bool COUNT, bool TWO, int ACC>
+template <bool COUNT, bool TWO, int ACC, class Stack>
 __device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams& P, uint32_t tile, bool reference,
-                                            bool accum, StreamSlots& sm, uint2* stk, Trav& t, RayPre& r,
+                                            bool accum, StreamSlots& sm, Stack stk, Trav& t, RayPre& r,
                                             ShadowLane& s, LaneStats& ls, uint32_t& nn, uint32_t& nt,
                                             const uint4* top, uint32_t ntop) {
     const uint32_t lane = threadIdx.x & 31, wb = threadIdx.x & ~31u;
@@ -492,10 +492,11 @@ __device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams&
 // adjacent pixels of one light.  Seeds as in k_shadow_group (LCG jump-ahead),
 // so the rays equal those of k_shadow.
 // ---------------------------------------------------------------------------------
-template <bool COUNT, bool ACCUM, int MINB, bool TWO = false>
+template <bool COUNT, bool ACCUM, int MINB, bool TWO = false, bool SHORT = false>
 __global__ void __launch_bounds__(128, MINB) k_shadow_stream(const SceneDev S, const PassParams P) {
     __shared__ StreamSlots sm;
     __shared__ uint4 s_top[kTopNodes * 5];
+    __shared__ uint2 s_stack[SHORT ? kShortStack * 128 : 1];
     const uint32_t ntop = stage_top(S, s_top, P.top_nodes);
     LaneStats ls;
     const uint32_t lane = threadIdx.x & 31;
@@ -513,8 +514,13 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_stream(const SceneDev S, c
             chunk_cur = t0;
             chunk_end = min(t0 + P.chunk, P.ntiles);
         }
-        stream_tile<COUNT, TWO, ACCUM ? 1 : 0>(S, P, chunk_cur++, P.rng_mode == HY_RNG_REFERENCE, ACCUM, sm, stk, t, r,
-                                               s, ls, nn, nt, s_top, ntop);
+        if (SHORT)
+            stream_tile<COUNT, TWO, ACCUM ? 1 : 0>(S, P, chunk_cur++, P.rng_mode == HY_RNG_REFERENCE, ACCUM, sm,
+                                                   SplitStack{s_stack + threadIdx.x, stk}, t, r, s, ls, nn, nt, s_top,
+                                                   ntop);
+        else
+            stream_tile<COUNT, TWO, ACCUM ? 1 : 0>(S, P, chunk_cur++, P.rng_mode == HY_RNG_REFERENCE, ACCUM, sm, stk, t,
+                                                   r, s, ls, nn, nt, s_top, ntop);
     }
     if (COUNT) { ls.nodes += nn; ls.tris += nt; }
     flush_stats(ls, P.stats);
@@ -1168,6 +1174,8 @@ static void* stream_kernel(bool count, int minb, bool two) {
     // two-level walk: 5 resident blocks (96 registers; at 6 its spills made the 4K
     // instanced frame 1.5x slower)
     if (two) return count ? (void*)k_shadow_stream<true, ACCUM, 5, true> : (void*)k_shadow_stream<false, ACCUM, 5, true>;
+    if (minb == 9)  // experiment: 8 resident blocks with the shared-memory short stack
+        return count ? (void*)k_shadow_stream<true, ACCUM, 8, false, true> : (void*)k_shadow_stream<false, ACCUM, 8, false, true>;
     if (minb >= 8) return count ? (void*)k_shadow_stream<true, ACCUM, 8> : (void*)k_shadow_stream<false, ACCUM, 8>;
     if (minb == 7) return count ? (void*)k_shadow_stream<true, ACCUM, 7> : (void*)k_shadow_stream<false, ACCUM, 7>;
     if (minb >= 6) return count ? (void*)k_shadow_stream<true, ACCUM, 6> : (void*)k_shadow_stream<false, ACCUM, 6>;

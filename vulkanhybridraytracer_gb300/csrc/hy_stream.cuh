@@ -63,9 +63,9 @@ __device__ __forceinline__ void stream_publish(StreamSlots& sm, bool traced, f3 
 // steps (sampleDisk's two draws per sample), its ray from position +
 // offset * dir to distance + 1.  On return sm.cnt holds each pixel's
 // unoccluded samples.
-template <bool COUNT, bool TWO>
+template <bool COUNT, bool TWO, class Stack>
 __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams& P, StreamSlots& sm, uint32_t nrays,
-                                             float radius, float offset, uint2* stk, Trav& t, RayPre& r,
+                                             float radius, float offset, Stack stk, Trav& t, RayPre& r,
                                              LaneStats& ls, uint32_t& nn, uint32_t& nt, const uint4* top,
                                              uint32_t ntop) {
     const uint32_t lane = threadIdx.x & 31, wb = threadIdx.x & ~31u;
