@@ -177,7 +177,10 @@ typedef struct HyPassConfig {
     uint32_t flags;         /* HY_FLAG_* */
     uint32_t block_size;    /* threads per block; 0 = default / autotuned */
     uint32_t queue_chunk;   /* work items fetched per warp from the ray queue; 0 = default */
-    uint32_t stack_depth;   /* traversal stack entries; 0 = default (max 64) */
+    uint32_t stack_depth;   /* short traversal stack of the tile-stream shadow kernel: 8 keeps the
+                               first 8 entries of each lane's stack in shared memory (deeper ones
+                               in local memory); 0 = the whole 64-entry stack in local memory
+                               (default; measured equal); other values: HY_ERR_UNSUPPORTED */
     uint32_t group_lanes;   /* DECORRELATED shadow rays: lanes per pixel-light group (power of two,
                                2..32, each lane traces spp / group_lanes samples in turn);
                                0 = the next power of two >= spp */

@@ -405,13 +405,15 @@ def test_group_kernel_equals_pixel_kernel(small, spp):
     se = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, L.HY_FLAG_LANE_GROUPS), e)
     assert torch.equal(a, b) and torch.equal(a, c) and torch.equal(a, e)
     assert sa["shadow_rays"] == sb["shadow_rays"] == sc["shadow_rays"] == se["shadow_rays"] > 0
-    # the same schedules with one node visit per round, and the tile streams at each register cap
-    for flags, minb, visits in ((L.HY_FLAG_LANE_GROUPS, 0, 1), (0, 5, 1), (0, 6, 3), (0, 8, 16)):
+    # the same schedules with one node visit per round, the tile streams at each register cap
+    # and with the shared-memory short stack
+    for flags, minb, visits, depth in ((L.HY_FLAG_LANE_GROUPS, 0, 1, 0), (0, 5, 1, 0), (0, 6, 3, 0), (0, 8, 16, 0),
+                                       (0, 0, 0, 8)):
         f = torch.zeros_like(a)
         torch.cuda.synchronize()
         small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 5, flags, min_blocks=minb,
-                                                       visits_per_round=visits), f)
-        assert torch.equal(a, f), (flags, minb, visits)
+                                                       visits_per_round=visits, stack_depth=depth), f)
+        assert torch.equal(a, f), (flags, minb, visits, depth)
     # smaller lane groups (several samples per lane in turn): the same images
     for G in (2, 4, 8):
         d = torch.zeros_like(a)

@@ -1170,21 +1170,22 @@ static void* shadow_kernel_two(bool count, int minb) {
 }
 
 template <bool ACCUM>
-static void* stream_kernel(bool count, int minb, bool two) {
+static void* stream_kernel(bool count, int minb, bool two, bool short_stack) {
     // two-level walk: 5 resident blocks (96 registers; at 6 its spills made the 4K
     // instanced frame 1.5x slower)
     if (two) return count ? (void*)k_shadow_stream<true, ACCUM, 5, true> : (void*)k_shadow_stream<false, ACCUM, 5, true>;
-    if (minb == 9)  // experiment: 8 resident blocks with the shared-memory short stack
-        return count ? (void*)k_shadow_stream<true, ACCUM, 8, false, true> : (void*)k_shadow_stream<false, ACCUM, 8, false, true>;
+    if (short_stack)  // 8 resident blocks, the first stack entries in shared memory
+        return count ? (void*)k_shadow_stream<true, ACCUM, 8, false, true>
+                     : (void*)k_shadow_stream<false, ACCUM, 8, false, true>;
     if (minb >= 8) return count ? (void*)k_shadow_stream<true, ACCUM, 8> : (void*)k_shadow_stream<false, ACCUM, 8>;
     if (minb == 7) return count ? (void*)k_shadow_stream<true, ACCUM, 7> : (void*)k_shadow_stream<false, ACCUM, 7>;
     if (minb >= 6) return count ? (void*)k_shadow_stream<true, ACCUM, 6> : (void*)k_shadow_stream<false, ACCUM, 6>;
     return count ? (void*)k_shadow_stream<true, ACCUM, 5> : (void*)k_shadow_stream<false, ACCUM, 5>;
 }
 
-static void* pixel_kernel(int mode, bool count, int minb, bool two) {
-    if (mode == MODE_SHADOW_S) return stream_kernel<false>(count, minb, two);
-    if (mode == MODE_SHADOW_ACCUM_S) return stream_kernel<true>(count, minb, two);
+static void* pixel_kernel(int mode, bool count, int minb, bool two, bool short_stack = false) {
+    if (mode == MODE_SHADOW_S) return stream_kernel<false>(count, minb, two, short_stack);
+    if (mode == MODE_SHADOW_ACCUM_S) return stream_kernel<true>(count, minb, two, short_stack);
     if (two) {
         switch (mode) {
             case MODE_SHADOW_G: return shadow_kernel_two<false>(count, minb);
@@ -1211,13 +1212,14 @@ static void* pixel_kernel(int mode, bool count, int minb, bool two) {
 cudaError_t launch_pixels(int mode, bool count, int minb, const SceneDev& S, const PassParams& P, int grid, int block,
                           cudaStream_t s) {
     void* args[] = {(void*)&S, (void*)&P};
-    void* k = pixel_kernel(mode, count, minb, S.two_level != 0);
+    void* k = pixel_kernel(mode, count, minb, S.two_level != 0, P.short_stack != 0);
     if (!k) return cudaErrorNotSupported;
     return cudaLaunchKernel(k, dim3(grid), dim3(block), args, 0, s);
 }
 
-cudaError_t pixel_occupancy(int mode, bool count, int minb, bool two, int block, int* blocks_per_sm) {
-    void* k = pixel_kernel(mode, count, minb, two);
+cudaError_t pixel_occupancy(int mode, bool count, int minb, bool two, bool short_stack, int block,
+                            int* blocks_per_sm) {
+    void* k = pixel_kernel(mode, count, minb, two, short_stack);
     if (!k) return cudaErrorNotSupported;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, block, 0);
 }
