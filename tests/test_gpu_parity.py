@@ -464,3 +464,29 @@ def test_tile_stream_one_ray_per_pixel_light(small, rng_mode, spp):
     sb = small.ctx.shadow_pass(planes, cam, pass_config(spp, 1, rng_mode, 2, L.HY_FLAG_PIXEL_PARALLEL), b)
     assert torch.equal(a, b)
     assert sa["shadow_rays"] == sb["shadow_rays"] > 0
+
+
+@pytest.mark.parametrize("w,h,spp", [(37, 23, 5), (8, 4, 64), (1, 1, 3), (130, 3, 2)])
+def test_tile_stream_ragged_frames(gpu_lib, oracle_lib, w, h, spp):
+    """Frames whose sides are not multiples of the 8x4 tile (lanes without a pixel
+    still take items), one tile, one pixel: the tile streams write the same
+    images as one lane per pixel."""
+    from vulkanhybridraytracer_gb300.hybrid import HybridContext, pass_config
+    torch = _torch()
+    wl = scenes.small(0, w, h)
+    ctx = HybridContext(0)
+    try:
+        ctx.set_scene(wl.scene)
+        ctx.build_bvh()
+        cam = wl.camera(4.0)
+        planes = ctx.gbuffer(cam, w, h)
+        nl = len(wl.scene.lights)
+        a = torch.zeros((nl, h, w), dtype=torch.uint8, device="cuda")
+        b = torch.zeros_like(a)
+        torch.cuda.synchronize()
+        sa = ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 4, 0), a)
+        sb = ctx.shadow_pass(planes, cam, pass_config(spp, 1, L.HY_RNG_DECORRELATED, 4, L.HY_FLAG_PIXEL_PARALLEL), b)
+        assert torch.equal(a, b)
+        assert sa["shadow_rays"] == sb["shadow_rays"] and sa["error_flags"] == 0
+    finally:
+        ctx.close()
