@@ -526,8 +526,8 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_stream(const SceneDev S, c
     flush_stats(ls, P.stats);
 }
 
-template <int MODE, bool COUNT>
-__global__ void __launch_bounds__(128) k_pixels(const SceneDev S, const PassParams P) {
+template <int MODE, bool COUNT, int MINB = 1>
+__global__ void __launch_bounds__(128, MINB) k_pixels(const SceneDev S, const PassParams P) {
     LaneStats ls;
     const uint32_t lane = threadIdx.x & 31;
     uint32_t* queue = P.queue;
@@ -925,7 +925,7 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_batch_stream(const BatchPa
 }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_pixels_batch(const BatchParams B);
+__global__ void __launch_bounds__(128, 8) k_pixels_batch(const BatchParams B);
 
 // ---------------------------------------------------------------------------------
 // DECORRELATED shadow rays as a per-warp ray pool.
@@ -1115,7 +1115,7 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_pool(const SceneDev S, con
 }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_pixels_batch(const BatchParams B) {
+__global__ void __launch_bounds__(128, 8) k_pixels_batch(const BatchParams B) {
     __shared__ uint32_t s_begin[kMaxBatchViews + 1];
     for (uint32_t i = threadIdx.x; i <= B.nviews; i += blockDim.x)
         s_begin[i] = i < B.nviews ? B.views[i].tile_begin : B.total_tiles;
@@ -1169,6 +1169,19 @@ static void* shadow_kernel_two(bool count, int minb) {
     return count ? (void*)k_shadow_group<true, ACCUM, 5, true> : (void*)k_shadow_group<false, ACCUM, 5, true>;
 }
 
+// the shade kernel (hybridRaygen + hybridHit): resident blocks it is compiled for
+template <int MINB>
+static void* shade_kernel_m(bool count) {
+    return count ? (void*)k_pixels<MODE_SHADE, true, MINB> : (void*)k_pixels<MODE_SHADE, false, MINB>;
+}
+static void* shade_kernel(bool count, int minb) {
+    if (minb >= 8) return shade_kernel_m<8>(count);
+    if (minb >= 6) return shade_kernel_m<6>(count);
+    if (minb == 5) return shade_kernel_m<5>(count);
+    if (minb == 4) return shade_kernel_m<4>(count);
+    return shade_kernel_m<1>(count);
+}
+
 template <bool ACCUM>
 static void* stream_kernel(bool count, int minb, bool two, bool short_stack) {
     // two-level walk: 5 resident blocks (96 registers; at 6 its spills made the 4K
@@ -1183,7 +1196,7 @@ static void* stream_kernel(bool count, int minb, bool two, bool short_stack) {
     return count ? (void*)k_shadow_stream<true, ACCUM, 5> : (void*)k_shadow_stream<false, ACCUM, 5>;
 }
 
-static void* pixel_kernel(int mode, bool count, int minb, bool two, bool short_stack = false) {
+static void* pixel_kernel(int mode, bool count, int minb, bool two, bool short_stack = false, int shade_minb = 0) {
     if (mode == MODE_SHADOW_S) return stream_kernel<false>(count, minb, two, short_stack);
     if (mode == MODE_SHADOW_ACCUM_S) return stream_kernel<true>(count, minb, two, short_stack);
     if (two) {
@@ -1194,7 +1207,7 @@ static void* pixel_kernel(int mode, bool count, int minb, bool two, bool short_s
                 return count ? (void*)k_shadow<true, false, 5, true> : (void*)k_shadow<false, false, 5, true>;
             case MODE_SHADOW_ACCUM:
                 return count ? (void*)k_shadow<true, true, 5, true> : (void*)k_shadow<false, true, 5, true>;
-            case MODE_SHADE: return count ? (void*)k_pixels<MODE_SHADE, true> : (void*)k_pixels<MODE_SHADE, false>;
+            case MODE_SHADE: return shade_kernel(count, shade_minb);
             default: return nullptr;
         }
     }
@@ -1205,21 +1218,21 @@ static void* pixel_kernel(int mode, bool count, int minb, bool two, bool short_s
         case MODE_SHADOW_ACCUM_G: return shadow_kernel<true, true>(count, minb);
         case MODE_SHADOW_P: return minb >= 8 ? pool_kernel<false, 8>(count) : pool_kernel<false, 5>(count);
         case MODE_SHADOW_ACCUM_P: return minb >= 8 ? pool_kernel<true, 8>(count) : pool_kernel<true, 5>(count);
-        default: return count ? (void*)k_pixels<MODE_SHADE, true> : (void*)k_pixels<MODE_SHADE, false>;
+        default: return shade_kernel(count, shade_minb);
     }
 }
 
 cudaError_t launch_pixels(int mode, bool count, int minb, const SceneDev& S, const PassParams& P, int grid, int block,
                           cudaStream_t s) {
     void* args[] = {(void*)&S, (void*)&P};
-    void* k = pixel_kernel(mode, count, minb, S.two_level != 0, P.short_stack != 0);
+    void* k = pixel_kernel(mode, count, minb, S.two_level != 0, P.short_stack != 0, (int)P.shade_minb);
     if (!k) return cudaErrorNotSupported;
     return cudaLaunchKernel(k, dim3(grid), dim3(block), args, 0, s);
 }
 
-cudaError_t pixel_occupancy(int mode, bool count, int minb, bool two, bool short_stack, int block,
+cudaError_t pixel_occupancy(int mode, bool count, int minb, bool two, bool short_stack, int shade_minb, int block,
                             int* blocks_per_sm) {
-    void* k = pixel_kernel(mode, count, minb, two, short_stack);
+    void* k = pixel_kernel(mode, count, minb, two, short_stack, shade_minb);
     if (!k) return cudaErrorNotSupported;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, block, 0);
 }

@@ -33,6 +33,7 @@ struct PassParams {
     uint32_t inner;          // node visits per scheduling round of that kernel (>= 1)
     uint32_t top_nodes;      // tile streams: top nodes staged in shared memory (<= kTopNodes)
     uint32_t short_stack;    // tile streams: the first stack entries in shared memory
+    uint32_t shade_minb;     // shade kernel: resident blocks it is compiled for
     unsigned long long* stats;
     uint32_t* status;
     uint32_t* queue;
@@ -101,7 +102,7 @@ cudaError_t launch_pathtrace(bool count, bool stream, int minb, const SceneDev& 
 
 cudaError_t launch_pixels(int mode, bool count, int minb, const SceneDev& S, const PassParams& P, int grid, int block,
                           cudaStream_t s);
-cudaError_t pixel_occupancy(int mode, bool count, int minb, bool two, bool short_stack, int block,
+cudaError_t pixel_occupancy(int mode, bool count, int minb, bool two, bool short_stack, int shade_minb, int block,
                             int* blocks_per_sm);
 cudaError_t launch_accumulate(const AccumParams& A, cudaStream_t s);
 cudaError_t launch_post(const uint8_t* in_bgra8, const float* in_rgba32f, uint32_t n, uint8_t* out_bgra8,
