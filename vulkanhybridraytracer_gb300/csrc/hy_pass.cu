@@ -1,14 +1,22 @@
 // The hybrid pass on sm_103a.
 //
 // Kernels of the three reference programs:
-//   k_shadow<ACCUM=false>  shadowRaygen.rgen:28-93 -> raw per-light shadow images
-//   k_shadow<ACCUM=true>   the same rays folded straight into the history with
-//                          blur.comp's running mean (frame > 0), so the raw
-//                          images never touch memory in the steady state
-//   k_accumulate           blur.comp:35-81 for the reset frame (frame <= 0),
-//                          whose 3x3 clamp needs the whole raw image first
-//   k_pixels<MODE_SHADE>   hybridRaygen.rgen:27-186 + hybridHit.rchit +
-//                          miss.rmiss, reading the accumulated images
+//   k_shadow_stream<ACCUM=false>  shadowRaygen.rgen:28-93 -> raw per-light shadow
+//                                 images, as tile streams (hy_stream.cuh; the
+//                                 default schedule)
+//   k_shadow_stream<ACCUM=true>   the same rays folded straight into the history
+//                                 with blur.comp's running mean (frame > 0), so the
+//                                 raw images never touch memory in the steady state
+//   k_shadow / k_shadow_group / k_shadow_pool
+//                                 the same rays on other schedules (one lane per
+//                                 pixel, lane groups per pixel-light, a ray pool)
+//   k_accumulate                  blur.comp:35-81 for the reset frame (frame <= 0),
+//                                 whose 3x3 clamp needs the whole raw image first
+//   k_pixels<MODE_SHADE>          hybridRaygen.rgen:27-186 + hybridHit.rchit +
+//                                 miss.rmiss, reading the accumulated images
+//   k_shadow_batch_stream, k_shadow_batch, k_pixels_batch
+//                                 the same over (view, tile) units of a batch
+//   k_trace, k_gbuffer            ray queries; the primary-ray G-buffer producer
 //
 // Work distribution: persistent warps pull 8x4 pixel tiles from a global
 // queue (one atomicAdd per `chunk` tiles) until it is drained; grids are
