@@ -2,10 +2,11 @@
 // pass (hy_pass.cu) and the path-traced mode (hy_pt.cu).  Per light, each lane
 // publishes one pixel's shadow-ray inputs (position, distance, sampleDisk's
 // frame, the RNG state of the pixel-light's first sample) in shared memory;
-// the warp then traces the 32 x n_rays samples as items q = lane + 32 n
-// (sample q % n_rays of pixel q / n_rays), each lane walking its items with
-// several node visits per scheduling round and without waiting for the
-// others; unoccluded samples are counted per pixel with shared-memory atomics.
+// the warp then traces the 32 x n_rays samples as items q (sample q % n_rays of
+// pixel q / n_rays), claimed in order from a per-warp counter by whichever
+// lanes are free, each lane walking its rays with several node visits per
+// scheduling round and without waiting for the others; unoccluded samples are
+// counted per pixel with shared-memory atomics.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -38,6 +39,7 @@ struct StreamSlots {
     float4 T[128];
     float4 B[128];
     uint32_t cnt[128];
+    uint32_t next[4];  // per warp: the next unclaimed item of the current light
 };
 
 constexpr uint32_t kNotTraced = 0xffffffffu;
@@ -56,6 +58,7 @@ __device__ __forceinline__ void stream_publish(StreamSlots& sm, bool traced, f3 
         sm.T[i].w = __uint_as_float(kNotTraced);
     }
     sm.cnt[i] = 0;
+    if ((i & 31) == 0) sm.next[i >> 5] = 0;
 }
 
 // The warp's items of one light (every lane calls it, after all lanes have
@@ -68,14 +71,23 @@ __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams
                                              float radius, float offset, Stack stk, Trav& t, RayPre& r,
                                              LaneStats& ls, uint32_t& nn, uint32_t& nt, const uint4* top,
                                              uint32_t ntop) {
-    const uint32_t lane = threadIdx.x & 31, wb = threadIdx.x & ~31u;
+    const uint32_t lane = threadIdx.x & 31, wb = threadIdx.x & ~31u, total = 32u * nrays;
+    uint32_t* next = &sm.next[threadIdx.x >> 5];
     __syncwarp();
-    bool live = false;
-    uint32_t n = 0, cur = 0;
+    bool live = false, more = true;
+    uint32_t cur = 0;
     for (;;) {
-        // ---- this lane's next item of a traced pixel ----
-        while (!live && n < nrays) {
-            const uint32_t q = lane + 32u * n++;
+        // ---- this lane's next item of a traced pixel, claimed from the warp's
+        //      counter: items go to whichever lanes are free, in order, so the
+        //      warp's work stays balanced until the light's last items ----
+        while (!live && more) {
+            // one shared atomic per group of lanes claiming together, lane order kept
+            const uint32_t m = __activemask(), leader = __ffs(m) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(next, (uint32_t)__popc(m));
+            base = __shfl_sync(m, base, leader);
+            const uint32_t q = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+            if (q >= total) { more = false; break; }
             const uint32_t pi = q / nrays, k = q - pi * nrays;
             const float4 tp = sm.T[wb + pi];
             if (__float_as_uint(tp.w) == kNotTraced) continue;
@@ -102,7 +114,7 @@ __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams
                 }
             }
         }
-        if (__ballot_sync(0xffffffffu, live || n < nrays) == 0) break;
+        if (__ballot_sync(0xffffffffu, live || more) == 0) break;
     }
     __syncwarp();
 }
