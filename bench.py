@@ -64,6 +64,9 @@ def workload(args):
     return scenes.hd(1, args.width, args.height, spp=args.spp)
 
 
+ANYHIT_ORDER = {1: "far first", 2: "near first"}  # HY_ANYHIT_FAR_FIRST / HY_ANYHIT_NEAR_FIRST
+
+
 def config_of(wl, args):
     return {"workload": wl.name, "width": wl.width, "height": wl.height, "triangles": wl.scene.num_tris,
             "lights": len(wl.scene.lights), "shadow_spp": wl.spp, "rng": "decorrelated",
@@ -445,6 +448,7 @@ def run_large(args):
     ctx2 = HybridContext(0, stream=stream.cuda_stream)
     ctx2.set_scene(wl.scene)
     bvh2 = ctx2.build_bvh(instanced=True)
+    order2 = ANYHIT_ORDER[ctx2.anyhit_order()]
     lay2 = ctx2.bvh_layout()
     st2 = ctx2.forward(planes, wl.camera(0.0), cfg(0, 0), hist, L.HY_ACCUM_U8, out_f=outf, out_8=out8)
     rays2 = st2["shadow_rays"] + st2["reflection_rays"] + st2["hit_shadow_rays"]
@@ -479,7 +483,8 @@ def run_large(args):
                        "instances": len(wl.scene.entities) - 1, "materials": len(wl.scene.materials),
                        "lights": NL, "shadow_spp_per_light": 1, "max_bounces": wl.max_bounces,
                        "rng": "decorrelated", "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)"},
-            "bvh": {"build_ms": bvh["build_ms"], "bvh8_nodes": bvh["num_bvh8_nodes"], "depth": bvh["depth"]},
+            "bvh": {"build_ms": bvh["build_ms"], "bvh8_nodes": bvh["num_bvh8_nodes"], "depth": bvh["depth"],
+                    "anyhit_order": ANYHIT_ORDER[ctx.anyhit_order()]},
             "rays_per_frame": rays,
             "adjoint": {"backward_ms": b_ms, "backward_over_forward": b_ms / f_ms,
                         "params": len(wl.scene.materials) * 5 + NL * 4,
@@ -488,6 +493,7 @@ def run_large(args):
                                       "batched_mrays_per_s": rays_b / (mb / 1e3) / 1e6,
                                       "batched_over_per_view": mp / mb},
             "two_level": {"build_ms": bvh2["build_ms"], "nodes": lay2["num_nodes"], "blas": lay2["num_blas"],
+                          "anyhit_order": order2,
                           "instances": lay2["num_instances"], "depth": lay2["depth"],
                           "node_bytes": lay2["num_nodes"] * 80, "flat_node_bytes": bvh["num_bvh8_nodes"] * 80,
                           "rays": rays2, "forward_ms": f2_ms, "mrays_per_s": rays2 / (f2_ms / 1e3) / 1e6,
@@ -759,7 +765,8 @@ def main():
             "rays_per_frame": rays,
             "rays_breakdown": {k: st_plain[k] for k in ("shadow_rays", "reflection_rays", "hit_shadow_rays")},
             "traversal_per_ray": {"nodes": st_count["nodes_visited"] / rays, "tris": st_count["tris_tested"] / rays},
-            "bvh": {"build_ms": bvh["build_ms"], "bvh8_nodes": bvh["num_bvh8_nodes"], "depth": bvh["depth"]},
+            "bvh": {"build_ms": bvh["build_ms"], "bvh8_nodes": bvh["num_bvh8_nodes"], "depth": bvh["depth"],
+                    "anyhit_order": ANYHIT_ORDER[ctx.anyhit_order()]},
             "wall_s": t_wall,
             "clocks": clk,
             "gpu_launches": 2 * args.steps,

@@ -296,6 +296,30 @@ int hy_bvh_layout(HyCtx* ctx, HyBvhLayout* out);
  * 0 as uint32 bits); boxes: 6 floats per instance (the TLAS box, lo then hi). */
 int hy_bvh_download_instances(HyCtx* ctx, float* records, float* boxes);
 
+/* Child order of any-hit traversal (shadow rays, hy_trace_rays with any_hit).
+ * Closest-hit rays always walk a node's children front to back (rank = slot
+ * ^ the ray's near octant).  Any-hit rays return the same occlusion either
+ * way, but the order sets how soon they meet an occluder and which nodes
+ * they touch:
+ *   HY_ANYHIT_FAR_FIRST  back to front (from the ray's far end): a shadow ray
+ *                        starts on a surface and meets its occluders away
+ *                        from it, so fewer node visits;
+ *   HY_ANYHIT_NEAR_FIRST front to back: a tile's rays to successive lights
+ *                        start at the same nodes, the better order when the
+ *                        structure does not fit in L2 and node fetches go to
+ *                        DRAM;
+ *   HY_ANYHIT_AUTO       (default) far first for a one-level structure whose
+ *                        nodes and leaf records fit in the device's L2, near
+ *                        first otherwise (two-level structures included).
+ * The order is a property of the scene: it applies to every pass on it,
+ * batched views included.  hy_scene_anyhit_order reports the order a pass
+ * uses now (HY_ERR_NOT_READY without a built structure).  Which triangle an
+ * any-hit query reports can differ between the orders; whether it hits
+ * cannot. */
+enum { HY_ANYHIT_AUTO = 0, HY_ANYHIT_FAR_FIRST = 1, HY_ANYHIT_NEAR_FIRST = 2 };
+int hy_scene_set_anyhit_order(HyCtx* ctx, uint32_t order);
+int hy_scene_anyhit_order(HyCtx* ctx, uint32_t* resolved);
+
 /* ---- ray queries (any_hit: TerminateOnFirstHit semantics) ---- */
 int hy_trace_rays(HyCtx* ctx, const HyRay* d_rays, uint32_t num_rays, int any_hit,
                   HyHit* d_hits, HyStats* stats);

@@ -557,9 +557,12 @@ static Hit trace_bvh8(const Scene& s, const float o[3], const float d[3], float 
         invd[a] = 1.0f / dd;
     }
     uint32_t near = (invd[0] < 0.f ? 1u : 0u) | (invd[1] < 0.f ? 2u : 0u) | (invd[2] < 0.f ? 4u : 0u);
+    // child rank = slot ^ ord: front to back for closest hits; any-hit rays
+    // in the scene's order (anyhit_flip)
+    const uint32_t ord = any_hit ? near ^ anyhit_flip(s) : near;
     uint32_t stk_base[kStackMax], stk_bits[kStackMax];
     int sp = 0;
-    uint32_t g_base = 0, g_bits = (1u << 24) | (1u << near);
+    uint32_t g_base = 0, g_bits = 1u << 24;  // one rank bit, empty slot mask: the root alone
     float cur_tmax = tmax;
     for (uint32_t iter = 0;; iter++) {
         if (iter >= kMaxIters) { if (c) c->status |= HY_STATUS_TIMEOUT; break; }
@@ -571,7 +574,7 @@ static Hit trace_bvh8(const Scene& s, const float o[3], const float d[3], float 
         }
         uint32_t rb = (uint32_t)__builtin_ctz(g_bits >> 24);
         g_bits &= ~(1u << (24 + rb));
-        uint32_t sl = rb ^ near;
+        uint32_t sl = rb ^ ord;
         uint32_t idx = g_base + (uint32_t)__builtin_popcount(g_bits & 0xffu & ((1u << sl) - 1u));
         if (g_bits & 0xff000000u) {
             if (sp >= kStackMax) { if (c) c->status |= HY_STATUS_STACK_OVERFLOW; break; }
@@ -605,7 +608,7 @@ static Hit trace_bvh8(const Scene& s, const float o[3], const float d[3], float 
             float tnear = fmax2(fmax2(tn[0], tn[1]), fmax2(tn[2], tmin));
             float tfar = fmin2(fmin2(tf[0], tf[1]), fmin2(tf[2], cur_tmax));
             if (!(tnear <= tfar * 1.0000003f)) continue;
-            if (imask & (1u << slot)) hit_int |= 1u << (slot ^ near);
+            if (imask & (1u << slot)) hit_int |= 1u << (slot ^ ord);
             else hit_tri |= ((1u << (m >> 5)) - 1u) << (m & 31u);
         }
         uint32_t tri_base = w[5];
@@ -789,8 +792,8 @@ static RayState ray_state(const float o[3], const float d[3]) {
 }
 
 // box tests of one node: internal children hit (rank order) and leaf records hit
-static void node_hits(const uint32_t* w, const RayState& r, float tmin, float tmax, uint32_t& hit_int,
-                      uint32_t& hit_tri) {
+static void node_hits(const uint32_t* w, const RayState& r, uint32_t ord, float tmin, float tmax,
+                      uint32_t& hit_int, uint32_t& hit_tri) {
     float adj[3], org[3];
     for (int a = 0; a < 3; a++) {
         uint32_t ea = (w[3] >> (8 * a)) & 0xffu;
@@ -815,7 +818,7 @@ static void node_hits(const uint32_t* w, const RayState& r, float tmin, float tm
         float tnear = fmax2(fmax2(tn[0], tn[1]), fmax2(tn[2], tmin));
         float tfar = fmin2(fmin2(tf[0], tf[1]), fmin2(tf[2], tmax));
         if (!(tnear <= tfar * 1.0000003f)) continue;
-        if (imask & (1u << slot)) hit_int |= 1u << (slot ^ r.near);
+        if (imask & (1u << slot)) hit_int |= 1u << (slot ^ ord);
         else hit_tri |= ((1u << (m >> 5)) - 1u) << (m & 31u);
     }
 }
@@ -838,7 +841,8 @@ static Hit trace_2l(const Scene& s, const float o[3], const float d[3], float tm
     int sp = 0, sp_base = 0;
     bool level = false;
     uint32_t inst_base = 0, inst_bits = 0, id_off = 0;
-    uint32_t g_base = 0, g_bits = (1u << 24) | (1u << r.near);
+    uint32_t g_base = 0, g_bits = 1u << 24;
+    const uint32_t flip = any_hit ? anyhit_flip(s) : 0u;  // rank order as in trace_bvh8
     float cur_tmax = tmax;
     const uint32_t nrec = (uint32_t)(T.tris.size() / 12), nnodes = (uint32_t)T.nodes.size();
     for (uint32_t iter = 0;; iter++) {
@@ -875,7 +879,7 @@ static Hit trace_2l(const Scene& s, const float o[3], const float d[3], float tm
                 sp_base = sp;
                 id_off = fbits(I[13]);
                 g_base = fbits(I[12]);
-                g_bits = (1u << 24) | (1u << r.near);
+                g_bits = 1u << 24;
                 break;
             }
             if (g_bits & 0xff000000u) break;
@@ -888,7 +892,7 @@ static Hit trace_2l(const Scene& s, const float o[3], const float d[3], float tm
         if (done) break;
         const uint32_t rb = (uint32_t)__builtin_ctz(g_bits >> 24);
         g_bits &= ~(1u << (24 + rb));
-        const uint32_t sl = rb ^ r.near;
+        const uint32_t sl = rb ^ r.near ^ flip;
         const uint32_t idx = g_base + (uint32_t)__builtin_popcount(g_bits & 0xffu & ((1u << sl) - 1u));
         if (g_bits & 0xff000000u) {
             if (sp >= kStackMax) { if (c) c->status |= HY_STATUS_STACK_OVERFLOW; break; }
@@ -900,7 +904,7 @@ static Hit trace_2l(const Scene& s, const float o[3], const float d[3], float tm
         const uint32_t* w = T.nodes[idx].w;
         if (c) c->nodes++;
         uint32_t hit_int, hit_tri;
-        node_hits(w, r, tmin, cur_tmax, hit_int, hit_tri);
+        node_hits(w, r, r.near ^ flip, tmin, cur_tmax, hit_int, hit_tri);
         const uint32_t tri_base = w[5];
         if (!level) {
             inst_base = tri_base;

@@ -82,6 +82,13 @@ static void layout_of(const Scene& s, uint32_t* L) {
     L[6] = T.tlas_nodes;
     L[7] = T.tlas_depth + T.blas_depth;
 }
+// any-hit child order (HY_ANYHIT_*), as hy_scene_set_anyhit_order
+int orc_scene_set_anyhit_order(void* sp, uint32_t order) {
+    if (order > HY_ANYHIT_NEAR_FIRST) return HY_ERR_INVALID_ARG;
+    ((Scene*)sp)->anyhit_order = order;
+    return HY_OK;
+}
+
 int orc_bvh_build_instanced(void* sp, uint32_t* layout) {
     Scene& s = *(Scene*)sp;
     bvh_build_instanced(s);

@@ -80,7 +80,18 @@ struct Scene {
     bool bvh_ok = false;
     Bvh2L two;                    // valid when two_level
     bool two_level = false;
+    uint32_t anyhit_order = HY_ANYHIT_AUTO;  // child order of any-hit traversal
 };
+
+// XOR applied to the near octant to rank the children of any-hit traversal:
+// 7 = far first, 0 = near first.  HY_ANYHIT_AUTO as the product resolves it
+// for structures that fit in L2 (every case the oracle runs): far first for
+// one level, near first for two levels.
+inline uint32_t anyhit_flip(const Scene& s) {
+    if (s.anyhit_order == HY_ANYHIT_FAR_FIRST) return 7u;
+    if (s.anyhit_order == HY_ANYHIT_NEAR_FIRST || s.two_level) return 0u;
+    return 7u;
+}
 
 // geometry / BVH
 void scene_derive(Scene& s);

@@ -309,6 +309,43 @@ def test_counts_match_oracle_pass(small):
     assert abs(st["tris_tested"] - ost["tris_tested"]) <= 1e-3 * ost["tris_tested"]
 
 
+@pytest.mark.parametrize("order", [L.HY_ANYHIT_FAR_FIRST, L.HY_ANYHIT_NEAR_FIRST])
+def test_anyhit_order(gpu_lib, oracle_lib, order):
+    """Both any-hit child orders: hits and traversal counts bit-exact with the
+    oracle walking in the same order; the occlusion of every ray, the pass's
+    shadow history and its image equal across the orders; closest-hit
+    queries do not depend on the order."""
+    torch = _torch()
+    p = Pair(scenes.small(0))
+    assert p.ctx.anyhit_order() == L.HY_ANYHIT_FAR_FIRST  # AUTO: the structure fits in L2
+    rays = _rays(np.random.default_rng(11), 40000)
+    base = {}
+    for o in (L.HY_ANYHIT_FAR_FIRST, order):
+        p.ctx.set_anyhit_order(o)
+        p.orc.set_anyhit_order(o)
+        assert p.ctx.anyhit_order() == o
+        for any_hit in (True, False):
+            hg, sg = p.ctx.trace(torch.from_numpy(rays).cuda(), any_hit, count=True)
+            ho, co = p.orc.trace(rays, any_hit)
+            hg = hg.cpu().numpy().view(np.uint32)
+            assert np.array_equal(hg, ho.view(np.uint32))
+            assert sg["nodes_visited"] == int(co[:, 0].sum()) and sg["tris_tested"] == int(co[:, 1].sum())
+            base.setdefault(any_hit, hg)
+            if any_hit:
+                assert np.array_equal(hg[:, 1] != L.HY_NO_HIT, base[True][:, 1] != L.HY_NO_HIT)
+            else:
+                assert np.array_equal(hg, base[False])
+        g, o_ = run_both(p, 1, 4, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8, flags=L.HY_FLAG_COUNT_TRAVERSAL)
+        check_parity(g, o_, L.HY_ACCUM_U8)
+        base.setdefault("pass", g)
+        assert np.array_equal(g[2], base["pass"][2]) and np.array_equal(g[1], base["pass"][1])
+    with pytest.raises(L.HyError):
+        p.ctx.set_anyhit_order(3)
+    p.ctx.set_anyhit_order(L.HY_ANYHIT_AUTO)
+    assert p.ctx.anyhit_order() == L.HY_ANYHIT_FAR_FIRST
+    p.ctx.close()
+
+
 def test_error_paths(gpu_lib, oracle_lib):
     from vulkanhybridraytracer_gb300.hybrid import HybridContext, pass_config
     torch = _torch()

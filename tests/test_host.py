@@ -46,6 +46,8 @@ def test_null_arguments_rejected(lib):
     assert lib.hy_create(None, None) == L.HY_ERR_INVALID_ARG
     assert lib.hy_scene_set_materials(None, None, 0) == L.HY_ERR_INVALID_ARG
     assert lib.hy_hybrid_forward(None, None, None, None, None, None, None, None) == L.HY_ERR_INVALID_ARG
+    assert lib.hy_scene_set_anyhit_order(None, L.HY_ANYHIT_FAR_FIRST) == L.HY_ERR_INVALID_ARG
+    assert lib.hy_scene_anyhit_order(None, None) == L.HY_ERR_INVALID_ARG
     assert lib.hy_bvh_build(None, None) == L.HY_ERR_INVALID_ARG
     lib.hy_destroy(None)
 

@@ -187,6 +187,7 @@ def test_gpu_instanced_trace_bitexact(gpu_lib, oracle_lib, any_hit):
     import torch
     wl = scenes.small(0, 32, 32)
     ctx, gi, o = _gpu_pair(wl)
+    assert ctx.anyhit_order() == L.HY_ANYHIT_NEAR_FIRST  # AUTO on a two-level structure
     rays = _rays(50000, 7)
     hg, sg = ctx.trace(torch.from_numpy(rays).cuda(), any_hit, count=True)
     ho, co = o.trace(rays, any_hit)

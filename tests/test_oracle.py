@@ -106,6 +106,41 @@ def test_bvh8_matches_brute_force(small_orc):
     assert cnt[:, 0].mean() < 40  # the 8-wide tree prunes: far fewer tests than 5122 triangles
 
 
+def test_anyhit_orders_agree(oracle_lib):
+    """Far-first and near-first any-hit traversal: the same occlusion for every
+    ray (and brute force's), the same closest hits; the order only changes
+    which nodes are visited.  Rays from the floor towards points above it,
+    like shadow rays, meet their occluders sooner far first."""
+    wl = scenes.small(0, 64, 64)
+    o = po.OracleScene()
+    o.set_scene(wl.scene)
+    o.build_bvh()
+    rng = np.random.default_rng(5)
+    n = 4000
+    rays = np.zeros((n, 8), np.float32)
+    org = np.stack([rng.uniform(-6, 6, n), np.full(n, 0.01), rng.uniform(-6, 6, n)], 1)
+    tgt = np.stack([rng.uniform(-6, 6, n), rng.uniform(4, 8, n), rng.uniform(-6, 6, n)], 1)
+    d = tgt - org
+    dist = np.linalg.norm(d, axis=1)
+    rays[:, 0:3], rays[:, 4:7], rays[:, 3], rays[:, 7] = org, d / dist[:, None], 1e-3, dist
+    ab, _ = o.trace(rays, True, po.TRACE_BRUTE)
+    res = {}
+    for order in (po.HY_ANYHIT_FAR_FIRST, po.HY_ANYHIT_NEAR_FIRST):
+        o.set_anyhit_order(order)
+        a, ca = o.trace(rays, True)
+        c, _ = o.trace(rays, False)
+        res[order] = (a.view(np.uint32)[:, 1] != 0xFFFFFFFF, c.view(np.uint32), ca[:, 0].sum())
+    far, near = res[po.HY_ANYHIT_FAR_FIRST], res[po.HY_ANYHIT_NEAR_FIRST]
+    assert np.array_equal(far[0], near[0])
+    assert np.array_equal(far[0], ab.view(np.uint32)[:, 1] != 0xFFFFFFFF)
+    assert far[0].any() and not far[0].all()
+    assert np.array_equal(far[1], near[1])
+    assert far[2] < near[2]
+    o.set_anyhit_order(po.HY_ANYHIT_AUTO)
+    a, _ = o.trace(rays, True)
+    assert np.array_equal(a.view(np.uint32)[:, 1] != 0xFFFFFFFF, far[0])
+
+
 def test_bvh_structure(small_orc):
     wl, o, info = small_orc
     n = info["num_tris"]

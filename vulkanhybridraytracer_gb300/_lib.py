@@ -39,6 +39,7 @@ HY_FLAG_NO_STATUS_SYNC = 0x8
 HY_FLAG_PIXEL_PARALLEL = 0x10
 HY_FLAG_RAY_POOL = 0x20
 HY_FLAG_LANE_GROUPS = 0x40
+HY_ANYHIT_AUTO, HY_ANYHIT_FAR_FIRST, HY_ANYHIT_NEAR_FIRST = 0, 1, 2
 HY_NO_HIT = 0xFFFFFFFF
 
 HY_STATUS_STACK_OVERFLOW = 0x1
@@ -148,6 +149,8 @@ PROTOTYPES = {
     "hy_bvh_build_instanced": (I32, [P, C.POINTER(HyBvhStats)]),
     "hy_bvh_layout": (I32, [P, C.POINTER(HyBvhLayout)]),
     "hy_bvh_download_instances": (I32, [P, P, P]),
+    "hy_scene_set_anyhit_order": (I32, [P, C.c_uint32]),
+    "hy_scene_anyhit_order": (I32, [P, C.POINTER(C.c_uint32)]),
     "hy_trace_rays": (I32, [P, P, U32, I32, P, C.POINTER(HyStats)]),
     "hy_gbuffer_primary": (I32, [P, C.POINTER(HyCamera), U32, U32, C.POINTER(C.c_void_p)]),
     "hy_shadow_pass": (I32, [P, C.POINTER(HyGBuffer), C.POINTER(HyCamera), C.POINTER(HyPassConfig), U32, P,

@@ -125,6 +125,18 @@ std::vector<float> normal_matrices(const float* xf, uint32_t n) {
     return out;
 }
 
+// HY_ANYHIT_AUTO: far first while the nodes (80 B) and leaf records (48 B)
+// fit in L2 — measured on a 1.5M-triangle scene (90 MB): 8.7 % fewer node
+// visits, 9.6 % faster; on a 7.35M-triangle one (440 MB): 26 % fewer visits
+// but 2 % slower, each visit's fetches going to DRAM — and near first for
+// two-level structures
+static uint32_t anyhit_flip(const HyCtx* c) {
+    if (c->anyhit_order == HY_ANYHIT_FAR_FIRST) return 7u;
+    if (c->anyhit_order == HY_ANYHIT_NEAR_FIRST || c->two_level) return 0u;
+    const uint64_t bytes = (uint64_t)c->n_bvh8 * 80u + (uint64_t)c->n_records * 48u;
+    return c->l2_bytes > 0 && bytes <= (uint64_t)c->l2_bytes ? 7u : 0u;
+}
+
 SceneDev scene_dev(HyCtx* c) {
     SceneDev S;
     S.nodes = c->nodes.as<Node8>();
@@ -149,6 +161,7 @@ SceneDev scene_dev(HyCtx* c) {
     S.inst = c->inst.as<float4>();
     S.num_inst = c->bvh_ok && c->two_level ? c->ninst : 0;
     S.two_level = c->bvh_ok && c->two_level ? 1u : 0u;
+    S.anyhit_flip = anyhit_flip(c);
     for (int i = 0; i < 2; i++) { S.env_w[i] = c->env_w[i]; S.env_h[i] = c->env_h[i]; }
     return S;
 }
@@ -417,6 +430,7 @@ int hy_create(HyCtx** out, const HyCreateInfo* info) {
     }
     cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (c->num_sms <= 0) c->num_sms = 1;
+    cudaDeviceGetAttribute(&c->l2_bytes, cudaDevAttrL2CacheSize, dev);
     int rc = ctx_alloc(c, c->dstats, ST_COUNT * 8 + 4 + WQ_COUNT * 4);
     if (rc == HY_OK && cudaMallocHost((void**)&c->h_stats, 64) != cudaSuccess) rc = HY_ERR_CUDA;
     if (rc) { hy_destroy(c); return rc; }
@@ -609,6 +623,19 @@ int hy_bvh_layout(HyCtx* c, HyBvhLayout* out) {
     L.tlas_nodes = c->two_level ? c->tlas_nodes : 0;
     L.depth = c->depth;
     *out = L;
+    return HY_OK;
+}
+
+int hy_scene_set_anyhit_order(HyCtx* c, uint32_t order) {
+    if (!c || order > HY_ANYHIT_NEAR_FIRST) return HY_ERR_INVALID_ARG;
+    c->anyhit_order = order;  // read by scene_dev at each call (a batch replay copies the scene table anew)
+    return HY_OK;
+}
+
+int hy_scene_anyhit_order(HyCtx* c, uint32_t* resolved) {
+    if (!c || !resolved) return HY_ERR_INVALID_ARG;
+    if (!c->bvh_ok) return HY_ERR_NOT_READY;
+    *resolved = anyhit_flip(c) ? HY_ANYHIT_FAR_FIRST : HY_ANYHIT_NEAR_FIRST;
     return HY_OK;
 }
 
@@ -1022,16 +1049,25 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
             while (G < v.config.shadow_spp && G < 32) G <<= 1;
         pv[i].group = G;
     }
-    // the queue hands out the costliest views' tiles first (shadow rays per tile:
-    // lights x samples), so the launch ends on cheap tiles instead of waiting
-    // for the last warps of an expensive one
+    // Queue order: scene by scene, the scene with the most work first, and
+    // within a scene the costliest views' tiles first (shadow rays per tile:
+    // lights x samples).  One scene's nodes and triangles at a time stay in L2
+    // (several scenes together can outgrow it), and the launch ends on the
+    // cheapest tiles of the cheapest scene instead of waiting for the last
+    // warps of an expensive tile.
     std::vector<uint32_t> order(nv);
     for (uint32_t i = 0; i < nv; i++) order[i] = i;
     auto tile_cost = [&](uint32_t i) {
         const uint64_t spp = views[i].config.rng_mode == HY_RNG_DECORRELATED ? views[i].config.shadow_spp : 1;
         return (uint64_t)pv[i].num_lights * spp + 1;
     };
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return tile_cost(a) > tile_cost(b); });
+    std::vector<uint64_t> scene_work(ns, 0);
+    for (uint32_t i = 0; i < nv; i++) scene_work[views[i].scene] += tile_cost(i) * pv[i].ntiles;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+        const uint32_t sa = views[a].scene, sb = views[b].scene;
+        if (sa != sb) return scene_work[sa] != scene_work[sb] ? scene_work[sa] > scene_work[sb] : sa < sb;
+        return tile_cost(a) > tile_cost(b);
+    });
     for (uint32_t i : order) {
         pv[i].tile_begin = total;
         total += pv[i].ntiles;

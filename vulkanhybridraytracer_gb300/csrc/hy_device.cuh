@@ -231,6 +231,9 @@ struct SceneDev {
     const float4* inst;
     uint32_t num_inst;
     uint32_t two_level;
+    // any-hit traversal ranks a node's children slot ^ near ^ anyhit_flip:
+    // 7 walks them far first, 0 near first (closest-hit rays: always near first)
+    uint32_t anyhit_flip;
 };
 
 struct Hit { float t; uint32_t id; float b1, b2; };
@@ -350,11 +353,11 @@ __device__ __forceinline__ uint32_t nonzero_bytes(uint32_t lo4, uint32_t hi4) {
     return ((a * 0x00204081u) >> 28) | (((b * 0x00204081u) >> 28) << 4);
 }
 
-// bit s of an 8-bit slot mask moved to bit s ^ near (the slots' traversal ranks)
-__device__ __forceinline__ uint32_t slots_to_ranks(uint32_t m, uint32_t near) {
-    if (near & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
-    if (near & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
-    if (near & 4u) m = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
+// bit s of an 8-bit slot mask moved to bit s ^ ord (the slots' traversal ranks)
+__device__ __forceinline__ uint32_t slots_to_ranks(uint32_t m, uint32_t ord) {
+    if (ord & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (ord & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (ord & 4u) m = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
     return m;
 }
 
@@ -382,7 +385,14 @@ __device__ __forceinline__ uint2 stack_get(const SplitStack& s, int i) {
 //
 // Traversal state of one ray.  A node group is (first child index, bits):
 // bits[31:24] hold the not-yet-visited hit children in traversal rank order
-// (rank = slot ^ near-octant), bits[7:0] the node's internal-child slot mask.
+// (rank = slot ^ ord), bits[7:0] the node's internal-child slot mask.  ord is
+// the ray's near octant for closest-hit rays (front to back); for any-hit
+// rays the scene chooses (SceneDev::anyhit_flip): the far octant (a shadow ray
+// starts on a surface and meets its occluders away from it, so walking from
+// the light's end reaches them before the boxes around the ray's own origin)
+// or the near one (successive rays of a tile start at the same nodes, which
+// matters when node fetches miss L2).  A group of one rank bit and an empty
+// slot mask stands for the single node at g_base (the root of a walk).
 struct Trav {
     uint32_t g_base, g_bits;
     int sp;
@@ -399,7 +409,7 @@ struct Trav {
 
 __device__ __forceinline__ void trav_init(Trav& t, const RayPre& r, float tmax) {
     t.g_base = 0;
-    t.g_bits = (1u << 24) | (1u << r.near);  // a virtual group holding the root
+    t.g_bits = 1u << 24;  // a virtual group holding the root
     t.sp = 0;
     t.iters = 0;
     t.tmax = tmax;
@@ -460,7 +470,7 @@ __device__ __forceinline__ bool two_level_settle(const SceneDev& S, const RayPre
             t.sp_base = t.sp;
             t.id_off = __float_as_uint(m.y);
             t.g_base = __float_as_uint(m.x);
-            t.g_bits = (1u << 24) | (1u << t.cur.near);  // virtual group holding the BLAS root
+            t.g_bits = 1u << 24;  // virtual group holding the BLAS root
             return true;
         }
         if (t.g_bits & 0xff000000u) return true;
@@ -499,7 +509,8 @@ __device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& rw, f
     const RayPre& r = TWO ? t.cur : rw;
     const uint32_t rb = __ffs(t.g_bits >> 24) - 1;
     t.g_bits &= ~(1u << (24 + rb));
-    const uint32_t sl = rb ^ r.near;
+    const uint32_t ord = ANY ? r.near ^ S.anyhit_flip : r.near;
+    const uint32_t sl = rb ^ ord;
     const uint32_t idx = t.g_base + __popc(t.g_bits & 0xffu & ((1u << sl) - 1u));
     if (t.g_bits & 0xff000000u) {
         if (t.sp >= kStackMax) { atomicOr(status, HY_STATUS_STACK_OVERFLOW); return true; }
@@ -571,7 +582,7 @@ __device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& rw, f
     // empty slots (meta byte 0) never count; internal children go to the stack
     // in rank order, leaf slots give their triangles
     hitbits &= nonzero_bytes(q1.z, q1.w);
-    const uint32_t hit_int = slots_to_ranks(hitbits & imask, r.near);
+    const uint32_t hit_int = slots_to_ranks(hitbits & imask, ord);
     uint32_t hit_leaf = hitbits & ~imask, hit_tri = 0;
     while (hit_leaf) {
         const uint32_t slot = __ffs(hit_leaf) - 1;

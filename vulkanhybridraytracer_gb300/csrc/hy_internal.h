@@ -36,6 +36,7 @@ struct HyCtx {
     uint64_t max_bytes = 0, used_bytes = 0;
     uint32_t fail_after = 0, alloc_calls = 0;
     int num_sms = 0;
+    int l2_bytes = 0;  // the device's L2 size (the automatic any-hit order compares the structure with it)
 
     // ---- scene ----
     hy::DevBuf verts, vattr, idx, prims, xf, nrm, prim_tri0, tri_prim, mats, lights, env[2];
@@ -77,6 +78,7 @@ struct HyCtx {
     std::vector<HyPrimitive> h_prims;
     std::vector<uint32_t> h_inst_prim, h_prim_mesh, h_mesh_prim, h_blas_node0;
     uint32_t ninst = 0, nblas = 0, tlas_region = 0, tlas_nodes = 0, tlas_depth = 0, blas_depth = 0;
+    uint32_t anyhit_order = 0;       // HY_ANYHIT_*: child order of any-hit traversal
     uint32_t n_records = 0;          // leaf records in tris
     HyBvhStats last_build{};
 

@@ -485,14 +485,15 @@ __device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams&
 // ---------------------------------------------------------------------------------
 // Shadow rays, light-major over a tile: a warp takes an 8x4 tile and, light
 // by light, traces all 32 x n_rays samples of its pixels (n_rays = spp for
-// DECORRELATED; 1 for REFERENCE, whose samples are one ray), item
-// q = lane + 32 n (n < n_rays) being sample q % n_rays of pixel q / n_rays.  Lane i sets
+// DECORRELATED; 1 for REFERENCE, whose samples are one ray), item q being
+// sample q % n_rays of pixel q / n_rays; free lanes claim the items in order
+// from a per-warp shared counter.  Lane i sets
 // up light l for pixel i (its G-buffer texel, the skip tests of
 // shadowRaygen.rgen:43-63) and publishes position, distance, sampleDisk's frame
 // (tangent, bitangent, position + L: the same for every sample of the
 // pixel-light) and the RNG state of its first sample in shared memory; every
-// lane then walks its n_rays items without waiting
-// for the others, counting unoccluded samples per pixel with shared-memory
+// lane then traces items without waiting for the others (a lane whose rays
+// are short takes more of them), counting unoccluded samples per pixel with shared-memory
 // atomics; once the warp's items for light l are all traced, lane i folds
 // pixel i's count into its factor.  A lane waits only at the end of a light
 // (for the slowest sum of spp rays) instead of after every pixel-light (for

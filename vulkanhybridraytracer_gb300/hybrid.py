@@ -148,6 +148,16 @@ class HybridContext:
         L.check(self.lib.hy_bvh_layout(self.h, C.byref(lay)), "bvh_layout")
         return {k: int(getattr(lay, k)) for k, _ in L.HyBvhLayout._fields_}
 
+    def set_anyhit_order(self, order: int):
+        """hy_scene_set_anyhit_order: HY_ANYHIT_AUTO (default), FAR_FIRST or NEAR_FIRST."""
+        L.check(self.lib.hy_scene_set_anyhit_order(self.h, order), "set_anyhit_order")
+
+    def anyhit_order(self) -> int:
+        """The order passes use now: HY_ANYHIT_FAR_FIRST or HY_ANYHIT_NEAR_FIRST."""
+        v = C.c_uint32()
+        L.check(self.lib.hy_scene_anyhit_order(self.h, C.byref(v)), "anyhit_order")
+        return int(v.value)
+
     def download_bvh_instanced(self):
         """(layout, nodes [num_nodes, 20] u32, records [num_records, 12] f32,
         instances [num_instances, 16] f32, instance boxes [num_instances, 6] f32)"""
