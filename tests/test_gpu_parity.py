@@ -503,6 +503,58 @@ def test_tile_stream_one_ray_per_pixel_light(small, rng_mode, spp):
     assert sa["shadow_rays"] == sb["shadow_rays"] > 0
 
 
+@pytest.mark.parametrize("rng_mode,spp", [(L.HY_RNG_REFERENCE, 4), (L.HY_RNG_DECORRELATED, 1)])
+@pytest.mark.parametrize("w,h", [(96, 64), (37, 23)])
+def test_one_ray_streams_many_lights(gpu_lib, oracle_lib, rng_mode, spp, w, h):
+    """One ray per pixel-light over 40 lights, some directional, out of range
+    or below the horizon: the tile streams' raw shadow images and fused
+    running mean equal one lane per pixel bit for bit, and the raw images
+    match the oracle."""
+    from vulkanhybridraytracer_gb300.hybrid import HybridContext, pass_config
+    from vulkanhybridraytracer_gb300.scene import Light
+    torch = _torch()
+    rng = np.random.default_rng(23)
+    wl = scenes.small(0, w, h)
+    lights = []
+    for i in range(40):
+        if i % 13 == 5:
+            lights.append(Light(scenes.DIRECTIONAL_LIGHT, (1, 1, 1), (0.3, 1.0, 0.2), 1.0, 500.0, 0.1))
+        else:
+            pos = (rng.uniform(-8, 8), rng.uniform(-1, 9), rng.uniform(-8, 8))
+            lights.append(Light(scenes.POINT_LIGHT, (1, 1, 1), pos, float(rng.uniform(5, 30)),
+                                float(rng.choice([3.0, 500.0])), float(rng.uniform(0.05, 0.6))))
+    wl.scene.lights = lights
+    ctx = HybridContext(0)
+    orc = po.OracleScene()
+    try:
+        ctx.set_scene(wl.scene)
+        ctx.build_bvh()
+        orc.set_scene(wl.scene)
+        orc.build_bvh()
+        cam = wl.camera(3.0)
+        planes_np = orc.gbuffer(cam, w, h)
+        planes = [torch.from_numpy(x).cuda() for x in planes_np]
+        nl = len(lights)
+        a = torch.zeros((nl, h, w), dtype=torch.uint8, device="cuda")
+        b = torch.zeros_like(a)
+        sa = ctx.shadow_pass(planes, cam, pass_config(spp, 1, rng_mode, 3, 0), a)
+        sb = ctx.shadow_pass(planes, cam, pass_config(spp, 1, rng_mode, 3, L.HY_FLAG_PIXEL_PARALLEL), b)
+        assert torch.equal(a, b)
+        assert sa["shadow_rays"] == sb["shadow_rays"] > 0 and sa["error_flags"] == 0
+        osh, _ = orc.shadow_pass(planes_np, cam, po.cfg_dict(spp, 1, rng_mode, 3), L.HY_ACCUM_U8)
+        assert np.mean(a.cpu().numpy() != osh) <= FLIP_TOL
+        h0 = torch.randint(0, 256, (nl, h, w), dtype=torch.uint8, generator=torch.Generator().manual_seed(3)).cuda()
+        outs = []
+        for flags in (0, L.HY_FLAG_PIXEL_PARALLEL):
+            hh = h0.clone()
+            o = torch.zeros((h, w, 4), dtype=torch.uint8, device="cuda")
+            ctx.forward(planes, cam, pass_config(spp, 1, rng_mode, 3, flags), hh, out_8=o)
+            outs.append((hh, o))
+        assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+    finally:
+        ctx.close()
+
+
 @pytest.mark.parametrize("w,h,spp", [(37, 23, 5), (8, 4, 64), (1, 1, 3), (130, 3, 2)])
 def test_tile_stream_ragged_frames(gpu_lib, oracle_lib, w, h, spp):
     """Frames whose sides are not multiples of the 8x4 tile (lanes without a pixel

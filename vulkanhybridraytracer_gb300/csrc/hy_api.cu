@@ -1049,25 +1049,16 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
             while (G < v.config.shadow_spp && G < 32) G <<= 1;
         pv[i].group = G;
     }
-    // Queue order: scene by scene, the scene with the most work first, and
-    // within a scene the costliest views' tiles first (shadow rays per tile:
-    // lights x samples).  One scene's nodes and triangles at a time stay in L2
-    // (several scenes together can outgrow it), and the launch ends on the
-    // cheapest tiles of the cheapest scene instead of waiting for the last
-    // warps of an expensive tile.
+    // the queue hands out the costliest views' tiles first (shadow rays per tile:
+    // lights x samples), so the launch ends on cheap tiles instead of waiting
+    // for the last warps of an expensive one
     std::vector<uint32_t> order(nv);
     for (uint32_t i = 0; i < nv; i++) order[i] = i;
     auto tile_cost = [&](uint32_t i) {
         const uint64_t spp = views[i].config.rng_mode == HY_RNG_DECORRELATED ? views[i].config.shadow_spp : 1;
         return (uint64_t)pv[i].num_lights * spp + 1;
     };
-    std::vector<uint64_t> scene_work(ns, 0);
-    for (uint32_t i = 0; i < nv; i++) scene_work[views[i].scene] += tile_cost(i) * pv[i].ntiles;
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
-        const uint32_t sa = views[a].scene, sb = views[b].scene;
-        if (sa != sb) return scene_work[sa] != scene_work[sb] ? scene_work[sa] > scene_work[sb] : sa < sb;
-        return tile_cost(a) > tile_cost(b);
-    });
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return tile_cost(a) > tile_cost(b); });
     for (uint32_t i : order) {
         pv[i].tile_begin = total;
         total += pv[i].ntiles;
