@@ -206,6 +206,14 @@ public:
         return st;
     }
 
+    // child order of the shadow rays' any-hit walk (HY_ANYHIT_*; AUTO by default)
+    void set_anyhit_order(uint32_t order) { check(hy_scene_set_anyhit_order(ctx_, order), "hy_scene_set_anyhit_order"); }
+    uint32_t anyhit_order() {
+        uint32_t o = 0;
+        check(hy_scene_anyhit_order(ctx_, &o), "hy_scene_anyhit_order");
+        return o;
+    }
+
     void update_lights(const Scene& s) {
         std::vector<HyLight> l;
         for (const Light& x : s._lights) l.push_back(x.toUbo());

@@ -122,6 +122,8 @@ int main() {
         r.load_data_to_gpu(s);
         HyBvhStats bs = r.create_acceleration_structures();
         if (bs.num_tris != 2 + 3 * 20) { std::fprintf(stderr, "triangles %u\n", bs.num_tris); return 1; }
+        // a small one-level structure fits in L2: shadow rays walk far first
+        if (r.anyhit_order() != HY_ANYHIT_FAR_FIRST) { std::fprintf(stderr, "any-hit order\n"); return 1; }
 
         // the same inputs through the C ABI directly
         HyCtx* raw = nullptr;
