@@ -894,20 +894,25 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_batch(const BatchParams B)
 // view's parameters; REFERENCE-RNG views trace one ray per pixel-light.
 // ANY_TWO: the batch holds a two-level scene (compiled separately: the second
 // traversal raises the register pressure of the one-level case)
+static_assert(sizeof(PassParams) % 4 == 0 && sizeof(SceneDev) % 4 == 0, "copied to shared memory as words");
 template <bool COUNT, int MINB, bool ANY_TWO>
 __global__ void __launch_bounds__(128, MINB) k_shadow_batch_stream(const BatchParams B) {
     __shared__ uint32_t s_begin[kMaxBatchViews + 1];
     __shared__ StreamSlots sm;
+    // per warp: its current view's parameters and scene, copied from the
+    // global tables when the warp moves to another view
+    __shared__ PassParams s_view[4];
+    __shared__ SceneDev s_scene[4];
     for (uint32_t i = threadIdx.x; i <= B.nviews; i += blockDim.x)
         s_begin[i] = i < B.nviews ? B.views[i].tile_begin : B.total_tiles;
     __syncthreads();
     LaneStats ls;
-    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint2 stk[kStackMax];
     ShadowLane s;
     Trav t;
     RayPre r;
-    uint32_t chunk_cur = 0, chunk_end = 0, nn = 0, nt = 0;
+    uint32_t chunk_cur = 0, chunk_end = 0, nn = 0, nt = 0, cur_view = 0xffffffffu;
     for (;;) {
         if (chunk_cur == chunk_end) {
             uint32_t t0 = 0;
@@ -918,8 +923,20 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_batch_stream(const BatchPa
             chunk_end = min(t0 + B.chunk, B.total_tiles);
         }
         const uint32_t unit = chunk_cur++;
-        const PassParams& P = B.views[view_of_tile(s_begin, B.nviews, unit)];
-        const SceneDev& S = B.scenes[P.scene];
+        const uint32_t v = view_of_tile(s_begin, B.nviews, unit);
+        if (v != cur_view) {
+            __syncwarp();
+            const uint32_t* vs = reinterpret_cast<const uint32_t*>(&B.views[v]);
+            uint32_t* vd = reinterpret_cast<uint32_t*>(&s_view[warp]);
+            for (uint32_t i = lane; i < sizeof(PassParams) / 4; i += 32) vd[i] = vs[i];
+            const uint32_t* ss = reinterpret_cast<const uint32_t*>(&B.scenes[B.views[v].scene]);
+            uint32_t* sd = reinterpret_cast<uint32_t*>(&s_scene[warp]);
+            for (uint32_t i = lane; i < sizeof(SceneDev) / 4; i += 32) sd[i] = ss[i];
+            __syncwarp();
+            cur_view = v;
+        }
+        const PassParams& P = s_view[warp];
+        const SceneDev& S = s_scene[warp];
         const bool accum = !(P.flags & HY_FLAG_NO_ACCUM) && P.accum_frame > 0;
         const bool reference = P.rng_mode == HY_RNG_REFERENCE;
         if (ANY_TWO && S.two_level)  // a two-level scene: the same tile with the instance walk
