@@ -293,6 +293,37 @@ def test_host_buffers_equal_device(small):
     assert st["shadow_rays"] > 0
 
 
+def test_host_buffers_back_to_back(small):
+    """Host-buffer calls queued without a host sync, each on another G-buffer
+    (planes 2-5 go up on a side stream that must wait for the previous call's
+    passes): frames 0 (raw images + blur) and 1-3 (fused running mean) equal
+    the device-buffer calls."""
+    from vulkanhybridraytracer_gb300.hybrid import pass_config
+    torch = _torch()
+    wl = small.wl
+    W, H, nl = wl.width, wl.height, len(wl.scene.lights)
+    frames = [0, 1, 2, 3]
+    gbs = [small.orc.gbuffer(wl.camera(float(5 + f)), W, H) for f in frames]
+    h_dev = torch.zeros((nl, H, W), dtype=torch.uint8, device="cuda")
+    h_host = h_dev.clone()
+    want = []
+    torch.cuda.synchronize()
+    for f, pn in zip(frames, gbs):
+        o = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
+        small.ctx.forward([torch.from_numpy(x).cuda() for x in pn], wl.camera(float(5 + f)),
+                          pass_config(4, 1, L.HY_RNG_DECORRELATED, f, 0), h_dev, L.HY_ACCUM_U8, out_8=o)
+        want.append(o.cpu().numpy())
+    got = [np.zeros((H, W, 4), np.uint8) for _ in frames]
+    for f, pn, o in zip(frames, gbs, got):
+        small.ctx.forward_host(pn, wl.camera(float(5 + f)),
+                               pass_config(4, 1, L.HY_RNG_DECORRELATED, f, L.HY_FLAG_NO_STATUS_SYNC), h_host,
+                               L.HY_ACCUM_U8, out_8=o, stats=False)
+    small.ctx.synchronize()
+    for f, a, b in zip(frames, want, got):
+        assert np.array_equal(a, b), f
+    assert torch.equal(h_dev, h_host)
+
+
 def test_deterministic(small):
     a = run_both(small, 3, 4, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8)[0]
     b = run_both(small, 3, 4, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8)[0]

@@ -458,6 +458,9 @@ void hy_destroy(HyCtx* c) {
     for (cudaEvent_t e : c->prof_pool) cudaEventDestroy(e);
     if (c->batch_exec) cudaGraphExecDestroy(c->batch_exec);
     if (c->batch_done) cudaEventDestroy(c->batch_done);
+    if (c->copy_start) cudaEventDestroy(c->copy_start);
+    if (c->copy_done) cudaEventDestroy(c->copy_done);
+    if (c->copy_stream) { cudaStreamSynchronize(c->copy_stream); cudaStreamDestroy(c->copy_stream); }
     if (c->h_batch_tab) cudaFreeHost(c->h_batch_tab);
     ctx_free(c, c->batch_tab);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -783,6 +786,15 @@ int hy_shade_pass(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const HyPa
     return finish_call(c, st, !(cfg->flags & HY_FLAG_NO_STATUS_SYNC));
 }
 
+// the shadow kernel reads G-buffer planes 0 and 1 only; what runs after it
+// waits here for planes 2-5 when hy_hybrid_forward_host copies them on its side stream
+static int wait_planes(HyCtx* c) {
+    if (!c->copy_pending) return HY_OK;
+    c->copy_pending = false;
+    HY_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->copy_done, 0));
+    return HY_OK;
+}
+
 static int forward_impl(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const HyPassConfig* cfg, HyAccum* acc,
                         float* out_f, uint8_t* out_8) {
     int rc;
@@ -792,6 +804,7 @@ static int forward_impl(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, cons
         PassParams P = make_params(c, gb, cam, cfg, acc->format, nullptr, acc->history, out_f, out_8);
         P.num_lights = acc->num_lights;
         if ((rc = run_pixels(c, MODE_SHADOW_ACCUM, P, cfg, WQ_SHADOW))) return rc;
+        if ((rc = wait_planes(c))) return rc;
         return run_pixels(c, MODE_SHADE, P, cfg, WQ_SHADE);
     }
     size_t bytes = (size_t)gb->width * gb->height * acc->num_lights * (acc->format == HY_ACCUM_U8 ? 1 : 4);
@@ -799,6 +812,7 @@ static int forward_impl(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, cons
     PassParams P = make_params(c, gb, cam, cfg, acc->format, c->raw_shadow.p, acc->history, out_f, out_8);
     P.num_lights = acc->num_lights;
     if ((rc = run_pixels(c, MODE_SHADOW, P, cfg, WQ_SHADOW))) return rc;
+    if ((rc = wait_planes(c))) return rc;
     if (!(cfg->flags & HY_FLAG_NO_ACCUM) && (rc = accumulate_impl(c, gb, cfg, c->raw_shadow.p, acc))) return rc;
     return run_pixels(c, MODE_SHADE, P, cfg, WQ_SHADE);
 }
@@ -953,11 +967,23 @@ int hy_hybrid_forward_host(HyCtx* c, const HyGBuffer* hgb, const HyCamera* cam, 
     const size_t npx = (size_t)hgb->width * hgb->height;
     HyGBuffer dgb = *hgb;
     for (int p = 0; p < 6; p++) {
-        size_t bytes = npx * fmt_bytes(hgb->format[p]);
-        if ((rc = ensure_size(c, c->host_in[p], bytes))) return rc;
-        HY_CUDA_TRY(cudaMemcpyAsync(c->host_in[p].p, hgb->plane[p], bytes, cudaMemcpyHostToDevice, c->stream));
+        if ((rc = ensure_size(c, c->host_in[p], npx * fmt_bytes(hgb->format[p])))) return rc;
         dgb.plane[p] = c->host_in[p].p;
     }
+    // planes 0 and 1 on the context's stream (the shadow kernel reads them);
+    // planes 2-5 on a side stream that starts once earlier work on the staging
+    // buffers is done and overlaps the shadow kernel
+    c->copy_pending = false;
+    if (!c->copy_stream) HY_CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    if (!c->copy_start) HY_CUDA_TRY(cudaEventCreateWithFlags(&c->copy_start, cudaEventDisableTiming));
+    if (!c->copy_done) HY_CUDA_TRY(cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming));
+    HY_CUDA_TRY(cudaEventRecord(c->copy_start, c->stream));
+    HY_CUDA_TRY(cudaStreamWaitEvent(c->copy_stream, c->copy_start, 0));
+    for (int p = 0; p < 6; p++)
+        HY_CUDA_TRY(cudaMemcpyAsync(c->host_in[p].p, hgb->plane[p], npx * fmt_bytes(hgb->format[p]),
+                                    cudaMemcpyHostToDevice, p < 2 ? c->stream : c->copy_stream));
+    HY_CUDA_TRY(cudaEventRecord(c->copy_done, c->copy_stream));
+    c->copy_pending = true;
     float* d_f = nullptr;
     uint8_t* d_8 = nullptr;
     if (h_out_f) { if ((rc = ensure_size(c, c->host_out_f, npx * 16))) return rc; d_f = c->host_out_f.as<float>(); }

@@ -87,6 +87,11 @@ struct HyCtx {
     hy::DevBuf raw_shadow;  // per-light raw shadow images (unfused path)
     hy::DevBuf hist_prev;   // history snapshot for the reprojection read
     hy::DevBuf host_in[6], host_out_f, host_out_8;  // device staging of hy_hybrid_forward_host
+    // hy_hybrid_forward_host copies G-buffer planes 2-5 on a side stream while
+    // the shadow kernel runs; the passes after it wait for copy_done
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_start = nullptr, copy_done = nullptr;
+    bool copy_pending = false;
     hy::DevBuf grad_partial;  // per-block partial gradient vectors of hy_hybrid_backward
 
     // ---- per-kernel timing (hy_profile_*) ----
