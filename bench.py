@@ -8,7 +8,11 @@ advances every step as it does for a static camera in the reference.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Prints one JSON line.  Under torchrun each rank renders its own frames
-(replicas, no collective); value = rays of all ranks / max wall time.
+(replicas, no collective); value = rays of all ranks / max wall time.  On
+rank 0 the line also carries the two other legs of the headline metric:
+"batch" (64 mixed views over 8 scenes, batched against view by view) and
+"diff" (512x512 forward + adjoint, backward / forward time, gradient check
+against central differences).
 """
 from __future__ import annotations
 
@@ -55,6 +59,10 @@ def parse():
                          "view; diff: 512x512 forward + adjoint; pathtrace: the path-traced mode at 1080p; "
                          "large: 4K, 7.35M triangles, 64 lights, forward + adjoint + batch")
     ap.add_argument("--views", type=int, default=64)
+    ap.add_argument("--no-legs", action="store_true", help="skip the batch and diff legs of the default line")
+    ap.add_argument("--mirror-reflection", action="store_true",
+                    help="the reference's perfect mirror reflection instead of the configuration's GGX-sampled ray")
+    ap.add_argument("--leg-steps", type=int, default=3, help="timed steps of the batch and diff legs")
     return ap.parse_args()
 
 
@@ -66,10 +74,49 @@ def workload(args):
 
 ANYHIT_ORDER = {1: "far first", 2: "near first"}  # HY_ANYHIT_FAR_FIRST / HY_ANYHIT_NEAR_FIRST
 
+# device sources of the pass kernels: a profile summary under profiles/ records the hash
+# of these files, so a figure measured on another version of the kernels is not reported
+# as this version's
+KERNEL_SOURCES = ("hy_device.cuh", "hy_stream.cuh", "hy_shade.cuh", "hy_pass.h", "hy_pass.cu")
+
+
+def kernel_source_sha() -> str:
+    import hashlib
+
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        h.update((ROOT / "vulkanhybridraytracer_gb300" / "csrc" / f).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def profile_records(kernel: str) -> dict:
+    """`bench_record <kernel> key=value ...` lines of the ncu summaries in profiles/:
+    {key: (value, file)} for this kernel."""
+    out = {}
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        for ln in f.read_text().splitlines():
+            parts = ln.split()
+            if len(parts) >= 3 and parts[0] == "bench_record" and parts[1] == kernel:
+                for kv in parts[2:]:
+                    k, _, v = kv.partition("=")
+                    out[k] = (v, f"profiles/{f.name}")
+    return out
+
+
+# the 1080p configuration's reflection ray: GGX-sampled for roughness < 0.3 texels
+# (shading model 3 in the synthetic scenes); --mirror-reflection keeps the reference's
+# perfect reflect()
+def reflection_flags(args) -> int:
+    from vulkanhybridraytracer_gb300 import _lib as L
+
+    return 0 if args.mirror_reflection else L.HY_FLAG_GGX_REFLECTION
+
 
 def config_of(wl, args):
     return {"workload": wl.name, "width": wl.width, "height": wl.height, "triangles": wl.scene.num_tris,
             "lights": len(wl.scene.lights), "shadow_spp": wl.spp, "rng": "decorrelated",
+            "reflection": ("perfect mirror (reflect)" if args.mirror_reflection else
+                           "GGX-sampled from the texel's lobe (roughness < 0.3 texels), 1 ray"),
             "max_bounces": wl.max_bounces, "accumulation": "u8 history, running mean (frame > 0)",
             "gbuffer": "6 planes fp32 (88 B/px), primary-ray producer, untimed",
             "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)"}
@@ -127,7 +174,7 @@ class Clocks:
 
 
 # ---- CPU baseline (the oracle restatement of the reference shaders) ---------------------
-def cpu_run(wl, cam, planes_np, threads: int, target_s: float, frame: int):
+def cpu_run(wl, cam, planes_np, threads: int, target_s: float, frame: int, flags: int = 0):
     """Times the CPU restatement on a band of rows of the same frame, growing the
     band until it takes about target_s; returns (Mrays/s, sample description)."""
     sys.path.insert(0, str(ROOT / "oracle"))
@@ -139,7 +186,7 @@ def cpu_run(wl, cam, planes_np, threads: int, target_s: float, frame: int):
     orc.build_bvh()
     H = planes_np[0].shape[0]
     rows = 4
-    cfg = po.cfg_dict(spp=wl.spp, max_bounces=wl.max_bounces, rng_mode=wl.rng_mode, accum_frame=frame)
+    cfg = po.cfg_dict(spp=wl.spp, max_bounces=wl.max_bounces, rng_mode=wl.rng_mode, accum_frame=frame, flags=flags)
     while True:
         y0 = max(0, H // 2 - rows // 2)
         band = [np.ascontiguousarray(p[y0:y0 + rows]) for p in planes_np]
@@ -184,7 +231,7 @@ def run_reference(args):
     sample = ""
     per_step = max(1.0, args.cpu_seconds / 4)
     for i in range(args.warmup + args.steps):
-        v, sample, _ = cpu_run(wl, cam, planes, threads, per_step, i + 1)
+        v, sample, _ = cpu_run(wl, cam, planes, threads, per_step, i + 1, reflection_flags(args))
         if i >= args.warmup:
             vals.append(v)
     value = float(np.mean(vals)) if vals else 0.0
@@ -201,19 +248,19 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def run_diff(args):
+def diff_leg(steps: int, warmup: int, fd_params: int = 32, clocks_index: int = 0) -> dict:
     """Differentiable form: 512x512, 64 icospheres (subdivision 3), 64 materials, 8 point
     lights, 16 shadow samples; L2 loss against a target rendered from parameters perturbed
     by N(0, 0.05).  Forward = G-buffer + shadow pass + shading at the current parameters;
-    backward = hy_hybrid_backward (visibility held fixed)."""
+    backward = hy_hybrid_backward (visibility held fixed).  The gradient is checked against
+    central differences of the same FP32 forward on `fd_params` seeded parameters, with
+    the shadow images held fixed (the adjoint's visibility) and the loss summed in FP64."""
     import torch
 
     from vulkanhybridraytracer_gb300 import diffrender, scenes
 
     dev = torch.device("cuda", 0)
-    torch.cuda.set_device(0)
-    stream = torch.cuda.Stream(device=dev)
-    torch.cuda.set_stream(stream)
+    stream = torch.cuda.current_stream(dev)
     wl = scenes.diff(3, 512, 512)
     r = diffrender.DiffRenderer(wl.scene, wl.camera(0.0), wl.width, wl.height, spp=wl.spp,
                                 max_bounces=wl.max_bounces)
@@ -225,7 +272,7 @@ def run_diff(args):
     target = target.clone()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
-    def step(timed):
+    def step():
         r.set_params(mp0, lp0)
         flush.zero_()
         e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
@@ -242,33 +289,80 @@ def run_diff(args):
         gm, gl, st = r.backward((planes, shadow), grad)
         e[3].record(stream)
         torch.cuda.synchronize()
-        return e[0].elapsed_time(e[1]), e[2].elapsed_time(e[3]), st, float(((img - target)[..., :3] ** 2).sum())
+        return e[0].elapsed_time(e[1]), e[2].elapsed_time(e[3]), st, (planes, shadow, img, gm, gl)
 
-    for _ in range(args.warmup):
-        step(False)
+    for _ in range(warmup):
+        step()
     fw, bw = [], []
-    clocks = Clocks(0)
+    clocks = Clocks(clocks_index)
     clocks.start()
-    for _ in range(args.steps):
-        f, b, st, loss = step(True)
+    for _ in range(steps):
+        f, b, st, state = step()
         fw.append(f)
         bw.append(b)
     clk = clocks.stop()
+    planes, shadow, img, gm, gl = state
+    loss0 = float(((img - target)[..., :3].double() ** 2).sum())
+
+    # central differences of the FP32 forward, visibility (shadow images) held fixed
+    g = np.concatenate([gm.cpu().numpy().ravel(), gl.cpu().numpy().ravel()]).astype(np.float64)
+    p0 = np.concatenate([mp0.ravel(), lp0.ravel()]).astype(np.float64)
+    nm = mp0.size
+    scale = float(np.abs(g).max())
+    cand = np.flatnonzero(np.abs(g) > 1e-2 * scale)
+    pick = np.random.default_rng(1).choice(cand, size=min(fd_params, len(cand)), replace=False)
+    out = torch.empty((r.H, r.W, 4), dtype=torch.float32, device=dev)
+
+    def loss(p):
+        r.set_params(p[:nm].reshape(mp0.shape).astype(np.float32), p[nm:].reshape(lp0.shape).astype(np.float32))
+        pl = r.ctx.gbuffer(r.cam, r.W, r.H)
+        r.ctx.shade_pass(pl, r.cam, r.cfg, shadow, r.fmt, out_f=out)
+        return float(((out - target)[..., :3].double() ** 2).sum())
+
+    fd = []
+    for j in pick:
+        h = 1e-2 * max(1.0, abs(p0[j]))
+        a, b = p0.copy(), p0.copy()
+        a[j] += h
+        b[j] -= h
+        fd.append((loss(a) - loss(b)) / (2 * h))
+    fd = np.array(fd)
+    rel = np.abs(g[pick] - fd) / np.maximum(np.abs(fd), 1e-2 * scale)
+    r.set_params(mp0, lp0)
     f_ms, b_ms = float(np.mean(fw)), float(np.mean(bw))
-    line = {"metric": "hybrid_backward_ms", "value": b_ms, "unit": "ms", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": b_ms, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": wl.name, "width": wl.width, "height": wl.height,
-                       "triangles": wl.scene.num_tris, "materials": len(wl.scene.materials),
-                       "lights": len(wl.scene.lights), "shadow_spp": wl.spp, "max_bounces": wl.max_bounces,
-                       "params": len(wl.scene.materials) * 5 + len(wl.scene.lights) * 4,
-                       "loss": "L2 vs target rendered from params + N(0, 0.05)",
-                       "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MB write)"},
-            "forward_ms": f_ms, "backward_over_forward": b_ms / f_ms,
-            "backward_rays": {"reflection_rays": st["reflection_rays"], "hit_shadow_rays": st["hit_shadow_rays"]},
-            "loss": loss, "clocks": clk, "gpu_launches": 2}
-    print(json.dumps(line))
+    out = {"workload": wl.name, "width": wl.width, "height": wl.height, "triangles": wl.scene.num_tris,
+           "materials": len(wl.scene.materials), "lights": len(wl.scene.lights), "shadow_spp": wl.spp,
+           "max_bounces": wl.max_bounces, "params": len(wl.scene.materials) * 5 + len(wl.scene.lights) * 4,
+           "loss": loss0, "loss_kind": "L2 vs target rendered from params + N(0, 0.05)",
+           "forward_ms": f_ms, "backward_ms": b_ms, "backward_over_forward": b_ms / f_ms,
+           "forward_parts": "G-buffer + 16-spp shadow pass + shading",
+           "backward_rays": {"reflection_rays": st["reflection_rays"], "hit_shadow_rays": st["hit_shadow_rays"]},
+           "grad_check": {"params": int(len(pick)), "max_rel_err": float(rel.max()) if len(rel) else None,
+                          "median_rel_err": float(np.median(rel)) if len(rel) else None,
+                          "method": "central differences of the FP32 forward (h = 1e-2 max(1, |p|)), shadow "
+                                    "images held fixed, loss summed in FP64; relative to max(|fd|, 1e-2 max|grad|)"},
+           "steps": steps, "warmup": warmup, "clocks": clk,
+           "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MB write)"}
     r.close()
+    return out
+
+
+def run_diff(args):
+    import torch
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream(device=torch.device("cuda", 0))
+    torch.cuda.set_stream(stream)
+    d = diff_leg(args.steps, args.warmup)
+    line = {"metric": "hybrid_backward_ms", "value": d["backward_ms"], "unit": "ms", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": d["backward_ms"], "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {k: d[k] for k in ("workload", "width", "height", "triangles", "materials", "lights",
+                                         "shadow_spp", "max_bounces", "params", "loss_kind", "l2")},
+            "forward_ms": d["forward_ms"], "backward_over_forward": d["backward_over_forward"],
+            "backward_rays": d["backward_rays"], "grad_check": d["grad_check"], "loss": d["loss"],
+            "clocks": d["clocks"], "gpu_launches": 2}
+    print(json.dumps(line))
 
 
 def run_pathtrace(args):
@@ -503,10 +597,11 @@ def run_large(args):
     ctx.close()
 
 
-def run_batch(args):
+def batch_leg(steps: int, warmup: int, n_views: int = 64, tune: bool = False, clocks_index: int = 0) -> dict:
     """64 views over 8 scenes (50k-2M triangles, 320x240..1920x1080, spp 1/4/16/64,
     1-8 lights): the views one by one through hy_hybrid_forward, then as one
-    batch through hy_batch_forward (one persistent launch, CUDA-graph replay)."""
+    batch through hy_batch_forward (one persistent launch, CUDA-graph replay).
+    tune: sweep the launch shapes (autotune) instead of the defaults / the cache."""
     import torch
 
     from vulkanhybridraytracer_gb300 import _lib as L
@@ -514,9 +609,8 @@ def run_batch(args):
     from vulkanhybridraytracer_gb300.hybrid import HybridContext, pass_config
 
     dev = torch.device("cuda", 0)
-    stream = torch.cuda.Stream(device=dev)
-    torch.cuda.set_stream(stream)
-    scs, specs = scenes.batch(2, n_views=args.views)
+    stream = torch.cuda.current_stream(dev)
+    scs, specs = scenes.batch(2, n_views=n_views)
     ctxs = []
     for sc in scs:
         c = HybridContext(0, stream=stream.cuda_stream)
@@ -569,30 +663,53 @@ def run_batch(args):
     st = runner.batch_forward(ctxs, views, graph=False)
     rays = st["shadow_rays"] + st["reflection_rays"] + st["hit_shadow_rays"]
     sig = f"batch{len(views)}-{sum(v['w'] * v['h'] for v in views)}px-{rays}rays"
-    tune = autotune.autotune(lambda ch, mb: batched(ch, mb), sig, torch.cuda.get_device_name(0), timer=dev_time)
-    for _ in range(args.warmup):
+    if tune:
+        tuned = autotune.autotune(lambda ch, mb: batched(ch, mb), sig, torch.cuda.get_device_name(0),
+                                  timer=dev_time)
+    else:
+        tuned = autotune.cached(sig, torch.cuda.get_device_name(0)) or {"chunk": 1, "min_blocks": 8,
+                                                                         "cached": False, "default": True}
+    for _ in range(warmup):
         plain()
-        batched(tune["chunk"], tune["min_blocks"])
-    t_plain = [dev_time(plain) for _ in range(args.steps)]
-    t_batch = [dev_time(lambda: batched(tune["chunk"], tune["min_blocks"])) for _ in range(args.steps)]
+        batched(tuned["chunk"], tuned["min_blocks"])
+    clocks = Clocks(clocks_index)
+    clocks.start()
+    t_plain = [dev_time(plain) for _ in range(steps)]
+    t_batch = [dev_time(lambda: batched(tuned["chunk"], tuned["min_blocks"])) for _ in range(steps)]
+    clk = clocks.stop()
     mp = float(np.median(t_plain))
     mb = float(np.median(t_batch))
-    line = {"metric": "hybrid_batch_mrays_per_s", "value": rays / mb / 1e6, "unit": "Mrays/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * mb, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"batch-{len(views)}views-8scenes", "views": len(views),
-                       "scene_triangles": [c.num_tris for c in ctxs],
-                       "pixels": sum(v["w"] * v["h"] for v in views), "rays_per_batch": rays,
-                       "spp": [v["spp"] for v in views], "lights": [v["hist"].shape[0] for v in views],
-                       "l2": "inputs (G-buffers ~%.1f GB) larger than L2" %
-                             (sum(v["w"] * v["h"] for v in views) * 88 / 1e9)},
-            "plain_per_view": {"value": rays / mp / 1e6, "unit": "Mrays/s", "ms_per_step": 1e3 * mp},
-            "batched_over_plain": mp / mb,
-            "autotune": tune,
-            "gpu_launches": 2}
-    print(json.dumps(line))
+    out = {"workload": f"batch-{len(views)}views-8scenes", "views": len(views),
+           "scene_triangles": [c.num_tris for c in ctxs],
+           "pixels": sum(v["w"] * v["h"] for v in views), "rays_per_batch": rays,
+           "spp": [v["spp"] for v in views], "lights": [v["hist"].shape[0] for v in views],
+           "batched_ms": 1e3 * mb, "plain_ms": 1e3 * mp, "batched_over_plain": mp / mb,
+           "batched_mrays_per_s": rays / mb / 1e6, "plain_mrays_per_s": rays / mp / 1e6,
+           "tuning": {k: tuned[k] for k in ("chunk", "min_blocks") if k in tuned},
+           "steps": steps, "warmup": warmup, "clocks": clk,
+           "l2": "inputs (G-buffers ~%.1f GB) larger than L2" % (sum(v["w"] * v["h"] for v in views) * 88 / 1e9)}
+    if tune:
+        out["autotune"] = tuned
     for c in ctxs + [runner]:
         c.close()
+    return out
+
+
+def run_batch(args):
+    import torch
+
+    stream = torch.cuda.Stream(device=torch.device("cuda", 0))
+    torch.cuda.set_stream(stream)
+    d = batch_leg(args.steps, args.warmup, args.views, tune=True)
+    line = {"metric": "hybrid_batch_mrays_per_s", "value": d["batched_mrays_per_s"], "unit": "Mrays/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": d["batched_ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {k: d[k] for k in ("workload", "views", "scene_triangles", "pixels", "rays_per_batch", "spp",
+                                         "lights", "l2")},
+            "plain_per_view": {"value": d["plain_mrays_per_s"], "unit": "Mrays/s", "ms_per_step": d["plain_ms"]},
+            "batched_over_plain": d["batched_over_plain"], "autotune": d.get("autotune"), "clocks": d["clocks"],
+            "gpu_launches": 2}
+    print(json.dumps(line))
 
 
 def main():
@@ -637,7 +754,7 @@ def main():
     out_8 = torch.empty((wl.height, wl.width, 4), dtype=torch.uint8, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
-    sched = {"pool": L.HY_FLAG_RAY_POOL, "groups": L.HY_FLAG_LANE_GROUPS}.get(args.sched, 0)
+    sched = {"pool": L.HY_FLAG_RAY_POOL, "groups": L.HY_FLAG_LANE_GROUPS}.get(args.sched, 0) | reflection_flags(args)
 
     def cfg(frame, flags=L.HY_FLAG_NO_STATUS_SYNC):
         return pass_config(spp=wl.spp, max_bounces=wl.max_bounces, rng_mode=wl.rng_mode, accum_frame=frame,
@@ -723,13 +840,27 @@ def main():
     else:  # no per-kernel record: the whole frame
         dom = "frame"
         achieved = alg_frame / (ms_per_step / 1e3) / 1e9
-    # DRAM bytes per launch from the committed ncu summary of the same workload
-    traffic = None
-    for f in sorted((ROOT / "profiles").glob(f"*-{wl.width}x{wl.height}_dram.md")):
-        for ln in f.read_text().splitlines():
-            parts = ln.split()
-            if len(parts) == 3 and parts[0] == "traffic_bytes_per_launch" and parts[1] == dom:
-                traffic = int(parts[2])
+    # DRAM bytes per launch and the issue counters from the committed ncu summaries
+    # (profiles/), used only when they were measured on these kernel sources
+    rec = profile_records(dom)
+    cur_sha = kernel_source_sha()
+
+    def rec_val(key, conv=float):
+        v = rec.get(key)
+        if v is None or rec.get("source_sha", ("", ""))[0] != cur_sha:
+            return None
+        return conv(v[0])
+
+    wkey = f"{wl.width}x{wl.height}"
+    traffic = rec_val(f"dram_bytes_{wkey}", int)
+    evidence = {"source_sha": cur_sha, "profile_sha": rec.get("source_sha", (None,))[0],
+                "current": rec.get("source_sha", ("",))[0] == cur_sha,
+                "files": sorted({v[1] for v in rec.values()}),
+                "issue_active_pct": rec_val("issue_active_pct"),
+                "lanes_per_inst": rec_val("lanes_per_inst"),
+                "alu_pipe_pct": rec_val("alu_pipe_pct"),
+                "l2_gbs": rec_val("l2_gbs"), "l2_bytes_per_launch": rec_val("l2_bytes"),
+                "dram_gbs": rec_val("dram_gbs"), "profiled_case": rec.get("case", (None,))[0]}
 
     # e2e: host G-buffer in, host BGRA8 image out, through hy_hybrid_forward_host
     planes_h = [p.cpu().pin_memory() for p in planes]
@@ -753,7 +884,7 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         planes_np = [p.cpu().numpy() for p in planes]
         threads = os.cpu_count() or 1
-        v, sample, _ = cpu_run(wl, wl.camera(1.0), planes_np, threads, args.cpu_seconds, 1)
+        v, sample, _ = cpu_run(wl, wl.camera(1.0), planes_np, threads, args.cpu_seconds, 1, reflection_flags(args))
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
 
     if rank == 0:
@@ -772,13 +903,23 @@ def main():
             "gpu_launches": 2 * args.steps,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": 1e3 * sum(e2e_t) / len(e2e_t)},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            # the dominant kernel's algorithmic bytes against the measured HBM copy
+            # bandwidth; what bounds it is instruction issue (ncu: issue-active
+            # share, active lanes per instruction, ALU pipe), not DRAM, whose traffic
+            # is a fraction of a percent of the algorithmic bytes (the BVH and
+            # triangles stay in L2)
+            "roofline": {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "kernel": dom,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
+                         "evidence": evidence,
                          "per_kernel": per_kernel,
                          "frame": {"alg_bytes": alg_frame, "achieved": alg_frame / (ms_per_step / 1e3) / 1e9}},
             "cpu_baseline": cpu,
         }
+        if not args.no_legs:
+            # the other two legs of the metric: batched vs plain, backward / forward
+            line["batch"] = batch_leg(args.leg_steps, 1, clocks_index=local)
+            line["diff"] = diff_leg(args.leg_steps, 2, clocks_index=local)
         print(json.dumps(line))
     ctx.close()
     replicas.finalize()

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define HY_ABI_VERSION 3
+#define HY_ABI_VERSION 4
 
 /* ---- error codes (the reference aborts through VK_CHECK, src/vk_engine.h:15-24) ---- */
 enum {
@@ -50,7 +50,8 @@ enum {
     HY_ERR_NAN_INPUT       = -7,
     HY_ERR_NOT_READY       = -8,  /* scene or BVH missing */
     HY_ERR_UNSUPPORTED     = -9,
-    HY_ERR_TOO_LARGE       = -10  /* input exceeds the fixed scratch of an allocation-free entry point */
+    HY_ERR_TOO_LARGE       = -10, /* input exceeds the fixed scratch of an allocation-free entry point */
+    HY_ERR_BAD_INDEX       = -11  /* a traversal met a node/record index outside the structure */
 };
 
 /* device status-word bits (HyStats.error_flags) */
@@ -168,6 +169,14 @@ enum { HY_RNG_REFERENCE = 0, HY_RNG_DECORRELATED = 1 };
                                             each lane as soon as its ray ends */
 #define HY_FLAG_LANE_GROUPS        0x40u /* the samples of a pixel-light on a fixed group of adjacent lanes,
                                             which waits for its slowest sample before the next pixel-light */
+/* GGX-sampled reflection ray for mirror texels (shading model 3: the benchmark scenes give it to
+ * materials with roughness < 0.3).  The reference reflects perfectly (hybridRaygen.rgen:125); with
+ * this flag the first bounce direction is reflect(-V, H) around a microfacet normal H drawn with
+ * density D(H) (N.H), D the reference's DistributionGGX (helpers.glsl:33-45, alpha = roughness^2
+ * from G-buffer plane 4), from two draws of the texel's TEA/LCG stream (random.glsl:3-33) made
+ * before the bounce loop; a direction below the surface falls back to the mirror direction.  The
+ * later bounces and everything else are the reference's. */
+#define HY_FLAG_GGX_REFLECTION     0x80u
 
 typedef struct HyPassConfig {
     uint32_t shadow_spp;    /* samplesBuffer.samples (1..64, src/renderer.cpp:656) */
@@ -189,7 +198,7 @@ typedef struct HyPassConfig {
                                0 = 6 for the lane-group kernel, 8 otherwise */
     uint32_t visits_per_round; /* BVH node visits a shadow lane makes between two scheduling rounds
                                   of the persistent shadow kernels (1..16; a lane whose ray ends
-                                  early waits for the round); 0 = 4 */
+                                  early waits for the round); 0 = 4 (tile streams: 8) */
 } HyPassConfig;
 
 typedef struct HyStats {
@@ -228,6 +237,16 @@ int         hy_synchronize(HyCtx* ctx);
 /* Allocation hook for fault-injection tests: the next `n`-th device
  * allocation made by the context fails with HY_ERR_OOM (0 disables). */
 int         hy_debug_fail_alloc_after(HyCtx* ctx, uint32_t n);
+/* Per-ray limits of every BVH walk of the context's passes, lowered for
+ * failure-detection tests: a ray that makes more than max_node_visits node
+ * visits stops and the call returns HY_ERR_TIMEOUT; one whose traversal stack
+ * would grow past max_stack_depth entries stops and the call returns
+ * HY_ERR_STACK_OVERFLOW.  Both limits are counters tested before the step
+ * they guard, so running out stops the ray and nothing else: the context
+ * stays usable.  0 restores the built-in limit (2^22 visits, 64 entries);
+ * max_stack_depth > 64 is HY_ERR_INVALID_ARG.  The reference's policy for a
+ * failed GPU call is to abort the process (VK_CHECK, src/vk_engine.h:15-24). */
+int         hy_debug_set_traversal_limits(HyCtx* ctx, uint32_t max_node_visits, uint32_t max_stack_depth);
 
 /* ---- scene upload (host arrays; replaces Renderer::load_data_to_gpu,
  *      src/renderer.cpp:1477-1530, and the per-entity rtVertexAttribute /
@@ -482,7 +501,9 @@ int hy_batch_forward(HyCtx* ctx, HyCtx* const* scenes, uint32_t num_scenes, cons
  * whose history (width * height * num_lights * 1 or 4 bytes) exceeds it
  * return HY_ERR_TOO_LARGE.  The first call on a device looks up the array's
  * device address (once per device); make that first call before any stream
- * capture.  All calls on a device share the one array, so calls whose work
+ * capture.  The address stays cached for the life of the process, so after a
+ * cudaDeviceReset of a device the entry point must not be called on that
+ * device again.  All calls on a device share the one array, so calls whose work
  * overlaps on the GPU (different streams, not ordered) race on it; order
  * them on one stream.  The array keeps the last call's contents; nothing in
  * it needs to start at zero. */

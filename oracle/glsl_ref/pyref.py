@@ -16,14 +16,26 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE.parent / "_ref" / "libglslref.so"
-REF_DIR = Path(os.environ.get("HY_REFERENCE_DIR", "/root/reference"))
+
+
+def _reference_dir() -> Path | None:
+    """The reference checkout: HY_REFERENCE_DIR, else the recipe's (Makefile) default."""
+    env = os.environ.get("HY_REFERENCE_DIR")
+    if env:
+        return Path(env)
+    r = subprocess.run(["make", "-s", "-C", str(HERE), "print-ref"], capture_output=True, text=True)
+    out = r.stdout.strip()
+    return Path(out) if r.returncode == 0 and out else None
+
+
+REF_DIR = _reference_dir()
 P = C.c_void_p
 U32 = C.c_uint32
 _lib = None
 
 
 def available() -> bool:
-    return LIB.exists() or (REF_DIR / "data" / "shaders" / "hybridRaygen.rgen").exists()
+    return LIB.exists() or (REF_DIR is not None and (REF_DIR / "data" / "shaders" / "hybridRaygen.rgen").exists())
 
 
 def build() -> Path:
@@ -37,7 +49,7 @@ def load():
     global _lib
     if _lib is not None:
         return _lib
-    if REF_DIR.exists():
+    if REF_DIR is not None and (REF_DIR / "data" / "shaders").exists():
         build()
     if not LIB.exists():
         raise RuntimeError("oracle/_ref/libglslref.so is not built (needs the reference checkout)")

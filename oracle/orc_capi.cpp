@@ -162,6 +162,18 @@ void orc_sample_disk(const float* light_radius, const float* pos, const float* L
     out[0] = d.x; out[1] = d.y; out[2] = d.z;
 }
 // out: D, G, F.rgb for one (N, V, L, roughness, F0) evaluation
+// ggx_reflect in float (dbl = 0) or double (dbl = 1); out: the direction (3 floats)
+void orc_ggx_reflect(const float* N, const float* V, float roughness, float u1, float u2, int dbl, float* out) {
+    if (dbl) {
+        const V3<double> d = ggx_reflect<double>(v3<double>(N[0], N[1], N[2]), v3<double>(V[0], V[1], V[2]),
+                                                 roughness, u1, u2);
+        out[0] = (float)d.x; out[1] = (float)d.y; out[2] = (float)d.z;
+    } else {
+        const V3<float> d = ggx_reflect<float>(v3(N[0], N[1], N[2]), v3(V[0], V[1], V[2]), roughness, u1, u2);
+        out[0] = d.x; out[1] = d.y; out[2] = d.z;
+    }
+}
+
 void orc_brdf(const float* N, const float* V, const float* L, float roughness, const float* F0, float cosTheta,
               float* out) {
     V3<float> n = v3(N[0], N[1], N[2]), v = v3(V[0], V[1], V[2]), l = v3(L[0], L[1], L[2]);

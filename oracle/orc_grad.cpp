@@ -355,6 +355,10 @@ void grad_record(const Scene& s, const GBufHost& g, const HyCamera& cam, const H
                     direction = radicand < 0.f ? reflect(Iv, p.N) : refract(Iv, refrN, eta);
                 }
             }
+            if ((cfg.flags & HY_FLAG_GGX_REFLECTION) && p.smode == 3 && cfg.max_bounces > 0) {
+                const float u1 = rnd(seed), u2 = rnd(seed);
+                direction = ggx_reflect<float>(p.N, p.V, g4[1], u1, u2);
+            }
             for (uint32_t depth = 0; depth < cfg.max_bounces && depth < (uint32_t)kGradMaxBounces; depth++) {
                 if (p.smode == 0) break;
                 const V3<float> ro = origin + direction * 1e-2f;

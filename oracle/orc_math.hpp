@@ -115,6 +115,31 @@ template <class T> inline V3<T> sampleDisk(const float lpos_radius, V3<T> positi
     return normalize(target - position);
 }
 
+// GGX-sampled reflection, the HY_FLAG_GGX_REFLECTION extension (the reference
+// reflects perfectly, hybridRaygen.rgen:125): a microfacet normal H with
+// density D(H) (N.H) for DistributionGGX above (alpha = roughness^2), from the
+// uniform draws u1 (azimuth 2 pi u1) and u2 (polar angle from the inverse of
+// the lobe's cumulative distribution, tan^2 = alpha^2 u2 / (1 - u2), a form
+// without the cancellation of 1 - cos^2 for narrow lobes), in a frame around N
+// built from the world axis least aligned with N; the ray is
+// reflect(normalize(-V), H), or the mirror direction when that would leave
+// below the surface.  The kernels run the same single-rounded sequence.
+template <class T> inline V3<T> ggx_reflect(V3<T> N, V3<T> V, T roughness, T u1, T u2) {
+    const T a = roughness * roughness;
+    const T a2 = a * a;
+    const T t2 = (a2 * u2) / (T(1) - u2);
+    const T cosT = T(1) / std::sqrt(T(1) + t2);
+    const T sinT = std::sqrt(t2) * cosT;
+    const T phi = T(2) * K<T>::PI * u1;
+    const V3<T> up = std::fabs(N.y) < T(0.999f) ? v3(T(0), T(1), T(0)) : v3(T(1), T(0), T(0));
+    const V3<T> Tn = normalize(cross(up, N));
+    const V3<T> Bn = cross(N, Tn);
+    const V3<T> Hm = Tn * (sinT * std::cos(phi)) + Bn * (sinT * std::sin(phi)) + N * cosT;
+    const V3<T> I = normalize(-V);
+    const V3<T> d = reflect(I, Hm);
+    return dot(d, N) > T(0) ? d : reflect(I, N);
+}
+
 // ---- bit helpers shared by the BVH code --------------------------------------
 inline uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
 inline float bitsf(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }

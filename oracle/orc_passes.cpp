@@ -545,6 +545,11 @@ void shade(const Scene& s, const GBufHost& g, const HyCamera& cam, const HyPassC
                                                          : irradiance * albedo * metallic);
                     }
                 }
+                // HY_FLAG_GGX_REFLECTION: the mirror texel's first bounce from its GGX lobe
+                if ((cfg.flags & HY_FLAG_GGX_REFLECTION) && smode == 3 && cfg.max_bounces > 0) {
+                    const float u1 = rnd(seed), u2 = rnd(seed);
+                    direction = ggx_reflect<float>(N, V, roughness, u1, u2);
+                }
                 for (uint32_t depth = 0; depth < cfg.max_bounces; depth++) {
                     if (smode == 0) break;
                     V3<float> ro = origin + direction * 1e-2f;

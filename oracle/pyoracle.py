@@ -57,6 +57,7 @@ def load():
         "orc_rnd_seq": (None, [U32, U32, P, P]),
         "orc_sample_disk": (None, [P, P, P, U32, P]),
         "orc_brdf": (None, [P, P, P, C.c_float, P, C.c_float, P]),
+        "orc_ggx_reflect": (None, [P, P, C.c_float, C.c_float, C.c_float, C.c_int, P]),
         "orc_gbuffer_primary": (C.c_int, [P, P, U32, U32, P, C.c_int]),
         "orc_shadow_pass": (C.c_int, [P, P, P, P, U32, P, C.c_int, P]),
         "orc_accumulate": (C.c_int, [P, P, P, P, P]),
@@ -141,6 +142,15 @@ def brdf(N, V, L, roughness, F0, cos_theta):
     out = np.zeros(5, np.float32)
     a = [np.ascontiguousarray(x, np.float32) for x in (N, V, L, F0)]
     load().orc_brdf(_p(a[0]), _p(a[1]), _p(a[2]), float(roughness), _p(a[3]), float(cos_theta), _p(out))
+    return out
+
+
+def ggx_reflect(N, V, roughness, u1, u2, double=False) -> np.ndarray:
+    """The GGX-sampled reflection direction (HY_FLAG_GGX_REFLECTION) for one texel."""
+    n = np.ascontiguousarray(N, np.float32)
+    v = np.ascontiguousarray(V, np.float32)
+    out = np.zeros(3, np.float32)
+    load().orc_ggx_reflect(_p(n), _p(v), float(roughness), float(u1), float(u2), int(double), _p(out))
     return out
 
 

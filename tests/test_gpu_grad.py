@@ -108,7 +108,8 @@ def test_autograd_harness_matches_direct_call(diff_case):
     import torch
     c = diff_case
     r = c["r"]
-    fn = diffrender.render_fn()
+    from grad_harness import render_fn
+    fn = render_fn()
     mp = torch.tensor(c["mp0"], dtype=torch.float32, requires_grad=True)
     lp = torch.tensor(c["lp0"], dtype=torch.float32, requires_grad=True)
     target = torch.tensor(c["target"][..., :3], device=r.dev)

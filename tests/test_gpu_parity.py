@@ -6,7 +6,11 @@ bit-exact.  Radiance follows the pass's stated tolerance: relative RMS
 <= 1e-3 and per-pixel max |err| <= 1e-2 on pixels whose shadow decisions
 agree; decisions may differ on at most 1e-4 of the shadow texels (a shadow
 ray direction built from cosf/sinf can differ by an ulp between CUDA and
-libm and graze an edge differently).
+libm and graze an edge differently).  Texels whose decision flipped are not
+exempt: the oracle also shades the frame from the GPU's own shadow history,
+and the GPU image must match that within 1e-2 per pixel everywhere, so a
+flip may change a pixel by exactly the flipped samples' share of their
+light and no more.
 """
 import numpy as np
 import pytest
@@ -174,14 +178,20 @@ def run_both(p: Pair, frame, spp, rng_mode, fmt, flags=0, max_bounces=None, hist
     st = p.ctx.forward(dplanes, cam, pass_config(spp, mb, rng_mode, frame, flags), hist_g, fmt, out_f=out_f,
                        out_8=out_8, formats=formats)
     hist_o = hist0.copy().astype(dt)
-    of, o8, osh, ost = p.orc.forward(planes, cam, po.cfg_dict(spp, mb, rng_mode, frame, flags), hist_o, fmt,
-                                     formats=formats)
-    return (out_f.cpu().numpy(), out_8.cpu().numpy(), hist_g.cpu().numpy(), st), (of, o8, hist_o, osh, ost)
+    ocfg = po.cfg_dict(spp, mb, rng_mode, frame, flags)
+    of, o8, osh, ost = p.orc.forward(planes, cam, ocfg, hist_o, fmt, formats=formats)
+    hg = hist_g.cpu().numpy()
+    of_g = None
+    if not flags & L.HY_FLAG_NO_ACCUM:
+        # the oracle's shading of the GPU's own shadow history: what the GPU image must be
+        # given the GPU's shadow decisions
+        of_g = p.orc.shade(planes, cam, ocfg, np.ascontiguousarray(hg), fmt, formats=formats)[0]
+    return (out_f.cpu().numpy(), out_8.cpu().numpy(), hg, st), (of, o8, hist_o, osh, ost, of_g)
 
 
 def check_parity(g, o, fmt):
     out_f, out_8, hist_g, st = g
-    of, o8, hist_o, osh, ost = o
+    of, o8, hist_o, osh, ost, of_g = o
     assert st["error_flags"] == 0
     flips = np.mean(hist_g != hist_o)
     assert flips <= FLIP_TOL, f"history differs on {flips:.2e} of texels"
@@ -190,6 +200,11 @@ def check_parity(g, o, fmt):
     rms = np.sqrt((err ** 2).sum() / max((of[..., :3].astype(np.float64) ** 2).sum(), 1e-30))
     assert rms <= RMS_TOL, f"relative RMS {rms:.3e}"
     assert err[agree].max(initial=0) <= MAX_TOL, f"max |err| {err[agree].max():.3e}"
+    if of_g is not None:
+        # every pixel, flipped shadow decisions included, against the oracle shading the
+        # GPU's history: a flip moves the pixel by its samples' share of the light only
+        err_g = np.abs(out_f[..., :3].astype(np.float64) - of_g[..., :3])
+        assert err_g.max(initial=0) <= MAX_TOL, f"max |err| vs shading of the GPU history {err_g.max():.3e}"
     assert np.all(out_f[..., 3] == 1)
     bad8 = np.abs(out_8.astype(int) - o8.astype(int)) > 1
     assert bad8[agree].mean() <= 1e-3
@@ -216,6 +231,31 @@ def test_forward_f32_history_and_flags(small, flags, frame):
 def test_forward_glass_mirror_bounces(glass, frame):
     g, o = run_both(glass, frame, 2, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8)
     assert g[3]["reflection_rays"] > g[3]["hit_shadow_rays"] > 0
+    check_parity(g, o, L.HY_ACCUM_U8)
+
+
+@pytest.mark.parametrize("rng_mode,spp", [(L.HY_RNG_REFERENCE, 1), (L.HY_RNG_DECORRELATED, 4)])
+def test_forward_ggx_reflection(small, rng_mode, spp):
+    """HY_FLAG_GGX_REFLECTION: the mirror texels' reflection ray sampled from their GGX
+    lobe with the texel's own RNG stream, against the oracle restating the same
+    sampling; the flag changes the mirror texels and no others."""
+    g, o = run_both(small, 2, spp, rng_mode, L.HY_ACCUM_U8, flags=L.HY_FLAG_GGX_REFLECTION)
+    check_parity(g, o, L.HY_ACCUM_U8)
+    g0, _ = run_both(small, 2, spp, rng_mode, L.HY_ACCUM_U8)
+    wl = small.wl
+    planes = small.orc.gbuffer(wl.camera(2.0), wl.width, wl.height)
+    mats = np.array([m.shading_model for m in wl.scene.materials])
+    mi = planes[0][..., 3].astype(np.int64)
+    mirror = (mats[np.clip(mi, 0, len(mats) - 1)] == 3) & ~((planes[0][..., 3] == 0) & (planes[1][..., 3] == 0))
+    changed = np.any(g[0] != g0[0], axis=-1)
+    assert changed.any() and not changed[~mirror].any()
+    assert g[3]["reflection_rays"] == g0[3]["reflection_rays"] > 0
+
+
+@pytest.mark.parametrize("frame", [0, 2])
+def test_forward_ggx_glass_mirror_bounces(glass, frame):
+    """The GGX-sampled first bounce followed by the reference's 8-bounce glass/mirror chain."""
+    g, o = run_both(glass, frame, 2, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8, flags=L.HY_FLAG_GGX_REFLECTION)
     check_parity(g, o, L.HY_ACCUM_U8)
 
 
@@ -294,10 +334,11 @@ def test_host_buffers_equal_device(small):
 
 
 def test_host_buffers_back_to_back(small):
-    """Host-buffer calls queued without a host sync, each on another G-buffer
-    (planes 2-5 go up on a side stream that must wait for the previous call's
-    passes): frames 0 (raw images + blur) and 1-3 (fused running mean) equal
-    the device-buffer calls."""
+    """Host-buffer calls one after another, each on another G-buffer: frames 0
+    (raw images + blur) and 1-3 (fused running mean) equal the device-buffer
+    calls.  hy_hybrid_forward_host always waits for its own result (it copies
+    the image back), so these calls run in sequence; the next test covers a
+    host-buffer call queued behind work still running on the stream."""
     from vulkanhybridraytracer_gb300.hybrid import pass_config
     torch = _torch()
     wl = small.wl
@@ -324,11 +365,78 @@ def test_host_buffers_back_to_back(small):
     assert torch.equal(h_dev, h_host)
 
 
+def test_host_buffers_behind_pending_work(small):
+    """A host-buffer call queued behind device-buffer calls that are still
+    running (HY_FLAG_NO_STATUS_SYNC, no host sync in between): its planes 2-5
+    go up on a side stream that must start only after the earlier passes, and
+    the shared history must see every frame in order.  Alternating device and
+    host calls give the same images and history as device calls alone."""
+    from vulkanhybridraytracer_gb300.hybrid import pass_config
+    torch = _torch()
+    wl = small.wl
+    W, H, nl = wl.width, wl.height, len(wl.scene.lights)
+    frames = [0, 1, 2, 3, 4, 5]
+    gbs = [small.orc.gbuffer(wl.camera(float(9 + f)), W, H) for f in frames]
+    h_ref = torch.zeros((nl, H, W), dtype=torch.uint8, device="cuda")
+    h_mix = h_ref.clone()
+    dplanes = [[torch.from_numpy(x).cuda() for x in pn] for pn in gbs]
+    outs_ref = [torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda") for _ in frames]
+    outs_dev = [torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda") for _ in frames]
+    torch.cuda.synchronize()   # torch's stream vs the context's own stream
+    want = []
+    for f, dp, o in zip(frames, dplanes, outs_ref):
+        small.ctx.forward(dp, wl.camera(float(9 + f)), pass_config(4, 1, L.HY_RNG_DECORRELATED, f, 0), h_ref,
+                          L.HY_ACCUM_U8, out_8=o)
+        want.append(o.cpu().numpy())
+    got = []
+    for f, pn, dp, od in zip(frames, gbs, dplanes, outs_dev):
+        if f % 2 == 0:   # queued, not waited for
+            small.ctx.forward(dp, wl.camera(float(9 + f)),
+                              pass_config(4, 1, L.HY_RNG_DECORRELATED, f, L.HY_FLAG_NO_STATUS_SYNC), h_mix,
+                              L.HY_ACCUM_U8, out_8=od, stats=False)
+            got.append(od)
+        else:            # host buffers, right behind the pending call
+            oh = np.zeros((H, W, 4), np.uint8)
+            small.ctx.forward_host(pn, wl.camera(float(9 + f)),
+                                   pass_config(4, 1, L.HY_RNG_DECORRELATED, f, 0), h_mix, L.HY_ACCUM_U8, out_8=oh)
+            got.append(oh)
+    small.ctx.synchronize()
+    for f, a, b in zip(frames, want, got):
+        b = b.cpu().numpy() if hasattr(b, "cpu") else b
+        assert np.array_equal(a, b), f
+    assert torch.equal(h_ref, h_mix)
+
+
 def test_deterministic(small):
     a = run_both(small, 3, 4, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8)[0]
     b = run_both(small, 3, 4, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8)[0]
     for x, y in zip(a[:3], b[:3]):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("visits", [1, 8, 16])
+def test_stream_counts_equal_per_lane_walk(small, visits):
+    """The tile streams split every ray's walk into scheduling rounds and hand
+    the samples to whichever lanes are free, but each ray makes the same node
+    visits and triangle tests: images and node/triangle counts equal one lane
+    per pixel's."""
+    from vulkanhybridraytracer_gb300.hybrid import pass_config
+    torch = _torch()
+    wl = small.wl
+    W, H, nl = wl.width, wl.height, len(wl.scene.lights)
+    cam = wl.camera(6.0)
+    planes = [torch.from_numpy(x).cuda() for x in small.orc.gbuffer(cam, W, H)]
+    a = torch.zeros((nl, H, W), dtype=torch.uint8, device="cuda")
+    b = torch.zeros_like(a)
+    torch.cuda.synchronize()
+    fl = L.HY_FLAG_COUNT_TRAVERSAL
+    sa = small.ctx.shadow_pass(planes, cam, pass_config(8, 1, L.HY_RNG_DECORRELATED, 6, fl, visits_per_round=visits),
+                               a)
+    sb = small.ctx.shadow_pass(planes, cam, pass_config(8, 1, L.HY_RNG_DECORRELATED, 6, fl | L.HY_FLAG_PIXEL_PARALLEL),
+                               b)
+    assert torch.equal(a, b)
+    for k in ("shadow_rays", "nodes_visited", "tris_tested"):
+        assert sa[k] == sb[k] > 0, k
 
 
 def test_counts_match_oracle_pass(small):
@@ -422,6 +530,44 @@ def test_error_paths(gpu_lib, oracle_lib):
     ctx.close()
 
 
+def test_traversal_limits_run_out(gpu_lib, oracle_lib):
+    """Failure detection without a GPU fault: with the per-ray node-visit budget
+    or the stack cap lowered at run time, every kind of walk stops at the
+    counter test and the call reports HY_ERR_TIMEOUT / HY_ERR_STACK_OVERFLOW;
+    with the limits restored the same context traces and renders exactly as
+    the oracle again."""
+    from vulkanhybridraytracer_gb300.hybrid import pass_config
+    torch = _torch()
+    p = Pair(glass_workload(48, 48))
+    lib, h = p.ctx.lib, p.ctx.h
+    rays = torch.from_numpy(_rays(np.random.default_rng(5), 20000)).cuda()
+    W, H, nl = p.wl.width, p.wl.height, len(p.wl.scene.lights)
+    cam = p.wl.camera(1.0)
+    planes = [torch.from_numpy(x).cuda() for x in p.orc.gbuffer(cam, W, H)]
+    hist = torch.zeros((nl, H, W), dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    cases = [((2, 0), L.HY_ERR_TIMEOUT), ((0, 1), L.HY_ERR_STACK_OVERFLOW)]
+    for (visits, depth), code in cases:
+        assert lib.hy_debug_set_traversal_limits(h, visits, depth) == L.HY_OK
+        for any_hit in (False, True):
+            with pytest.raises(L.HyError) as e:
+                p.ctx.trace(rays, any_hit)
+            assert e.value.code == code, (visits, depth, any_hit)
+        for frame, flags in ((0, 0), (3, 0), (3, L.HY_FLAG_PIXEL_PARALLEL)):
+            with pytest.raises(L.HyError) as e:
+                p.ctx.forward(planes, cam, pass_config(4, 8, L.HY_RNG_DECORRELATED, frame, flags), hist)
+            assert e.value.code == code, (visits, depth, frame, flags)
+    assert lib.hy_debug_set_traversal_limits(h, 0, 65) == L.HY_ERR_INVALID_ARG
+    assert lib.hy_debug_set_traversal_limits(h, 0, 0) == L.HY_OK
+    hg, sg = p.ctx.trace(rays, False, count=True)
+    ho, co = p.orc.trace(rays.cpu().numpy(), False)
+    assert np.array_equal(hg.cpu().numpy().view(np.uint32), ho.view(np.uint32)) and sg["error_flags"] == 0
+    g, o = run_both(p, 2, 2, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8)
+    check_parity(g, o, L.HY_ACCUM_U8)
+    assert lib.hy_error_string(L.HY_ERR_BAD_INDEX).decode().startswith("acceleration structure index")
+    p.ctx.close()
+
+
 def test_device_memory_cap(gpu_lib):
     from vulkanhybridraytracer_gb300.hybrid import HybridContext
     wl = scenes.small(0, 32, 32)
@@ -444,10 +590,14 @@ def test_hd_bvh_bitexact(hd):
     assert_bvh_equal(hd)
 
 
-def test_hd_forward_parity(hd):
-    """Whole 1920x1080 frame, 4 lights x 16 decorrelated samples, against the oracle."""
-    g, o = run_both(hd, 3, 16, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8)
+@pytest.mark.parametrize("flags", [0, L.HY_FLAG_GGX_REFLECTION])
+def test_hd_forward_parity(hd, flags):
+    """Whole 1920x1080 frame, 4 lights x 16 decorrelated samples, against the oracle;
+    with perfect mirror reflections (the reference's) and with the configuration's
+    GGX-sampled reflection ray for roughness < 0.3 texels."""
+    g, o = run_both(hd, 3, 16, L.HY_RNG_DECORRELATED, L.HY_ACCUM_U8, flags=flags)
     check_parity(g, o, L.HY_ACCUM_U8)
+    assert g[3]["reflection_rays"] > 0
 
 
 @pytest.mark.parametrize("spp", [2, 3, 16, 40])

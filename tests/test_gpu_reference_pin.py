@@ -2,7 +2,8 @@
 (tests/golden/ref_pass_small.npz, see tests/golden/make_golden.py), through
 the C ABI.  The GPU traverses its BVH8 and uses CUDA's cosf/sinf, the fixture
 came from brute-force traversal and libm: shadow decisions may differ on
-exact ties/edges (<= 1e-3 of texels), radiance within 1e-3 relative RMS."""
+exact ties/edges (<= 1e-4 of texels, the bar of every other parity test),
+radiance within 1e-3 relative RMS."""
 from pathlib import Path
 
 import numpy as np
@@ -37,7 +38,7 @@ def test_gpu_shadow_pass_vs_reference(setup, spp):
     nl, H, W = fx[f"shadow_spp{spp}"].shape
     sh = torch.zeros((nl, H, W), dtype=torch.uint8, device="cuda")
     ctx.shadow_pass(planes, fx["camera"], pass_config(spp, 8, L.HY_RNG_REFERENCE, 3), sh, L.HY_ACCUM_U8)
-    assert np.mean(sh.cpu().numpy() != fx[f"shadow_spp{spp}"]) <= 1e-3
+    assert np.mean(sh.cpu().numpy() != fx[f"shadow_spp{spp}"]) <= 1e-4
 
 
 def test_gpu_shade_pass_vs_reference(setup):
@@ -54,7 +55,7 @@ def test_gpu_shade_pass_vs_reference(setup):
     rms = np.sqrt((err ** 2).sum() / (ref[..., :3].astype(np.float64) ** 2).sum())
     assert st["reflection_rays"] > 0
     assert rms <= 1e-3, rms
-    assert np.mean(err.max(-1) > 1e-2) <= 1e-3
+    assert err.max() <= 1e-2, err.max()
 
 
 def test_gpu_blur_vs_reference(setup):

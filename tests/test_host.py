@@ -33,11 +33,11 @@ def test_library_exports_every_header_symbol(lib):
     for n in names:
         assert hasattr(lib, n), n
     assert set(names) == set(L.PROTOTYPES), "ctypes prototypes and the header disagree"
-    assert lib.hy_get_abi_version() == 3
+    assert lib.hy_get_abi_version() == 4
 
 
 def test_error_strings(lib):
-    for code in range(0, -11, -1):
+    for code in range(0, -12, -1):
         s = lib.hy_error_string(code).decode()
         assert s and s != "unknown error"
 
@@ -117,6 +117,28 @@ def test_workload_sizes():
     assert scenes.icosphere(5).num_tris == 20480
     ter, _ = scenes.terrain(np.random.default_rng(0), 512)
     assert ter.num_tris == 511 * 511 * 2
+    # the 4K configuration: 4096 instances of 8 base meshes of ~2k triangles + the terrain
+    assert scenes.geodesic_sphere(10).num_tris == 2000
+    assert scenes.torus(np.random.default_rng(0)).num_tris == 2048
+    large = scenes.large()
+    assert len(large.scene.entities) == 4097
+    assert 8.2e6 < large.scene.num_tris - 511 * 511 * 2 < 8.4e6
+    # the mixed batch: 8 scenes of log-uniform [50k, 2M] triangles
+    scs, views = scenes.batch(2)
+    assert len(scs) == 8 and len(views) == 64
+    assert all(45_000 < sc.num_tris < 2_100_000 for sc in scs)
+
+
+def test_geodesic_sphere_is_closed_and_outward():
+    g = scenes.geodesic_sphere(7)
+    f = g.indices.reshape(-1, 3).astype(np.int64)
+    e = np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]]), 1)
+    _, counts = np.unique(e, axis=0, return_counts=True)
+    assert g.num_tris == 20 * 49 and set(counts.tolist()) == {2}   # every edge shared by two triangles
+    v = g.vertices[:, :3].astype(np.float64)
+    n = np.cross(v[f[:, 1]] - v[f[:, 0]], v[f[:, 2]] - v[f[:, 0]])
+    assert np.all((n * (v[f[:, 0]] + v[f[:, 1]] + v[f[:, 2]])).sum(1) > 0)
+    np.testing.assert_allclose(np.linalg.norm(v, axis=1), 1.0, atol=1e-6)
 
 
 def test_scene_pack_roundtrip():

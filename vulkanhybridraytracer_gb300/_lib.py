@@ -23,6 +23,7 @@ HY_ERR_NAN_INPUT = -7
 HY_ERR_NOT_READY = -8
 HY_ERR_UNSUPPORTED = -9
 HY_ERR_TOO_LARGE = -10
+HY_ERR_BAD_INDEX = -11
 HY_NOALLOC_SCRATCH_BYTES = 16 << 20
 HY_GRAD_MATERIAL_PARAMS = 5
 HY_GRAD_LIGHT_PARAMS = 4
@@ -39,11 +40,13 @@ HY_FLAG_NO_STATUS_SYNC = 0x8
 HY_FLAG_PIXEL_PARALLEL = 0x10
 HY_FLAG_RAY_POOL = 0x20
 HY_FLAG_LANE_GROUPS = 0x40
+HY_FLAG_GGX_REFLECTION = 0x80
 HY_ANYHIT_AUTO, HY_ANYHIT_FAR_FIRST, HY_ANYHIT_NEAR_FIRST = 0, 1, 2
 HY_NO_HIT = 0xFFFFFFFF
 
 HY_STATUS_STACK_OVERFLOW = 0x1
 HY_STATUS_TIMEOUT = 0x2
+HY_STATUS_BAD_INDEX = 0x10
 
 
 class HyCreateInfo(C.Structure):
@@ -139,6 +142,7 @@ PROTOTYPES = {
     "hy_profile_enable": (I32, [P, I32]),
     "hy_profile_read": (I32, [P, C.POINTER(HyKernelTime), C.c_uint32, C.POINTER(C.c_uint32)]),
     "hy_debug_fail_alloc_after": (I32, [P, U32]),
+    "hy_debug_set_traversal_limits": (I32, [P, U32, U32]),
     "hy_scene_set_geometry": (I32, [P, P, U32, P, U32, P, U32, P, U32]),
     "hy_scene_set_materials": (I32, [P, P, U32]),
     "hy_scene_set_lights": (I32, [P, P, U32]),

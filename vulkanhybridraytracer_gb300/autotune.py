@@ -35,6 +35,18 @@ def _save(path: Path, data: dict) -> None:
         pass
 
 
+def cached(signature: str, device_name: str, cache_path: Path | None = DEFAULT_CACHE) -> dict | None:
+    """The cached winner for this GPU and workload, or None."""
+    if not cache_path:
+        return None
+    hit = _load(cache_path).get(f"{device_name}|{signature}")
+    if hit is None:
+        return None
+    out = dict(hit)
+    out["cached"] = True
+    return out
+
+
 def autotune(run, signature: str, device_name: str, chunks=CHUNKS, min_blocks=MIN_BLOCKS, reps: int = 2,
              cache_path: Path | None = DEFAULT_CACHE, timer=None) -> dict:
     """run(chunk, min_blocks) executes the workload once.  timer(fn) returns

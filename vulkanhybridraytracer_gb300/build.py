@@ -82,15 +82,25 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_LIB
 
 
-REFERENCE_DIR = Path(os.environ.get("HY_REFERENCE_DIR", "/root/reference"))
+def reference_dir() -> Path | None:
+    """The reference checkout: HY_REFERENCE_DIR, else the default of the recipe
+    that reads it (oracle/glsl_ref/Makefile)."""
+    env = os.environ.get("HY_REFERENCE_DIR")
+    if env:
+        return Path(env)
+    r = subprocess.run(["make", "-s", "-C", str(ORACLE_DIR / "glsl_ref"), "print-ref"], capture_output=True,
+                       text=True)
+    out = r.stdout.strip()
+    return Path(out) if r.returncode == 0 and out else None
 
 
 def build_reference_pin(force: bool = False):
     """The reference's own shaders compiled as C++ into oracle/_ref (test
     infrastructure); only where the reference checkout exists."""
-    if not (REFERENCE_DIR / "data" / "shaders").exists():
+    ref = reference_dir()
+    if ref is None or not (ref / "data" / "shaders").exists():
         return None
-    args = ["make", "-C", str(ORACLE_DIR / "glsl_ref"), f"REF={REFERENCE_DIR}"]
+    args = ["make", "-C", str(ORACLE_DIR / "glsl_ref"), f"REF={ref}"]
     if force:
         args.insert(1, "-B")
     r = subprocess.run(args, capture_output=True, text=True)

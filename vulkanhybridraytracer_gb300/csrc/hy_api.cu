@@ -162,6 +162,8 @@ SceneDev scene_dev(HyCtx* c) {
     S.num_inst = c->bvh_ok && c->two_level ? c->ninst : 0;
     S.two_level = c->bvh_ok && c->two_level ? 1u : 0u;
     S.anyhit_flip = anyhit_flip(c);
+    S.max_iters = c->dbg_max_iters ? c->dbg_max_iters : kMaxIters;
+    S.stack_cap = c->dbg_stack_cap ? (int)std::min<uint32_t>(c->dbg_stack_cap, kStackMax) : kStackMax;
     for (int i = 0; i < 2; i++) { S.env_w[i] = c->env_w[i]; S.env_h[i] = c->env_h[i]; }
     return S;
 }
@@ -180,7 +182,7 @@ int status_to_code(uint32_t s) {
     if (s & HY_STATUS_TIMEOUT) return HY_ERR_TIMEOUT;
     if (s & HY_STATUS_QUEUE_OVERFLOW) return HY_ERR_QUEUE_OVERFLOW;
     if (s & HY_STATUS_NAN_INPUT) return HY_ERR_NAN_INPUT;
-    if (s & HY_STATUS_BAD_INDEX) return HY_ERR_CUDA;
+    if (s & HY_STATUS_BAD_INDEX) return HY_ERR_BAD_INDEX;
     return HY_OK;
 }
 
@@ -253,6 +255,10 @@ int grid_for(HyCtx* c, int mode, bool count, int minb, bool short_stack, int sha
         per = 1;
     return per * c->num_sms;
 }
+
+// tile streams: node visits per scheduling round (at 8 resident blocks: 4: -3.9 %,
+// 6: -1.7 %, 12: -3.6 %, 16: -2.7 % against 8 on the 1080p workload)
+constexpr uint32_t kStreamSteps = 8;
 
 PassParams make_params(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const HyPassConfig* cfg,
                        uint32_t accum_fmt, void* shadow, void* hist, float* out_f, uint8_t* out_8) {
@@ -369,7 +375,7 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
     const bool grouped = mode == MODE_SHADOW_G || mode == MODE_SHADOW_ACCUM_G;
     const bool streams = mode == MODE_SHADOW_S || mode == MODE_SHADOW_ACCUM_S;
     int minb = cfg->min_blocks ? (int)cfg->min_blocks : (grouped ? 6 : 8);
-    if (streams && !cfg->visits_per_round) P.inner = 8;
+    if (streams && !cfg->visits_per_round) P.inner = kStreamSteps;
     P.top_nodes = 73;  // levels 0-2 of the 8-wide tree (measured neutral against 0, 9 and 128)
     if (cfg->stack_depth && cfg->stack_depth != 8) return HY_ERR_UNSUPPORTED;
     P.short_stack = streams && !c->two_level && cfg->stack_depth == 8;
@@ -402,6 +408,7 @@ const char* hy_error_string(int code) {
         case HY_ERR_NOT_READY: return "scene or acceleration structure not ready";
         case HY_ERR_UNSUPPORTED: return "unsupported";
         case HY_ERR_TOO_LARGE: return "input exceeds the fixed scratch of the allocation-free entry point";
+        case HY_ERR_BAD_INDEX: return "acceleration structure index out of range (corrupt structure)";
         default: return "unknown error";
     }
 }
@@ -477,6 +484,13 @@ int hy_synchronize(HyCtx* c) {
 int hy_debug_fail_alloc_after(HyCtx* c, uint32_t n) {
     if (!c) return HY_ERR_INVALID_ARG;
     c->fail_after = n ? c->alloc_calls + n : 0;
+    return HY_OK;
+}
+
+int hy_debug_set_traversal_limits(HyCtx* c, uint32_t max_node_visits, uint32_t max_stack_depth) {
+    if (!c || max_stack_depth > (uint32_t)kStackMax) return HY_ERR_INVALID_ARG;
+    c->dbg_max_iters = max_node_visits;
+    c->dbg_stack_cap = max_stack_depth;
     return HY_OK;
 }
 
@@ -894,7 +908,7 @@ int hy_pathtrace_pass(HyCtx* c, const HyCamera* cam, uint32_t W, uint32_t H, con
     const bool count = (cfg->flags & HY_FLAG_COUNT_TRAVERSAL) != 0;
     // shadow rays of each hit as tile streams (default), or on the hit's own lane
     const bool stream = !(cfg->flags & HY_FLAG_PIXEL_PARALLEL);
-    P.inner = cfg->visits_per_round ? std::min(cfg->visits_per_round, 16u) : 8u;
+    P.inner = cfg->visits_per_round ? std::min(cfg->visits_per_round, 16u) : kStreamSteps;
     // resident blocks the tile-stream kernel is compiled for: 6 (80 registers)
     // measured fastest at 1080p (uncapped 195 registers: 1,015; 3: 1,351; 4: 1,536;
     // 5: 1,697; 6: 1,769; 8: 1,774 Mrays/s) — occupancy beats the spills
@@ -970,26 +984,40 @@ int hy_hybrid_forward_host(HyCtx* c, const HyGBuffer* hgb, const HyCamera* cam, 
         if ((rc = ensure_size(c, c->host_in[p], npx * fmt_bytes(hgb->format[p])))) return rc;
         dgb.plane[p] = c->host_in[p].p;
     }
-    // planes 0 and 1 on the context's stream (the shadow kernel reads them);
-    // planes 2-5 on a side stream that starts once earlier work on the staging
-    // buffers is done and overlaps the shadow kernel
-    c->copy_pending = false;
-    if (!c->copy_stream) HY_CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-    if (!c->copy_start) HY_CUDA_TRY(cudaEventCreateWithFlags(&c->copy_start, cudaEventDisableTiming));
-    if (!c->copy_done) HY_CUDA_TRY(cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming));
-    HY_CUDA_TRY(cudaEventRecord(c->copy_start, c->stream));
-    HY_CUDA_TRY(cudaStreamWaitEvent(c->copy_stream, c->copy_start, 0));
-    for (int p = 0; p < 6; p++)
-        HY_CUDA_TRY(cudaMemcpyAsync(c->host_in[p].p, hgb->plane[p], npx * fmt_bytes(hgb->format[p]),
-                                    cudaMemcpyHostToDevice, p < 2 ? c->stream : c->copy_stream));
-    HY_CUDA_TRY(cudaEventRecord(c->copy_done, c->copy_stream));
-    c->copy_pending = true;
     float* d_f = nullptr;
     uint8_t* d_8 = nullptr;
     if (h_out_f) { if ((rc = ensure_size(c, c->host_out_f, npx * 16))) return rc; d_f = c->host_out_f.as<float>(); }
     if (h_out_8) { if ((rc = ensure_size(c, c->host_out_8, npx * 4))) return rc; d_8 = c->host_out_8.as<uint8_t>(); }
-    if ((rc = reset_counters(c))) return rc;
-    if ((rc = forward_impl(c, &dgb, cam, cfg, acc, d_f, d_8))) return rc;
+    if (!c->copy_stream) HY_CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    if (!c->copy_start) HY_CUDA_TRY(cudaEventCreateWithFlags(&c->copy_start, cudaEventDisableTiming));
+    if (!c->copy_done) HY_CUDA_TRY(cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming));
+    // planes 0 and 1 on the context's stream (the shadow kernel reads them);
+    // planes 2-5 on a side stream that starts once earlier work on the staging
+    // buffers is done and overlaps the shadow kernel
+    c->copy_pending = false;
+    rc = [&]() -> int {
+        HY_CUDA_TRY(cudaEventRecord(c->copy_start, c->stream));
+        HY_CUDA_TRY(cudaStreamWaitEvent(c->copy_stream, c->copy_start, 0));
+        c->copy_pending = true;
+        for (int p = 0; p < 6; p++)
+            HY_CUDA_TRY(cudaMemcpyAsync(c->host_in[p].p, hgb->plane[p], npx * fmt_bytes(hgb->format[p]),
+                                        cudaMemcpyHostToDevice, p < 2 ? c->stream : c->copy_stream));
+        HY_CUDA_TRY(cudaEventRecord(c->copy_done, c->copy_stream));
+        int r;
+        if ((r = reset_counters(c))) return r;
+        return forward_impl(c, &dgb, cam, cfg, acc, d_f, d_8);
+    }();
+    if (rc) {
+        // an error after the uploads were queued: the caller's buffers may still be
+        // read by the side stream, so wait for it before returning
+        if (c->copy_pending) {
+            c->copy_pending = false;
+            cudaStreamSynchronize(c->copy_stream);
+            cudaStreamSynchronize(c->stream);
+            cudaGetLastError();
+        }
+        return rc;
+    }
     if (h_out_f) HY_CUDA_TRY(cudaMemcpyAsync(h_out_f, d_f, npx * 16, cudaMemcpyDeviceToHost, c->stream));
     if (h_out_8) HY_CUDA_TRY(cudaMemcpyAsync(h_out_8, d_8, npx * 4, cudaMemcpyDeviceToHost, c->stream));
     return finish_call(c, st, true);
@@ -1069,7 +1097,7 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
                             v.out_rgba32f, v.out_bgra8);
         pv[i].scene = v.scene;
         pv[i].num_lights = v.accum.num_lights;
-        if (stream && !v.config.visits_per_round) pv[i].inner = 8;
+        if (stream && !v.config.visits_per_round) pv[i].inner = kStreamSteps;
         uint32_t G = 1;
         if (v.config.rng_mode == HY_RNG_DECORRELATED)
             while (G < v.config.shadow_spp && G < 32) G <<= 1;

@@ -154,6 +154,32 @@ __device__ __forceinline__ f3 sampleDisk(float light_radius, f3 position, f3 L, 
     return sampleDisk(light_radius, position, disk_frame(position, L), seed);
 }
 
+// GGX-sampled reflection (HY_FLAG_GGX_REFLECTION): a microfacet normal H with
+// density D(H) (N.H) for the reference's DistributionGGX (helpers.glsl:33-45,
+// alpha = roughness^2), from the uniform draws u1 (azimuth) and u2 (polar:
+// tan^2 = alpha^2 u2 / (1 - u2); u2 < 1 on rnd()'s grid), around N in a frame
+// built from the world axis least aligned with N; the ray is reflect(normalize(-V), H),
+// or the mirror direction reflect(normalize(-V), N) when that would leave
+// below the surface.  Single-rounded ops in the written order (the oracle's
+// ggx_reflect is the same sequence).
+__device__ __forceinline__ f3 reflect_rn(f3 I, f3 N) { return sub_rn(I, scale_rn(N, __fmul_rn(2.0f, dot_rn(N, I)))); }
+__device__ __forceinline__ f3 ggx_reflect(f3 N, f3 V, float roughness, float u1, float u2) {
+    const float a = __fmul_rn(roughness, roughness);
+    const float a2 = __fmul_rn(a, a);
+    const float t2 = __fdiv_rn(__fmul_rn(a2, u2), __fsub_rn(1.0f, u2));
+    const float cosT = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(1.0f, t2)));
+    const float sinT = __fmul_rn(__fsqrt_rn(t2), cosT);
+    const float phi = __fmul_rn(__fmul_rn(2.0f, PI), u1);
+    const f3 up = fabsf(N.y) < 0.999f ? mk(0.f, 1.f, 0.f) : mk(1.f, 0.f, 0.f);
+    const f3 T = normalize_rn(cross_rn(up, N));
+    const f3 B = cross_rn(N, T);
+    const f3 Hm = add_rn(add_rn(scale_rn(T, __fmul_rn(sinT, cosf(phi))), scale_rn(B, __fmul_rn(sinT, sinf(phi)))),
+                         scale_rn(N, cosT));
+    const f3 I = normalize_rn(mk(-V.x, -V.y, -V.z));
+    const f3 d = reflect_rn(I, Hm);
+    return dot_rn(d, N) > 0.f ? d : reflect_rn(I, N);
+}
+
 // ------------------------------------------------------------------------------
 // texel decode
 // ------------------------------------------------------------------------------
@@ -234,6 +260,11 @@ struct SceneDev {
     // any-hit traversal ranks a node's children slot ^ near ^ anyhit_flip:
     // 7 walks them far first, 0 near first (closest-hit rays: always near first)
     uint32_t anyhit_flip;
+    // per-ray limits of the walk: node visits (HY_STATUS_TIMEOUT beyond) and
+    // stack entries (HY_STATUS_STACK_OVERFLOW beyond, <= kStackMax); both are
+    // tested before the access they guard, so a ray that runs out stops cleanly
+    uint32_t max_iters;
+    int stack_cap;
 };
 
 struct Hit { float t; uint32_t id; float b1, b2; };
@@ -399,6 +430,10 @@ struct Trav {
     uint32_t iters;
     float tmax;
     Hit h;
+    // triangles of the last visited node's hit leaf slots, not yet tested: bit b
+    // is the record at pend_base + b (trav_node leaves them, trav_tri tests them
+    // one by one before the ray's next node visit)
+    uint32_t pend_base, pend_bits;
     // two-level walk only (dead, and dropped by the compiler, in one-level code)
     RayPre cur;                  // the ray in the frame of the level being walked
     uint32_t inst_base, inst_bits;  // hit instance entries of the last TLAS leaf set
@@ -414,6 +449,8 @@ __device__ __forceinline__ void trav_init(Trav& t, const RayPre& r, float tmax) 
     t.iters = 0;
     t.tmax = tmax;
     t.h = Hit{tmax, HY_NO_HIT, 0.f, 0.f};
+    t.pend_base = 0;
+    t.pend_bits = 0;
     t.cur = r;
     t.inst_base = 0;
     t.inst_bits = 0;
@@ -453,7 +490,7 @@ __device__ __forceinline__ bool two_level_settle(const SceneDev& S, const RayPre
     for (;;) {
         if (!t.level && t.inst_bits) {
             if (t.g_bits & 0xff000000u) {
-                if (t.sp >= kStackMax) { atomicOr(status, HY_STATUS_STACK_OVERFLOW); return false; }
+                if (t.sp >= S.stack_cap) { atomicOr(status, HY_STATUS_STACK_OVERFLOW); return false; }
                 stack_put(stk, t.sp, make_uint2(t.g_base, t.g_bits));
                 t.sp++;
             }
@@ -487,16 +524,22 @@ __device__ __forceinline__ bool two_level_settle(const SceneDev& S, const RayPre
     }
 }
 
-// One node visit (its box tests and the triangles of its leaf slots).
-// Returns true when the ray is finished: t.h holds the hit, or id HY_NO_HIT.
+// One node visit: its 8 box tests; hit internal children become the next
+// node group (the rest of the current group goes to the stack), the
+// triangles of hit leaf slots become the ray's pending triangles
+// (t.pend_base / t.pend_bits), which trav_tri tests before the ray's next
+// node visit.  Returns true when the walk is over (nothing left, or a limit
+// ran out).  A caller that interleaves trav_node and trav_tri this way makes
+// the same node visits and triangle tests, in the same order, as a walk that
+// tests each node's triangles at once.
 // TWO: the two-level structure (r is the world ray; t.cur the current one).
 // top / ntop: the structure's first ntop nodes (its top levels, BFS order)
 // staged in shared memory by the caller's block.
 template <bool ANY, bool COUNT, bool TWO = false, class Stack = uint2*>
-__device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& rw, float tmin, Trav& t, Stack stk,
-                                          uint32_t& nodes_ctr, uint32_t& tris_ctr, uint32_t* status,
-                                          const uint4* top = nullptr, uint32_t ntop = 0) {
-    if (++t.iters > kMaxIters) { atomicOr(status, HY_STATUS_TIMEOUT); return true; }
+__device__ __forceinline__ bool trav_node(const SceneDev& S, const RayPre& rw, float tmin, Trav& t, Stack stk,
+                                          uint32_t& nodes_ctr, uint32_t* status, const uint4* top = nullptr,
+                                          uint32_t ntop = 0) {
+    if (++t.iters > S.max_iters) { atomicOr(status, HY_STATUS_TIMEOUT); return true; }
     if (TWO) {
         if (!two_level_settle(S, rw, t, stk, status)) return true;
     } else if ((t.g_bits & 0xff000000u) == 0) {
@@ -513,7 +556,7 @@ __device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& rw, f
     const uint32_t sl = rb ^ ord;
     const uint32_t idx = t.g_base + __popc(t.g_bits & 0xffu & ((1u << sl) - 1u));
     if (t.g_bits & 0xff000000u) {
-        if (t.sp >= kStackMax) { atomicOr(status, HY_STATUS_STACK_OVERFLOW); return true; }
+        if (t.sp >= S.stack_cap) { atomicOr(status, HY_STATUS_STACK_OVERFLOW); return true; }
         stack_put(stk, t.sp, make_uint2(t.g_base, t.g_bits));
         t.sp++;
     }
@@ -590,31 +633,52 @@ __device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& rw, f
         const uint32_t m = __byte_perm(q1.z, q1.w, slot) & 0xffu;
         hit_tri |= ((1u << (m >> 5)) - 1u) << (m & 31u);
     }
-    const uint32_t tri_base = q1.y;
     if (TWO && !t.level) {  // TLAS leaves: instance entries, walked by two_level_settle
-        t.inst_base = tri_base;
+        t.inst_base = q1.y;
         t.inst_bits = hit_tri;
         hit_tri = 0;
     }
-    while (hit_tri) {
-        const uint32_t b = __ffs(hit_tri) - 1;
-        hit_tri &= hit_tri - 1u;
-        if (tri_base + b >= S.num_tris) { atomicOr(status, HY_STATUS_BAD_INDEX); return true; }
-        const float4* tp = S.tris + (size_t)(tri_base + b) * 3;
-        const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
-        const uint32_t id = TWO ? t.id_off + __float_as_uint(v0.w) : __float_as_uint(v0.w);
-        if (COUNT) tris_ctr++;
-        float tt, b1, b2;
-        if (tri_test(r, v0, v1, v2, tmin, t.tmax, tt, b1, b2)) {
-            if (t.h.id == HY_NO_HIT || tt < t.h.t || (tt == t.h.t && id < t.h.id)) {
-                t.h = Hit{tt, id, b1, b2};
-                t.tmax = tt;
-            }
-            if (ANY) return true;
-        }
-    }
+    t.pend_base = q1.y;
+    t.pend_bits = hit_tri;
     t.g_base = q1.x;
     t.g_bits = (hit_int << 24) | imask;
+    return false;
+}
+
+// The next pending triangle of the ray (t.pend_bits must be nonzero).
+// Returns true when the walk is over: an any-hit ray that hit, or a bad index.
+template <bool ANY, bool COUNT, bool TWO = false>
+__device__ __forceinline__ bool trav_tri(const SceneDev& S, const RayPre& rw, float tmin, Trav& t,
+                                         uint32_t& tris_ctr, uint32_t* status) {
+    const RayPre& r = TWO ? t.cur : rw;
+    const uint32_t b = __ffs(t.pend_bits) - 1;
+    t.pend_bits &= t.pend_bits - 1u;
+    const uint32_t rec = t.pend_base + b;
+    if (rec >= S.num_tris) { atomicOr(status, HY_STATUS_BAD_INDEX); t.pend_bits = 0; return true; }
+    const float4* tp = S.tris + (size_t)rec * 3;
+    const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+    const uint32_t id = TWO ? t.id_off + __float_as_uint(v0.w) : __float_as_uint(v0.w);
+    if (COUNT) tris_ctr++;
+    float tt, b1, b2;
+    if (tri_test(r, v0, v1, v2, tmin, t.tmax, tt, b1, b2)) {
+        if (t.h.id == HY_NO_HIT || tt < t.h.t || (tt == t.h.t && id < t.h.id)) {
+            t.h = Hit{tt, id, b1, b2};
+            t.tmax = tt;
+        }
+        if (ANY) { t.pend_bits = 0; return true; }
+    }
+    return false;
+}
+
+// One node visit and then its triangles (the walk of a single ray).
+// Returns true when the ray is finished: t.h holds the hit, or id HY_NO_HIT.
+template <bool ANY, bool COUNT, bool TWO = false, class Stack = uint2*>
+__device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& rw, float tmin, Trav& t, Stack stk,
+                                          uint32_t& nodes_ctr, uint32_t& tris_ctr, uint32_t* status,
+                                          const uint4* top = nullptr, uint32_t ntop = 0) {
+    if (trav_node<ANY, COUNT, TWO>(S, rw, tmin, t, stk, nodes_ctr, status, top, ntop)) return true;
+    while (t.pend_bits)
+        if (trav_tri<ANY, COUNT, TWO>(S, rw, tmin, t, tris_ctr, status)) return true;
     return false;
 }
 

@@ -275,6 +275,11 @@ __device__ __forceinline__ void grad_pixel(const SceneDev& S, const GradParams& 
     int nb = 0;
     if (active && smode != 0) {
         uint32_t seed = tea(y * P.W + x, P.frame_u);
+        // the forward's GGX-sampled first bounce (a constant here: visibility is held fixed)
+        if ((P.flags & HY_FLAG_GGX_REFLECTION) && smode == 3 && P.max_bounces > 0) {
+            const float u1 = rnd(seed), u2 = rnd(seed);
+            direction = ggx_reflect(N, V, g4.y, u1, u2);
+        }
         for (uint32_t depth = 0; depth < P.max_bounces && depth < (uint32_t)kGradMaxBounces; depth++) {
             const f3 ro = origin + direction * 1e-2f;
             const Hit h = trace<false, false>(S, ro, direction, 0.001f, 1000.0f, ls, P.status);

@@ -35,6 +35,7 @@ struct HyCtx {
     bool own_stream = false;
     uint64_t max_bytes = 0, used_bytes = 0;
     uint32_t fail_after = 0, alloc_calls = 0;
+    uint32_t dbg_max_iters = 0, dbg_stack_cap = 0;  // hy_debug_set_traversal_limits (0: the built-in limits)
     int num_sms = 0;
     int l2_bytes = 0;  // the device's L2 size (the automatic any-hit order compares the structure with it)
 

@@ -26,7 +26,10 @@ void* g_scratch_addr[kMaxDevices] = {};
 
 // Device address of the scratch array on the current device.  In host code
 // the array's name is only a host-side stand-in, so the address is looked up
-// once per device (with that device current) and cached.
+// once per device (with that device current) and cached.  cudaDeviceReset
+// unloads the module that holds the array, so a process that resets a device
+// must not call the entry point on that device again: the cached address
+// would point at freed memory.
 int scratch_address(void** out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return HY_ERR_CUDA; }
@@ -61,6 +64,8 @@ extern "C" int hy_accumulate_pass_noalloc(const HyGBuffer* gb, const HyPassConfi
         return HY_ERR_INVALID_ARG;
     if (gb->width == 0 || gb->height == 0 || !gb->plane[3] || plane_bytes(gb->format[3]) == 0)
         return HY_ERR_INVALID_ARG;
+    // the same bound as every other pass: pixel indices are 32-bit
+    if ((unsigned long long)gb->width * gb->height >= (1ull << 31)) return HY_ERR_INVALID_ARG;
     if ((uintptr_t)gb->plane[3] % plane_bytes(gb->format[3]) != 0) return HY_ERR_INVALID_ARG;
     hy::AccumParams A;
     A.W = gb->width;

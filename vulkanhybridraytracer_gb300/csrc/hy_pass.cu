@@ -124,6 +124,12 @@ __device__ __forceinline__ void do_pixel(const SceneDev& S, const PassParams& P,
             rayColor = rayColor + ((I > 0.f) ? I * lc * attenuation * albedo * metallic : irradiance * albedo * metallic);
         }
     }
+    // HY_FLAG_GGX_REFLECTION: the mirror texel's first bounce sampled from its
+    // GGX lobe with the texel's own RNG stream
+    if ((P.flags & HY_FLAG_GGX_REFLECTION) && smode == 3 && P.max_bounces > 0) {
+        const float u1 = rnd(seed_h), u2 = rnd(seed_h);
+        direction = ggx_reflect(N, V, roughness, u1, u2);
+    }
     // hybridRaygen.rgen:151-170
     for (uint32_t depth = 0; depth < P.max_bounces; depth++) {
         if (smode == 0) break;

@@ -1,11 +1,12 @@
-"""Differentiable form of the hybrid pass.
+"""Differentiable form of the hybrid pass: the host side of the
+forward/backward pair.
 
 The product interface is the C ABI pair hy_shade_pass (forward, after
 hy_gbuffer_primary and hy_shadow_pass) and hy_hybrid_backward (its adjoint,
 visibility held fixed).  This module names the parameters the gradient
-covers, renders an image from a parameter vector and, for the
-gradient-check harness, wraps forward and backward in a
-``torch.autograd.Function``.
+covers and renders an image from a parameter vector; it has no autograd
+code (the ``torch.autograd.Function`` of the gradient check lives with the
+tests, tests/grad_harness.py).
 
 Parameters (float32):
   materials (num_mats, 5): HyMaterial diffuse[0..2], roughness (smr[2]),
@@ -98,35 +99,3 @@ class DiffRenderer:
 
     def close(self):
         self.ctx.close()
-
-
-def _autograd_function():
-    import torch
-
-    class HybridRenderFn(torch.autograd.Function):
-        """image[..., :3] = shade(materials, lights); backward = hy_hybrid_backward."""
-
-        @staticmethod
-        def forward(ctx, mat_p, light_p, renderer):
-            img, state = renderer.render(mat_p.detach().cpu().numpy(), light_p.detach().cpu().numpy())
-            ctx.renderer = renderer
-            ctx.state = state
-            ctx.shapes = (mat_p.shape, light_p.shape, mat_p.device, light_p.device, mat_p.dtype)
-            return img[..., :3]
-
-        @staticmethod
-        def backward(ctx, grad):
-            r = ctx.renderer
-            g4 = torch.zeros((r.H, r.W, 4), dtype=torch.float32, device=r.dev)
-            g4[..., :3] = grad
-            gm, gl, _ = r.backward(ctx.state, g4)
-            ms, ls, md, ld, dt = ctx.shapes
-            return gm.reshape(ms).to(md, dt), gl.reshape(ls).to(ld, dt), None
-
-    return HybridRenderFn
-
-
-def render_fn():
-    """The torch.autograd.Function of the gradient-check harness:
-    ``render_fn().apply(mat_params, light_params, renderer)``."""
-    return _autograd_function()

@@ -69,6 +69,40 @@ def icosphere(subdiv: int) -> Mesh:
     return Mesh(_vertices(v, v, uv), f.reshape(-1).astype(np.uint32))
 
 
+def geodesic_sphere(freq: int) -> Mesh:
+    """Unit geodesic icosphere: each icosahedron face cut into freq^2 triangles on a
+    barycentric grid and projected onto the sphere (20 freq^2 triangles: 2,000 at
+    freq 10; freq 2^k is icosphere(k)'s triangle count), outward normals."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    ico = np.array([(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t),
+                    (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)], np.float64)
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5),
+             (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    key_to_index, pos, tris = {}, [], []
+
+    def vert(a, b, c, i, j):
+        # grid point i steps from a toward b, j steps toward c; shared edge points get one key
+        w = {a: freq - i - j, b: i, c: j}
+        key = tuple(sorted((k, v) for k, v in w.items() if v))
+        if key not in key_to_index:
+            p = sum(ico[k] * v for k, v in w.items()) / freq
+            key_to_index[key] = len(pos)
+            pos.append(p / np.linalg.norm(p))
+        return key_to_index[key]
+
+    for a, b, c in faces:
+        for i in range(freq):
+            for j in range(freq - i):
+                v0, v1, v2 = vert(a, b, c, i, j), vert(a, b, c, i + 1, j), vert(a, b, c, i, j + 1)
+                tris.append((v0, v1, v2))
+                if i + j < freq - 1:
+                    tris.append((v1, vert(a, b, c, i + 1, j + 1), v2))
+    v = np.array(pos)
+    uv = np.stack([0.5 + np.arctan2(v[:, 0], v[:, 2]) / (2 * np.pi), 0.5 - np.arcsin(np.clip(v[:, 1], -1, 1)) / np.pi], 1)
+    return Mesh(_vertices(v, v, uv), np.array(tris, np.int64).reshape(-1).astype(np.uint32))
+
+
 def quad(size: float) -> Mesh:
     h = size / 2.0
     pos = np.array([[-h, 0, -h], [h, 0, -h], [h, 0, h], [-h, 0, h]], np.float64)
@@ -309,18 +343,18 @@ def _rotation(q: np.ndarray) -> np.ndarray:
 
 def large(seed: int = 4, width: int = 3840, height: int = 2160, n_instances: int = 4096, terrain_n: int = 512,
           n_materials: int = 1024, n_lights: int = 64) -> Workload:
-    """3840x2160: 4096 instances of 8 base meshes (4 icospheres of subdivision 3, 1,280
-    triangles, and 4 displaced tori of 2,048) under random rotations, scale U[0.2, 4] and
-    positions over the terrain, flattened into one BVH (~6.8M triangles) plus the 1080p
-    configuration's 512x512 terrain; 1024 materials; 64 area lights (radius 0.5, intensity
-    U[10, 50]); 64 shadow samples per pixel spread over the lights (1 per light,
-    DECORRELATED); 2 reflection bounces."""
+    """3840x2160: 4096 instances of 8 base meshes of ~2k triangles (4 geodesic icospheres of
+    2,000 triangles and 4 displaced tori of 2,048) under random rotations, scale U[0.2, 4]
+    and positions over the terrain, flattened into one BVH (~8.3M triangles) plus the 1080p
+    configuration's 512x512 terrain (~8.8M in all); 1024 materials; 64 area lights (radius
+    0.5, intensity U[10, 50]); 64 shadow samples per pixel spread over the lights (1 per
+    light, DECORRELATED); 2 reflection bounces."""
     rng = np.random.default_rng(seed)
     sc = Scene()
     ter, hmap = terrain(rng, terrain_n)
     sc.materials = random_materials(rng, n_materials)
     sc.entities.append(Object(ter, int(rng.integers(n_materials)), trs()))
-    bases = [icosphere(3) for _ in range(4)] + [torus(rng) for _ in range(4)]
+    bases = [geodesic_sphere(10) for _ in range(4)] + [torus(rng) for _ in range(4)]
     n = hmap.shape[0]
     for _ in range(n_instances):
         mesh = bases[int(rng.integers(len(bases)))]
@@ -345,15 +379,16 @@ BATCH_SPP = (1, 4, 16, 64)
 
 
 def batch_scene(rng: np.random.Generator, n_tris: int) -> Scene:
-    """A terrain + icosphere scene built like the 1080p one with about n_tris
-    triangles (35 % terrain, 65 % spheres of 5,120 triangles), 256 materials
-    and 8 area lights (a view uses the first 1..8)."""
+    """A scene generated as the 1080p one (fBm terrain + icospheres of subdivision 5,
+    20,480 triangles each, scale U[0.5, 3]; 256 materials; area lights of radius 0.5,
+    intensity U[10, 50]) with about n_tris triangles (35 % terrain, 65 % spheres) and 8
+    lights (a view uses the first 1..8)."""
     sc = Scene()
     n_ter = max(8, int(round(np.sqrt(0.35 * n_tris / 2.0))) + 1)
     ter, _ = terrain(rng, n_ter)
     sc.materials = random_materials(rng, 256)
     sc.entities.append(Object(ter, int(rng.integers(256)), trs()))
-    ico = icosphere(4)
+    ico = icosphere(5)
     for _ in range(max(1, int(round(0.65 * n_tris / ico.num_tris)))):
         s = rng.uniform(0.5, 3.0)
         x, z = rng.uniform(-40, 40), rng.uniform(-40, 40)
