@@ -321,7 +321,9 @@ def diff_leg(steps: int, warmup: int, fd_params: int = 32, clocks_index: int = 0
 
     fd = []
     for j in pick:
-        h = 1e-2 * max(1.0, abs(p0[j]))
+        # small steps: a light moved by h also moves the shadow rays the shading traces
+        # from bounce hits, whose visibility the adjoint holds fixed
+        h = 1e-3 * max(1.0, abs(p0[j]))
         a, b = p0.copy(), p0.copy()
         a[j] += h
         b[j] -= h
@@ -339,7 +341,9 @@ def diff_leg(steps: int, warmup: int, fd_params: int = 32, clocks_index: int = 0
            "backward_rays": {"reflection_rays": st["reflection_rays"], "hit_shadow_rays": st["hit_shadow_rays"]},
            "grad_check": {"params": int(len(pick)), "max_rel_err": float(rel.max()) if len(rel) else None,
                           "median_rel_err": float(np.median(rel)) if len(rel) else None,
-                          "method": "central differences of the FP32 forward (h = 1e-2 max(1, |p|)), shadow "
+                          "max_rel_err_materials": float(rel[pick < nm].max()) if np.any(pick < nm) else None,
+                          "max_rel_err_lights": float(rel[pick >= nm].max()) if np.any(pick >= nm) else None,
+                          "method": "central differences of the FP32 forward (h = 1e-3 max(1, |p|)), shadow "
                                     "images held fixed, loss summed in FP64; relative to max(|fd|, 1e-2 max|grad|)"},
            "steps": steps, "warmup": warmup, "clocks": clk,
            "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MB write)"}

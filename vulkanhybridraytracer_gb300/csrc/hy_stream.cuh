@@ -33,6 +33,9 @@ __device__ __forceinline__ uint32_t stage_top(const SceneDev& S, uint4* top, uin
 // sampleDisk (position + L, tangent, bitangent); the RNG state of the
 // pixel-light's first sample (w of PL, as bits); a not-traced mark (w of T,
 // 0xffffffff); the unoccluded count.
+// Items of a light are traced in the order of their disk samples (kSortItems at
+// most per warp and light; more are traced in item order).
+constexpr uint32_t kSortItems = 512, kSortBuckets = 64;
 struct StreamSlots {
     float4 pos[128];
     float4 PL[128];
@@ -40,6 +43,11 @@ struct StreamSlots {
     float4 B[128];
     uint32_t cnt[128];
     uint32_t next[4];  // per warp: the next unclaimed item of the current light
+    // per warp: the traced items of the light ordered by their disk sample, the
+    // sample's cell per item, and the cell counts / cursors of the counting sort
+    uint16_t order[4][kSortItems];
+    uint8_t key[4][kSortItems];
+    uint32_t bucket[4][kSortBuckets];
 };
 
 constexpr uint32_t kNotTraced = 0xffffffffu;
@@ -71,9 +79,60 @@ __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams
                                              float radius, float offset, Stack stk, Trav& t, RayPre& r,
                                              LaneStats& ls, uint32_t& nn, uint32_t& nt, const uint4* top,
                                              uint32_t ntop) {
-    const uint32_t lane = threadIdx.x & 31, wb = threadIdx.x & ~31u, total = 32u * nrays;
-    uint32_t* next = &sm.next[threadIdx.x >> 5];
+    const uint32_t lane = threadIdx.x & 31, wb = threadIdx.x & ~31u, warp = threadIdx.x >> 5;
+    uint32_t total = 32u * nrays;
+    uint32_t* next = &sm.next[warp];
     __syncwarp();
+    // ---- the order of the light's items: a counting sort of the traced items by
+    //      the cell of their disk sample on an 8x8 grid over the disk (cells in
+    //      Morton order), so that the lanes' rays at any moment are nearly
+    //      parallel rays from the tile's nearby pixels and walk the same nodes.
+    //      The rays themselves do not change: only which lane traces which ray,
+    //      and when ----
+    const bool sorted = nrays > 1 && total <= kSortItems;
+    if (sorted) {
+        uint32_t* bk = sm.bucket[warp];
+        bk[lane] = 0;
+        bk[lane + 32] = 0;
+        __syncwarp();
+        for (uint32_t q = lane; q < total; q += 32) {
+            const uint32_t pi = q / nrays, k = q - pi * nrays;
+            uint32_t key = 0xffu;
+            if (__float_as_uint(sm.T[wb + pi].w) != kNotTraced) {
+                uint32_t st = lcg_jump(__float_as_uint(sm.PL[wb + pi].w), 2u * k);
+                const float r1 = rnd(st), r2 = rnd(st);
+                // the disk point in units of the radius (approximate: it only orders the items)
+                float sn, cs;
+                __sincosf(6.2831853f * r2, &sn, &cs);
+                const float rr = sqrtf(r1);
+                const uint32_t ix = min(7u, (uint32_t)fmaxf((rr * cs + 1.0f) * 4.0f, 0.0f));
+                const uint32_t iy = min(7u, (uint32_t)fmaxf((rr * sn + 1.0f) * 4.0f, 0.0f));
+                key = (ix & 1u) | ((iy & 1u) << 1) | ((ix & 2u) << 1) | ((iy & 2u) << 2) | ((ix & 4u) << 2) |
+                      ((iy & 4u) << 3);
+                atomicAdd(&bk[key], 1u);
+            }
+            sm.key[warp][q] = (uint8_t)key;
+        }
+        __syncwarp();
+        // exclusive scan of the 64 counts, two per lane
+        const uint32_t c0 = bk[2 * lane], c1 = bk[2 * lane + 1], c = c0 + c1;
+        uint32_t incl = c;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= (uint32_t)d) incl += y;
+        }
+        total = __shfl_sync(0xffffffffu, incl, 31);  // the traced items
+        __syncwarp();
+        bk[2 * lane] = incl - c;
+        bk[2 * lane + 1] = incl - c + c0;
+        __syncwarp();
+        for (uint32_t q = lane; q < 32u * nrays; q += 32) {
+            const uint32_t key = sm.key[warp][q];
+            if (key != 0xffu) sm.order[warp][atomicAdd(&bk[key], 1u)] = (uint16_t)q;
+        }
+        __syncwarp();
+    }
     bool live = false, more = true;
     uint32_t cur = 0;
     for (;;) {
@@ -86,8 +145,9 @@ __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams
             uint32_t base = 0;
             if (lane == leader) base = atomicAdd(next, (uint32_t)__popc(m));
             base = __shfl_sync(m, base, leader);
-            const uint32_t q = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+            uint32_t q = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
             if (q >= total) { more = false; break; }
+            if (sorted) q = sm.order[warp][q];
             const uint32_t pi = q / nrays, k = q - pi * nrays;
             const float4 tp = sm.T[wb + pi];
             if (__float_as_uint(tp.w) == kNotTraced) continue;
