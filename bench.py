@@ -647,11 +647,10 @@ def batch_leg(steps: int, warmup: int, n_views: int = 64, tune: bool = False, cl
         for v in views:
             ctxs[v["scene"]].forward(v["planes"], v["camera"], v["config"], v["hist"], out_8=v["out_8"], stats=False)
 
-    def batched(chunk=1, minb=8):
+    def batched(shape=autotune.DEFAULT):
         frame[0] += 1
         set_frame(frame[0])
-        runner.batch_forward(ctxs, views, graph=True, tuning=pass_config(1, queue_chunk=chunk, min_blocks=minb),
-                             sync=False)
+        runner.batch_forward(ctxs, views, graph=True, tuning=autotune.tuning_config(shape), sync=False)
 
     def dev_time(fn):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -668,18 +667,19 @@ def batch_leg(steps: int, warmup: int, n_views: int = 64, tune: bool = False, cl
     rays = st["shadow_rays"] + st["reflection_rays"] + st["hit_shadow_rays"]
     sig = f"batch{len(views)}-{sum(v['w'] * v['h'] for v in views)}px-{rays}rays"
     if tune:
-        tuned = autotune.autotune(lambda ch, mb: batched(ch, mb), sig, torch.cuda.get_device_name(0),
-                                  timer=dev_time)
+        frame[0] += 1
+        set_frame(frame[0])
+        tuned = autotune.autotune(runner, ctxs, views, sig, torch.cuda.get_device_name(0))
     else:
-        tuned = autotune.cached(sig, torch.cuda.get_device_name(0)) or {"chunk": 1, "min_blocks": 8,
-                                                                         "cached": False, "default": True}
+        tuned = autotune.cached(sig, torch.cuda.get_device_name(0)) or dict(autotune.DEFAULT, cached=False,
+                                                                            default=True)
     for _ in range(warmup):
         plain()
-        batched(tuned["chunk"], tuned["min_blocks"])
+        batched(tuned)
     clocks = Clocks(clocks_index)
     clocks.start()
     t_plain = [dev_time(plain) for _ in range(steps)]
-    t_batch = [dev_time(lambda: batched(tuned["chunk"], tuned["min_blocks"])) for _ in range(steps)]
+    t_batch = [dev_time(lambda: batched(tuned)) for _ in range(steps)]
     clk = clocks.stop()
     mp = float(np.median(t_plain))
     mb = float(np.median(t_batch))
@@ -689,7 +689,7 @@ def batch_leg(steps: int, warmup: int, n_views: int = 64, tune: bool = False, cl
            "spp": [v["spp"] for v in views], "lights": [v["hist"].shape[0] for v in views],
            "batched_ms": 1e3 * mb, "plain_ms": 1e3 * mp, "batched_over_plain": mp / mb,
            "batched_mrays_per_s": rays / mb / 1e6, "plain_mrays_per_s": rays / mp / 1e6,
-           "tuning": {k: tuned[k] for k in ("chunk", "min_blocks") if k in tuned},
+           "tuning": {k: tuned[k] for k in ("chunk", "block", "min_blocks", "stack_depth", "cached") if k in tuned},
            "steps": steps, "warmup": warmup, "clocks": clk,
            "l2": "inputs (G-buffers ~%.1f GB) larger than L2" % (sum(v["w"] * v["h"] for v in views) * 88 / 1e9)}
     if tune:

@@ -184,17 +184,20 @@ typedef struct HyPassConfig {
     uint32_t rng_mode;      /* HY_RNG_* */
     int32_t  accum_frame;   /* frameCountBuffer = _denoise_frame (src/vk_engine.cpp:722) */
     uint32_t flags;         /* HY_FLAG_* */
-    uint32_t block_size;    /* threads per block; 0 = default / autotuned */
+    uint32_t block_size;    /* threads per block: the single-view passes take 32..128 in steps of 32
+                               (0 = 128); a batch's tuning 64, 128 or 256 (0 = 256) */
     uint32_t queue_chunk;   /* work items fetched per warp from the ray queue; 0 = default */
-    uint32_t stack_depth;   /* short traversal stack of the tile-stream shadow kernel: 8 keeps the
-                               first 8 entries of each lane's stack in shared memory (deeper ones
-                               in local memory); 0 = the whole 64-entry stack in local memory
-                               (default; measured equal); other values: HY_ERR_UNSUPPORTED */
+    uint32_t stack_depth;   /* short traversal stack: the first stack_depth entries of each lane's
+                               stack in shared memory, deeper ones in local memory.  Single-view
+                               tile-stream shadow kernel: 0 (default, all local; measured equal)
+                               or 8; a batch's tuning: 0, 8, 16 or 32; other values:
+                               HY_ERR_UNSUPPORTED / HY_ERR_INVALID_ARG */
     uint32_t group_lanes;   /* DECORRELATED shadow rays: lanes per pixel-light group (power of two,
                                2..32, each lane traces spp / group_lanes samples in turn);
                                0 = the next power of two >= spp */
     uint32_t min_blocks;    /* shadow-kernel variant: compiled for 5 (96 registers) or 8 (64 registers)
-                               resident blocks per SM, the lane-group kernel also for 6 and 7;
+                               resident 128-thread blocks per SM, the lane-group kernel also for 6
+                               and 7, a batch's tile-stream kernel for 6 (80) and 8 (64);
                                0 = 6 for the lane-group kernel, 8 otherwise */
     uint32_t visits_per_round; /* BVH node visits a shadow lane makes between two scheduling rounds
                                   of the persistent shadow kernels (1..16; a lane whose ray ends
@@ -464,8 +467,16 @@ int hy_hybrid_backward(HyCtx* ctx, const HyGBuffer* gb, const HyCamera* cam, con
  * seen and replayed afterwards; the per-view parameters travel through a
  * pinned table copied in by the graph, so cameras, frames and buffers may
  * change between replays.  Runs on ctx's stream; all contexts must share
- * its device.  tuning->queue_chunk / min_blocks select the launch shape
- * (NULL: defaults); its other fields are ignored. */
+ * its device.  tuning (NULL: defaults) selects the launch shape of the shadow
+ * kernel: queue_chunk (tiles per queue pull, 1..1024), block_size (threads per
+ * block: 64, 128 or 256), min_blocks (register cap as resident 128-thread
+ * blocks per SM: 6 or 8, i.e. 80 or 64 registers) and stack_depth (entries of
+ * each lane's traversal stack in shared memory: 0, 8, 16 or 32); flags may
+ * hold HY_FLAG_LANE_GROUPS (the lane-group kernel, 128 threads, no shared
+ * stack) and HY_FLAG_COUNT_TRAVERSAL.  Counting launches and batches holding
+ * a two-level scene run one shape (128 threads, no shared stack); other
+ * shapes return HY_ERR_UNSUPPORTED for them.  The shape changes speed, never
+ * the images. */
 typedef struct HyView {
     uint32_t     scene;        /* index into scenes[] */
     uint32_t     _pad;
@@ -483,6 +494,20 @@ typedef struct HyView {
 
 int hy_batch_forward(HyCtx* ctx, HyCtx* const* scenes, uint32_t num_scenes, const HyView* views,
                      uint32_t num_views, uint32_t batch_flags, const HyPassConfig* tuning, HyStats* stats);
+
+/* Launch-shape autotuner of hy_batch_forward (the tuning space of the
+ * reference's one-view-per-frame renderer has no counterpart): times the batch
+ * under candidate shapes, one axis at a time (queue chunk {1..32 tiles = 32..1024
+ * pixels}, block size {64, 128, 256}, register cap {6, 8}, shared stack entries
+ * {0, 8, 16, 32}) with the others at their best so far, each shape as the
+ * fastest of `reps` (1..64) graph replays, and writes the fastest shape to
+ * *tuning (queue_chunk, block_size, min_blocks, stack_depth; the other fields
+ * 0 / defaults) and its time to *best_ms (may be NULL).  It runs the batch as
+ * given about 16 x (reps + 1) times, so the views' histories and outputs are
+ * overwritten: tune on the frames' first batch or on copies.  Pass the result
+ * to hy_batch_forward; a C++ application can keep it per GPU and workload. */
+int hy_batch_autotune(HyCtx* ctx, HyCtx* const* scenes, uint32_t num_scenes, const HyView* views,
+                      uint32_t num_views, uint32_t reps, HyPassConfig* tuning, float* best_ms);
 
 /* ---- allocation-free accumulation (no counterpart in the reference) ----
  *

@@ -176,6 +176,8 @@ PROTOTYPES = {
     "hy_accumulate_pass_noalloc": (I32, [C.POINTER(HyGBuffer), C.POINTER(HyPassConfig), P, C.POINTER(HyAccum), P]),
     "hy_batch_forward": (I32, [P, C.POINTER(P), U32, C.POINTER(HyView), U32, U32, C.POINTER(HyPassConfig),
                                C.POINTER(HyStats)]),
+    "hy_batch_autotune": (I32, [P, C.POINTER(P), U32, C.POINTER(HyView), U32, U32, C.POINTER(HyPassConfig),
+                                C.POINTER(C.c_float)]),
 }
 
 _lib = None

@@ -1024,29 +1024,37 @@ int hy_hybrid_forward_host(HyCtx* c, const HyGBuffer* hgb, const HyCamera* cam, 
 }
 
 // ---- batches -------------------------------------------------------------------
+// launch shape of a batch's tile-stream shadow kernel
+struct BatchShape {
+    int minb;    // register cap as resident 128-thread blocks per SM
+    int block;   // threads per block
+    int shortd;  // shared-memory stack entries per lane
+};
+
 static int batch_enqueue(HyCtx* c, const std::vector<PassParams>& pv, const std::vector<SceneDev>& sd,
                          const HyView* views, const std::vector<uint32_t>& reset_views, const BatchParams& B,
-                         bool count, int minb, bool stream, bool two, size_t tab_bytes) {
+                         bool count, const BatchShape& sh, bool stream, bool two, size_t tab_bytes) {
     cudaStream_t s = c->stream;
     HY_CUDA_TRY(cudaMemcpyAsync(c->batch_tab.p, c->h_batch_tab, tab_bytes, cudaMemcpyHostToDevice, s));
     HY_CUDA_TRY(cudaMemsetAsync(c->dstats.p, 0, c->dstats.bytes, s));
     int per = 0;
-    if (batch_occupancy(false, count, minb, stream, two, &per) != cudaSuccess || per <= 0) per = 1;
-    int grid = std::max(1, std::min<int>(per * c->num_sms, (int)((B.total_tiles * 32ull + 127) / 128)));
+    if (batch_occupancy(false, count, sh.minb, stream, two, sh.block, sh.shortd, &per) != cudaSuccess || per <= 0)
+        per = 1;
+    int grid = std::max(1, std::min<int>(per * c->num_sms, (int)((B.total_tiles * 32ull + sh.block - 1) / sh.block)));
     BatchParams Bs = B;
     Bs.queue = dev_queue(c, WQ_SHADOW);
-    HY_CUDA_TRY(launch_batch(false, count, minb, stream, two, Bs, grid, s));
+    HY_CUDA_TRY(launch_batch(false, count, sh.minb, stream, two, sh.block, sh.shortd, Bs, grid, s));
     for (uint32_t v : reset_views) {
         const HyView& vw = views[v];
         HyAccum acc = vw.accum;
         int rc = accumulate_impl(c, &vw.gbuffer, &vw.config, pv[v].shadow, &acc);
         if (rc) return rc;
     }
-    if (batch_occupancy(true, count, minb, false, false, &per) != cudaSuccess || per <= 0) per = 1;
+    if (batch_occupancy(true, count, sh.minb, false, false, 128, 0, &per) != cudaSuccess || per <= 0) per = 1;
     grid = std::max(1, std::min<int>(per * c->num_sms, (int)((B.total_tiles * 32ull + 127) / 128)));
     BatchParams Bh = B;
     Bh.queue = dev_queue(c, WQ_SHADE);
-    HY_CUDA_TRY(launch_batch(true, count, minb, false, false, Bh, grid, s));
+    HY_CUDA_TRY(launch_batch(true, count, sh.minb, false, false, 128, 0, Bh, grid, s));
     (void)sd;
     return HY_OK;
 }
@@ -1065,10 +1073,28 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
     DeviceGuard g(c->device);
     const bool count = tuning && (tuning->flags & HY_FLAG_COUNT_TRAVERSAL);
     const uint32_t chunk = tuning && tuning->queue_chunk ? tuning->queue_chunk : 1;
-    const int minb = tuning && tuning->min_blocks ? (int)tuning->min_blocks : 8;
     const bool stream = !(tuning && (tuning->flags & HY_FLAG_LANE_GROUPS));
     bool any_two = false;
     for (uint32_t i = 0; i < ns; i++) any_two = any_two || scenes[i]->two_level;
+    // the tile-stream kernel's launch shape: threads per block {64, 128, 256}, register
+    // cap {6, 8} resident 128-thread blocks (80 / 64 registers), shared stack entries
+    // {0, 8, 16, 32}; counting launches and two-level batches run the 128 / 8 (5) / 0 shape
+    // default: 256 threads, 64 registers, no shared stack, one tile per pull, the shape
+    // hy_batch_autotune picked for the 64-view mixed batch on a GB300
+    BatchShape sh{tuning && tuning->min_blocks ? (int)tuning->min_blocks : 8,
+                  tuning && tuning->block_size ? (int)tuning->block_size : (stream && !count && !any_two ? 256 : 128),
+                  tuning ? (int)tuning->stack_depth : 0};
+    if (chunk > 1024) return HY_ERR_INVALID_ARG;
+    if (sh.block != 64 && sh.block != 128 && sh.block != 256) return HY_ERR_INVALID_ARG;
+    if (sh.shortd != 0 && sh.shortd != 8 && sh.shortd != 16 && sh.shortd != 32) return HY_ERR_INVALID_ARG;
+    if (stream && !count && !any_two) {
+        if (sh.minb != 6 && sh.minb != 8) return HY_ERR_INVALID_ARG;
+    } else {
+        if ((sh.block != 128 || sh.shortd != 0) && stream) return HY_ERR_UNSUPPORTED;
+        if (!stream && (sh.block != 128 || sh.shortd != 0)) return HY_ERR_UNSUPPORTED;
+        if (stream) sh.minb = 8;
+    }
+    const int minb = sh.minb;
     // per-view parameters
     std::vector<PassParams> pv(nv);
     std::vector<uint32_t> reset_views;
@@ -1152,11 +1178,11 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
     B.status = dev_status(c);
     B.queue = nullptr;
     if (bflags & HY_BATCH_NO_GRAPH) {
-        if ((rc = batch_enqueue(c, pv, sd, views, reset_views, B, count, minb, stream, any_two, tab_bytes))) return rc;
+        if ((rc = batch_enqueue(c, pv, sd, views, reset_views, B, count, sh, stream, any_two, tab_bytes))) return rc;
     } else {
         // the graph bakes pointers of the tables, scratch and reset-view launches
         std::vector<uint64_t> key = {nv, ns, total, chunk, (uint64_t)minb, (uint64_t)count, (uint64_t)stream,
-                                     (uint64_t)any_two,
+                                     (uint64_t)any_two, (uint64_t)sh.block, (uint64_t)sh.shortd,
                                      (uint64_t)(uintptr_t)c->batch_tab.p,
                                      (uint64_t)(uintptr_t)c->h_batch_tab, (uint64_t)(uintptr_t)c->raw_shadow.p,
                                      (uint64_t)(uintptr_t)c->hist_prev.p, (uint64_t)(uintptr_t)c->stream};
@@ -1174,7 +1200,7 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
             c->batch_key.clear();
             cudaGraph_t graph = nullptr;
             HY_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            rc = batch_enqueue(c, pv, sd, views, reset_views, B, count, minb, stream, any_two, tab_bytes);
+            rc = batch_enqueue(c, pv, sd, views, reset_views, B, count, sh, stream, any_two, tab_bytes);
             cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
             if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
             if (e != cudaSuccess) { cudaGetLastError(); return HY_ERR_CUDA; }
@@ -1188,6 +1214,74 @@ int hy_batch_forward(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* 
     if (!c->batch_done) HY_CUDA_TRY(cudaEventCreateWithFlags(&c->batch_done, cudaEventDisableTiming));
     HY_CUDA_TRY(cudaEventRecord(c->batch_done, c->stream));
     return finish_call(c, st, !(bflags & HY_BATCH_NO_STATUS_SYNC));
+}
+
+// Coordinate descent over the tile-stream batch kernel's launch shape: each axis in
+// turn (queue chunk, threads per block, register cap, shared stack entries) is
+// swept with the others at their best so far; a shape is timed by CUDA events on
+// the context's stream around `reps` graph replays after one untimed call (which
+// captures the shape's graph), and its time is the fastest replay.
+int hy_batch_autotune(HyCtx* c, HyCtx* const* scenes, uint32_t ns, const HyView* views, uint32_t nv,
+                      uint32_t reps, HyPassConfig* tuning, float* best_ms) {
+    if (!c || !tuning || reps == 0 || reps > 64) return HY_ERR_INVALID_ARG;
+    DeviceGuard g(c->device);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        cudaGetLastError();
+        if (e0) cudaEventDestroy(e0);
+        return HY_ERR_CUDA;
+    }
+    HyPassConfig best;
+    std::memset(&best, 0, sizeof(best));
+    best.shadow_spp = 1;
+    best.queue_chunk = 1;
+    best.block_size = 128;
+    best.min_blocks = 8;
+    best.stack_depth = 0;
+    float best_t = 0.f;
+    auto time_shape = [&](const HyPassConfig& cand, float* ms) -> int {
+        int rc = hy_batch_forward(c, scenes, ns, views, nv, HY_BATCH_NO_STATUS_SYNC, &cand, nullptr);
+        if (rc) return rc;
+        float t_min = 0.f;
+        for (uint32_t k = 0; k < reps; k++) {
+            HY_CUDA_TRY(cudaEventRecord(e0, c->stream));
+            if ((rc = hy_batch_forward(c, scenes, ns, views, nv, HY_BATCH_NO_STATUS_SYNC, &cand, nullptr))) return rc;
+            HY_CUDA_TRY(cudaEventRecord(e1, c->stream));
+            HY_CUDA_TRY(cudaEventSynchronize(e1));
+            float t = 0.f;
+            HY_CUDA_TRY(cudaEventElapsedTime(&t, e0, e1));
+            if (k == 0 || t < t_min) t_min = t;
+        }
+        // a device-side error of the shape (timeout, overflow) disqualifies nothing silently
+        if ((rc = finish_call(c, nullptr, true))) return rc;
+        *ms = t_min;
+        return HY_OK;
+    };
+    int rc = time_shape(best, &best_t);
+    static const uint32_t chunks[] = {1, 2, 4, 8, 16, 32}, blocks[] = {64, 128, 256}, minbs[] = {6, 8},
+                          stacks[] = {0, 8, 16, 32};
+    struct Axis { const uint32_t* v; int n; uint32_t HyPassConfig::*field; };
+    const Axis axes[] = {{chunks, 6, &HyPassConfig::queue_chunk}, {blocks, 3, &HyPassConfig::block_size},
+                         {minbs, 2, &HyPassConfig::min_blocks}, {stacks, 4, &HyPassConfig::stack_depth}};
+    for (const Axis& a : axes) {
+        if (rc) break;
+        HyPassConfig cur = best;
+        for (int i = 0; i < a.n && !rc; i++) {
+            if (a.v[i] == best.*(a.field)) continue;
+            HyPassConfig cand = cur;
+            cand.*(a.field) = a.v[i];
+            float t = 0.f;
+            rc = time_shape(cand, &t);
+            if (rc == HY_ERR_UNSUPPORTED) { rc = HY_OK; continue; }  // a shape the batch cannot take
+            if (!rc && t < best_t) { best = cand; best_t = t; }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    *tuning = best;
+    if (best_ms) *best_ms = best_t;
+    return HY_OK;
 }
 
 }  // extern "C"

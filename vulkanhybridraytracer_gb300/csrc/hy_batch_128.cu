@@ -1,0 +1,8 @@
+// The batched tile-stream shadow kernels of 128 threads per block (hy_batch.cuh).
+#include "hy_batch.cuh"
+
+namespace hy {
+void* batch_stream_kernel_128(bool count, int minb, int shortd, bool two) {
+    return batch_stream_kernel_b<128>(count, minb, shortd, two);
+}
+}  // namespace hy

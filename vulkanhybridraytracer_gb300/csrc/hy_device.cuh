@@ -397,18 +397,22 @@ __device__ __forceinline__ uint32_t slots_to_ranks(uint32_t m, uint32_t ord) {
 // sh[i * 128 + t]: conflict-free) and whose deeper entries spill to the
 // lane's local array.
 constexpr int kShortStack = 8;
-struct SplitStack {
-    uint2* sh;    // &smem[threadIdx.x], entries 128 apart
-    uint2* deep;  // local array of kStackMax - kShortStack entries
+template <int SH, int STRIDE>  // SH entries in shared memory, STRIDE = threads per block
+struct SplitStackT {
+    uint2* sh;    // &smem[threadIdx.x], entries STRIDE apart
+    uint2* deep;  // local array for the entries past SH
 };
+using SplitStack = SplitStackT<kShortStack, 128>;
 __device__ __forceinline__ void stack_put(uint2* s, int i, uint2 v) { s[i] = v; }
 __device__ __forceinline__ uint2 stack_get(const uint2* s, int i) { return s[i]; }
-__device__ __forceinline__ void stack_put(const SplitStack& s, int i, uint2 v) {
-    if (i < kShortStack) s.sh[i * 128] = v;
-    else s.deep[i - kShortStack] = v;
+template <int SH, int STRIDE>
+__device__ __forceinline__ void stack_put(const SplitStackT<SH, STRIDE>& s, int i, uint2 v) {
+    if (i < SH) s.sh[i * STRIDE] = v;
+    else s.deep[i - SH] = v;
 }
-__device__ __forceinline__ uint2 stack_get(const SplitStack& s, int i) {
-    return i < kShortStack ? s.sh[i * 128] : s.deep[i - kShortStack];
+template <int SH, int STRIDE>
+__device__ __forceinline__ uint2 stack_get(const SplitStackT<SH, STRIDE>& s, int i) {
+    return i < SH ? s.sh[i * STRIDE] : s.deep[i - SH];
 }
 
 // Stack traversal of the 8-wide BVH.  ANY: TerminateOnFirstHit semantics.

@@ -30,10 +30,6 @@
 
 namespace hy {
 
-__device__ __forceinline__ float roundtrip(uint32_t fmt, float v) {
-    return fmt == HY_ACCUM_U8 ? __fdiv_rn((float)quant8(v), 255.0f) : v;
-}
-
 template <int MODE, bool COUNT>
 __device__ __forceinline__ void do_pixel(const SceneDev& S, const PassParams& P, uint32_t x, uint32_t y,
                                          LaneStats& ls) {
@@ -169,28 +165,6 @@ __device__ __forceinline__ void do_pixel(const SceneDev& S, const PassParams& P,
 // ACCUM: fold each light's factor into the history with blur.comp's running
 // mean (frame > 0) instead of writing the raw image.
 // ---------------------------------------------------------------------------------
-struct ShadowLane {
-    f3 position, N, L;
-    float dist, radius;
-    uint32_t pix, seed, light, k, nrays;
-    float sf;
-    int smode;
-    bool in_blur, setup;
-};
-
-template <bool ACCUM>
-__device__ __forceinline__ void shadow_finalize(const PassParams& P, const ShadowLane& s, size_t plane, float v) {
-    const size_t li = (size_t)s.light * plane + s.pix;
-    if (!ACCUM) {
-        accum_store(P.accum_fmt, P.shadow, li, v);
-    } else if (s.in_blur) {
-        const float center = roundtrip(P.accum_fmt, v);
-        const float old = accum_load(P.accum_fmt, P.hist, li);
-        const float a = __fdiv_rn(1.0f, __fadd_rn((float)P.accum_frame, 1.0f));
-        accum_store(P.accum_fmt, P.hist, li, __fadd_rn(__fmul_rn(old, __fsub_rn(1.0f, a)), __fmul_rn(center, a)));
-    }
-}
-
 template <bool COUNT, bool ACCUM, int MINB, bool TWO = false>
 __global__ void __launch_bounds__(128, MINB) k_shadow(const SceneDev S, const PassParams P) {
     LaneStats ls;
@@ -425,67 +399,6 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, co
     }
     if (COUNT) { ls.nodes += nn; ls.tris += nt; }
     flush_stats(ls, P.stats);
-}
-
-// ---------------------------------------------------------------------------------
-// One 8x4 tile of a view, light by light.  ACC: 0 raw shadow images, 1 the
-// running mean into the history, 2 either (accum) at run time.  reference:
-// REFERENCE RNG (one ray per pixel-light from the pixel's seed, by value).
-template <bool COUNT, bool TWO, int ACC, class Stack>
-__device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams& P, uint32_t tile, bool reference,
-                                            bool accum, StreamSlots& sm, Stack stk, Trav& t, RayPre& r,
-                                            ShadowLane& s, LaneStats& ls, uint32_t& nn, uint32_t& nt,
-                                            const uint4* top, uint32_t ntop) {
-    const uint32_t lane = threadIdx.x & 31, wb = threadIdx.x & ~31u;
-    const size_t plane = (size_t)P.W * P.H;
-    const uint32_t spp = P.spp, nrays = reference ? 1u : spp;
-    const uint32_t x = (tile % P.tiles_x) * 8 + (lane & 7), y = (tile / P.tiles_x) * 4 + (lane >> 3);
-    const bool present = x < P.W && y < P.H;
-    auto finalize = [&](float v) {
-        if (ACC == 0 || (ACC == 2 && !accum)) shadow_finalize<false>(P, s, plane, v);
-        else shadow_finalize<true>(P, s, plane, v);
-    };
-    uint32_t seed0 = 0, rays_before = 0;
-    if (present) {
-        s.pix = y * P.W + x;
-        const float4 g0 = fetch_texel(P.plane[0], P.fmt[0], s.pix);
-        const float4 g1 = fetch_texel(P.plane[1], P.fmt[1], s.pix);
-        s.position = mk(g0.x, g0.y, g0.z);
-        s.N = normalize_rn(mk(__fsub_rn(__fmul_rn(g1.x, 2.0f), 1.0f), __fsub_rn(__fmul_rn(g1.y, 2.0f), 1.0f),
-                              __fsub_rn(__fmul_rn(g1.z, 2.0f), 1.0f)));
-        const int mi = mat_index(g0.w, S.num_mats);
-        s.smode = mi >= 0 ? (int)S.mats[mi].smr[0] : 0;
-        s.in_blur = x < P.blur_w && y < P.blur_h;
-        seed0 = tea(s.pix, P.frame_u);
-    }
-    for (uint32_t l = 0; l < P.num_lights; l++) {
-        // ---- light l for this lane's pixel ----
-        bool traced = false;
-        s.light = l;
-        if (present) {
-            const LightGeo lg = light_geo(S.lights[l], s.position, s.N);
-            float v = -1.f;
-            if (s.smode == 4) v = 1.0f;
-            else if (!(lg.NdotL > 0.f)) v = 0.0f;
-            else if (!(lg.dist < lg.maxd)) v = 1.0f;
-            if (v >= 0.f) finalize(v);
-            else traced = true;
-            stream_publish(sm, traced, s.position, lg.L, lg.dist,
-                           !traced || reference ? seed0 : lcg_jump(seed0, 2u * rays_before));
-        } else {
-            stream_publish(sm, false, s.position, s.position, 0.f, 0u);
-        }
-        if (__ballot_sync(0xffffffffu, traced) != 0) {
-            // shadowRaygen.rgen:78: origin position + 0.1 dir, tmax distance + 1
-            stream_light<COUNT, TWO>(S, P, sm, nrays, S.lights[l].radius, 1e-1f, stk, t, r, ls, nn, nt, top, ntop);
-            if (traced) {
-                const uint32_t unocc = sm.cnt[wb + lane];
-                finalize(reference ? (float)unocc : __fdiv_rn((float)unocc, (float)spp));
-            }
-        }
-        if (traced) rays_before += spp;
-        __syncwarp();  // the slots are rewritten by the next light's set-up
-    }
 }
 
 // ---------------------------------------------------------------------------------
@@ -724,22 +637,6 @@ __global__ void __launch_bounds__(128) k_gbuffer(const SceneDev S, const GbufPar
 // different views.  REFERENCE views run with one lane per pixel (their
 // samples are one ray), DECORRELATED views with spp lanes per pixel-light.
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t view_of_tile(const uint32_t* s_begin, uint32_t nviews, uint32_t tile) {
-    uint32_t lo = 0, hi = nviews;  // s_begin[lo] <= tile < s_begin[hi]
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (s_begin[mid] <= tile) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
-__device__ __forceinline__ void finalize_rt(const PassParams& P, bool accum, const ShadowLane& s, size_t plane,
-                                            float v) {
-    if (accum) shadow_finalize<true>(P, s, plane, v);
-    else shadow_finalize<false>(P, s, plane, v);
-}
-
 template <bool COUNT, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_shadow_batch(const BatchParams B) {
     __shared__ uint32_t s_begin[kMaxBatchViews + 1];
@@ -890,67 +787,6 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_batch(const BatchParams B)
             s.light++;
             s.setup = true;
         }
-    }
-    if (COUNT) { ls.nodes += nn; ls.tris += nt; }
-    flush_stats(ls, B.stats);
-}
-
-// The batch over tile streams: a warp pulls (view, tile) units from the
-// batch's queue and walks each tile light by light (stream_tile) with that
-// view's parameters; REFERENCE-RNG views trace one ray per pixel-light.
-// ANY_TWO: the batch holds a two-level scene (compiled separately: the second
-// traversal raises the register pressure of the one-level case)
-static_assert(sizeof(PassParams) % 4 == 0 && sizeof(SceneDev) % 4 == 0, "copied to shared memory as words");
-template <bool COUNT, int MINB, bool ANY_TWO>
-__global__ void __launch_bounds__(128, MINB) k_shadow_batch_stream(const BatchParams B) {
-    __shared__ uint32_t s_begin[kMaxBatchViews + 1];
-    __shared__ StreamSlots sm;
-    // per warp: its current view's parameters and scene, copied from the
-    // global tables when the warp moves to another view
-    __shared__ PassParams s_view[4];
-    __shared__ SceneDev s_scene[4];
-    for (uint32_t i = threadIdx.x; i <= B.nviews; i += blockDim.x)
-        s_begin[i] = i < B.nviews ? B.views[i].tile_begin : B.total_tiles;
-    __syncthreads();
-    LaneStats ls;
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint2 stk[kStackMax];
-    ShadowLane s;
-    Trav t;
-    RayPre r;
-    uint32_t chunk_cur = 0, chunk_end = 0, nn = 0, nt = 0, cur_view = 0xffffffffu;
-    for (;;) {
-        if (chunk_cur == chunk_end) {
-            uint32_t t0 = 0;
-            if (lane == 0) t0 = atomicAdd(B.queue, B.chunk);
-            t0 = __shfl_sync(0xffffffffu, t0, 0);
-            if (t0 >= B.total_tiles) break;
-            chunk_cur = t0;
-            chunk_end = min(t0 + B.chunk, B.total_tiles);
-        }
-        const uint32_t unit = chunk_cur++;
-        const uint32_t v = view_of_tile(s_begin, B.nviews, unit);
-        if (v != cur_view) {
-            __syncwarp();
-            const uint32_t* vs = reinterpret_cast<const uint32_t*>(&B.views[v]);
-            uint32_t* vd = reinterpret_cast<uint32_t*>(&s_view[warp]);
-            for (uint32_t i = lane; i < sizeof(PassParams) / 4; i += 32) vd[i] = vs[i];
-            const uint32_t* ss = reinterpret_cast<const uint32_t*>(&B.scenes[B.views[v].scene]);
-            uint32_t* sd = reinterpret_cast<uint32_t*>(&s_scene[warp]);
-            for (uint32_t i = lane; i < sizeof(SceneDev) / 4; i += 32) sd[i] = ss[i];
-            __syncwarp();
-            cur_view = v;
-        }
-        const PassParams& P = s_view[warp];
-        const SceneDev& S = s_scene[warp];
-        const bool accum = !(P.flags & HY_FLAG_NO_ACCUM) && P.accum_frame > 0;
-        const bool reference = P.rng_mode == HY_RNG_REFERENCE;
-        if (ANY_TWO && S.two_level)  // a two-level scene: the same tile with the instance walk
-            stream_tile<COUNT, true, 2>(S, P, unit - P.tile_begin, reference, accum, sm, stk, t, r, s, ls, nn, nt,
-                                        nullptr, 0);
-        else
-            stream_tile<COUNT, false, 2>(S, P, unit - P.tile_begin, reference, accum, sm, stk, t, r, s, ls, nn, nt,
-                                         nullptr, 0);
     }
     if (COUNT) { ls.nodes += nn; ls.tris += nt; }
     flush_stats(ls, B.stats);
@@ -1295,34 +1131,52 @@ cudaError_t launch_gbuffer(const SceneDev& S, const GbufParams& G, cudaStream_t 
     return cudaGetLastError();
 }
 
-template <int MINB>
-static void* batch_stream_kernel(bool count, bool two) {
-    if (two)
-        return count ? (void*)k_shadow_batch_stream<true, MINB, true> : (void*)k_shadow_batch_stream<false, MINB, true>;
-    return count ? (void*)k_shadow_batch_stream<true, MINB, false> : (void*)k_shadow_batch_stream<false, MINB, false>;
+// the tile-stream batch kernel of a launch shape (hy_batch_*.cu); nullptr where none is compiled
+static void* batch_stream_kernel(bool count, int minb, int block, int shortd, bool two) {
+    switch (block) {
+        case 64: return batch_stream_kernel_64(count, minb, shortd, two);
+        case 128: return batch_stream_kernel_128(count, minb, shortd, two);
+        case 256: return batch_stream_kernel_256(count, minb, shortd, two);
+        default: return nullptr;
+    }
 }
 
-static void* batch_kernel(bool shade, bool count, int minb, bool stream, bool two) {
+static void* batch_kernel(bool shade, bool count, int minb, bool stream, bool two, int block, int shortd) {
     if (shade) return count ? (void*)k_pixels_batch<true> : (void*)k_pixels_batch<false>;
-    if (stream) {
-        if (two) return batch_stream_kernel<5>(count, true);
-        if (minb >= 8) return batch_stream_kernel<8>(count, false);
-        if (minb >= 6) return batch_stream_kernel<6>(count, false);
-        return batch_stream_kernel<5>(count, false);
-    }
+    if (stream) return batch_stream_kernel(count, minb, block, shortd, two);
+    if (block != 128 || shortd != 0) return nullptr;
     if (minb >= 8) return count ? (void*)k_shadow_batch<true, 8> : (void*)k_shadow_batch<false, 8>;
     return count ? (void*)k_shadow_batch<true, 5> : (void*)k_shadow_batch<false, 5>;
 }
 
-cudaError_t launch_batch(bool shade, bool count, int minb, bool stream, bool two, const BatchParams& B, int grid,
-                         cudaStream_t s) {
-    void* args[] = {(void*)&B};
-    return cudaLaunchKernel(batch_kernel(shade, count, minb, stream, two), dim3(grid), dim3(128), args, 0, s);
+// dynamic shared memory of a batch kernel: the shared part of the traversal stacks
+static size_t batch_dyn_smem(bool shade, bool stream, int block, int shortd) {
+    return (!shade && stream) ? (size_t)shortd * (size_t)block * sizeof(uint2) : 0;
 }
 
-cudaError_t batch_occupancy(bool shade, bool count, int minb, bool stream, bool two, int* blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, batch_kernel(shade, count, minb, stream, two),
-                                                         128, 0);
+cudaError_t launch_batch(bool shade, bool count, int minb, bool stream, bool two, int block, int shortd,
+                         const BatchParams& B, int grid, cudaStream_t s) {
+    void* k = batch_kernel(shade, count, minb, stream, two, shade ? 128 : block, shortd);
+    if (!k) return cudaErrorNotSupported;
+    const size_t dyn = batch_dyn_smem(shade, stream, block, shortd);
+    if (dyn) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+        if (e != cudaSuccess) return e;
+    }
+    void* args[] = {(void*)&B};
+    return cudaLaunchKernel(k, dim3(grid), dim3(shade ? 128 : block), args, dyn, s);
+}
+
+cudaError_t batch_occupancy(bool shade, bool count, int minb, bool stream, bool two, int block, int shortd,
+                            int* blocks_per_sm) {
+    void* k = batch_kernel(shade, count, minb, stream, two, shade ? 128 : block, shortd);
+    if (!k) return cudaErrorNotSupported;
+    const size_t dyn = batch_dyn_smem(shade, stream, block, shortd);
+    if (dyn) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, shade ? 128 : block, dyn);
 }
 
 }  // namespace hy

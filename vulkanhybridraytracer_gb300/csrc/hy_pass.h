@@ -110,8 +110,14 @@ cudaError_t launch_post(const uint8_t* in_bgra8, const float* in_rgba32f, uint32
 cudaError_t launch_trace(const SceneDev& S, const HyRay* rays, uint32_t n, bool any, bool count, HyHit* hits,
                          unsigned long long* stats, uint32_t* status, int grid, cudaStream_t s);
 cudaError_t launch_gbuffer(const SceneDev& S, const GbufParams& G, cudaStream_t s);
-cudaError_t launch_batch(bool shade, bool count, int minb, bool stream, bool two, const BatchParams& B, int grid,
-                         cudaStream_t s);
-cudaError_t batch_occupancy(bool shade, bool count, int minb, bool stream, bool two, int* blocks_per_sm);
+// batches: block / shortd are the tile-stream kernel's threads per block and
+// shared stack entries (the shade and lane-group kernels: 128 / 0)
+cudaError_t launch_batch(bool shade, bool count, int minb, bool stream, bool two, int block, int shortd,
+                         const BatchParams& B, int grid, cudaStream_t s);
+cudaError_t batch_occupancy(bool shade, bool count, int minb, bool stream, bool two, int block, int shortd,
+                            int* blocks_per_sm);
+void* batch_stream_kernel_64(bool count, int minb, int shortd, bool two);
+void* batch_stream_kernel_128(bool count, int minb, int shortd, bool two);
+void* batch_stream_kernel_256(bool count, int minb, int shortd, bool two);
 
 }  // namespace hy

@@ -36,24 +36,27 @@ __device__ __forceinline__ uint32_t stage_top(const SceneDev& S, uint4* top, uin
 // Items of a light are traced in the order of their disk samples (kSortItems at
 // most per warp and light; more are traced in item order).
 constexpr uint32_t kSortItems = 512, kSortBuckets = 64;
-struct StreamSlots {
-    float4 pos[128];
-    float4 PL[128];
-    float4 T[128];
-    float4 B[128];
-    uint32_t cnt[128];
-    uint32_t next[4];  // per warp: the next unclaimed item of the current light
+template <int NW>  // warps per block
+struct StreamSlotsT {
+    float4 pos[NW * 32];
+    float4 PL[NW * 32];
+    float4 T[NW * 32];
+    float4 B[NW * 32];
+    uint32_t cnt[NW * 32];
+    uint32_t next[NW];  // per warp: the next unclaimed item of the current light
     // per warp: the traced items of the light ordered by their disk sample, the
     // sample's cell per item, and the cell counts / cursors of the counting sort
-    uint16_t order[4][kSortItems];
-    uint8_t key[4][kSortItems];
-    uint32_t bucket[4][kSortBuckets];
+    uint16_t order[NW][kSortItems];
+    uint8_t key[NW][kSortItems];
+    uint32_t bucket[NW][kSortBuckets];
 };
+using StreamSlots = StreamSlotsT<4>;
 
 constexpr uint32_t kNotTraced = 0xffffffffu;
 
 // lane's slot for the current light; first_state: the RNG state of sample 0
-__device__ __forceinline__ void stream_publish(StreamSlots& sm, bool traced, f3 position, f3 L, float dist,
+template <class Slots>
+__device__ __forceinline__ void stream_publish(Slots& sm, bool traced, f3 position, f3 L, float dist,
                                                uint32_t first_state) {
     const uint32_t i = threadIdx.x;
     if (traced) {
@@ -74,110 +77,221 @@ __device__ __forceinline__ void stream_publish(StreamSlots& sm, bool traced, f3 
 // steps (sampleDisk's two draws per sample), its ray from position +
 // offset * dir to distance + 1.  On return sm.cnt holds each pixel's
 // unoccluded samples.
-template <bool COUNT, bool TWO, class Stack>
-__device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams& P, StreamSlots& sm, uint32_t nrays,
+template <bool COUNT, bool TWO, class Stack, class Slots>
+__device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams& P, Slots& sm, uint32_t nrays,
                                              float radius, float offset, Stack stk, Trav& t, RayPre& r,
                                              LaneStats& ls, uint32_t& nn, uint32_t& nt, const uint4* top,
                                              uint32_t ntop) {
     const uint32_t lane = threadIdx.x & 31, wb = threadIdx.x & ~31u, warp = threadIdx.x >> 5;
-    uint32_t total = 32u * nrays;
     uint32_t* next = &sm.next[warp];
+    const uint32_t all = 32u * nrays;
     __syncwarp();
-    // ---- the order of the light's items: a counting sort of the traced items by
-    //      the cell of their disk sample on an 8x8 grid over the disk (cells in
-    //      Morton order), so that the lanes' rays at any moment are nearly
-    //      parallel rays from the tile's nearby pixels and walk the same nodes.
-    //      The rays themselves do not change: only which lane traces which ray,
-    //      and when ----
-    const bool sorted = nrays > 1 && total <= kSortItems;
-    if (sorted) {
-        uint32_t* bk = sm.bucket[warp];
-        bk[lane] = 0;
-        bk[lane + 32] = 0;
-        __syncwarp();
-        for (uint32_t q = lane; q < total; q += 32) {
-            const uint32_t pi = q / nrays, k = q - pi * nrays;
-            uint32_t key = 0xffu;
-            if (__float_as_uint(sm.T[wb + pi].w) != kNotTraced) {
-                uint32_t st = lcg_jump(__float_as_uint(sm.PL[wb + pi].w), 2u * k);
-                const float r1 = rnd(st), r2 = rnd(st);
-                // the disk point in units of the radius (approximate: it only orders the items)
-                float sn, cs;
-                __sincosf(6.2831853f * r2, &sn, &cs);
-                const float rr = sqrtf(r1);
-                const uint32_t ix = min(7u, (uint32_t)fmaxf((rr * cs + 1.0f) * 4.0f, 0.0f));
-                const uint32_t iy = min(7u, (uint32_t)fmaxf((rr * sn + 1.0f) * 4.0f, 0.0f));
-                key = (ix & 1u) | ((iy & 1u) << 1) | ((ix & 2u) << 1) | ((iy & 2u) << 2) | ((ix & 4u) << 2) |
-                      ((iy & 4u) << 3);
-                atomicAdd(&bk[key], 1u);
+    // the light's items in chunks of kSortItems (one chunk unless spp > 16)
+    for (uint32_t c0 = 0; c0 < all; c0 += kSortItems) {
+        const uint32_t cn = min(kSortItems, all - c0);
+        uint32_t total = cn;
+        // ---- the order of the chunk's items: a counting sort of the traced items by
+        //      the cell of their disk sample on an 8x8 grid over the disk (cells in
+        //      Morton order), so that the lanes' rays at any moment are nearly
+        //      parallel rays from the tile's nearby pixels and walk the same nodes
+        //      (1080p: 31.96 -> 29.90 ms per shadow launch).  The rays themselves do
+        //      not change: only which lane traces which ray, and when ----
+        const bool sorted = nrays > 1;
+        if (sorted) {
+            uint32_t* bk = sm.bucket[warp];
+            bk[lane] = 0;
+            bk[lane + 32] = 0;
+            __syncwarp();
+            for (uint32_t j = lane; j < cn; j += 32) {
+                const uint32_t q = c0 + j, pi = q / nrays, k = q - pi * nrays;
+                uint32_t key = 0xffu;
+                if (__float_as_uint(sm.T[wb + pi].w) != kNotTraced) {
+                    uint32_t st = lcg_jump(__float_as_uint(sm.PL[wb + pi].w), 2u * k);
+                    const float r1 = rnd(st), r2 = rnd(st);
+                    // the disk point in units of the radius (approximate: it only orders the items)
+                    float sn, cs;
+                    __sincosf(6.2831853f * r2, &sn, &cs);
+                    const float rr = sqrtf(r1);
+                    const uint32_t ix = min(7u, (uint32_t)fmaxf((rr * cs + 1.0f) * 4.0f, 0.0f));
+                    const uint32_t iy = min(7u, (uint32_t)fmaxf((rr * sn + 1.0f) * 4.0f, 0.0f));
+                    key = (ix & 1u) | ((iy & 1u) << 1) | ((ix & 2u) << 1) | ((iy & 2u) << 2) | ((ix & 4u) << 2) |
+                          ((iy & 4u) << 3);
+                    atomicAdd(&bk[key], 1u);
+                }
+                sm.key[warp][j] = (uint8_t)key;
             }
-            sm.key[warp][q] = (uint8_t)key;
+            __syncwarp();
+            // exclusive scan of the 64 counts, two per lane
+            const uint32_t cnt0 = bk[2 * lane], cnt1 = bk[2 * lane + 1], c = cnt0 + cnt1;
+            uint32_t incl = c;
+    #pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= (uint32_t)d) incl += y;
+            }
+            total = __shfl_sync(0xffffffffu, incl, 31);  // the chunk's traced items
+            __syncwarp();
+            bk[2 * lane] = incl - c;
+            bk[2 * lane + 1] = incl - c + cnt0;
+            __syncwarp();
+            for (uint32_t j = lane; j < cn; j += 32) {
+                const uint32_t key = sm.key[warp][j];
+                if (key != 0xffu) sm.order[warp][atomicAdd(&bk[key], 1u)] = (uint16_t)j;
+            }
         }
+        if (lane == 0) *next = 0;
         __syncwarp();
-        // exclusive scan of the 64 counts, two per lane
-        const uint32_t c0 = bk[2 * lane], c1 = bk[2 * lane + 1], c = c0 + c1;
-        uint32_t incl = c;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
-            if (lane >= (uint32_t)d) incl += y;
-        }
-        total = __shfl_sync(0xffffffffu, incl, 31);  // the traced items
-        __syncwarp();
-        bk[2 * lane] = incl - c;
-        bk[2 * lane + 1] = incl - c + c0;
-        __syncwarp();
-        for (uint32_t q = lane; q < 32u * nrays; q += 32) {
-            const uint32_t key = sm.key[warp][q];
-            if (key != 0xffu) sm.order[warp][atomicAdd(&bk[key], 1u)] = (uint16_t)q;
-        }
-        __syncwarp();
-    }
-    bool live = false, more = true;
-    uint32_t cur = 0;
-    for (;;) {
-        // ---- this lane's next item of a traced pixel, claimed from the warp's
-        //      counter: items go to whichever lanes are free, in order, so the
-        //      warp's work stays balanced until the light's last items ----
-        while (!live && more) {
-            // one shared atomic per group of lanes claiming together, lane order kept
-            const uint32_t m = __activemask(), leader = __ffs(m) - 1;
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(next, (uint32_t)__popc(m));
-            base = __shfl_sync(m, base, leader);
-            uint32_t q = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
-            if (q >= total) { more = false; break; }
-            if (sorted) q = sm.order[warp][q];
-            const uint32_t pi = q / nrays, k = q - pi * nrays;
-            const float4 tp = sm.T[wb + pi];
-            if (__float_as_uint(tp.w) == kNotTraced) continue;
-            const float4 pp = sm.pos[wb + pi], pl = sm.PL[wb + pi], bp = sm.B[wb + pi];
-            const f3 pos = mk(pp.x, pp.y, pp.z);
-            const DiskFrame d{mk(tp.x, tp.y, tp.z), mk(bp.x, bp.y, bp.z), mk(pl.x, pl.y, pl.z)};
-            uint32_t st = lcg_jump(__float_as_uint(pl.w), 2u * k);
-            const f3 dir = sampleDisk(radius, pos, d, st);
-            r = ray_pre(add_rn(pos, scale_rn(dir, offset)), dir);
-            trav_init(t, r, __fadd_rn(pp.w, 1.0f));
-            cur = pi;
-            live = true;
-            ls.shadow++;
-        }
-        // ---- up to P.inner node visits, each with its leaf triangles (testing
-        //      the triangles of many lanes together instead, once enough lanes
-        //      have some, measured slower: 2,190 against 2,899 Mrays/s at 1080p,
-        //      the lanes waiting on triangles idle through the node visits) ----
-        if (live) {
-            for (uint32_t it = 0, ni = max(P.inner, 1u); it < ni; it++) {
-                if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status, top, ntop)) {
-                    live = false;
-                    if (t.h.id == HY_NO_HIT) atomicAdd(&sm.cnt[wb + cur], 1u);
-                    break;
+        bool live = false, more = true;
+        uint32_t cur = 0;
+        for (;;) {
+            // ---- this lane's next item of a traced pixel, claimed from the warp's
+            //      counter: items go to whichever lanes are free, in order, so the
+            //      warp's work stays balanced until the light's last items ----
+            while (!live && more) {
+                // one shared atomic per group of lanes claiming together, lane order kept
+                const uint32_t m = __activemask(), leader = __ffs(m) - 1;
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(next, (uint32_t)__popc(m));
+                base = __shfl_sync(m, base, leader);
+                uint32_t q = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+                if (q >= total) { more = false; break; }
+                q = c0 + (sorted ? (uint32_t)sm.order[warp][q] : q);
+                const uint32_t pi = q / nrays, k = q - pi * nrays;
+                const float4 tp = sm.T[wb + pi];
+                if (__float_as_uint(tp.w) == kNotTraced) continue;
+                const float4 pp = sm.pos[wb + pi], pl = sm.PL[wb + pi], bp = sm.B[wb + pi];
+                const f3 pos = mk(pp.x, pp.y, pp.z);
+                const DiskFrame d{mk(tp.x, tp.y, tp.z), mk(bp.x, bp.y, bp.z), mk(pl.x, pl.y, pl.z)};
+                uint32_t st = lcg_jump(__float_as_uint(pl.w), 2u * k);
+                const f3 dir = sampleDisk(radius, pos, d, st);
+                r = ray_pre(add_rn(pos, scale_rn(dir, offset)), dir);
+                trav_init(t, r, __fadd_rn(pp.w, 1.0f));
+                cur = pi;
+                live = true;
+                ls.shadow++;
+            }
+            // ---- up to P.inner node visits, each with its leaf triangles (testing
+            //      the triangles of many lanes together instead, once enough lanes
+            //      have some, measured slower: 2,190 against 2,899 Mrays/s at 1080p,
+            //      the lanes waiting on triangles idle through the node visits) ----
+            if (live) {
+                for (uint32_t it = 0, ni = max(P.inner, 1u); it < ni; it++) {
+                    if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status, top, ntop)) {
+                        live = false;
+                        if (t.h.id == HY_NO_HIT) atomicAdd(&sm.cnt[wb + cur], 1u);
+                        break;
+                    }
                 }
             }
+            if (__ballot_sync(0xffffffffu, live || more) == 0) break;
         }
-        if (__ballot_sync(0xffffffffu, live || more) == 0) break;
+        __syncwarp();
     }
-    __syncwarp();
+}
+
+__device__ __forceinline__ float roundtrip(uint32_t fmt, float v) {
+    return fmt == HY_ACCUM_U8 ? __fdiv_rn((float)quant8(v), 255.0f) : v;
+}
+
+// A lane's pixel in the shadow kernels (set-up, current light, sample state).
+struct ShadowLane {
+    f3 position, N, L;
+    float dist, radius;
+    uint32_t pix, seed, light, k, nrays;
+    float sf;
+    int smode;
+    bool in_blur, setup;
+};
+
+template <bool ACCUM>
+__device__ __forceinline__ void shadow_finalize(const PassParams& P, const ShadowLane& s, size_t plane, float v) {
+    const size_t li = (size_t)s.light * plane + s.pix;
+    if (!ACCUM) {
+        accum_store(P.accum_fmt, P.shadow, li, v);
+    } else if (s.in_blur) {
+        const float center = roundtrip(P.accum_fmt, v);
+        const float old = accum_load(P.accum_fmt, P.hist, li);
+        const float a = __fdiv_rn(1.0f, __fadd_rn((float)P.accum_frame, 1.0f));
+        accum_store(P.accum_fmt, P.hist, li, __fadd_rn(__fmul_rn(old, __fsub_rn(1.0f, a)), __fmul_rn(center, a)));
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// One 8x4 tile of a view, light by light.  ACC: 0 raw shadow images, 1 the
+// running mean into the history, 2 either (accum) at run time.  reference:
+// REFERENCE RNG (one ray per pixel-light from the pixel's seed, by value).
+template <bool COUNT, bool TWO, int ACC, class Stack, class Slots>
+__device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams& P, uint32_t tile, bool reference,
+                                            bool accum, Slots& sm, Stack stk, Trav& t, RayPre& r,
+                                            ShadowLane& s, LaneStats& ls, uint32_t& nn, uint32_t& nt,
+                                            const uint4* top, uint32_t ntop) {
+    const uint32_t lane = threadIdx.x & 31, wb = threadIdx.x & ~31u;
+    const size_t plane = (size_t)P.W * P.H;
+    const uint32_t spp = P.spp, nrays = reference ? 1u : spp;
+    const uint32_t x = (tile % P.tiles_x) * 8 + (lane & 7), y = (tile / P.tiles_x) * 4 + (lane >> 3);
+    const bool present = x < P.W && y < P.H;
+    auto finalize = [&](float v) {
+        if (ACC == 0 || (ACC == 2 && !accum)) shadow_finalize<false>(P, s, plane, v);
+        else shadow_finalize<true>(P, s, plane, v);
+    };
+    uint32_t seed0 = 0, rays_before = 0;
+    if (present) {
+        s.pix = y * P.W + x;
+        const float4 g0 = fetch_texel(P.plane[0], P.fmt[0], s.pix);
+        const float4 g1 = fetch_texel(P.plane[1], P.fmt[1], s.pix);
+        s.position = mk(g0.x, g0.y, g0.z);
+        s.N = normalize_rn(mk(__fsub_rn(__fmul_rn(g1.x, 2.0f), 1.0f), __fsub_rn(__fmul_rn(g1.y, 2.0f), 1.0f),
+                              __fsub_rn(__fmul_rn(g1.z, 2.0f), 1.0f)));
+        const int mi = mat_index(g0.w, S.num_mats);
+        s.smode = mi >= 0 ? (int)S.mats[mi].smr[0] : 0;
+        s.in_blur = x < P.blur_w && y < P.blur_h;
+        seed0 = tea(s.pix, P.frame_u);
+    }
+    for (uint32_t l = 0; l < P.num_lights; l++) {
+        // ---- light l for this lane's pixel ----
+        bool traced = false;
+        s.light = l;
+        if (present) {
+            const LightGeo lg = light_geo(S.lights[l], s.position, s.N);
+            float v = -1.f;
+            if (s.smode == 4) v = 1.0f;
+            else if (!(lg.NdotL > 0.f)) v = 0.0f;
+            else if (!(lg.dist < lg.maxd)) v = 1.0f;
+            if (v >= 0.f) finalize(v);
+            else traced = true;
+            stream_publish(sm, traced, s.position, lg.L, lg.dist,
+                           !traced || reference ? seed0 : lcg_jump(seed0, 2u * rays_before));
+        } else {
+            stream_publish(sm, false, s.position, s.position, 0.f, 0u);
+        }
+        if (__ballot_sync(0xffffffffu, traced) != 0) {
+            // shadowRaygen.rgen:78: origin position + 0.1 dir, tmax distance + 1
+            stream_light<COUNT, TWO>(S, P, sm, nrays, S.lights[l].radius, 1e-1f, stk, t, r, ls, nn, nt, top, ntop);
+            if (traced) {
+                const uint32_t unocc = sm.cnt[wb + lane];
+                finalize(reference ? (float)unocc : __fdiv_rn((float)unocc, (float)spp));
+            }
+        }
+        if (traced) rays_before += spp;
+        __syncwarp();  // the slots are rewritten by the next light's set-up
+    }
+}
+
+// the view of a batch tile: s_begin holds each view's first tile (ascending)
+__device__ __forceinline__ uint32_t view_of_tile(const uint32_t* s_begin, uint32_t nviews, uint32_t tile) {
+    uint32_t lo = 0, hi = nviews;  // s_begin[lo] <= tile < s_begin[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (s_begin[mid] <= tile) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void finalize_rt(const PassParams& P, bool accum, const ShadowLane& s, size_t plane,
+                                            float v) {
+    if (accum) shadow_finalize<true>(P, s, plane, v);
+    else shadow_finalize<false>(P, s, plane, v);
 }
 
 }  // namespace hy

@@ -333,13 +333,7 @@ class HybridContext:
                 "hybrid_backward")
         return grad_mats, grad_lights[: self.num_lights], st.as_dict()
 
-    def batch_forward(self, scenes, views, graph: bool = True, tuning: L.HyPassConfig | None = None,
-                      sync: bool = True):
-        """One batch of views over scene contexts (hy_batch_forward).
-
-        views: list of dicts with keys scene, planes, camera (36 floats), config
-        (HyPassConfig), hist, fmt and optionally out_f / out_8 (device tensors).
-        """
+    def _views(self, scenes, views):
         arr = (C.c_void_p * len(scenes))(*[s.h.value for s in scenes])
         vs = (L.HyView * len(views))()
         keep = []
@@ -354,12 +348,32 @@ class HybridContext:
             vs[i].out_rgba32f = _ptr(v["out_f"]) if v.get("out_f") is not None else None
             vs[i].out_bgra8 = _ptr(v["out_8"]) if v.get("out_8") is not None else None
             keep.append(planes)
+        return arr, vs, keep
+
+    def batch_forward(self, scenes, views, graph: bool = True, tuning: L.HyPassConfig | None = None,
+                      sync: bool = True):
+        """One batch of views over scene contexts (hy_batch_forward).
+
+        views: list of dicts with keys scene, planes, camera (36 floats), config
+        (HyPassConfig), hist, fmt and optionally out_f / out_8 (device tensors).
+        """
+        arr, vs, keep = self._views(scenes, views)
         flags = (0 if graph else L.HY_BATCH_NO_GRAPH) | (0 if sync else L.HY_BATCH_NO_STATUS_SYNC)
         st = L.HyStats()
         L.check(self.lib.hy_batch_forward(self.h, arr, len(scenes), vs, len(views), flags,
                                           C.byref(tuning) if tuning is not None else None,
                                           C.byref(st) if sync else None), "batch_forward")
         return st.as_dict()
+
+    def batch_autotune(self, scenes, views, reps: int = 2):
+        """hy_batch_autotune: the fastest launch shape of the batch, (HyPassConfig, ms).
+        Runs the batch many times (its histories and outputs are overwritten)."""
+        arr, vs, keep = self._views(scenes, views)
+        tuning = L.HyPassConfig()
+        ms = C.c_float()
+        L.check(self.lib.hy_batch_autotune(self.h, arr, len(scenes), vs, len(views), reps, C.byref(tuning),
+                                           C.byref(ms)), "batch_autotune")
+        return tuning, ms.value
 
     def synchronize(self):
         L.check(self.lib.hy_synchronize(self.h), "synchronize")
