@@ -503,7 +503,7 @@ int hy_batch_forward(HyCtx* ctx, HyCtx* const* scenes, uint32_t num_scenes, cons
  * fastest of `reps` (1..64) graph replays, and writes the fastest shape to
  * *tuning (queue_chunk, block_size, min_blocks, stack_depth; the other fields
  * 0 / defaults) and its time to *best_ms (may be NULL).  It runs the batch as
- * given about 16 x (reps + 1) times, so the views' histories and outputs are
+ * given about 12 x (reps + 1) times (12 shapes), so the views' histories and outputs are
  * overwritten: tune on the frames' first batch or on copies.  Pass the result
  * to hy_batch_forward; a C++ application can keep it per GPU and workload. */
 int hy_batch_autotune(HyCtx* ctx, HyCtx* const* scenes, uint32_t num_scenes, const HyView* views,
