@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--mirror-reflection", action="store_true",
                     help="the reference's perfect mirror reflection instead of the configuration's GGX-sampled ray")
     ap.add_argument("--leg-steps", type=int, default=3, help="timed steps of the batch and diff legs")
+    ap.add_argument("--build-mode", default="sah", choices=["sah", "lbvh"],
+                    help="binary tree under the 8-wide nodes (hy_scene_set_build_mode)")
     return ap.parse_args()
 
 
@@ -77,7 +79,7 @@ ANYHIT_ORDER = {1: "far first", 2: "near first"}  # HY_ANYHIT_FAR_FIRST / HY_ANY
 # device sources of the pass kernels: a profile summary under profiles/ records the hash
 # of these files, so a figure measured on another version of the kernels is not reported
 # as this version's
-KERNEL_SOURCES = ("hy_device.cuh", "hy_stream.cuh", "hy_shade.cuh", "hy_pass.h", "hy_pass.cu")
+KERNEL_SOURCES = ("hy_device.cuh", "hy_stream.cuh", "hy_shade.cuh", "hy_pass.h", "hy_pass.cu", "hy_bvh.cu", "hy_sah.cu")
 
 
 def kernel_source_sha() -> str:
@@ -119,7 +121,21 @@ def config_of(wl, args):
                            "GGX-sampled from the texel's lobe (roughness < 0.3 texels), 1 ray"),
             "max_bounces": wl.max_bounces, "accumulation": "u8 history, running mean (frame > 0)",
             "gbuffer": "6 planes fp32 (88 B/px), primary-ray producer, untimed",
-            "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)"}
+            "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)",
+            "structure": STRUCTURE[BUILD_MODE["mode"]]}
+
+
+BUILD_MODE = {"mode": "sah"}
+STRUCTURE = {"sah": "binned SAH (32 bins per axis) binary tree -> compressed BVH8",
+             "lbvh": "LBVH (Karras radix tree over 30-bit Morton codes) -> compressed BVH8"}
+
+
+def build_structure(ctx, instanced: bool = False):
+    """hy_bvh_build(_instanced) with the build mode of --build-mode."""
+    from vulkanhybridraytracer_gb300 import _lib as L
+
+    ctx.set_build_mode(L.HY_BUILD_SAH if BUILD_MODE["mode"] == "sah" else L.HY_BUILD_LBVH)
+    return ctx.build_bvh(instanced=instanced)
 
 
 # ---- clocks sampling -------------------------------------------------------------------
@@ -183,6 +199,7 @@ def cpu_run(wl, cam, planes_np, threads: int, target_s: float, frame: int, flags
     po.set_threads(threads)
     orc = po.OracleScene()
     orc.set_scene(wl.scene)
+    orc.set_build_mode(po.HY_BUILD_SAH if BUILD_MODE["mode"] == "sah" else po.HY_BUILD_LBVH)
     orc.build_bvh()
     H = planes_np[0].shape[0]
     rows = 4
@@ -224,6 +241,7 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     orc = po.OracleScene()
     orc.set_scene(wl.scene)
+    orc.set_build_mode(po.HY_BUILD_SAH if BUILD_MODE["mode"] == "sah" else po.HY_BUILD_LBVH)
     orc.build_bvh()
     cam = wl.camera(1.0)
     planes = orc.gbuffer(cam, wl.width, wl.height)
@@ -385,7 +403,7 @@ def run_pathtrace(args):
     wl = workload(args)
     ctx = HybridContext(0, stream=stream.cuda_stream)
     ctx.set_scene(wl.scene)
-    ctx.build_bvh()
+    build_structure(ctx)
     img = torch.zeros((wl.height, wl.width, 4), dtype=torch.uint8, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     cfg = pass_config(spp=wl.spp, max_bounces=8, rng_mode=L.HY_RNG_DECORRELATED, flags=L.HY_FLAG_NO_STATUS_SYNC,
@@ -414,7 +432,8 @@ def run_pathtrace(args):
             "config": {"workload": wl.name.replace("hd-", "pathtrace-"), "width": wl.width, "height": wl.height,
                        "triangles": wl.scene.num_tris, "lights": len(wl.scene.lights), "shadow_spp": wl.spp,
                        "rng": "decorrelated", "max_bounces": 8,
-                       "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)"},
+                       "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)",
+            "structure": STRUCTURE[BUILD_MODE["mode"]]},
             "rays_per_frame": rays, "rays_breakdown": {"shadow_rays": st["shadow_rays"],
                                                        "camera_and_bounce_rays": st["reflection_rays"]},
             "per_kernel": kernels, "clocks": clk, "gpu_launches": args.steps}
@@ -441,7 +460,7 @@ def run_large(args):
     wl = scenes.large()
     ctx = HybridContext(0, stream=stream.cuda_stream)
     ctx.set_scene(wl.scene)
-    bvh = ctx.build_bvh()
+    bvh = build_structure(ctx)
     W, H, NL = wl.width, wl.height, len(wl.scene.lights)
     cam0 = wl.camera(1.0)
     planes = ctx.gbuffer(cam0, W, H)
@@ -545,7 +564,7 @@ def run_large(args):
     xf = wl.scene.pack()[3]
     ctx2 = HybridContext(0, stream=stream.cuda_stream)
     ctx2.set_scene(wl.scene)
-    bvh2 = ctx2.build_bvh(instanced=True)
+    bvh2 = build_structure(ctx2, instanced=True)
     order2 = ANYHIT_ORDER[ctx2.anyhit_order()]
     lay2 = ctx2.bvh_layout()
     st2 = ctx2.forward(planes, wl.camera(0.0), cfg(0, 0), hist, L.HY_ACCUM_U8, out_f=outf, out_8=out8)
@@ -619,7 +638,7 @@ def batch_leg(steps: int, warmup: int, n_views: int = 64, tune: bool = False, cl
     for sc in scs:
         c = HybridContext(0, stream=stream.cuda_stream)
         c.set_scene(sc)
-        c.build_bvh()
+        build_structure(c)
         ctxs.append(c)
     runner = HybridContext(0, stream=stream.cuda_stream)
     views = []
@@ -718,6 +737,7 @@ def run_batch(args):
 
 def main():
     args = parse()
+    BUILD_MODE["mode"] = args.build_mode
     if args.impl == "reference":
         run_reference(args)
         return
@@ -749,7 +769,7 @@ def main():
     torch.cuda.set_stream(stream)  # torch ops and the library share one stream
     ctx = HybridContext(local, stream=stream.cuda_stream)
     ctx.set_scene(wl.scene)
-    bvh = ctx.build_bvh()
+    bvh = build_structure(ctx)
     cam0 = wl.camera(1.0)
     planes = ctx.gbuffer(cam0, wl.width, wl.height)
     torch.cuda.synchronize()

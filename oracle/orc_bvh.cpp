@@ -9,7 +9,11 @@
 //   1. world triangles: M * v with the fixed, unfused order ((m0 x + m1 y) + m2 z) + m3
 //   2. 30-bit Morton codes of the AABB centroids over the centroid bounds
 //   3. stable sort by Morton code (ties keep triangle order)
-//   4. Karras 2012 binary radix tree over the 64-bit keys (morton << 32 | id)
+//   4. binary tree over that order, by the scene's build mode:
+//      SAH  — top down, each range split where the binned surface area
+//             heuristic is lowest (32 bins per axis over its centroid bounds),
+//             the two sides stably partitioned (sah_tree below);
+//      LBVH — Karras 2012 binary radix tree over the 64-bit keys (morton << 32 | id)
 //   5. bottom-up box refit
 //   6. BFS collapse into 8-wide nodes: greedily open the child with the
 //      largest surface area, then assign children to octant slots by a
@@ -135,7 +139,7 @@ static void refit_bvh2(Bvh& B, const std::vector<Box>& tb) {
     if (n < 2) return;
     std::vector<uint32_t> stack;
     std::vector<uint8_t> done(n - 1, 0);
-    stack.push_back(0);
+    stack.push_back(B.root);
     while (!stack.empty()) {
         uint32_t i = stack.back();
         Bvh2Node& nd = B.bvh2[i];
@@ -235,12 +239,156 @@ static inline float surface(const Box& b) {
     return a;
 }
 
+// ---- top-down binned SAH (HY_BUILD_SAH) --------------------------------------
+// Min and max run on order-preserving integer keys of the float bits (-0 below
+// +0, NaNs beyond the infinities), so they are exact and independent of the
+// order the GPU's atomics apply them in.
+constexpr int kSahBins = 32;
+static inline int32_t okey(float x) {
+    const int32_t b = (int32_t)fbits(x);
+    return b >= 0 ? b : b ^ 0x7fffffff;
+}
+static inline float unkey(int32_t k) { return bitsf((uint32_t)(k >= 0 ? k : k ^ 0x7fffffff)); }
+
+// bin of a centroid coordinate: floor((c - lo) * (32 / extent)) clamped to
+// [0, 31] (a NaN goes to bin 0)
+static inline int sah_bin(float c, float lo, float scale) {
+    const float v = (c - lo) * scale;
+    return v >= 0.f ? (v < (float)kSahBins ? (int)v : kSahBins - 1) : 0;
+}
+
+// surface area / 2 of a box given as keys: dx dy + dy dz + dz dx
+static inline float area_keys(const int32_t* lo, const int32_t* hi) {
+    const float dx = unkey(hi[0]) - unkey(lo[0]), dy = unkey(hi[1]) - unkey(lo[1]),
+                dz = unkey(hi[2]) - unkey(lo[2]);
+    float a = dx * dy;
+    a = a + dy * dz;
+    a = a + dz * dx;
+    return a;
+}
+
+// Binary tree over B.order (Morton sorted on entry; permuted by the stable
+// partitions).  Each range [f, l] of c >= 2 items:
+//   centroid bounds (keys); an axis takes part when hi - lo > 0, its scale
+//   32 / (hi - lo); per axis and bin: item count and box (keys);
+//   for each axis and q = 0..30: left = bins 0..q, right = bins q+1..31, both
+//   non-empty, cost = (area(left) * count(left) + area(right) * count(right)) + 0;
+//   the first strictly lowest finite cost in (axis, q) order wins; the items
+//   with bin <= q move to the front, order kept on both sides, m = f +
+//   count(left).  No candidate: m = f + c / 2, order unchanged.
+// The range's node is node m - 1 (split positions are distinct, so every index
+// in [0, n - 1) is used once); a one-item side is the leaf at its position.
+static void sah_tree(Bvh& B, const std::vector<Box>& tb, const std::vector<float>& cen) {
+    const uint32_t n = B.n;
+    B.bvh2.assign(n - 1, Bvh2Node());
+    struct Task { uint32_t f, l, parent, side; };
+    std::vector<Task> st;
+    st.push_back({0, n - 1, 0xffffffffu, 0});
+    std::vector<uint32_t> tmp(n);
+    while (!st.empty()) {
+        const Task T = st.back();
+        st.pop_back();
+        const uint32_t f = T.f, l = T.l, c = l - f + 1;
+        int32_t klo[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, khi[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+        for (uint32_t i = f; i <= l; i++)
+            for (int a = 0; a < 3; a++) {
+                const int32_t k = okey(cen[(size_t)B.order[i] * 3 + a]);
+                klo[a] = std::min(klo[a], k);
+                khi[a] = std::max(khi[a], k);
+            }
+        float clo[3], scale[3];
+        bool ok[3];
+        for (int a = 0; a < 3; a++) {
+            clo[a] = unkey(klo[a]);
+            const float ext = unkey(khi[a]) - clo[a];
+            ok[a] = ext > 0.f;
+            scale[a] = ok[a] ? (float)kSahBins / ext : 0.f;
+        }
+        uint32_t cnt[3][kSahBins] = {};
+        int32_t blo[3][kSahBins][3], bhi[3][kSahBins][3];
+        for (int a = 0; a < 3; a++)
+            for (int q = 0; q < kSahBins; q++)
+                for (int k = 0; k < 3; k++) { blo[a][q][k] = INT32_MAX; bhi[a][q][k] = INT32_MIN; }
+        for (uint32_t i = f; i <= l; i++) {
+            const uint32_t t = B.order[i];
+            for (int a = 0; a < 3; a++) {
+                if (!ok[a]) continue;
+                const int q = sah_bin(cen[(size_t)t * 3 + a], clo[a], scale[a]);
+                cnt[a][q]++;
+                for (int k = 0; k < 3; k++) {
+                    blo[a][q][k] = std::min(blo[a][q][k], okey(tb[t].lo[k]));
+                    bhi[a][q][k] = std::max(bhi[a][q][k], okey(tb[t].hi[k]));
+                }
+            }
+        }
+        int best_a = -1, best_q = -1;
+        uint32_t best_lc = 0;
+        float best = INFINITY;
+        for (int a = 0; a < 3; a++) {
+            if (!ok[a]) continue;
+            uint32_t rc[kSahBins];
+            int32_t rlo[kSahBins][3], rhi[kSahBins][3];
+            uint32_t acc = 0;
+            int32_t alo[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, ahi[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+            for (int q = kSahBins - 1; q >= 0; q--) {
+                acc += cnt[a][q];
+                for (int k = 0; k < 3; k++) {
+                    alo[k] = std::min(alo[k], blo[a][q][k]);
+                    ahi[k] = std::max(ahi[k], bhi[a][q][k]);
+                    rlo[q][k] = alo[k];
+                    rhi[q][k] = ahi[k];
+                }
+                rc[q] = acc;
+            }
+            uint32_t lc = 0;
+            int32_t llo[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, lhi[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+            for (int q = 0; q + 1 < kSahBins; q++) {
+                lc += cnt[a][q];
+                for (int k = 0; k < 3; k++) {
+                    llo[k] = std::min(llo[k], blo[a][q][k]);
+                    lhi[k] = std::max(lhi[k], bhi[a][q][k]);
+                }
+                const uint32_t r = rc[q + 1];
+                if (lc == 0 || r == 0) continue;
+                const float t1 = area_keys(llo, lhi) * (float)lc;
+                const float t2 = area_keys(rlo[q + 1], rhi[q + 1]) * (float)r;
+                const float cost = (t1 + t2) + 0.f;
+                if (cost < best) { best = cost; best_a = a; best_q = q; best_lc = lc; }
+            }
+        }
+        uint32_t m;
+        if (best_a >= 0) {
+            uint32_t nl = 0, nr = 0;
+            m = f + best_lc;
+            for (uint32_t i = f; i <= l; i++) {
+                const uint32_t t = B.order[i];
+                if (sah_bin(cen[(size_t)t * 3 + best_a], clo[best_a], scale[best_a]) <= best_q) tmp[f + nl++] = t;
+                else tmp[m + nr++] = t;
+            }
+            std::copy(tmp.begin() + f, tmp.begin() + l + 1, B.order.begin() + f);
+        } else {
+            m = f + c / 2;
+        }
+        const uint32_t id = m - 1;
+        Bvh2Node& nd = B.bvh2[id];
+        nd.first = f;
+        nd.last = l;
+        if (T.parent == 0xffffffffu) B.root = id;
+        else if (T.side) B.bvh2[T.parent].right = id;
+        else B.bvh2[T.parent].left = id;
+        if (m - f == 1) nd.left = kLeafBit | f;
+        else st.push_back({f, m - 1, id, 0});
+        if (l - m + 1 == 1) nd.right = kLeafBit | m;
+        else st.push_back({m, l, id, 1});
+    }
+}
+
 // LBVH -> BVH8 over n items of three points each (9 floats: a triangle, or an
 // instance box as (lo, hi, hi)); an item's box is the min/max of its points.
 // Records hold the item's points and its index; node and record numbers in the
 // emitted nodes are offset by node_off / rec_off (BLASes and the TLAS of the
 // two-level structure share one node array and one record array).
-static void build_core(const float* items, uint32_t n, Bvh& B, uint32_t node_off, uint32_t rec_off) {
+static void build_core(const float* items, uint32_t n, Bvh& B, uint32_t node_off, uint32_t rec_off, uint32_t mode) {
     B = Bvh();
     B.n = n;
     if (n == 0) return;
@@ -282,12 +430,21 @@ static void build_core(const float* items, uint32_t n, Bvh& B, uint32_t node_off
         B.morton[i] = code[B.order[i]];
         key[i] = ((uint64_t)B.morton[i] << 32) | B.order[i];
     }
+    if (mode == HY_BUILD_SAH) {
+        B.root = n > 1 ? 0u : kLeafBit;
+        if (n > 1) {
+            sah_tree(B, tb, cen);
+            refit_bvh2(B, tb);
+        }
+        for (uint32_t i = 0; i < n; i++) B.morton[i] = code[B.order[i]];
+    }
     // ---- Karras 2012 ----
     auto delta = [&](int64_t i, int64_t j) -> int {
         if (j < 0 || j >= (int64_t)n) return -1;
         return clz64(key[i] ^ key[j]);
     };
-    if (n > 1) {
+    if (mode == HY_BUILD_LBVH && n > 1) {
+        B.root = 0;
         B.bvh2.resize(n - 1);
         for (int64_t i = 0; i < (int64_t)n - 1; i++) {
             int d = (delta(i, i + 1) - delta(i, i - 1)) >= 0 ? 1 : -1;
@@ -332,7 +489,7 @@ static void build_core(const float* items, uint32_t n, Bvh& B, uint32_t node_off
     // ---- BFS collapse to BVH8 ----
     std::vector<uint32_t> queue;       // BVH2 ref of each BVH8 node, BFS order
     std::vector<uint32_t> level;       // level of each node
-    queue.push_back(n > 1 ? 0u : (kLeafBit | 0u));
+    queue.push_back(n > 1 ? B.root : (kLeafBit | 0u));
     level.push_back(0);
     uint32_t tri_count = 0;
     B.tris.assign((size_t)n * 12, 0.f);
@@ -440,7 +597,7 @@ static void build_core(const float* items, uint32_t n, Bvh& B, uint32_t node_off
 void bvh_build(Scene& s) {
     s.two_level = false;
     s.two = Bvh2L();
-    build_core(s.world.data(), s.ntri, s.bvh, 0, 0);
+    build_core(s.world.data(), s.ntri, s.bvh, 0, 0, s.build_mode);
     s.bvh_ok = s.ntri > 0;
 }
 
@@ -703,7 +860,7 @@ static void tlas_build(Scene& s) {
         for (int a = 0; a < 3; a++) { it[a] = b[a]; it[3 + a] = b[3 + a]; it[6 + a] = b[3 + a]; }
     }
     Bvh tl;
-    build_core(items.data(), T.ninst, tl, 0, 0);
+    build_core(items.data(), T.ninst, tl, 0, 0, s.build_mode);
     T.tlas_nodes = (uint32_t)tl.bvh8.size();
     T.tlas_depth = tl.depth;
     for (uint32_t k = 0; k < T.tlas_region; k++) std::memset(T.nodes[k].w, 0, 80);
@@ -752,7 +909,7 @@ void bvh_build_instanced(Scene& s) {
             }
         const uint32_t node0 = (uint32_t)T.nodes.size();
         Bvh b;
-        build_core(items.data(), nt, b, node0, rec);
+        build_core(items.data(), nt, b, node0, rec, s.build_mode);
         T.blas_node0.push_back(node0);
         T.blas_rec0.push_back(rec);
         T.blas_nodes.push_back((uint32_t)b.bvh8.size());

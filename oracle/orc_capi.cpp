@@ -89,6 +89,11 @@ int orc_scene_set_anyhit_order(void* sp, uint32_t order) {
     return HY_OK;
 }
 
+int orc_scene_set_build_mode(void* sp, uint32_t mode) {
+    if (mode > HY_BUILD_LBVH) return HY_ERR_INVALID_ARG;
+    ((Scene*)sp)->build_mode = mode;
+    return 0;
+}
 int orc_bvh_build_instanced(void* sp, uint32_t* layout) {
     Scene& s = *(Scene*)sp;
     bvh_build_instanced(s);

@@ -27,7 +27,8 @@ struct Bvh {
     uint32_t n = 0;
     float slo[3], shi[3];
     std::vector<uint32_t> morton, order;   // sorted morton codes and triangle ids
-    std::vector<Bvh2Node> bvh2;            // n-1 internal nodes (Karras)
+    std::vector<Bvh2Node> bvh2;            // n-1 internal nodes
+    uint32_t root = 0;                     // root reference (kLeafBit | 0 for one triangle)
     std::vector<Bvh8Node> bvh8;            // BFS order
     std::vector<float> tris;               // 12 floats per packed triangle
     uint32_t depth = 0;
@@ -81,6 +82,7 @@ struct Scene {
     Bvh2L two;                    // valid when two_level
     bool two_level = false;
     uint32_t anyhit_order = HY_ANYHIT_AUTO;  // child order of any-hit traversal
+    uint32_t build_mode = HY_BUILD_SAH;      // binary tree under the 8-wide nodes
 };
 
 // XOR applied to the near octant to rank the children of any-hit traversal:

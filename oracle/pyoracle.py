@@ -51,6 +51,7 @@ def load():
         "orc_bvh_refit": (C.c_int, [P, P, U32]),
         "orc_bvh_build_instanced": (C.c_int, [P, P]),
         "orc_scene_set_anyhit_order": (C.c_int, [P, U32]),
+        "orc_scene_set_build_mode": (C.c_int, [P, U32]),
         "orc_bvh_download_instanced": (None, [P, P, P, P, P, P]),
         "orc_trace": (None, [P, P, U32, C.c_int, C.c_int, P, P]),
         "orc_tea": (U32, [U32, U32]),
@@ -108,6 +109,7 @@ class _Stats(C.Structure):
 FP32_FORMATS = (0, 0, 0, 1, 0, 0)
 TRACE_BRUTE, TRACE_BVH8 = 0, 1
 HY_ANYHIT_AUTO, HY_ANYHIT_FAR_FIRST, HY_ANYHIT_NEAR_FIRST = 0, 1, 2  # any-hit child orders
+HY_BUILD_SAH, HY_BUILD_LBVH = 0, 1  # binary tree under the 8-wide nodes
 
 
 def set_threads(n: int):
@@ -225,6 +227,11 @@ class OracleScene:
 
     LAYOUT_FIELDS = ("two_level", "num_nodes", "num_records", "num_instances", "num_blas", "tlas_region",
                      "tlas_nodes", "depth")
+
+    def set_build_mode(self, mode: int):
+        """Binary tree of the next build: HY_BUILD_SAH (default) or HY_BUILD_LBVH."""
+        if self.lib.orc_scene_set_build_mode(self.h, mode) != 0:
+            raise ValueError(f"bad build mode {mode}")
 
     def set_anyhit_order(self, order: int):
         """Child order of any-hit traversal (HY_ANYHIT_AUTO / FAR_FIRST / NEAR_FIRST)."""

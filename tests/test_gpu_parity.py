@@ -33,13 +33,16 @@ def _torch():
 class Pair:
     """The same scene in the GPU context and in the oracle."""
 
-    def __init__(self, wl, build=True):
+    def __init__(self, wl, build=True, mode=None):
         from vulkanhybridraytracer_gb300.hybrid import HybridContext
         self.wl = wl
         self.ctx = HybridContext(0)
         self.ctx.set_scene(wl.scene)
         self.orc = po.OracleScene()
         self.orc.set_scene(wl.scene)
+        if mode is not None:  # binary tree of the build: HY_BUILD_SAH (default) or HY_BUILD_LBVH
+            self.ctx.set_build_mode(mode)
+            self.orc.set_build_mode(mode)
         if build:
             self.gi = self.ctx.build_bvh()
             self.oi = self.orc.build_bvh()
@@ -79,8 +82,18 @@ def test_bvh_bitexact_small(small):
     assert small.gi["scene_lo"] == small.oi["scene_lo"] and small.gi["scene_hi"] == small.oi["scene_hi"]
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 17, 33, 1000])
-def test_bvh_bitexact_tiny_and_degenerate(gpu_lib, oracle_lib, n):
+def test_bvh_bitexact_small_lbvh(gpu_lib, oracle_lib):
+    p = Pair(scenes.small(0), mode=L.HY_BUILD_LBVH)
+    assert_bvh_equal(p)
+    morton, _, bvh2, _, _ = p.ctx.download_bvh(p.gi["num_bvh8_nodes"])
+    assert np.all(np.diff(morton.astype(np.int64)) >= 0)  # Karras: sorted codes, root 0 over everything
+    assert bvh2[0, 2] == 0 and bvh2[0, 3] == p.gi["num_tris"] - 1
+    p.ctx.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 17, 33, 1000, 5000, 9000])
+def test_bvh_bitexact_tiny_and_degenerate(gpu_lib, oracle_lib, n, mode):
     """Few triangles, duplicated positions (equal Morton codes) and zero-area triangles."""
     from vulkanhybridraytracer_gb300.hybrid import HybridContext
     rng = np.random.default_rng(100 + n)
@@ -98,8 +111,10 @@ def test_bvh_bitexact_tiny_and_degenerate(gpu_lib, oracle_lib, n):
     lights = np.zeros((0, 12), np.float32)
     ctx = HybridContext(0)
     ctx.set_scene_arrays(v, idx, prims, xf, mats, lights)
+    ctx.set_build_mode(mode)
     orc = po.OracleScene()
     orc.set_scene_arrays(v, idx, prims, xf, mats, lights)
+    orc.set_build_mode(mode)
     p = Pair.__new__(Pair)
     p.ctx, p.orc, p.gi, p.oi = ctx, orc, ctx.build_bvh(), orc.build_bvh()
     assert_bvh_equal(p)
@@ -588,6 +603,12 @@ def hd(gpu_lib, oracle_lib):
 def test_hd_bvh_bitexact(hd):
     assert hd.gi["num_tris"] == 1505282
     assert_bvh_equal(hd)
+
+
+def test_hd_bvh_bitexact_lbvh(gpu_lib, oracle_lib):
+    p = Pair(scenes.hd(1), mode=L.HY_BUILD_LBVH)
+    assert_bvh_equal(p)
+    p.ctx.close()
 
 
 @pytest.mark.parametrize("flags", [0, L.HY_FLAG_GGX_REFLECTION])

@@ -33,7 +33,7 @@ def test_library_exports_every_header_symbol(lib):
     for n in names:
         assert hasattr(lib, n), n
     assert set(names) == set(L.PROTOTYPES), "ctypes prototypes and the header disagree"
-    assert lib.hy_get_abi_version() == 4
+    assert lib.hy_get_abi_version() == 5
 
 
 def test_error_strings(lib):

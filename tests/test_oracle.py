@@ -93,6 +93,16 @@ def small_orc(oracle_lib):
     return wl, o, info
 
 
+@pytest.fixture(scope="module")
+def lbvh_orc(oracle_lib):
+    wl = scenes.small(0, 64, 64)
+    o = po.OracleScene()
+    o.set_scene(wl.scene)
+    o.set_build_mode(po.HY_BUILD_LBVH)
+    info = o.build_bvh()
+    return wl, o, info
+
+
 def test_bvh8_matches_brute_force(small_orc):
     wl, o, _ = small_orc
     rays = _rays(np.random.default_rng(2), 4000)
@@ -110,10 +120,12 @@ def test_anyhit_orders_agree(oracle_lib):
     """Far-first and near-first any-hit traversal: the same occlusion for every
     ray (and brute force's), the same closest hits; the order only changes
     which nodes are visited.  Rays from the floor towards points above it,
-    like shadow rays, meet their occluders sooner far first."""
+    like shadow rays, meet their occluders sooner far first (on this scene's
+    LBVH; the SAH structure's case is in test_sah.py)."""
     wl = scenes.small(0, 64, 64)
     o = po.OracleScene()
     o.set_scene(wl.scene)
+    o.set_build_mode(po.HY_BUILD_LBVH)
     o.build_bvh()
     rng = np.random.default_rng(5)
     n = 4000
@@ -141,8 +153,8 @@ def test_anyhit_orders_agree(oracle_lib):
     assert np.array_equal(a.view(np.uint32)[:, 1] != 0xFFFFFFFF, far[0])
 
 
-def test_bvh_structure(small_orc):
-    wl, o, info = small_orc
+def test_bvh_structure(lbvh_orc):
+    wl, o, info = lbvh_orc
     n = info["num_tris"]
     morton, order, bvh2, bvh8, tris = o.download_bvh(info["num_bvh8_nodes"])
     assert np.all(np.diff(morton.astype(np.int64)) >= 0)
@@ -164,9 +176,9 @@ def test_bvh_structure(small_orc):
         assert lr[0] == f and rr[1] == la and lr[1] + 1 == rr[0]
 
 
-def test_morton_restatement(small_orc):
+def test_morton_restatement(lbvh_orc):
     """Morton codes recomputed in numpy float32 (one rounding per op) equal the oracle's."""
-    wl, o, info = small_orc
+    wl, o, info = lbvh_orc
     w = o.world_tris().reshape(-1, 3, 3)
     lo, hi = w.min(1), w.max(1)
     c = ((lo + hi) * np.float32(0.5)).astype(np.float32)

@@ -42,6 +42,7 @@ HY_FLAG_RAY_POOL = 0x20
 HY_FLAG_LANE_GROUPS = 0x40
 HY_FLAG_GGX_REFLECTION = 0x80
 HY_ANYHIT_AUTO, HY_ANYHIT_FAR_FIRST, HY_ANYHIT_NEAR_FIRST = 0, 1, 2
+HY_BUILD_SAH, HY_BUILD_LBVH = 0, 1
 HY_NO_HIT = 0xFFFFFFFF
 
 HY_STATUS_STACK_OVERFLOW = 0x1
@@ -153,6 +154,7 @@ PROTOTYPES = {
     "hy_bvh_build_instanced": (I32, [P, C.POINTER(HyBvhStats)]),
     "hy_bvh_layout": (I32, [P, C.POINTER(HyBvhLayout)]),
     "hy_bvh_download_instances": (I32, [P, P, P]),
+    "hy_scene_set_build_mode": (I32, [P, C.c_uint32]),
     "hy_scene_set_anyhit_order": (I32, [P, C.c_uint32]),
     "hy_scene_anyhit_order": (I32, [P, C.POINTER(C.c_uint32)]),
     "hy_trace_rays": (I32, [P, P, U32, I32, P, C.POINTER(HyStats)]),

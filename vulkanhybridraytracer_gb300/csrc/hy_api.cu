@@ -459,7 +459,8 @@ void hy_destroy(HyCtx* c) {
                       &c->host_in[3], &c->host_in[4], &c->host_in[5], &c->host_out_f, &c->host_out_8,
                       &c->grad_partial, &c->tex_px, &c->tex_tab, &c->xinv, &c->inst, &c->inst_box,
                       &c->inst_prim, &c->prim_mesh, &c->blas_node0, &c->mesh_vrange, &c->inst_chunks,
-                      &c->inst_keys};
+                      &c->inst_keys, &c->sah_ranges[0], &c->sah_ranges[1], &c->sah_small, &c->sah_bins,
+                      &c->sah_split, &c->sah_chunks, &c->sah_first, &c->sah_ccnt, &c->sah_coff, &c->sah_ctr};
     for (DevBuf* b : bufs) ctx_free(c, *b);
     if (c->h_stats) cudaFreeHost(c->h_stats);
     for (cudaEvent_t e : c->prof_pool) cudaEventDestroy(e);
@@ -640,6 +641,12 @@ int hy_bvh_layout(HyCtx* c, HyBvhLayout* out) {
     L.tlas_nodes = c->two_level ? c->tlas_nodes : 0;
     L.depth = c->depth;
     *out = L;
+    return HY_OK;
+}
+
+int hy_scene_set_build_mode(HyCtx* c, uint32_t mode) {
+    if (!c || mode > HY_BUILD_LBVH) return HY_ERR_INVALID_ARG;
+    c->build_mode = mode;
     return HY_OK;
 }
 

@@ -8,6 +8,8 @@
 //   k_morton        30-bit Morton codes over the centroid bounds
 //   k_radix_*       stable LSD radix sort (8-bit digits, warp-match ranking)
 //   k_karras        Karras 2012 binary radix tree over (morton << 32 | id)
+//                   (HY_BUILD_LBVH), or the binned-SAH tree of hy_sah.cu
+//                   over the same order (HY_BUILD_SAH, the default)
 //   k_refit         bottom-up boxes, last-arriver-computes (no waiting)
 //   k_collapse_*    BFS collapse into compressed 8-wide nodes, one level per
 //                   launch pair with prefix sums for deterministic numbering
@@ -95,17 +97,13 @@ __device__ __forceinline__ uint32_t expand10(uint32_t v) {
     return v;
 }
 
-__global__ void k_morton(const float4* __restrict__ cen, uint32_t n, const int* __restrict__ b,
-                         uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
+__device__ __forceinline__ uint32_t morton_of(float4 c, const int* __restrict__ b) {
     float lo[3], inv[3];
     for (int a = 0; a < 3; a++) {
         lo[a] = ord2f(b[a]);
         float ext = __fsub_rn(ord2f(b[3 + a]), lo[a]);
         inv[a] = ext > 0.f ? __fdiv_rn(1024.0f, ext) : 0.f;
     }
-    float4 c = cen[t];
     float cc[3] = {c.x, c.y, c.z};
     uint32_t q[3];
     for (int a = 0; a < 3; a++) {
@@ -113,8 +111,23 @@ __global__ void k_morton(const float4* __restrict__ cen, uint32_t n, const int* 
         v = fminf(fmaxf(v, 0.f), 1023.f);
         q[a] = (uint32_t)v;
     }
-    keys[t] = (expand10(q[0]) << 2) | (expand10(q[1]) << 1) | expand10(q[2]);
+    return (expand10(q[0]) << 2) | (expand10(q[1]) << 1) | expand10(q[2]);
+}
+
+__global__ void k_morton(const float4* __restrict__ cen, uint32_t n, const int* __restrict__ b,
+                         uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    keys[t] = morton_of(cen[t], b);
     vals[t] = t;
+}
+
+// the codes in leaf order after the SAH build reordered the ids
+__global__ void k_morton_at(const float4* __restrict__ cen, uint32_t n, const int* __restrict__ b,
+                            const uint32_t* __restrict__ ord, uint32_t* __restrict__ keys) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    keys[i] = morton_of(cen[ord[i]], b);
 }
 
 // ---------------------------------------------------------------------------------
@@ -575,7 +588,7 @@ int world_tris_impl(HyCtx* c) {
     return HY_OK;
 }
 
-// LBVH -> BVH8 over the n items in c->world / c->tribox / c->centroid (three
+// Binary tree (SAH or LBVH) -> BVH8 over the n items in c->world / c->tribox / c->centroid (three
 // points per item: a triangle, or an instance box as (lo, hi, hi)).  Nodes go
 // to nodes[node_off ...], leaf records to records rec_off ...; the emitted
 // child and record indices include the offsets.  Records carry the item's
@@ -623,16 +636,25 @@ static int build_core(HyCtx* c, uint32_t n, uint32_t node_off, uint32_t rec_off,
     const uint32_t* mort = c->keys[cur].as<uint32_t>();
     const uint32_t* ord = c->vals[cur].as<uint32_t>();
     uint32_t* bvh2 = c->bvh2.as<uint32_t>();
+    // root reference of the collapse
+    uint32_t root = n > 1 ? 0u : kLeaf;
+    HY_CUDA_TRY(cudaMemcpyAsync(c->lvl_ref[0].p, &root, 4, cudaMemcpyHostToDevice, s));
     if (n > 1) {
-        k_karras<<<cdiv(n - 1, 256), 256, 0, s>>>(mort, ord, n, bvh2, c->parent.as<uint32_t>());
+        if (c->build_mode == HY_BUILD_SAH) {
+            // ids reordered in place; the SAH tree writes its root id into lvl_ref[0]
+            if ((rc = sah_tree_impl(c, n, c->vals[cur].as<uint32_t>(), c->vals[cur ^ 1].as<uint32_t>(), bvh2,
+                                    c->parent.as<uint32_t>(), c->lvl_ref[0].as<uint32_t>())))
+                return rc;
+            k_morton_at<<<cdiv(n, 256), 256, 0, s>>>(c->centroid.as<float4>(), n, bnd, ord,
+                                                     c->keys[cur].as<uint32_t>());
+        } else {
+            k_karras<<<cdiv(n - 1, 256), 256, 0, s>>>(mort, ord, n, bvh2, c->parent.as<uint32_t>());
+        }
         HY_CUDA_TRY(cudaMemsetAsync(c->flags.p, 0, (size_t)n * 4, s));
         k_refit<<<cdiv(n, 256), 256, 0, s>>>(ord, c->tribox.as<float>(), n, bvh2, c->parent.as<uint32_t>(),
                                              c->flags.as<uint32_t>());
     }
     HY_CUDA_TRY(cudaGetLastError());
-    // root reference
-    uint32_t root = n > 1 ? 0u : kLeaf;
-    HY_CUDA_TRY(cudaMemcpyAsync(c->lvl_ref[0].p, &root, 4, cudaMemcpyHostToDevice, s));
     uint32_t level_start = 0, tri_start = 0, m = 1, depth = 0;
     int lv = 0;
     uint32_t* tot = c->total.as<uint32_t>();

@@ -61,6 +61,9 @@ struct HyCtx {
     hy::DevBuf scan_tmp, hist, total;
     hy::DevBuf nodes, tris;
     hy::DevBuf node_ref, node_plan;  // per BVH8 node: its BVH2 subtree, its 8 slot children (refits)
+    uint32_t build_mode = HY_BUILD_SAH;  // hy_scene_set_build_mode
+    // binned-SAH build scratch (hy_sah.cu): range queues, bins, chunk maps, counters
+    hy::DevBuf sah_ranges[2], sah_small, sah_bins, sah_split, sah_chunks, sah_first, sah_ccnt, sah_coff, sah_ctr;
     uint32_t n_bvh8 = 0, depth = 0;
     bool bvh_ok = false;
 
@@ -120,6 +123,9 @@ int bvh_build_instanced_impl(HyCtx* c, HyBvhStats* st);
 int tlas_build_impl(HyCtx* c);   // instance records + TLAS from the current transforms
 int world_tris_impl(HyCtx* c);
 int scan_exclusive(HyCtx* c, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* d_total);
+// binned-SAH binary tree over the n >= 2 Morton-sorted ids in ord (hy_sah.cu)
+int sah_tree_impl(HyCtx* c, uint32_t n, uint32_t* ord, uint32_t* ord2, uint32_t* bvh2, uint32_t* parent,
+                  uint32_t* d_root);
 }  // namespace hy
 
 #define HY_CUDA_TRY(expr)                               \

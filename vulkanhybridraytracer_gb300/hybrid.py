@@ -148,6 +148,10 @@ class HybridContext:
         L.check(self.lib.hy_bvh_layout(self.h, C.byref(lay)), "bvh_layout")
         return {k: int(getattr(lay, k)) for k, _ in L.HyBvhLayout._fields_}
 
+    def set_build_mode(self, mode: int):
+        """hy_scene_set_build_mode: HY_BUILD_SAH (default) or HY_BUILD_LBVH, from the next build."""
+        L.check(self.lib.hy_scene_set_build_mode(self.h, mode), "set_build_mode")
+
     def set_anyhit_order(self, order: int):
         """hy_scene_set_anyhit_order: HY_ANYHIT_AUTO (default), FAR_FIRST or NEAR_FIRST."""
         L.check(self.lib.hy_scene_set_anyhit_order(self.h, order), "set_anyhit_order")
