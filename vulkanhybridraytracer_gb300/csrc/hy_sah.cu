@@ -21,14 +21,16 @@
 // Every float op is an IEEE-rounded intrinsic, so the order, the tree and the
 // 8-wide nodes collapsed from it equal the CPU oracle's bit for bit.
 //
-// Schedule: ranges above kSmallMax triangles are split level by level, each
+// Schedule: ranges above small_max triangles are split level by level, each
 // level by four launches over chunks of kChunk triangles (bin: shared-memory
 // bins flushed with global atomics; eval: a block per range picks the split
 // and the chunks' output offsets; scatter: the stable partition into scratch
-// with a block scan; copy back).  Ranges of up to kSmallMax triangles are
+// with a block scan; copy back).  Ranges of up to small_max triangles are
 // whole subtrees for one warp each (k_sah_small), which walks them with a
 // short explicit stack (the larger side pushed, the smaller taken first, so at
-// most log2(kSmallMax) entries).
+// most log2(small_max) entries).  small_max (64..4096) is picked per build so
+// that about 16 warps per SM get a subtree; it changes the schedule only, not
+// the tree.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -47,9 +49,9 @@ constexpr int kBins = 32;
 constexpr int kBinWords = 7;                       // count, lo xyz keys, hi xyz keys
 constexpr int kAxisWords = kBins * kBinWords;      // 224
 constexpr int kNodeBinWords = 3 * kAxisWords;      // 672
-constexpr uint32_t kSmallMax = 4096;               // a warp builds ranges up to this size
+constexpr uint32_t kSmallMaxCap = 4096;            // a warp builds ranges up to small_max <= this
 constexpr uint32_t kChunk = 2048;                  // triangles per block in the level passes
-constexpr int kStackMax = 16;                      // > log2(kSmallMax) + 1
+constexpr int kStackMax = 16;                      // > log2(kSmallMaxCap) + 1
 constexpr unsigned kFull = 0xffffffffu;
 
 struct SahRange {
@@ -235,7 +237,7 @@ __global__ void k_sah_root_bounds(const float4* __restrict__ cen, uint32_t n, Sa
         for (int j = 0; j < 3; j++) { atomicMin(&r->ck[j], k[j]); atomicMax(&r->ck[3 + j], k[3 + j]); }
 }
 
-// ---- level passes over ranges above kSmallMax ------------------------------------
+// ---- level passes over ranges above small_max ------------------------------------
 __global__ void k_sah_bins_init(int* __restrict__ gbins, uint32_t nwords) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwords; i += gridDim.x * blockDim.x) {
         const uint32_t k = i % kBinWords;
@@ -280,8 +282,9 @@ __global__ void __launch_bounds__(256) k_sah_eval(const SahRange* __restrict__ r
                                                   const uint32_t* __restrict__ first_chunk,
                                                   const uint32_t* __restrict__ ccnt, uint32_t* __restrict__ coff,
                                                   SahSplit* __restrict__ split, SahRange* __restrict__ next,
-                                                  SahRange* __restrict__ small, uint32_t n, uint32_t* __restrict__ bvh2,
-                                                  uint32_t* __restrict__ parent, uint32_t* __restrict__ ctr) {
+                                                  SahRange* __restrict__ small, uint32_t n, uint32_t small_max,
+                                                  uint32_t* __restrict__ bvh2, uint32_t* __restrict__ parent,
+                                                  uint32_t* __restrict__ ctr) {
     __shared__ unsigned long long s_key[3];
     __shared__ uint32_t s_part[256];
     const SahRange R = ranges[blockIdx.x];
@@ -335,7 +338,7 @@ __global__ void __launch_bounds__(256) k_sah_eval(const SahRange* __restrict__ r
             ch.parent = id;
             ch.side = (uint32_t)s;
             keys_init(ch.ck);
-            if (cs > kSmallMax) {
+            if (cs > small_max) {
                 const uint32_t slot = atomicAdd(ctr + CTR_NEXT, 1u);
                 next[slot] = ch;
                 sp.child[s] = (1u << 30) | slot;
@@ -457,7 +460,7 @@ __global__ void k_sah_copy(const SahChunk* __restrict__ chunks, const uint32_t* 
     for (uint32_t i = ch.start + threadIdx.x; i < ch.end; i += blockDim.x) ord[i] = ord2[i];
 }
 
-// ---- one warp per range of up to kSmallMax triangles --------------------------
+// ---- one warp per range of up to small_max triangles --------------------------
 constexpr int kSmallWarps = 4;
 
 __global__ void __launch_bounds__(32 * kSmallWarps) k_sah_small(const SahRange* __restrict__ tasks, uint32_t ntask,
@@ -548,7 +551,7 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_sah_small(const SahRange* 
         for (int k = 0; k < 6; k++) { L.ck[k] = kl[k]; R.ck[k] = kr[k]; }
         if (li && ri) {
             const bool lsmall = (m - f) <= (l - m + 1);
-            if (sp >= kStackMax) {  // cannot happen (the stack holds at most log2(kSmallMax) ranges)
+            if (sp >= kStackMax) {  // cannot happen (the stack holds at most log2(kSmallMaxCap) ranges)
                 if (lane == 0) atomicExch(ctr + CTR_ERR, 1u);
                 return;
             }
@@ -580,7 +583,10 @@ int sah_tree_impl(HyCtx* c, uint32_t n, uint32_t* ord, uint32_t* ord2, uint32_t*
                   uint32_t* d_root) {
     if (n < 2) return HY_ERR_INVALID_ARG;
     cudaStream_t s = c->stream;
-    const uint32_t bigcap = n / (kSmallMax + 1) + 2;
+    // subtrees for about 16 warps per SM, each of 64..4096 triangles
+    uint32_t small_max = 64;
+    while (small_max < kSmallMaxCap && (uint64_t)small_max * 16u * (uint32_t)c->num_sms < n) small_max <<= 1;
+    const uint32_t bigcap = n / (small_max + 1) + 2;
     const uint32_t smallcap = n / 2 + 2;
     const uint32_t chunkcap = n / kChunk + bigcap + 2;
     int rc;
@@ -596,7 +602,7 @@ int sah_tree_impl(HyCtx* c, uint32_t n, uint32_t* ord, uint32_t* ord2, uint32_t*
         return rc;
     uint32_t* ctr = c->sah_ctr.as<uint32_t>();
     HY_CUDA_TRY(cudaMemsetAsync(ctr, 0, 16, s));
-    const bool root_small = n <= kSmallMax;
+    const bool root_small = n <= small_max;
     SahRange* root = root_small ? c->sah_small.as<SahRange>() : c->sah_ranges[0].as<SahRange>();
     k_sah_root_init<<<1, 32, 0, s>>>(root, n);
     k_sah_root_bounds<<<std::min<uint32_t>(cdiv_u(n, 256), 4 * (uint32_t)c->num_sms), 256, 0, s>>>(
@@ -640,8 +646,8 @@ int sah_tree_impl(HyCtx* c, uint32_t n, uint32_t* ord, uint32_t* ord2, uint32_t*
                                       c->sah_bins.as<int>(), c->sah_ccnt.as<uint32_t>());
         k_sah_eval<<<nbig, 256, 0, s>>>(ranges, c->sah_bins.as<int>(), c->sah_first.as<uint32_t>(),
                                         c->sah_ccnt.as<uint32_t>(), c->sah_coff.as<uint32_t>(),
-                                        c->sah_split.as<SahSplit>(), next, c->sah_small.as<SahRange>(), n, bvh2,
-                                        parent, ctr);
+                                        c->sah_split.as<SahSplit>(), next, c->sah_small.as<SahRange>(), n,
+                                        small_max, bvh2, parent, ctr);
         k_sah_scatter<<<nch, 256, 0, s>>>(chunks, ranges, c->sah_split.as<SahSplit>(), c->sah_coff.as<uint32_t>(),
                                           ord, ord2, c->centroid.as<float4>(), next, c->sah_small.as<SahRange>());
         k_sah_copy<<<nch, 256, 0, s>>>(chunks, ord2, ord);
