@@ -82,12 +82,23 @@ ANYHIT_ORDER = {1: "far first", 2: "near first"}  # HY_ANYHIT_FAR_FIRST / HY_ANY
 KERNEL_SOURCES = ("hy_device.cuh", "hy_stream.cuh", "hy_shade.cuh", "hy_pass.h", "hy_pass.cu", "hy_bvh.cu", "hy_sah.cu")
 
 
-def kernel_source_sha() -> str:
+def code_of(text: str) -> str:
+    """C++/CUDA source without comments and blank lines (what the hash covers)."""
+    import re
+
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    lines = (re.sub(r"//.*$", "", ln).rstrip() for ln in text.splitlines())
+    return "\n".join(ln for ln in lines if ln.strip())
+
+
+def kernel_source_sha(read=None) -> str:
+    """Hash of the code (comments stripped) of the kernels and structure build."""
     import hashlib
 
     h = hashlib.sha256()
     for f in KERNEL_SOURCES:
-        h.update((ROOT / "vulkanhybridraytracer_gb300" / "csrc" / f).read_bytes())
+        text = read(f) if read else (ROOT / "vulkanhybridraytracer_gb300" / "csrc" / f).read_text()
+        h.update(code_of(text).encode())
     return h.hexdigest()[:16]
 
 

@@ -1,8 +1,8 @@
 // Top-down binned-SAH binary tree on the GPU (HY_BUILD_SAH): the tree that the
 // BVH8 collapse of hy_bvh.cu turns into 8-wide nodes, in place of the LBVH's
-// radix tree.  It stands in for the build quality of the driver's BLAS/TLAS
-// builds (src/renderer.cpp:1696-1865), which the reference asks for with
-// default build flags.
+// radix tree.  It stands in for the driver's trace-quality builds
+// (src/renderer.cpp:1696-1865; BLASes and the TLAS are built with
+// PREFER_FAST_TRACE, src/renderer.h:246 and src/renderer.cpp:1687).
 //
 // Each range [f, l] of c >= 2 triangles of the Morton-sorted order:
 //   * centroid bounds as order-preserving integer keys (exact min/max, -0 below
