@@ -79,7 +79,8 @@ ANYHIT_ORDER = {1: "far first", 2: "near first"}  # HY_ANYHIT_FAR_FIRST / HY_ANY
 # device sources of the pass kernels: a profile summary under profiles/ records the hash
 # of these files, so a figure measured on another version of the kernels is not reported
 # as this version's
-KERNEL_SOURCES = ("hy_device.cuh", "hy_stream.cuh", "hy_shade.cuh", "hy_pass.h", "hy_pass.cu", "hy_bvh.cu", "hy_sah.cu")
+KERNEL_SOURCES = ("hy_device.cuh", "hy_stream.cuh", "hy_stream_kernel.cuh", "hy_stream_accum.cu", "hy_shade.cuh",
+                  "hy_pass.h", "hy_pass.cu", "hy_bvh.cu", "hy_sah.cu")
 
 
 def code_of(text: str) -> str:
@@ -277,7 +278,7 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def diff_leg(steps: int, warmup: int, fd_params: int = 32, clocks_index: int = 0) -> dict:
+def diff_leg(steps: int, warmup: int, fd_params: int = 32, clocks_index: int = 0, visits: int = 0) -> dict:
     """Differentiable form: 512x512, 64 icospheres (subdivision 3), 64 materials, 8 point
     lights, 16 shadow samples; L2 loss against a target rendered from parameters perturbed
     by N(0, 0.05).  Forward = G-buffer + shadow pass + shading at the current parameters;
@@ -293,6 +294,9 @@ def diff_leg(steps: int, warmup: int, fd_params: int = 32, clocks_index: int = 0
     wl = scenes.diff(3, 512, 512)
     r = diffrender.DiffRenderer(wl.scene, wl.camera(0.0), wl.width, wl.height, spp=wl.spp,
                                 max_bounces=wl.max_bounces)
+    if visits:  # node visits per scheduling round of the shadow kernel (--visits)
+        from vulkanhybridraytracer_gb300.hybrid import pass_config
+        r.cfg = pass_config(spp=wl.spp, max_bounces=wl.max_bounces, rng_mode=r.cfg.rng_mode, visits_per_round=visits)
     mp0, lp0 = r.params0
     rng = np.random.default_rng(3)
     mp_t = np.clip(mp0 + rng.normal(0, 0.05, mp0.shape), 0.0, 1.0).astype(np.float32)
@@ -386,7 +390,7 @@ def run_diff(args):
     torch.cuda.set_device(0)
     stream = torch.cuda.Stream(device=torch.device("cuda", 0))
     torch.cuda.set_stream(stream)
-    d = diff_leg(args.steps, args.warmup)
+    d = diff_leg(args.steps, args.warmup, visits=args.visits)
     line = {"metric": "hybrid_backward_ms", "value": d["backward_ms"], "unit": "ms", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": d["backward_ms"], "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",

@@ -21,7 +21,8 @@ ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "liboracle.so"
 
 SOURCES = ["hy_api.cu", "hy_bvh.cu", "hy_sah.cu", "hy_pass.cu", "hy_grad.cu", "hy_pt.cu", "hy_noalloc.cu",
-           "hy_batch_64.cu", "hy_batch_128.cu", "hy_batch_256.cu"]
+           "hy_batch_64.cu", "hy_batch_128.cu", "hy_batch_256.cu", "hy_stream_raw.cu", "hy_stream_accum.cu",
+           "hy_stream_two.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = [
     "-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",

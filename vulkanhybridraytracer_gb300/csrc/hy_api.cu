@@ -258,7 +258,7 @@ int grid_for(HyCtx* c, int mode, bool count, int minb, bool short_stack, int sha
 
 // tile streams: node visits per scheduling round (at 8 resident blocks: 4: -3.9 %,
 // 6: -1.7 %, 12: -3.6 %, 16: -2.7 % against 8 on the 1080p workload)
-constexpr uint32_t kStreamSteps = 8;
+constexpr uint32_t kStreamSteps = 12;
 
 PassParams make_params(HyCtx* c, const HyGBuffer* gb, const HyCamera* cam, const HyPassConfig* cfg,
                        uint32_t accum_fmt, void* shadow, void* hist, float* out_f, uint8_t* out_8) {

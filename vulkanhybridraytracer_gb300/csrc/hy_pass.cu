@@ -2,7 +2,8 @@
 //
 // Kernels of the three reference programs:
 //   k_shadow_stream<ACCUM=false>  shadowRaygen.rgen:28-93 -> raw per-light shadow
-//                                 images, as tile streams (hy_stream.cuh; the
+//                                 images, as tile streams (hy_stream_kernel.cuh,
+//                                 instantiated in hy_stream_{raw,accum,two}.cu; the
 //                                 default schedule)
 //   k_shadow_stream<ACCUM=true>   the same rays folded straight into the history
 //                                 with blur.comp's running mean (frame > 0), so the
@@ -396,59 +397,6 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, co
             s.light++;
             s.setup = true;
         }
-    }
-    if (COUNT) { ls.nodes += nn; ls.tris += nt; }
-    flush_stats(ls, P.stats);
-}
-
-// ---------------------------------------------------------------------------------
-// Shadow rays, light-major over a tile: a warp takes an 8x4 tile and, light
-// by light, traces all 32 x n_rays samples of its pixels (n_rays = spp for
-// DECORRELATED; 1 for REFERENCE, whose samples are one ray), item q being
-// sample q % n_rays of pixel q / n_rays; free lanes claim the items in order
-// from a per-warp shared counter.  Lane i sets
-// up light l for pixel i (its G-buffer texel, the skip tests of
-// shadowRaygen.rgen:43-63) and publishes position, distance, sampleDisk's frame
-// (tangent, bitangent, position + L: the same for every sample of the
-// pixel-light) and the RNG state of its first sample in shared memory; every
-// lane then traces items without waiting for the others (a lane whose rays
-// are short takes more of them), counting unoccluded samples per pixel with shared-memory
-// atomics; once the warp's items for light l are all traced, lane i folds
-// pixel i's count into its factor.  A lane waits only at the end of a light
-// (for the slowest sum of spp rays) instead of after every pixel-light (for
-// the slowest single ray), and the samples in flight stay within a few
-// adjacent pixels of one light.  Seeds as in k_shadow_group (LCG jump-ahead),
-// so the rays equal those of k_shadow.
-// ---------------------------------------------------------------------------------
-template <bool COUNT, bool ACCUM, int MINB, bool TWO = false, bool SHORT = false>
-__global__ void __launch_bounds__(128, MINB) k_shadow_stream(const SceneDev S, const PassParams P) {
-    __shared__ StreamSlots sm;
-    __shared__ uint4 s_top[kTopNodes * 5];
-    __shared__ uint2 s_stack[SHORT ? kShortStack * 128 : 1];
-    const uint32_t ntop = stage_top(S, s_top, P.top_nodes);
-    LaneStats ls;
-    const uint32_t lane = threadIdx.x & 31;
-    uint2 stk[kStackMax];
-    ShadowLane s;
-    Trav t;
-    RayPre r;
-    uint32_t chunk_cur = 0, chunk_end = 0, nn = 0, nt = 0;
-    for (;;) {
-        if (chunk_cur == chunk_end) {
-            uint32_t t0 = 0;
-            if (lane == 0) t0 = atomicAdd(P.queue, P.chunk);
-            t0 = __shfl_sync(0xffffffffu, t0, 0);
-            if (t0 >= P.ntiles) break;
-            chunk_cur = t0;
-            chunk_end = min(t0 + P.chunk, P.ntiles);
-        }
-        if (SHORT)
-            stream_tile<COUNT, TWO, ACCUM ? 1 : 0>(S, P, chunk_cur++, P.rng_mode == HY_RNG_REFERENCE, ACCUM, sm,
-                                                   SplitStack{s_stack + threadIdx.x, stk}, t, r, s, ls, nn, nt, s_top,
-                                                   ntop);
-        else
-            stream_tile<COUNT, TWO, ACCUM ? 1 : 0>(S, P, chunk_cur++, P.rng_mode == HY_RNG_REFERENCE, ACCUM, sm, stk, t,
-                                                   r, s, ls, nn, nt, s_top, ntop);
     }
     if (COUNT) { ls.nodes += nn; ls.tris += nt; }
     flush_stats(ls, P.stats);
@@ -1050,23 +998,12 @@ static void* shade_kernel(bool count, int minb) {
     return shade_kernel_m<1>(count);
 }
 
-template <bool ACCUM>
-static void* stream_kernel(bool count, int minb, bool two, bool short_stack) {
-    // two-level walk: 5 resident blocks (96 registers; at 6 its spills made the 4K
-    // instanced frame 1.5x slower)
-    if (two) return count ? (void*)k_shadow_stream<true, ACCUM, 5, true> : (void*)k_shadow_stream<false, ACCUM, 5, true>;
-    if (short_stack)  // 8 resident blocks, the first stack entries in shared memory
-        return count ? (void*)k_shadow_stream<true, ACCUM, 8, false, true>
-                     : (void*)k_shadow_stream<false, ACCUM, 8, false, true>;
-    if (minb >= 8) return count ? (void*)k_shadow_stream<true, ACCUM, 8> : (void*)k_shadow_stream<false, ACCUM, 8>;
-    if (minb == 7) return count ? (void*)k_shadow_stream<true, ACCUM, 7> : (void*)k_shadow_stream<false, ACCUM, 7>;
-    if (minb >= 6) return count ? (void*)k_shadow_stream<true, ACCUM, 6> : (void*)k_shadow_stream<false, ACCUM, 6>;
-    return count ? (void*)k_shadow_stream<true, ACCUM, 5> : (void*)k_shadow_stream<false, ACCUM, 5>;
-}
-
 static void* pixel_kernel(int mode, bool count, int minb, bool two, bool short_stack = false, int shade_minb = 0) {
-    if (mode == MODE_SHADOW_S) return stream_kernel<false>(count, minb, two, short_stack);
-    if (mode == MODE_SHADOW_ACCUM_S) return stream_kernel<true>(count, minb, two, short_stack);
+    if (mode == MODE_SHADOW_S || mode == MODE_SHADOW_ACCUM_S) {
+        const bool accum = mode == MODE_SHADOW_ACCUM_S;
+        if (two) return stream_kernel_two(accum, count);
+        return accum ? stream_kernel_accum(count, minb, short_stack) : stream_kernel_raw(count, minb, short_stack);
+    }
     if (two) {
         switch (mode) {
             case MODE_SHADOW_G: return shadow_kernel_two<false>(count, minb);

@@ -116,6 +116,10 @@ cudaError_t launch_batch(bool shade, bool count, int minb, bool stream, bool two
                          const BatchParams& B, int grid, cudaStream_t s);
 cudaError_t batch_occupancy(bool shade, bool count, int minb, bool stream, bool two, int block, int shortd,
                             int* blocks_per_sm);
+// tile-stream shadow kernels (hy_stream_raw.cu, hy_stream_accum.cu, hy_stream_two.cu)
+void* stream_kernel_raw(bool count, int minb, bool short_stack);
+void* stream_kernel_accum(bool count, int minb, bool short_stack);
+void* stream_kernel_two(bool accum, bool count);
 void* batch_stream_kernel_64(bool count, int minb, int shortd, bool two);
 void* batch_stream_kernel_128(bool count, int minb, int shortd, bool two);
 void* batch_stream_kernel_256(bool count, int minb, int shortd, bool two);
