@@ -371,12 +371,11 @@ int run_pixels(HyCtx* c, int mode, const PassParams& P0, const HyPassConfig* cfg
     }
     // measured fastest on the 1080p workload: 6 resident blocks (80 registers)
     // for the lane-group kernel (1.4 % ahead of 8), 8 (64 registers) otherwise;
-    // 8 node visits per round for the tile streams (4 for the others)
+    // 12 node visits per round for the tile streams (4 for the others)
     const bool grouped = mode == MODE_SHADOW_G || mode == MODE_SHADOW_ACCUM_G;
     const bool streams = mode == MODE_SHADOW_S || mode == MODE_SHADOW_ACCUM_S;
     int minb = cfg->min_blocks ? (int)cfg->min_blocks : (grouped ? 6 : 8);
     if (streams && !cfg->visits_per_round) P.inner = kStreamSteps;
-    P.top_nodes = 73;  // levels 0-2 of the 8-wide tree (measured neutral against 0, 9 and 128)
     if (cfg->stack_depth && cfg->stack_depth != 8) return HY_ERR_UNSUPPORTED;
     P.short_stack = streams && !c->two_level && cfg->stack_depth == 8;
     // the shade kernel at 8 resident blocks (64 registers): 1.69 ms per 1080p frame

@@ -31,7 +31,6 @@ struct PassParams {
     uint32_t blur_w, blur_h; // texels the blur dispatch covers
     uint32_t group;          // lanes per pixel-light in the sample-parallel shadow kernel
     uint32_t inner;          // node visits per scheduling round of that kernel (>= 1)
-    uint32_t top_nodes;      // tile streams: top nodes staged in shared memory (<= kTopNodes)
     uint32_t short_stack;    // tile streams: the first stack entries in shared memory
     uint32_t shade_minb;     // shade kernel: resident blocks it is compiled for
     unsigned long long* stats;

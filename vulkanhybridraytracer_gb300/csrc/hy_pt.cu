@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(128, MINB) k_pathtrace_stream(const SceneDev S
                     if (hit) {
                         float sf = 0.f;
                         if (g.NdotL > 0.f) {
-                            const uint32_t cnt = traced ? sm.cnt[wb + lane] : 0u;
+                            const uint32_t cnt = traced ? *unocc_count(sm, wb + lane) : 0u;
                             sf = reference ? (cnt ? spp : 0.f) : (float)cnt;
                             sf /= spp;
                         }

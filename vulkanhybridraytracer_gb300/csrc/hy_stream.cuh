@@ -16,38 +16,34 @@
 
 namespace hy {
 
-// The top levels of the node array (BFS order: levels 0-2 of an 8-wide tree
-// are its first 73 nodes) staged in shared memory once per block.  Measured
-// neutral at 1080p (0 / 9 / 73 / 128 staged nodes: 2,551 / 2,547 / 2,560 /
-// 2,553 Mrays/s): those nodes are L1-resident anyway.
-constexpr uint32_t kTopNodes = 73;
-__device__ __forceinline__ uint32_t stage_top(const SceneDev& S, uint4* top, uint32_t limit) {
-    const uint32_t ntop = min(min(S.num_nodes, kTopNodes), limit);
-    for (uint32_t i = threadIdx.x; i < ntop * 5; i += blockDim.x) top[i] = __ldg(&S.nodes[i / 5].q[i % 5]);
-    __syncthreads();
-    return ntop;
-}
-
 // Per-warp shared state of the tile streams, per pixel of the warp's tile and
 // the current light: position and distance to the light; the disk frame of
 // sampleDisk (position + L, tangent, bitangent); the RNG state of the
 // pixel-light's first sample (w of PL, as bits); a not-traced mark (w of T,
-// 0xffffffff); the unoccluded count.
-// Items of a light are traced in the order of their disk samples (kSortItems at
-// most per warp and light; more are traced in item order).
+// 0xffffffff); the unoccluded count (w of B, as bits).
+// Items of a light are traced in the order of their disk samples, sorted in
+// chunks of SORT items per warp and light.
+// The size matters beyond occupancy: shared memory and L1 share each SM's
+// 256 KB, and the driver carves shared memory in steps (..., 100, 132, 164,
+// 196 KB).  At 4 warps per block and 8 blocks per SM this layout (15.4 KB, + 1
+// KB the driver keeps per block) takes the 132 KB step and leaves the kernel
+// 124 KB of L1 for the nodes, triangles and traversal stacks it re-reads
+// (the same slots with a separate count array and 73 top nodes staged per
+// block took the 196 KB step: 1080p shadow kernel 22.5 ms against 22.2 ms with
+// 92 KB of L1 and no staging).
 constexpr uint32_t kSortItems = 512, kSortBuckets = 64;
-template <int NW>  // warps per block
+template <int NW, uint32_t SORT = kSortItems>  // warps per block, items sorted together
 struct StreamSlotsT {
+    static constexpr uint32_t kSort = SORT;
     float4 pos[NW * 32];
     float4 PL[NW * 32];
     float4 T[NW * 32];
     float4 B[NW * 32];
-    uint32_t cnt[NW * 32];
     uint32_t next[NW];  // per warp: the next unclaimed item of the current light
     // per warp: the traced items of the light ordered by their disk sample, the
     // sample's cell per item, and the cell counts / cursors of the counting sort
-    uint16_t order[NW][kSortItems];
-    uint8_t key[NW][kSortItems];
+    uint16_t order[NW][SORT];
+    uint8_t key[NW][SORT];
     uint32_t bucket[NW][kSortBuckets];
 };
 using StreamSlots = StreamSlotsT<4>;
@@ -55,6 +51,12 @@ using StreamSlots = StreamSlotsT<4>;
 constexpr uint32_t kNotTraced = 0xffffffffu;
 
 // lane's slot for the current light; first_state: the RNG state of sample 0
+// the current light's unoccluded-sample count of slot i
+template <class Slots>
+__device__ __forceinline__ uint32_t* unocc_count(Slots& sm, uint32_t i) {
+    return reinterpret_cast<uint32_t*>(&sm.B[i].w);
+}
+
 template <class Slots>
 __device__ __forceinline__ void stream_publish(Slots& sm, bool traced, f3 position, f3 L, float dist,
                                                uint32_t first_state) {
@@ -64,18 +66,18 @@ __device__ __forceinline__ void stream_publish(Slots& sm, bool traced, f3 positi
         sm.pos[i] = make_float4(position.x, position.y, position.z, dist);
         sm.PL[i] = make_float4(d.PL.x, d.PL.y, d.PL.z, __uint_as_float(first_state));
         sm.T[i] = make_float4(d.T.x, d.T.y, d.T.z, 0.f);
-        sm.B[i] = make_float4(d.B.x, d.B.y, d.B.z, 0.f);
+        sm.B[i] = make_float4(d.B.x, d.B.y, d.B.z, 0.f);  // w: the unoccluded count, 0
     } else {
         sm.T[i].w = __uint_as_float(kNotTraced);
+        sm.B[i].w = 0.f;
     }
-    sm.cnt[i] = 0;
     if ((i & 31) == 0) sm.next[i >> 5] = 0;
 }
 
 // The warp's items of one light (every lane calls it, after all lanes have
 // published): sample k of a pixel starts from its first state advanced 2k LCG
 // steps (sampleDisk's two draws per sample), its ray from position +
-// offset * dir to distance + 1.  On return sm.cnt holds each pixel's
+// offset * dir to distance + 1.  On return unocc_count holds each pixel's
 // unoccluded samples.
 template <bool COUNT, bool TWO, class Stack, class Slots>
 __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams& P, Slots& sm, uint32_t nrays,
@@ -86,9 +88,9 @@ __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams
     uint32_t* next = &sm.next[warp];
     const uint32_t all = 32u * nrays;
     __syncwarp();
-    // the light's items in chunks of kSortItems (one chunk unless spp > 16)
-    for (uint32_t c0 = 0; c0 < all; c0 += kSortItems) {
-        const uint32_t cn = min(kSortItems, all - c0);
+    // the light's items in chunks of Slots::kSort (one chunk unless spp > 16)
+    for (uint32_t c0 = 0; c0 < all; c0 += Slots::kSort) {
+        const uint32_t cn = min(Slots::kSort, all - c0);
         uint32_t total = cn;
         // ---- the order of the chunk's items: a counting sort of the traced items by
         //      the cell of their disk sample on an 8x8 grid over the disk (cells in
@@ -178,7 +180,7 @@ __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams
                 for (uint32_t it = 0, ni = max(P.inner, 1u); it < ni; it++) {
                     if (trav_step<true, COUNT, TWO>(S, r, 0.001f, t, stk, nn, nt, P.status, top, ntop)) {
                         live = false;
-                        if (t.h.id == HY_NO_HIT) atomicAdd(&sm.cnt[wb + cur], 1u);
+                        if (t.h.id == HY_NO_HIT) atomicAdd(unocc_count(sm, wb + cur), 1u);
                         break;
                     }
                 }
@@ -268,7 +270,7 @@ __device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams&
             // shadowRaygen.rgen:78: origin position + 0.1 dir, tmax distance + 1
             stream_light<COUNT, TWO>(S, P, sm, nrays, S.lights[l].radius, 1e-1f, stk, t, r, ls, nn, nt, top, ntop);
             if (traced) {
-                const uint32_t unocc = sm.cnt[wb + lane];
+                const uint32_t unocc = *unocc_count(sm, wb + lane);
                 finalize(reference ? (float)unocc : __fdiv_rn((float)unocc, (float)spp));
             }
         }

@@ -44,11 +44,8 @@ static_assert(sizeof(RayPreSlot) == 68, "RayPreSlot stride");
 template <bool COUNT, bool ACCUM, int MINB, bool TWO = false, bool SHORT = false>
 __global__ void __launch_bounds__(128, MINB) k_shadow_stream(const SceneDev S, const PassParams P) {
     __shared__ StreamSlots sm;
-    __shared__ uint4 s_top[TWO ? 1 : kTopNodes * 5];
     __shared__ uint2 s_stack[SHORT ? kShortStack * 128 : 1];
     __shared__ RayPreSlot s_ray[TWO ? 128 : 1];
-    // two-level: no top-node staging (its shared memory holds the world rays)
-    const uint32_t ntop = TWO ? 0u : stage_top(S, s_top, P.top_nodes);
     LaneStats ls;
     const uint32_t lane = threadIdx.x & 31;
     uint2 stk[kStackMax];
@@ -68,11 +65,11 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_stream(const SceneDev S, c
         }
         if (SHORT)
             stream_tile<COUNT, TWO, ACCUM ? 1 : 0>(S, P, chunk_cur++, P.rng_mode == HY_RNG_REFERENCE, ACCUM, sm,
-                                                   SplitStack{s_stack + threadIdx.x, stk}, t, r, s, ls, nn, nt, s_top,
-                                                   ntop);
+                                                   SplitStack{s_stack + threadIdx.x, stk}, t, r, s, ls, nn, nt, nullptr,
+                                                   0u);
         else
             stream_tile<COUNT, TWO, ACCUM ? 1 : 0>(S, P, chunk_cur++, P.rng_mode == HY_RNG_REFERENCE, ACCUM, sm, stk, t,
-                                                   r, s, ls, nn, nt, s_top, ntop);
+                                                   r, s, ls, nn, nt, nullptr, 0u);
     }
     if (COUNT) { ls.nodes += nn; ls.tris += nt; }
     flush_stats(ls, P.stats);
