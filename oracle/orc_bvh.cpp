@@ -15,9 +15,10 @@
 //             the two sides stably partitioned (sah_tree below);
 //      LBVH — Karras 2012 binary radix tree over the 64-bit keys (morton << 32 | id)
 //   5. bottom-up box refit
-//   6. BFS collapse into 8-wide nodes: greedily open the child with the
-//      largest surface area, then assign children to octant slots by a
-//      greedy maximum of dot(child centroid - node centroid, slot corner)
+//   6. BFS collapse into 8-wide nodes: each node's 8 slots spread over its
+//      subtree by a surface-area-heuristic dynamic program over slot budgets,
+//      then children assigned to octant slots by a greedy maximum of
+//      dot(child centroid - node centroid, slot corner)
 //   7. quantise child boxes to 8 bits per axis against a power-of-two scale
 //      (Ylitie, Karras & Laine 2017 node format), rounding outwards
 //
@@ -486,6 +487,56 @@ static void build_core(const float* items, uint32_t n, Bvh& B, uint32_t node_off
         if (r & kLeafBit) return r & ~kLeafBit;
         return B.bvh2[r].first;
     };
+    // ---- slot budgets of the collapse (surface area heuristic) ----
+    // f(n, i): the lowest cost of representing subtree n by at most i slots of
+    // its parent, a slot being a leaf of <= kLeafMax triangles (area x triangles
+    // x kCostTri) or an internal node (area x kCostNode + its own 8 slots); a
+    // one-triangle leaf costs area x kCostTri.  Split choices: how many of the
+    // i slots go to the left child, or 0 for "f(n, i - 1)"; a node's own 8 slots
+    // (k to the left, 8 - k to the right) at [n * 9].  Float ops in the written
+    // order; the first strict minimum in k order wins.
+    std::vector<float> dpf;
+    std::vector<uint8_t> dpk;
+    if (n > 1) {
+        dpf.assign((size_t)(n - 1) * 8, 0.f);
+        dpk.assign((size_t)(n - 1) * 9, 0);
+        auto f = [&](uint32_t m, int i) -> float {
+            if (m & kLeafBit) return surface(tb[B.order[m & ~kLeafBit]]) * kCostTri;
+            return dpf[(size_t)m * 8 + i - 1];
+        };
+        std::vector<uint32_t> st{B.root};
+        std::vector<uint8_t> done(n - 1, 0);
+        while (!st.empty()) {
+            const uint32_t m = st.back();
+            bool ready = true;
+            for (uint32_t c : {B.bvh2[m].left, B.bvh2[m].right})
+                if (!(c & kLeafBit) && !done[c]) { st.push_back(c); ready = false; }
+            if (!ready) continue;
+            st.pop_back();
+            const uint32_t L = B.bvh2[m].left, R = B.bvh2[m].right;
+            const float A = surface(ref_box(m));
+            const uint32_t cnt = B.bvh2[m].last - B.bvh2[m].first + 1;
+            float best8 = INFINITY;
+            int bk = 1;
+            for (int k = 1; k <= 7; k++) {
+                const float v = f(L, k) + f(R, 8 - k);
+                if (v < best8) { best8 = v; bk = k; }
+            }
+            dpk[(size_t)m * 9] = (uint8_t)bk;
+            dpf[(size_t)m * 8] = cnt <= (uint32_t)kLeafMax ? (A * (float)cnt) * kCostTri : A * kCostNode + best8;
+            for (int i = 2; i <= 8; i++) {
+                float v = dpf[(size_t)m * 8 + i - 2];
+                int kk = 0;
+                for (int k = 1; k < i; k++) {
+                    const float w = f(L, k) + f(R, i - k);
+                    if (w < v) { v = w; kk = k; }
+                }
+                dpf[(size_t)m * 8 + i - 1] = v;
+                dpk[(size_t)m * 9 + i] = (uint8_t)kk;
+            }
+            done[m] = 1;
+        }
+    }
     // ---- BFS collapse to BVH8 ----
     std::vector<uint32_t> queue;       // BVH2 ref of each BVH8 node, BFS order
     std::vector<uint32_t> level;       // level of each node
@@ -496,22 +547,27 @@ static void build_core(const float* items, uint32_t n, Bvh& B, uint32_t node_off
     for (size_t k = 0; k < queue.size(); k++) {
         uint32_t r = queue[k];
         // children list
+        // children: the node's 8 slots spread over its subtree by the budget
+        // choices, left subtree first
         uint32_t C[8];
         int nc = 0;
-        if (r & kLeafBit) { C[nc++] = r; }
-        else { C[nc++] = B.bvh2[r].left; C[nc++] = B.bvh2[r].right; }
-        while (nc < 8) {
-            int best = -1;
-            float bestA = -1.f;
-            for (int i = 0; i < nc; i++) {
-                if (C[i] & kLeafBit) continue;
-                float A = surface(ref_box(C[i]));
-                if (best < 0 || A > bestA || (A == bestA && C[i] < C[best])) { best = i; bestA = A; }
+        if (r & kLeafBit) {
+            C[nc++] = r;
+        } else {
+            uint32_t sm_[8];
+            int si_[8], sp = 0;
+            const int k0 = dpk[(size_t)r * 9];
+            sm_[sp] = B.bvh2[r].right; si_[sp++] = 8 - k0;
+            sm_[sp] = B.bvh2[r].left; si_[sp++] = k0;
+            while (sp > 0) {
+                const uint32_t m = sm_[--sp];
+                int i = si_[sp];
+                while (!(m & kLeafBit) && i > 1 && dpk[(size_t)m * 9 + i] == 0) i--;
+                if ((m & kLeafBit) || i == 1) { C[nc++] = m; continue; }
+                const int k = dpk[(size_t)m * 9 + i];
+                sm_[sp] = B.bvh2[m].right; si_[sp++] = i - k;
+                sm_[sp] = B.bvh2[m].left; si_[sp++] = k;
             }
-            if (best < 0) break;
-            uint32_t open = C[best];
-            C[best] = B.bvh2[open].left;
-            C[nc++] = B.bvh2[open].right;
         }
         // slot assignment
         Box nb = ref_box(r);

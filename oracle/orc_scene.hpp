@@ -10,6 +10,8 @@
 namespace orc {
 
 constexpr int kLeafMax = 3;           // triangles per BVH8 leaf slot
+constexpr float kCostNode = 1.0f;     // collapse: cost of a node visit (per unit area)
+constexpr float kCostTri = 0.5f;      // collapse: cost of a triangle test (a node visit ~2 tests)
 constexpr int kStackMax = 64;         // traversal stack entries
 constexpr uint32_t kMaxIters = 1u << 22;  // node visits per ray before giving up
 

@@ -459,7 +459,8 @@ void hy_destroy(HyCtx* c) {
                       &c->grad_partial, &c->tex_px, &c->tex_tab, &c->xinv, &c->inst, &c->inst_box,
                       &c->inst_prim, &c->prim_mesh, &c->blas_node0, &c->mesh_vrange, &c->inst_chunks,
                       &c->inst_keys, &c->sah_ranges[0], &c->sah_ranges[1], &c->sah_small, &c->sah_bins,
-                      &c->sah_split, &c->sah_chunks, &c->sah_first, &c->sah_ccnt, &c->sah_coff, &c->sah_ctr};
+                      &c->sah_split, &c->sah_chunks, &c->sah_first, &c->sah_ccnt, &c->sah_coff, &c->sah_ctr,
+                      &c->dp_cost, &c->dp_k};
     for (DevBuf* b : bufs) ctx_free(c, *b);
     if (c->h_stats) cudaFreeHost(c->h_stats);
     for (cudaEvent_t e : c->prof_pool) cudaEventDestroy(e);

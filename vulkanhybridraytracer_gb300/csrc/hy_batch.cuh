@@ -25,16 +25,12 @@ static_assert(sizeof(PassParams) % 4 == 0 && sizeof(SceneDev) % 4 == 0, "copied 
 template <bool COUNT, int BLOCK, int MINB, int SHORT, bool ANY_TWO>
 __global__ void __launch_bounds__(BLOCK, MINB) k_shadow_batch_stream(const BatchParams B) {
     constexpr int NW = BLOCK / 32;
-    __shared__ uint32_t s_begin[kMaxBatchViews + 1];
     __shared__ StreamSlotsT<NW> sm;
     // per warp: its current view's parameters and scene, copied from the
     // global tables when the warp moves to another view
     __shared__ PassParams s_view[NW];
     __shared__ SceneDev s_scene[NW];
     extern __shared__ uint2 s_stack[];
-    for (uint32_t i = threadIdx.x; i <= B.nviews; i += blockDim.x)
-        s_begin[i] = i < B.nviews ? B.views[i].tile_begin : B.total_tiles;
-    __syncthreads();
     LaneStats ls;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint2 stk[kStackMax - SHORT];
@@ -52,7 +48,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_shadow_batch_stream(const Batch
             chunk_end = min(t0 + B.chunk, B.total_tiles);
         }
         const uint32_t unit = chunk_cur++;
-        const uint32_t v = view_of_tile(s_begin, B.nviews, unit);
+        const uint32_t v = view_of_tile(B.views, B.nviews, unit);
         if (v != cur_view) {
             __syncwarp();
             const uint32_t* vs = reinterpret_cast<const uint32_t*>(&B.views[v]);

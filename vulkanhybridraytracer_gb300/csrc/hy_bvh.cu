@@ -11,6 +11,8 @@
 //                   (HY_BUILD_LBVH), or the binned-SAH tree of hy_sah.cu
 //                   over the same order (HY_BUILD_SAH, the default)
 //   k_refit         bottom-up boxes, last-arriver-computes (no waiting)
+//   k_collapse_dp   slot budgets of the collapse by the surface area heuristic
+//                   (bottom up, last arriver computes)
 //   k_collapse_*    BFS collapse into compressed 8-wide nodes, one level per
 //                   launch pair with prefix sums for deterministic numbering
 //
@@ -379,29 +381,107 @@ __device__ __forceinline__ float surface(const Ref& b) {
     return a;
 }
 
+// Slot budgets of the collapse (surface area heuristic), bottom up: f(n, i) =
+// the lowest cost of representing subtree n by at most i slots of its parent
+// (a leaf slot of <= kLeafMax triangles: area x triangles x kCostTri; an
+// internal node: area x kCostNode + its own 8 slots); a one-triangle leaf
+// costs area x kCostTri.  dpk[n * 9]: left share k of the node's own 8 slots;
+// dpk[n * 9 + i]: the left share of i slots, 0 for "i - 1 slots".  The second
+// child to finish computes its parent (as k_refit), reading the first's
+// values through L2; the float ops and tie rule (first strict minimum in k
+// order) are the oracle's.
+constexpr float kCostNode = 1.0f, kCostTri = 0.5f;
+
+__device__ __forceinline__ float dp_cost(uint32_t m, int i, const float* dpf, const uint32_t* order,
+                                         const float* tribox) {
+    if (m & kLeaf) return __fmul_rn(surface(load_ref(m, nullptr, order, tribox)), kCostTri);
+    return __ldcg(dpf + (size_t)m * 8 + i - 1);
+}
+
+__global__ void k_collapse_dp(const uint32_t* __restrict__ order, const float* __restrict__ tribox, uint32_t n,
+                              const uint32_t* __restrict__ bvh2, const uint32_t* __restrict__ parent,
+                              uint32_t* flags, float* dpf, uint8_t* dpk) {
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    uint32_t p = parent[n - 1 + j];
+    while (p != 0xffffffffu) {
+        __threadfence();
+        if (atomicAdd(flags + p, 1u) == 0u) return;  // the sibling's thread computes this node
+        __threadfence();
+        const uint32_t* nd = bvh2 + (size_t)p * 10;
+        const uint32_t L = __ldcg(nd + 0), R = __ldcg(nd + 1);
+        float fl[8], fr[8];
+#pragma unroll
+        for (int i = 1; i <= 8; i++) {
+            fl[i - 1] = dp_cost(L, i, dpf, order, tribox);
+            fr[i - 1] = dp_cost(R, i, dpf, order, tribox);
+        }
+        Ref nb;
+        for (int a = 0; a < 3; a++) {
+            nb.lo[a] = __uint_as_float(__ldcg(nd + 4 + a));
+            nb.hi[a] = __uint_as_float(__ldcg(nd + 7 + a));
+        }
+        const float A = surface(nb);
+        const uint32_t cnt = __ldcg(nd + 3) - __ldcg(nd + 2) + 1;
+        float best8 = INFINITY;
+        int bk = 1;
+#pragma unroll
+        for (int k = 1; k <= 7; k++) {
+            const float v = __fadd_rn(fl[k - 1], fr[8 - k - 1]);
+            if (v < best8) { best8 = v; bk = k; }
+        }
+        float f[8];
+        f[0] = cnt <= (uint32_t)kLeafMax ? __fmul_rn(__fmul_rn(A, __uint2float_rn(cnt)), kCostTri)
+                                         : __fadd_rn(__fmul_rn(A, kCostNode), best8);
+        uint8_t* kd = dpk + (size_t)p * 9;
+        kd[0] = (uint8_t)bk;
+#pragma unroll
+        for (int i = 2; i <= 8; i++) {
+            float v = f[i - 2];
+            int kk = 0;
+            for (int k = 1; k < i; k++) {
+                const float w = __fadd_rn(fl[k - 1], fr[i - k - 1]);
+                if (w < v) { v = w; kk = k; }
+            }
+            f[i - 1] = v;
+            kd[i] = (uint8_t)kk;
+        }
+        float* fo = dpf + (size_t)p * 8;
+#pragma unroll
+        for (int i = 0; i < 8; i++) __stcg(fo + i, f[i]);
+        p = parent[p];
+    }
+}
+
 // plan: 8 BVH2 refs per node in slot order (0xffffffff = empty)
 __global__ void k_collapse_plan(const uint32_t* __restrict__ lvl, uint32_t m, const uint32_t* __restrict__ bvh2,
                                 const uint32_t* __restrict__ order, const float* __restrict__ tribox,
-                                uint32_t* __restrict__ plan, uint32_t* __restrict__ ni, uint32_t* __restrict__ nt) {
+                                const uint8_t* __restrict__ dpk, uint32_t* __restrict__ plan,
+                                uint32_t* __restrict__ ni, uint32_t* __restrict__ nt) {
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m) return;
     uint32_t r = lvl[k];
+    // children: the node's 8 slots spread over its subtree by the slot budgets,
+    // left subtree first
     uint32_t C[8];
     int nc = 0;
-    if (r & kLeaf) C[nc++] = r;
-    else { C[nc++] = bvh2[(size_t)r * 10 + 0]; C[nc++] = bvh2[(size_t)r * 10 + 1]; }
-    while (nc < 8) {
-        int best = -1;
-        float bestA = -1.f;
-        for (int i = 0; i < nc; i++) {
-            if (C[i] & kLeaf) continue;
-            float A = surface(load_ref(C[i], bvh2, order, tribox));
-            if (best < 0 || A > bestA || (A == bestA && C[i] < C[best])) { best = i; bestA = A; }
+    if (r & kLeaf) {
+        C[nc++] = r;
+    } else {
+        uint32_t sm_[8];
+        int si_[8], sp = 0;
+        const int k0 = dpk[(size_t)r * 9];
+        sm_[sp] = bvh2[(size_t)r * 10 + 1]; si_[sp++] = 8 - k0;
+        sm_[sp] = bvh2[(size_t)r * 10 + 0]; si_[sp++] = k0;
+        while (sp > 0) {
+            const uint32_t mm = sm_[--sp];
+            int i = si_[sp];
+            while (!(mm & kLeaf) && i > 1 && dpk[(size_t)mm * 9 + i] == 0) i--;
+            if ((mm & kLeaf) || i == 1) { C[nc++] = mm; continue; }
+            const int kk = dpk[(size_t)mm * 9 + i];
+            sm_[sp] = bvh2[(size_t)mm * 10 + 1]; si_[sp++] = i - kk;
+            sm_[sp] = bvh2[(size_t)mm * 10 + 0]; si_[sp++] = kk;
         }
-        if (best < 0) break;
-        uint32_t open = C[best];
-        C[best] = bvh2[(size_t)open * 10 + 0];
-        C[nc++] = bvh2[(size_t)open * 10 + 1];
     }
     Ref nb = load_ref(r, bvh2, order, tribox);
     float pc[3];
@@ -611,7 +691,9 @@ static int build_core(HyCtx* c, uint32_t n, uint32_t node_off, uint32_t rec_off,
         (rc = ctx_alloc(c, c->nt, (size_t)n * 4)) || (rc = ctx_alloc(c, c->ni_scan, (size_t)n * 4)) ||
         (rc = ctx_alloc(c, c->nt_scan, (size_t)n * 4)) ||
         (rc = ctx_alloc(c, c->node_ref, (size_t)std::max<uint32_t>(n, 1) * 4)) ||
-        (rc = ctx_alloc(c, c->node_plan, (size_t)std::max<uint32_t>(n, 1) * 32)))
+        (rc = ctx_alloc(c, c->node_plan, (size_t)std::max<uint32_t>(n, 1) * 32)) ||
+        (rc = ctx_alloc(c, c->dp_cost, (size_t)std::max<uint32_t>(n, 1) * 32)) ||
+        (rc = ctx_alloc(c, c->dp_k, (size_t)std::max<uint32_t>(n, 1) * 9)))
         return rc;
     cudaStream_t s = c->stream;
     int* bnd = c->bounds.as<int>();
@@ -653,6 +735,10 @@ static int build_core(HyCtx* c, uint32_t n, uint32_t node_off, uint32_t rec_off,
         HY_CUDA_TRY(cudaMemsetAsync(c->flags.p, 0, (size_t)n * 4, s));
         k_refit<<<cdiv(n, 256), 256, 0, s>>>(ord, c->tribox.as<float>(), n, bvh2, c->parent.as<uint32_t>(),
                                              c->flags.as<uint32_t>());
+        HY_CUDA_TRY(cudaMemsetAsync(c->flags.p, 0, (size_t)n * 4, s));
+        k_collapse_dp<<<cdiv(n, 256), 256, 0, s>>>(ord, c->tribox.as<float>(), n, bvh2, c->parent.as<uint32_t>(),
+                                                   c->flags.as<uint32_t>(), c->dp_cost.as<float>(),
+                                                   c->dp_k.as<uint8_t>());
     }
     HY_CUDA_TRY(cudaGetLastError());
     uint32_t level_start = 0, tri_start = 0, m = 1, depth = 0;
@@ -660,7 +746,8 @@ static int build_core(HyCtx* c, uint32_t n, uint32_t node_off, uint32_t rec_off,
     uint32_t* tot = c->total.as<uint32_t>();
     while (m > 0) {
         const uint32_t* lvl = c->lvl_ref[lv].as<uint32_t>();
-        k_collapse_plan<<<cdiv(m, 128), 128, 0, s>>>(lvl, m, bvh2, ord, c->tribox.as<float>(), c->plan.as<uint32_t>(),
+        k_collapse_plan<<<cdiv(m, 128), 128, 0, s>>>(lvl, m, bvh2, ord, c->tribox.as<float>(),
+                                                     c->dp_k.as<uint8_t>(), c->plan.as<uint32_t>(),
                                                      c->ni.as<uint32_t>(), c->nt.as<uint32_t>());
         if ((rc = scan_exclusive(c, c->ni.as<uint32_t>(), c->ni_scan.as<uint32_t>(), m, tot))) return rc;
         if ((rc = scan_exclusive(c, c->nt.as<uint32_t>(), c->nt_scan.as<uint32_t>(), m, tot + 1))) return rc;

@@ -61,6 +61,7 @@ struct HyCtx {
     hy::DevBuf scan_tmp, hist, total;
     hy::DevBuf nodes, tris;
     hy::DevBuf node_ref, node_plan;  // per BVH8 node: its BVH2 subtree, its 8 slot children (refits)
+    hy::DevBuf dp_cost, dp_k;        // collapse slot budgets: 8 costs, 9 choices per binary-tree node
     uint32_t build_mode = HY_BUILD_SAH;  // hy_scene_set_build_mode
     // binned-SAH build scratch (hy_sah.cu): range queues, bins, chunk maps, counters
     hy::DevBuf sah_ranges[2], sah_small, sah_bins, sah_split, sah_chunks, sah_first, sah_ccnt, sah_coff, sah_ctr;

@@ -35,15 +35,20 @@ constexpr uint32_t kSortItems = 512, kSortBuckets = 64;
 template <int NW, uint32_t SORT = kSortItems>  // warps per block, items sorted together
 struct StreamSlotsT {
     static constexpr uint32_t kSort = SORT;
+    // the sort keys of a light's items: in shared memory up to 4 warps per block,
+    // in a chain of registers beyond (8-warp batch blocks: 30 KB instead of 34 KB,
+    // under the 132 KB shared-memory step at 4 blocks per SM)
+    static constexpr bool kKeysShared = NW <= 4;
     float4 pos[NW * 32];
     float4 PL[NW * 32];
     float4 T[NW * 32];
     float4 B[NW * 32];
     uint32_t next[NW];  // per warp: the next unclaimed item of the current light
     // per warp: the traced items of the light ordered by their disk sample, the
-    // sample's cell per item, and the cell counts / cursors of the counting sort
+    // sample's cell per item (kKeysShared) and the cell counts / cursors of the
+    // counting sort
     uint16_t order[NW][SORT];
-    uint8_t key[NW][SORT];
+    uint8_t key[kKeysShared ? NW : 1][kKeysShared ? SORT : 1];
     uint32_t bucket[NW][kSortBuckets];
 };
 using StreamSlots = StreamSlotsT<4>;
@@ -104,10 +109,19 @@ __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams
             bk[lane] = 0;
             bk[lane + 32] = 0;
             __syncwarp();
-            for (uint32_t j = lane; j < cn; j += 32) {
-                const uint32_t q = c0 + j, pi = q / nrays, k = q - pi * nrays;
+            // each lane's item keys (items lane + 32 i, one byte each) go to shared
+            // memory or through a shift chain of registers: after the kSort / 32
+            // steps item i's key is byte i
+            constexpr uint32_t kSteps = Slots::kSort / 32, kWords = kSteps / 4;
+            static_assert(kSteps % 4 == 0, "whole key words");
+            uint32_t keys[kWords];
+#pragma unroll
+            for (uint32_t w = 0; w < kWords; w++) keys[w] = 0;
+            for (uint32_t i = 0; i < kSteps; i++) {
+                const uint32_t j = lane + 32u * i;
                 uint32_t key = 0xffu;
-                if (__float_as_uint(sm.T[wb + pi].w) != kNotTraced) {
+                const uint32_t q = c0 + j, pi = j < cn ? q / nrays : 0u, k = q - pi * nrays;
+                if (j < cn && __float_as_uint(sm.T[wb + pi].w) != kNotTraced) {
                     uint32_t st = lcg_jump(__float_as_uint(sm.PL[wb + pi].w), 2u * k);
                     const float r1 = rnd(st), r2 = rnd(st);
                     // the disk point in units of the radius (approximate: it only orders the items)
@@ -120,7 +134,13 @@ __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams
                           ((iy & 4u) << 3);
                     atomicAdd(&bk[key], 1u);
                 }
-                sm.key[warp][j] = (uint8_t)key;
+                if constexpr (Slots::kKeysShared) {
+                    if (j < cn) sm.key[warp][j] = (uint8_t)key;
+                } else {
+#pragma unroll
+                    for (uint32_t w = 0; w + 1 < kWords; w++) keys[w] = (keys[w] >> 8) | (keys[w + 1] << 24);
+                    keys[kWords - 1] = (keys[kWords - 1] >> 8) | (key << 24);
+                }
             }
             __syncwarp();
             // exclusive scan of the 64 counts, two per lane
@@ -136,8 +156,19 @@ __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams
             bk[2 * lane] = incl - c;
             bk[2 * lane + 1] = incl - c + cnt0;
             __syncwarp();
-            for (uint32_t j = lane; j < cn; j += 32) {
-                const uint32_t key = sm.key[warp][j];
+            for (uint32_t i = 0; i < kSteps; i++) {
+                const uint32_t j = lane + 32u * i;
+                uint32_t key;
+                if constexpr (Slots::kKeysShared) {
+                    if (j >= cn) break;
+                    key = sm.key[warp][j];
+                } else {
+                    key = keys[0] & 0xffu;
+#pragma unroll
+                    for (uint32_t w = 0; w + 1 < kWords; w++) keys[w] = (keys[w] >> 8) | (keys[w + 1] << 24);
+                    keys[kWords - 1] >>= 8;
+                    if (j >= cn) continue;
+                }
                 if (key != 0xffu) sm.order[warp][atomicAdd(&bk[key], 1u)] = (uint16_t)j;
             }
         }
@@ -285,6 +316,18 @@ __device__ __forceinline__ uint32_t view_of_tile(const uint32_t* s_begin, uint32
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
         if (s_begin[mid] <= tile) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// the same from the views' own first tiles in the batch's table (global memory,
+// L1-cached): the tile-stream batch kernel keeps its shared memory for the slots
+__device__ __forceinline__ uint32_t view_of_tile(const PassParams* views, uint32_t nviews, uint32_t tile) {
+    uint32_t lo = 0, hi = nviews;  // views[lo].tile_begin <= tile < views[hi].tile_begin
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&views[mid].tile_begin) <= tile) lo = mid;
         else hi = mid;
     }
     return lo;
