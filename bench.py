@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--mirror-reflection", action="store_true",
                     help="the reference's perfect mirror reflection instead of the configuration's GGX-sampled ray")
     ap.add_argument("--leg-steps", type=int, default=3, help="timed steps of the batch and diff legs")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="batch workload: the default launch shape instead of the autotuner's sweep")
     ap.add_argument("--build-mode", default="sah", choices=["sah", "lbvh"],
                     help="binary tree under the 8-wide nodes (hy_scene_set_build_mode)")
     return ap.parse_args()
@@ -717,10 +719,20 @@ def batch_leg(steps: int, warmup: int, n_views: int = 64, tune: bool = False, cl
     clk = clocks.stop()
     mp = float(np.median(t_plain))
     mb = float(np.median(t_batch))
+    # per-view census for the launch-list analysis of the view-by-view path: one
+    # more view-by-view pass with its rays counted (the launches of this pass are
+    # the last 64 shadow + shade pairs of the run)
+    frame[0] += 1
+    set_frame(frame[0])
+    view_rays = []
+    for v in views:
+        sv = ctxs[v["scene"]].forward(v["planes"], v["camera"], v["config"], v["hist"], out_8=v["out_8"])
+        view_rays.append(int(sv["shadow_rays"] + sv["reflection_rays"] + sv["hit_shadow_rays"]))
     out = {"workload": f"batch-{len(views)}views-8scenes", "views": len(views),
            "scene_triangles": [c.num_tris for c in ctxs],
            "pixels": sum(v["w"] * v["h"] for v in views), "rays_per_batch": rays,
            "spp": [v["spp"] for v in views], "lights": [v["hist"].shape[0] for v in views],
+           "view_res": [f"{v['w']}x{v['h']}" for v in views], "view_rays": view_rays,
            "batched_ms": 1e3 * mb, "plain_ms": 1e3 * mp, "batched_over_plain": mp / mb,
            "batched_mrays_per_s": rays / mb / 1e6, "plain_mrays_per_s": rays / mp / 1e6,
            "tuning": {k: tuned[k] for k in ("chunk", "block", "min_blocks", "stack_depth", "cached") if k in tuned},
@@ -738,7 +750,7 @@ def run_batch(args):
 
     stream = torch.cuda.Stream(device=torch.device("cuda", 0))
     torch.cuda.set_stream(stream)
-    d = batch_leg(args.steps, args.warmup, args.views, tune=True)
+    d = batch_leg(args.steps, args.warmup, args.views, tune=not args.no_tune)
     line = {"metric": "hybrid_batch_mrays_per_s", "value": d["batched_mrays_per_s"], "unit": "Mrays/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": d["batched_ms"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -746,7 +758,7 @@ def run_batch(args):
                                          "lights", "l2")},
             "plain_per_view": {"value": d["plain_mrays_per_s"], "unit": "Mrays/s", "ms_per_step": d["plain_ms"]},
             "batched_over_plain": d["batched_over_plain"], "autotune": d.get("autotune"), "clocks": d["clocks"],
-            "gpu_launches": 2}
+            "view_res": d["view_res"], "view_rays": d["view_rays"], "gpu_launches": 2}
     print(json.dumps(line))
 
 
