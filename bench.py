@@ -63,6 +63,10 @@ def parse():
     ap.add_argument("--mirror-reflection", action="store_true",
                     help="the reference's perfect mirror reflection instead of the configuration's GGX-sampled ray")
     ap.add_argument("--leg-steps", type=int, default=3, help="timed steps of the batch and diff legs")
+    ap.add_argument("--large-div", type=int, default=1,
+                    help="large workload: the 4K resolution divided by this (small ncu cases); the scene is unchanged")
+    ap.add_argument("--anyhit", default="auto", choices=["auto", "far", "near"],
+                    help="any-hit child order of the scenes (hy_scene_set_anyhit_order)")
     ap.add_argument("--no-tune", action="store_true",
                     help="batch workload: the default launch shape instead of the autotuner's sweep")
     ap.add_argument("--build-mode", default="sah", choices=["sah", "lbvh"],
@@ -139,16 +143,18 @@ def config_of(wl, args):
             "structure": STRUCTURE[BUILD_MODE["mode"]]}
 
 
-BUILD_MODE = {"mode": "sah"}
+BUILD_MODE = {"mode": "sah", "anyhit": "auto"}
 STRUCTURE = {"sah": "binned SAH (32 bins per axis) binary tree -> compressed BVH8",
              "lbvh": "LBVH (Karras radix tree over 30-bit Morton codes) -> compressed BVH8"}
 
 
 def build_structure(ctx, instanced: bool = False):
-    """hy_bvh_build(_instanced) with the build mode of --build-mode."""
+    """hy_bvh_build(_instanced) with the build mode of --build-mode and the any-hit order of --anyhit."""
     from vulkanhybridraytracer_gb300 import _lib as L
 
     ctx.set_build_mode(L.HY_BUILD_SAH if BUILD_MODE["mode"] == "sah" else L.HY_BUILD_LBVH)
+    ctx.set_anyhit_order({"auto": L.HY_ANYHIT_AUTO, "far": L.HY_ANYHIT_FAR_FIRST,
+                          "near": L.HY_ANYHIT_NEAR_FIRST}[BUILD_MODE["anyhit"]])
     return ctx.build_bvh(instanced=instanced)
 
 
@@ -460,7 +466,7 @@ def run_pathtrace(args):
 
 def run_large(args):
     """The large combined configuration: 3840x2160, 4096 instances of 8 base meshes + the
-    terrain (7.35M triangles in one BVH8), 64 area lights x 1 sample, 2 bounces; the frame,
+    terrain (8.81M triangles in one BVH8), 64 area lights x 1 sample, 2 bounces; the frame,
     its adjoint over 1024 materials and 64 lights, and the frame batched with 4 extra 1080p
     views (hy_batch_forward) against the same 5 views one by one."""
     import torch
@@ -474,7 +480,7 @@ def run_large(args):
     torch.cuda.set_device(0)
     stream = torch.cuda.Stream(device=dev)
     torch.cuda.set_stream(stream)
-    wl = scenes.large()
+    wl = scenes.large(width=3840 // args.large_div, height=2160 // args.large_div)
     ctx = HybridContext(0, stream=stream.cuda_stream)
     ctx.set_scene(wl.scene)
     bvh = build_structure(ctx)
@@ -765,6 +771,7 @@ def run_batch(args):
 def main():
     args = parse()
     BUILD_MODE["mode"] = args.build_mode
+    BUILD_MODE["anyhit"] = args.anyhit
     if args.impl == "reference":
         run_reference(args)
         return

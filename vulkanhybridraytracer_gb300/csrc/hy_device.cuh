@@ -474,13 +474,60 @@ __device__ __forceinline__ f3 xform_point(float4 r0, float4 r1, float4 r2, f3 o)
                          R[k].w);
     return mk(v[0], v[1], v[2]);
 }
-__device__ __forceinline__ f3 xform_dir(float4 r0, float4 r1, float4 r2, const float* d) {
+__device__ __forceinline__ f3 xform_dir(float4 r0, float4 r1, float4 r2, f3 d) {
     const float4 R[3] = {r0, r1, r2};
     float v[3];
 #pragma unroll
     for (int k = 0; k < 3; k++)
-        v[k] = __fadd_rn(__fadd_rn(__fmul_rn(R[k].x, d[0]), __fmul_rn(R[k].y, d[1])), __fmul_rn(R[k].z, d[2]));
+        v[k] = __fadd_rn(__fadd_rn(__fmul_rn(R[k].x, d.x), __fmul_rn(R[k].y, d.y)), __fmul_rn(R[k].z, d.z));
     return mk(v[0], v[1], v[2]);
+}
+
+// A lane's world ray: its set-up in registers (RayPre), or, for the two-level
+// walk, in shared memory (WorldRaySlot: word k of lane t at p[128 k], the 16
+// words of RayPre, conflict-free; 64 B a lane).  The two-level walk reads the
+// world ray only to enter and leave instances, so its registers go to the walk.
+// (Keeping only the origin and direction there and recomputing the set-up on
+// leaving an instance freed more shared memory for L1 but made the 4K two-level
+// frame slower: 293.4 against 282 ms.)
+struct WorldRaySlot {
+    float* p;
+};
+__device__ __forceinline__ f3 world_o(const RayPre& r) { return r.o; }
+__device__ __forceinline__ f3 world_d(const RayPre& r) { return mk(r.d[0], r.d[1], r.d[2]); }
+__device__ __forceinline__ const RayPre& world_pre(const RayPre& r) { return r; }
+__device__ __forceinline__ const RayPre& world_set(RayPre& r, f3 o, f3 d) {
+    r = ray_pre(o, d);
+    return r;
+}
+__device__ __forceinline__ f3 world_o(const WorldRaySlot& w) { return mk(w.p[0], w.p[128], w.p[256]); }
+__device__ __forceinline__ f3 world_d(const WorldRaySlot& w) { return mk(w.p[384], w.p[512], w.p[640]); }
+__device__ __forceinline__ RayPre world_pre(const WorldRaySlot& w) {
+    RayPre r;
+    r.o = world_o(w);
+    r.d[0] = w.p[384]; r.d[1] = w.p[512]; r.d[2] = w.p[640];
+    r.kx = __float_as_int(w.p[768]); r.ky = __float_as_int(w.p[896]); r.kz = __float_as_int(w.p[1024]);
+    r.Sx = w.p[1152]; r.Sy = w.p[1280]; r.Sz = w.p[1408];
+    r.invd[0] = w.p[1536]; r.invd[1] = w.p[1664]; r.invd[2] = w.p[1792];
+    r.near = __float_as_uint(w.p[1920]);
+    return r;
+}
+__device__ __forceinline__ RayPre world_set(WorldRaySlot& w, f3 o, f3 d) {
+    const RayPre r = ray_pre(o, d);
+    w.p[0] = r.o.x; w.p[128] = r.o.y; w.p[256] = r.o.z;
+    w.p[384] = r.d[0]; w.p[512] = r.d[1]; w.p[640] = r.d[2];
+    w.p[768] = __int_as_float(r.kx); w.p[896] = __int_as_float(r.ky); w.p[1024] = __int_as_float(r.kz);
+    w.p[1152] = r.Sx; w.p[1280] = r.Sy; w.p[1408] = r.Sz;
+    w.p[1536] = r.invd[0]; w.p[1664] = r.invd[1]; w.p[1792] = r.invd[2];
+    w.p[1920] = __uint_as_float(r.near);
+    return r;
+}
+
+// the ray of the level being walked: the world ray, or (two-level) t.cur
+template <bool TWO, class RW>
+__device__ __forceinline__ const RayPre& cur_ray(const Trav& t, const RW& rw) {
+    if constexpr (TWO) return t.cur;
+    else return rw;
 }
 
 // Two-level walk: brings t to a non-empty node group.  A TLAS leaf hands its
@@ -488,8 +535,8 @@ __device__ __forceinline__ f3 xform_dir(float4 r0, float4 r1, float4 r2, const f
 // TLAS group on the stack, moves the ray into object space and walks the
 // BLAS above the saved stack height; once that part of the stack is empty
 // the world ray is restored.  Returns false when the walk is over.
-template <class Stack>
-__device__ __forceinline__ bool two_level_settle(const SceneDev& S, const RayPre& rw, Trav& t, Stack stk,
+template <class Stack, class RW>
+__device__ __forceinline__ bool two_level_settle(const SceneDev& S, const RW& rw, Trav& t, Stack stk,
                                                  uint32_t* status) {
     for (;;) {
         if (!t.level && t.inst_bits) {
@@ -506,7 +553,7 @@ __device__ __forceinline__ bool two_level_settle(const SceneDev& S, const RayPre
             if (iid >= S.num_inst) { atomicOr(status, HY_STATUS_BAD_INDEX); return false; }
             const float4* I = S.inst + (size_t)iid * 4;
             const float4 r0 = __ldg(I), r1 = __ldg(I + 1), r2 = __ldg(I + 2), m = __ldg(I + 3);
-            t.cur = ray_pre(xform_point(r0, r1, r2, rw.o), xform_dir(r0, r1, r2, rw.d));
+            t.cur = ray_pre(xform_point(r0, r1, r2, world_o(rw)), xform_dir(r0, r1, r2, world_d(rw)));
             t.level = true;
             t.sp_base = t.sp;
             t.id_off = __float_as_uint(m.y);
@@ -517,7 +564,7 @@ __device__ __forceinline__ bool two_level_settle(const SceneDev& S, const RayPre
         if (t.g_bits & 0xff000000u) return true;
         if (t.level && t.sp == t.sp_base) {
             t.level = false;
-            t.cur = rw;
+            t.cur = world_pre(rw);
             continue;
         }
         if (t.sp == 0) return false;
@@ -539,8 +586,8 @@ __device__ __forceinline__ bool two_level_settle(const SceneDev& S, const RayPre
 // TWO: the two-level structure (r is the world ray; t.cur the current one).
 // top / ntop: the structure's first ntop nodes (its top levels, BFS order)
 // staged in shared memory by the caller's block.
-template <bool ANY, bool COUNT, bool TWO = false, class Stack = uint2*>
-__device__ __forceinline__ bool trav_node(const SceneDev& S, const RayPre& rw, float tmin, Trav& t, Stack stk,
+template <bool ANY, bool COUNT, bool TWO = false, class Stack = uint2*, class RW = RayPre>
+__device__ __forceinline__ bool trav_node(const SceneDev& S, const RW& rw, float tmin, Trav& t, Stack stk,
                                           uint32_t& nodes_ctr, uint32_t* status, const uint4* top = nullptr,
                                           uint32_t ntop = 0) {
     if (++t.iters > S.max_iters) { atomicOr(status, HY_STATUS_TIMEOUT); return true; }
@@ -553,7 +600,7 @@ __device__ __forceinline__ bool trav_node(const SceneDev& S, const RayPre& rw, f
         t.g_base = e.x;
         t.g_bits = e.y;
     }
-    const RayPre& r = TWO ? t.cur : rw;
+    const RayPre& r = cur_ray<TWO>(t, rw);
     const uint32_t rb = __ffs(t.g_bits >> 24) - 1;
     t.g_bits &= ~(1u << (24 + rb));
     const uint32_t ord = ANY ? r.near ^ S.anyhit_flip : r.near;
@@ -651,10 +698,10 @@ __device__ __forceinline__ bool trav_node(const SceneDev& S, const RayPre& rw, f
 
 // The next pending triangle of the ray (t.pend_bits must be nonzero).
 // Returns true when the walk is over: an any-hit ray that hit, or a bad index.
-template <bool ANY, bool COUNT, bool TWO = false>
-__device__ __forceinline__ bool trav_tri(const SceneDev& S, const RayPre& rw, float tmin, Trav& t,
+template <bool ANY, bool COUNT, bool TWO = false, class RW = RayPre>
+__device__ __forceinline__ bool trav_tri(const SceneDev& S, const RW& rw, float tmin, Trav& t,
                                          uint32_t& tris_ctr, uint32_t* status) {
-    const RayPre& r = TWO ? t.cur : rw;
+    const RayPre& r = cur_ray<TWO>(t, rw);
     const uint32_t b = __ffs(t.pend_bits) - 1;
     t.pend_bits &= t.pend_bits - 1u;
     const uint32_t rec = t.pend_base + b;
@@ -676,8 +723,8 @@ __device__ __forceinline__ bool trav_tri(const SceneDev& S, const RayPre& rw, fl
 
 // One node visit and then its triangles (the walk of a single ray).
 // Returns true when the ray is finished: t.h holds the hit, or id HY_NO_HIT.
-template <bool ANY, bool COUNT, bool TWO = false, class Stack = uint2*>
-__device__ __forceinline__ bool trav_step(const SceneDev& S, const RayPre& rw, float tmin, Trav& t, Stack stk,
+template <bool ANY, bool COUNT, bool TWO = false, class Stack = uint2*, class RW = RayPre>
+__device__ __forceinline__ bool trav_step(const SceneDev& S, const RW& rw, float tmin, Trav& t, Stack stk,
                                           uint32_t& nodes_ctr, uint32_t& tris_ctr, uint32_t* status,
                                           const uint4* top = nullptr, uint32_t ntop = 0) {
     if (trav_node<ANY, COUNT, TWO>(S, rw, tmin, t, stk, nodes_ctr, status, top, ntop)) return true;

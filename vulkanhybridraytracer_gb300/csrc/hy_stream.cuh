@@ -84,9 +84,9 @@ __device__ __forceinline__ void stream_publish(Slots& sm, bool traced, f3 positi
 // steps (sampleDisk's two draws per sample), its ray from position +
 // offset * dir to distance + 1.  On return unocc_count holds each pixel's
 // unoccluded samples.
-template <bool COUNT, bool TWO, class Stack, class Slots>
+template <bool COUNT, bool TWO, class Stack, class Slots, class RW>
 __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams& P, Slots& sm, uint32_t nrays,
-                                             float radius, float offset, Stack stk, Trav& t, RayPre& r,
+                                             float radius, float offset, Stack stk, Trav& t, RW& r,
                                              LaneStats& ls, uint32_t& nn, uint32_t& nt, const uint4* top,
                                              uint32_t ntop) {
     const uint32_t lane = threadIdx.x & 31, wb = threadIdx.x & ~31u, warp = threadIdx.x >> 5;
@@ -197,8 +197,7 @@ __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams
                 const DiskFrame d{mk(tp.x, tp.y, tp.z), mk(bp.x, bp.y, bp.z), mk(pl.x, pl.y, pl.z)};
                 uint32_t st = lcg_jump(__float_as_uint(pl.w), 2u * k);
                 const f3 dir = sampleDisk(radius, pos, d, st);
-                r = ray_pre(add_rn(pos, scale_rn(dir, offset)), dir);
-                trav_init(t, r, __fadd_rn(pp.w, 1.0f));
+                trav_init(t, world_set(r, add_rn(pos, scale_rn(dir, offset)), dir), __fadd_rn(pp.w, 1.0f));
                 cur = pi;
                 live = true;
                 ls.shadow++;
@@ -253,9 +252,9 @@ __device__ __forceinline__ void shadow_finalize(const PassParams& P, const Shado
 // One 8x4 tile of a view, light by light.  ACC: 0 raw shadow images, 1 the
 // running mean into the history, 2 either (accum) at run time.  reference:
 // REFERENCE RNG (one ray per pixel-light from the pixel's seed, by value).
-template <bool COUNT, bool TWO, int ACC, class Stack, class Slots>
+template <bool COUNT, bool TWO, int ACC, class Stack, class Slots, class RW>
 __device__ __forceinline__ void stream_tile(const SceneDev& S, const PassParams& P, uint32_t tile, bool reference,
-                                            bool accum, Slots& sm, Stack stk, Trav& t, RayPre& r,
+                                            bool accum, Slots& sm, Stack stk, Trav& t, RW& r,
                                             ShadowLane& s, LaneStats& ls, uint32_t& nn, uint32_t& nt,
                                             const uint4* top, uint32_t ntop) {
     const uint32_t lane = threadIdx.x & 31, wb = threadIdx.x & ~31u;

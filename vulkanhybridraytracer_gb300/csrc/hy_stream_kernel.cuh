@@ -5,6 +5,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "hy_device.cuh"
 #include "hy_pass.h"
 #include "hy_shade.cuh"
@@ -31,28 +33,21 @@ namespace hy {
 // adjacent pixels of one light.  Seeds as in k_shadow_group (LCG jump-ahead),
 // so the rays equal those of k_shadow.
 // ---------------------------------------------------------------------------------
-// a lane's world ray in shared memory (two-level walk: read only when an
-// instance is entered or left, so its 16 registers are free for the walk: 96 ->
-// 64 registers at the spills of the one-level kernel); 17 words apart, so a
-// warp's lanes hit 32 different banks
-struct RayPreSlot {
-    RayPre r;
-    float pad;
-};
-static_assert(sizeof(RayPreSlot) == 68, "RayPreSlot stride");
-
 template <bool COUNT, bool ACCUM, int MINB, bool TWO = false, bool SHORT = false>
 __global__ void __launch_bounds__(128, MINB) k_shadow_stream(const SceneDev S, const PassParams P) {
     __shared__ StreamSlots sm;
     __shared__ uint2 s_stack[SHORT ? kShortStack * 128 : 1];
-    __shared__ RayPreSlot s_ray[TWO ? 128 : 1];
+    // two-level: each lane's world ray set-up (WorldRaySlot, 64 B a lane): 8
+    // blocks at 23.6 KB stay on the 196 KB shared-memory step (the 68-byte
+    // padded layout of the same data took 24.1 KB and the 228 KB step)
+    __shared__ float s_world[TWO ? 16 * 128 : 1];
     LaneStats ls;
     const uint32_t lane = threadIdx.x & 31;
     uint2 stk[kStackMax];
     ShadowLane s;
     Trav t;
-    RayPre r_reg;
-    RayPre& r = TWO ? s_ray[threadIdx.x].r : r_reg;
+    std::conditional_t<TWO, WorldRaySlot, RayPre> r{};
+    if constexpr (TWO) r.p = s_world + threadIdx.x;
     uint32_t chunk_cur = 0, chunk_end = 0, nn = 0, nt = 0;
     for (;;) {
         if (chunk_cur == chunk_end) {
