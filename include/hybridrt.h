@@ -286,6 +286,9 @@ int hy_scene_set_textures(HyCtx* ctx, const uint8_t* const* rgba8, const uint32_
  *                 centroids coincide is split at its middle.  Fewer node visits
  *                 per ray (about 30 % on a 1.5 M-triangle terrain-and-spheres
  *                 scene) for a longer build.
+ * Either tree is collapsed into 8-wide nodes by a surface-area-heuristic
+ * program over slot budgets (how many of a node's 8 child slots each subtree
+ * gets).
  *   HY_BUILD_LBVH Karras's radix tree over the Morton keys: the fastest build.
  * The 8-wide node format, the traversal and every result but node and
  * triangle counts are the same.  The mode applies from the next build. */
