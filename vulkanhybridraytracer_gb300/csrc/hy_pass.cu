@@ -31,7 +31,7 @@
 
 namespace hy {
 
-template <int MODE, bool COUNT>
+template <int MODE, bool COUNT, int LV = 0>
 __device__ __forceinline__ void do_pixel(const SceneDev& S, const PassParams& P, uint32_t x, uint32_t y,
                                          LaneStats& ls) {
     const size_t pix = (size_t)y * P.W + x;
@@ -131,7 +131,7 @@ __device__ __forceinline__ void do_pixel(const SceneDev& S, const PassParams& P,
     for (uint32_t depth = 0; depth < P.max_bounces; depth++) {
         if (smode == 0) break;
         f3 ro = origin + direction * 1e-2f;
-        Hit h = trace<false, COUNT>(S, ro, direction, 0.001f, 1000.0f, ls, P.status);
+        Hit h = trace<false, COUNT, LV>(S, ro, direction, 0.001f, 1000.0f, ls, P.status);
         ls.refl++;
         f3 pc, pdir = direction, porg = origin;
         float pt, pw = 0.f;
@@ -139,7 +139,7 @@ __device__ __forceinline__ void do_pixel(const SceneDev& S, const PassParams& P,
             pc = miss_color(S, direction);
             pt = -1.f;
         } else {
-            Payload p = closest_hit<COUNT>(S, P, h, ro, direction, seed_h, ls);
+            Payload p = closest_hit<COUNT, false, LV>(S, P, h, ro, direction, seed_h, ls);
             pc = p.color; pt = p.t; pdir = p.dir; pw = p.scattered; porg = p.origin;
         }
         rayColor = rayColor * pc;
@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(128, MINB) k_shadow_group(const SceneDev S, co
     flush_stats(ls, P.stats);
 }
 
-template <int MODE, bool COUNT, int MINB = 1>
+template <int MODE, bool COUNT, int MINB = 1, int LV = 0>
 __global__ void __launch_bounds__(128, MINB) k_pixels(const SceneDev S, const PassParams P) {
     LaneStats ls;
     const uint32_t lane = threadIdx.x & 31;
@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(128, MINB) k_pixels(const SceneDev S, const Pa
         for (uint32_t t = t0; t < t1; t++) {
             uint32_t tx = t % P.tiles_x, ty = t / P.tiles_x;
             uint32_t x = tx * 8 + (lane & 7), y = ty * 4 + (lane >> 3);
-            if (x < P.W && y < P.H) do_pixel<MODE, COUNT>(S, P, x, y, ls);
+            if (x < P.W && y < P.H) do_pixel<MODE, COUNT, LV>(S, P, x, y, ls);
         }
     }
     flush_stats(ls, P.stats);
@@ -985,13 +985,18 @@ static void* shadow_kernel_two(bool count, int minb) {
     return count ? (void*)k_shadow_group<true, ACCUM, 5, true> : (void*)k_shadow_group<false, ACCUM, 5, true>;
 }
 
-// the shade kernel (hybridRaygen + hybridHit): resident blocks it is compiled for
+// the shade kernel (hybridRaygen + hybridHit): resident blocks it is compiled for;
+// at 8 (the default) one variant per structure level, each holding one copy of
+// the walk, else one variant for either level
 template <int MINB>
 static void* shade_kernel_m(bool count) {
     return count ? (void*)k_pixels<MODE_SHADE, true, MINB> : (void*)k_pixels<MODE_SHADE, false, MINB>;
 }
-static void* shade_kernel(bool count, int minb) {
-    if (minb >= 8) return shade_kernel_m<8>(count);
+static void* shade_kernel(bool count, int minb, bool two) {
+    if (minb >= 8) {
+        if (two) return count ? (void*)k_pixels<MODE_SHADE, true, 8, 2> : (void*)k_pixels<MODE_SHADE, false, 8, 2>;
+        return count ? (void*)k_pixels<MODE_SHADE, true, 8, 1> : (void*)k_pixels<MODE_SHADE, false, 8, 1>;
+    }
     if (minb >= 6) return shade_kernel_m<6>(count);
     if (minb == 5) return shade_kernel_m<5>(count);
     if (minb == 4) return shade_kernel_m<4>(count);
@@ -1012,7 +1017,7 @@ static void* pixel_kernel(int mode, bool count, int minb, bool two, bool short_s
                 return count ? (void*)k_shadow<true, false, 5, true> : (void*)k_shadow<false, false, 5, true>;
             case MODE_SHADOW_ACCUM:
                 return count ? (void*)k_shadow<true, true, 5, true> : (void*)k_shadow<false, true, 5, true>;
-            case MODE_SHADE: return shade_kernel(count, shade_minb);
+            case MODE_SHADE: return shade_kernel(count, shade_minb, true);
             default: return nullptr;
         }
     }
@@ -1023,7 +1028,7 @@ static void* pixel_kernel(int mode, bool count, int minb, bool two, bool short_s
         case MODE_SHADOW_ACCUM_G: return shadow_kernel<true, true>(count, minb);
         case MODE_SHADOW_P: return minb >= 8 ? pool_kernel<false, 8>(count) : pool_kernel<false, 5>(count);
         case MODE_SHADOW_ACCUM_P: return minb >= 8 ? pool_kernel<true, 8>(count) : pool_kernel<true, 5>(count);
-        default: return shade_kernel(count, shade_minb);
+        default: return shade_kernel(count, shade_minb, false);
     }
 }
 

@@ -24,13 +24,20 @@ __device__ __forceinline__ void flush_stats(const LaneStats& s, unsigned long lo
     }
 }
 
-template <bool ANY, bool COUNT>
+// LV: the structure the caller's kernel is compiled for — 1 one-level, 2
+// two-level, 0 either (chosen per call from the scene).  A kernel compiled for
+// one holds one copy of the walk instead of both (the shade kernel's
+// instruction-cache misses were its top stall).
+template <bool ANY, bool COUNT, int LV = 0>
 __device__ __forceinline__ Hit trace(const SceneDev& S, f3 o, f3 d, float tmin, float tmax, LaneStats& ls,
                                      uint32_t* status) {
     RayPre r = ray_pre(o, d);
     uint32_t nn = 0, nt = 0;
-    Hit h = S.two_level ? traverse<ANY, COUNT, true>(S, r, tmin, tmax, &nn, &nt, status)
-                        : traverse<ANY, COUNT, false>(S, r, tmin, tmax, &nn, &nt, status);
+    Hit h;
+    if constexpr (LV == 1) h = traverse<ANY, COUNT, false>(S, r, tmin, tmax, &nn, &nt, status);
+    else if constexpr (LV == 2) h = traverse<ANY, COUNT, true>(S, r, tmin, tmax, &nn, &nt, status);
+    else h = S.two_level ? traverse<ANY, COUNT, true>(S, r, tmin, tmax, &nn, &nt, status)
+                         : traverse<ANY, COUNT, false>(S, r, tmin, tmax, &nn, &nt, status);
     if (COUNT) { ls.nodes += nn; ls.tris += nt; }
     return h;
 }
@@ -159,7 +166,7 @@ struct Payload { f3 color; float t; f3 dir; float scattered; f3 origin; };
 // hybridHit.rchit:24-183.  REC: also record, per light, whether the shadow
 // factor came out 2 (lit side and unoccluded) into bit i of *vis — the
 // visibility the adjoint holds fixed.
-template <bool COUNT, bool REC = false>
+template <bool COUNT, bool REC = false, int LV = 0>
 __device__ Payload closest_hit(const SceneDev& S, const PassParams& P, const Hit& h, f3 ro, f3 rd, uint32_t& seed,
                                LaneStats& ls, unsigned long long* vis = nullptr) {
     HitAttr a = hit_attributes(S, h);
@@ -208,7 +215,7 @@ __device__ Payload closest_hit(const SceneDev& S, const PassParams& P, const Hit
                     uint32_t sd = seed;
                     f3 dir = P.rng_mode == HY_RNG_REFERENCE ? sampleDisk(lt.radius, worldPos, L, sd)
                                                             : sampleDisk(lt.radius, worldPos, L, seed);
-                    Hit sh = trace<true, COUNT>(S, add_rn(worldPos, scale_rn(dir, 1e-2f)), dir, 0.001f,
+                    Hit sh = trace<true, COUNT, LV>(S, add_rn(worldPos, scale_rn(dir, 1e-2f)), dir, 0.001f,
                                                 __fadd_rn(dist, 1.0f), ls, P.status);
                     ls.hshadow++;
                     shadowed = sh.id != HY_NO_HIT;
