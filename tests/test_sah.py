@@ -207,3 +207,112 @@ def test_sah_fewer_visits_than_lbvh(oracle_lib):
             assert cnt[:, 0].mean() < cn[:, 0].mean()
     assert np.array_equal(res[po.HY_BUILD_SAH][0], res[po.HY_BUILD_LBVH][0])
     assert res[po.HY_BUILD_SAH][1] < 0.9 * res[po.HY_BUILD_LBVH][1]
+
+
+def _surface32(lo, hi):
+    d = (np.asarray(hi, F32) - np.asarray(lo, F32)).astype(F32)
+    a = F32(d[0] * d[1])
+    a = F32(a + F32(d[1] * d[2]))
+    return F32(a + F32(d[2] * d[0]))
+
+
+def test_collapse_slot_budgets_restated(sah_small):
+    """Every 8-wide node's children are its binary subtree spread over 8 slots by the
+    surface-area program (leaf slot: area x triangles x 0.5; internal node: area +
+    its own 8 slots; first strict minimum in split order), restated here in numpy
+    float32 from the downloaded binary tree and compared as sets of triangles."""
+    wl, o, info = sah_small
+    n = info["num_tris"]
+    _, order, bvh2, bvh8, tris = o.download_bvh(info["num_bvh8_nodes"])
+    box = bvh2[:, 4:10].view(F32)
+    w = o.world_tris().reshape(-1, 3, 3)
+    tlo, thi = w.min(1), w.max(1)
+    ids = tris[:, 3].view(np.uint32)
+
+    memo = {}
+
+    def f(m):  # the 8 costs f(m, 1..8)
+        if m & LEAF:
+            t = order[m & ~LEAF]
+            return [F32(_surface32(tlo[t], thi[t]) * F32(0.5))] * 8, None
+        if m in memo:
+            return memo[m]
+        L, R, first, last = (int(v) for v in bvh2[m, :4])
+        fl, _ = f(L)
+        fr, _ = f(R)
+        A = _surface32(box[m, :3], box[m, 3:])
+        cnt = last - first + 1
+        best8, bk = np.float32(np.inf), 1
+        for k in range(1, 8):
+            v = F32(fl[k - 1] + fr[8 - k - 1])
+            if v < best8:
+                best8, bk = v, k
+        fv = [F32(F32(A * F32(cnt)) * F32(0.5)) if cnt <= 3 else F32(F32(A * F32(1.0)) + best8)]
+        kk = [bk, 0]
+        for i in range(2, 9):
+            v, ki = fv[i - 2], 0
+            for k in range(1, i):
+                w_ = F32(fl[k - 1] + fr[i - k - 1])
+                if w_ < v:
+                    v, ki = w_, k
+            fv.append(v)
+            kk.append(ki)
+        memo[m] = (fv, kk)
+        return memo[m]
+
+    def expand(m, i, out):
+        while not (m & LEAF) and i > 1 and f(m)[1][i] == 0:
+            i -= 1
+        if (m & LEAF) or i == 1:
+            out.append(m)
+            return
+        k = f(m)[1][i]
+        expand(int(bvh2[m, 0]), k, out)
+        expand(int(bvh2[m, 1]), i - k, out)
+
+    import sys
+    sys.setrecursionlimit(10000)
+
+    def tri_set(ref):
+        if ref & LEAF:
+            return frozenset([int(order[ref & ~LEAF])])
+        return frozenset(int(t) for t in order[bvh2[ref, 2]:bvh2[ref, 3] + 1])
+
+    node_of_set = {tri_set(m): m for m in range(n - 1)}
+
+    def bvh8_children(k):
+        w8 = bvh8[k]
+        meta = list(w8[6:8].view(np.uint8))
+        base, tbase, rank, kids = int(w8[4]), int(w8[5]), 0, []
+        for sl in range(8):
+            mb = int(meta[sl])
+            if mb == 0:
+                continue
+            if mb == 0x80:
+                kids.append(("node", base + rank))
+                rank += 1
+            else:
+                c, off = mb >> 5, mb & 31
+                kids.append(("tris", frozenset(int(t) for t in ids[tbase + off:tbase + off + c])))
+        return kids
+
+    sets8 = {}
+
+    def subtree_set(k):
+        if k not in sets8:
+            s = set()
+            for kind, v in bvh8_children(k):
+                s |= subtree_set(v) if kind == "node" else v
+            sets8[k] = frozenset(s)
+        return sets8[k]
+
+    for k in range(len(bvh8)):
+        whole = subtree_set(k)
+        m = node_of_set[whole]
+        want = []
+        expand(int(bvh2[m, 1]), 8 - f(m)[1][0], want)
+        left = []
+        expand(int(bvh2[m, 0]), f(m)[1][0], left)
+        want = {tri_set(r) for r in left + want}
+        got = {subtree_set(v) if kind == "node" else v for kind, v in bvh8_children(k)}
+        assert got == want, k
