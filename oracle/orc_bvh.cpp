@@ -759,6 +759,16 @@ static inline uint8_t byte_of(const uint32_t* w, int word0, int slot) {
     return (uint8_t)(w[word0 + (slot >> 2)] >> ((slot & 3) * 8));
 }
 
+// Plane distances of the one-level walk, as its kernels compute them: plane
+// byte q as q * 2^-24 (the kernels convert it from a subnormal half, exactly)
+// times the node scale over d scaled by 2^24, plus org, in one fma: q * adj +
+// org rounded once, the value fma(q, adj, org) gives (unless adj * 2^24
+// overflows, which both sides then share).
+static const struct PlaneValues24 {
+    float v[256];
+    PlaneValues24() { for (int q = 0; q < 256; q++) v[q] = (float)q * 5.9604644775390625e-8f; }
+} kPlane24;
+
 static Hit trace_bvh8(const Scene& s, const float o[3], const float d[3], float tmin, float tmax, bool any_hit,
                       Counters* c) {
     const Bvh& B = s.bvh;
@@ -797,11 +807,11 @@ static Hit trace_bvh8(const Scene& s, const float o[3], const float d[3], float 
         }
         const uint32_t* w = B.bvh8[idx].w;
         if (c) c->nodes++;
-        float adj[3], org[3];
+        float adj24[3], org[3];
         for (int a = 0; a < 3; a++) {
             uint32_t ea = (w[3] >> (8 * a)) & 0xffu;
             float sc = bitsf(ea << 23);
-            adj[a] = sc * invd[a];
+            adj24[a] = (sc * invd[a]) * 16777216.0f;
             org[a] = (bitsf(w[a]) - o[a]) * invd[a];
         }
         uint32_t imask = w[3] >> 24;
@@ -811,12 +821,12 @@ static Hit trace_bvh8(const Scene& s, const float o[3], const float d[3], float 
             if (m == 0) continue;
             float tn[3], tf[3];
             for (int a = 0; a < 3; a++) {
-                float ql = (float)byte_of(w, 8 + 2 * a, slot);
-                float qh = (float)byte_of(w, 14 + 2 * a, slot);
+                float ql = kPlane24.v[byte_of(w, 8 + 2 * a, slot)];
+                float qh = kPlane24.v[byte_of(w, 14 + 2 * a, slot)];
                 float lo = invd[a] < 0.f ? qh : ql;
                 float hi = invd[a] < 0.f ? ql : qh;
-                tn[a] = std::fma(lo, adj[a], org[a]);
-                tf[a] = std::fma(hi, adj[a], org[a]);
+                tn[a] = std::fma(lo, adj24[a], org[a]);
+                tf[a] = std::fma(hi, adj24[a], org[a]);
             }
             float tnear = fmax2(fmax2(tn[0], tn[1]), fmax2(tn[2], tmin));
             float tfar = fmin2(fmin2(tf[0], tf[1]), fmin2(tf[2], cur_tmax));
