@@ -759,7 +759,7 @@ static inline uint8_t byte_of(const uint32_t* w, int word0, int slot) {
     return (uint8_t)(w[word0 + (slot >> 2)] >> ((slot & 3) * 8));
 }
 
-// Plane distances of the one-level walk, as its kernels compute them: plane
+// Plane distances of both walks, as the kernels compute them: plane
 // byte q as q * 2^-24 (the kernels convert it from a subnormal half, exactly)
 // times the node scale over d scaled by 2^24, plus org, in one fma: q * adj +
 // org rounded once, the value fma(q, adj, org) gives (unless adj * 2^24
@@ -1014,13 +1014,14 @@ static RayState ray_state(const float o[3], const float d[3]) {
     return r;
 }
 
-// box tests of one node: internal children hit (rank order) and leaf records hit
+// box tests of one node: internal children hit (rank order) and leaf records
+// hit (plane distances as in trace_bvh8)
 static void node_hits(const uint32_t* w, const RayState& r, uint32_t ord, float tmin, float tmax,
                       uint32_t& hit_int, uint32_t& hit_tri) {
-    float adj[3], org[3];
+    float adj24[3], org[3];
     for (int a = 0; a < 3; a++) {
         uint32_t ea = (w[3] >> (8 * a)) & 0xffu;
-        adj[a] = bitsf(ea << 23) * r.invd[a];
+        adj24[a] = (bitsf(ea << 23) * r.invd[a]) * 16777216.0f;
         org[a] = (bitsf(w[a]) - r.p.o[a]) * r.invd[a];
     }
     const uint32_t imask = w[3] >> 24;
@@ -1031,12 +1032,12 @@ static void node_hits(const uint32_t* w, const RayState& r, uint32_t ord, float 
         if (m == 0) continue;
         float tn[3], tf[3];
         for (int a = 0; a < 3; a++) {
-            float ql = (float)byte_of(w, 8 + 2 * a, slot);
-            float qh = (float)byte_of(w, 14 + 2 * a, slot);
+            float ql = kPlane24.v[byte_of(w, 8 + 2 * a, slot)];
+            float qh = kPlane24.v[byte_of(w, 14 + 2 * a, slot)];
             float lo = r.invd[a] < 0.f ? qh : ql;
             float hi = r.invd[a] < 0.f ? ql : qh;
-            tn[a] = std::fma(lo, adj[a], org[a]);
-            tf[a] = std::fma(hi, adj[a], org[a]);
+            tn[a] = std::fma(lo, adj24[a], org[a]);
+            tf[a] = std::fma(hi, adj24[a], org[a]);
         }
         float tnear = fmax2(fmax2(tn[0], tn[1]), fmax2(tn[2], tmin));
         float tfar = fmin2(fmin2(tf[0], tf[1]), fmin2(tf[2], tmax));

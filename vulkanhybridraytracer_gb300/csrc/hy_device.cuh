@@ -654,65 +654,36 @@ __device__ __forceinline__ bool trav_node(const SceneDev& S, const RW& rw, float
         }
     }
     uint32_t hitbits = 0;
-    if constexpr (!TWO) {
-        // Plane bytes as subnormal halves: one PRMT makes 0x00qq:0x00qq, the
-        // halves q * 2^-24 of two slots, whose conversion to float is exact; with
-        // adj scaled by 2^24 (exact) one fma gives q * adj + org rounded once, the
-        // same value as fma(q, adj, org).  Per axis, the (near, far) pair of a
-        // slot is one f32x2 fma.
-        unsigned long long adj2[3], org2[3];
+    // Plane bytes as subnormal halves: one PRMT makes 0x00qq:0x00qq, the
+    // halves q * 2^-24 of two slots, whose conversion to float is exact; with
+    // adj scaled by 2^24 (exact) one fma gives q * adj + org rounded once, the
+    // same value as fma(q, adj, org).  Per axis, the (near, far) pair of a
+    // slot is one f32x2 fma.
+    unsigned long long adj2[3], org2[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float a24 = __fmul_rn(adj[a], 16777216.0f);
+        adj2[a] = f2_pack(a24, a24);
+        org2[a] = f2_pack(org[a], org[a]);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {  // the slot pair 2j, 2j + 1: bytes (2j) & 3 and the next of word j / 2
+        const uint32_t kSel = (j & 1) ? 0x4342u : 0x4140u;
+        float tn[2][3], tf[2][3];
 #pragma unroll
         for (int a = 0; a < 3; a++) {
-            const float a24 = __fmul_rn(adj[a], 16777216.0f);
-            adj2[a] = f2_pack(a24, a24);
-            org2[a] = f2_pack(org[a], org[a]);
+            float n0, n1, f0, f1;
+            h2_to_f2(__byte_perm(qn[a][j >> 1], 0u, kSel), n0, n1);
+            h2_to_f2(__byte_perm(qf[a][j >> 1], 0u, kSel), f0, f1);
+            f2_unpack(f2_fma(f2_pack(n0, f0), adj2[a], org2[a]), tn[0][a], tf[0][a]);
+            f2_unpack(f2_fma(f2_pack(n1, f1), adj2[a], org2[a]), tn[1][a], tf[1][a]);
         }
 #pragma unroll
-        for (int j = 0; j < 4; j++) {  // the slot pair 2j, 2j + 1: bytes (2j) & 3 and the next of word j / 2
-            const uint32_t kSel = (j & 1) ? 0x4342u : 0x4140u;
-            float tn[2][3], tf[2][3];
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                float n0, n1, f0, f1;
-                h2_to_f2(__byte_perm(qn[a][j >> 1], 0u, kSel), n0, n1);
-                h2_to_f2(__byte_perm(qf[a][j >> 1], 0u, kSel), f0, f1);
-                f2_unpack(f2_fma(f2_pack(n0, f0), adj2[a], org2[a]), tn[0][a], tf[0][a]);
-                f2_unpack(f2_fma(f2_pack(n1, f1), adj2[a], org2[a]), tn[1][a], tf[1][a]);
-            }
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                // max(max(tn0, tn1), max(tn2, tmin)) and its min twin, as two instructions each
-                const float tnear = fmaxf(fmax3(tn[h][0], tn[h][1], tn[h][2]), tmin);
-                const float tfar = fminf(fmin3(tf[h][0], tf[h][1], tf[h][2]), t.tmax);
-                if (tnear <= __fmul_rn(tfar, 1.0000003f)) hitbits |= 1u << (2 * j + h);
-            }
-        }
-    } else {
-        // The two-level walk, whose instance entries hold more registers, keeps
-        // one plane byte per PRMT: 0x4B0000qq (= 2^23 + q), the add removes 2^23
-        // exactly, and tn / tf are fma(q, adj, org) itself.  Two bytes per PRMT
-        // raise its register spills at the 64-register cap, and made its 4K
-        // frame 2 % slower where the one-level walks gained 1-2 %.
-        unsigned long long adj2[3], org2[3];
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-            adj2[a] = f2_pack(adj[a], adj[a]);
-            org2[a] = f2_pack(org[a], org[a]);
-        }
-        const unsigned long long kMinus2p23 = f2_pack(-8388608.0f, -8388608.0f);
-#pragma unroll
-        for (int slot = 0; slot < 8; slot++) {
-            float tn[3], tf[3];
-            const uint32_t kSel = 0x7540u | (uint32_t)(slot & 3);  // an immediate once the loop unrolls
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                const unsigned long long q2 = f2_pack_bits(__byte_perm(qn[a][slot >> 2], 0x4B000000u, kSel),
-                                                           __byte_perm(qf[a][slot >> 2], 0x4B000000u, kSel));
-                f2_unpack(f2_fma(f2_add(q2, kMinus2p23), adj2[a], org2[a]), tn[a], tf[a]);
-            }
-            const float tnear = fmaxf(fmax3(tn[0], tn[1], tn[2]), tmin);
-            const float tfar = fminf(fmin3(tf[0], tf[1], tf[2]), t.tmax);
-            if (tnear <= __fmul_rn(tfar, 1.0000003f)) hitbits |= 1u << slot;
+        for (int h = 0; h < 2; h++) {
+            // max(max(tn0, tn1), max(tn2, tmin)) and its min twin, as two instructions each
+            const float tnear = fmaxf(fmax3(tn[h][0], tn[h][1], tn[h][2]), tmin);
+            const float tfar = fminf(fmin3(tf[h][0], tf[h][1], tf[h][2]), t.tmax);
+            if (tnear <= __fmul_rn(tfar, 1.0000003f)) hitbits |= 1u << (2 * j + h);
         }
     }
     // empty slots (meta byte 0) never count; internal children go to the stack
