@@ -99,6 +99,32 @@ __device__ __forceinline__ uint32_t lcg_jump(uint32_t s, uint32_t n) {
     }
     return s;
 }
+// The maps of 2k LCG steps, x -> a x + c (mod 2^32), for k < 64: sample k of a
+// pixel-light starts 2k steps (two draws per sample) after its first state,
+// and one load plus one multiply-add replaces the squaring loop.
+struct LcgJumpTable {
+    alignas(8) uint32_t ac[128];  // (a, c) of 2k steps at ac[2k], ac[2k + 1]
+    constexpr LcgJumpTable() : ac() {
+        const uint32_t A2 = 1664525u * 1664525u, C2 = (1664525u + 1u) * 1013904223u;  // two steps
+        uint32_t a = 1u, c = 0u;
+        for (int k = 0; k < 64; k++) {
+            ac[2 * k] = a;
+            ac[2 * k + 1] = c;
+            c = A2 * c + C2;
+            a = A2 * a;
+        }
+    }
+};
+__device__ const LcgJumpTable g_lcg_jump2{};
+
+// lcg_jump(s, 2k)
+__device__ __forceinline__ uint32_t lcg_jump_even(uint32_t s, uint32_t k) {
+    if (k < 64u) {
+        const uint2 m = __ldg(reinterpret_cast<const uint2*>(g_lcg_jump2.ac) + k);
+        return m.x * s + m.y;
+    }
+    return lcg_jump(s, 2u * k);
+}
 // float(lcg) / 16777216: the division by 2^24 is the exact product with 2^-24
 __device__ __forceinline__ float rnd(uint32_t& prev) { return __fmul_rn((float)lcg(prev), 0x1p-24f); }
 

@@ -122,12 +122,12 @@ __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams
                 uint32_t key = 0xffu;
                 const uint32_t q = c0 + j, pi = j < cn ? q / nrays : 0u, k = q - pi * nrays;
                 if (j < cn && __float_as_uint(sm.T[wb + pi].w) != kNotTraced) {
-                    uint32_t st = lcg_jump(__float_as_uint(sm.PL[wb + pi].w), 2u * k);
+                    uint32_t st = lcg_jump_even(__float_as_uint(sm.PL[wb + pi].w), k);
                     const float r1 = rnd(st), r2 = rnd(st);
                     // the disk point in units of the radius (approximate: it only orders the items)
                     float sn, cs;
                     __sincosf(6.2831853f * r2, &sn, &cs);
-                    const float rr = sqrtf(r1);
+                    const float rr = r1 > 0.f ? r1 * rsqrtf(r1) : 0.f;
                     const uint32_t ix = min(7u, (uint32_t)fmaxf((rr * cs + 1.0f) * 4.0f, 0.0f));
                     const uint32_t iy = min(7u, (uint32_t)fmaxf((rr * sn + 1.0f) * 4.0f, 0.0f));
                     key = (ix & 1u) | ((iy & 1u) << 1) | ((ix & 2u) << 1) | ((iy & 2u) << 2) | ((ix & 4u) << 2) |
@@ -195,7 +195,7 @@ __device__ __forceinline__ void stream_light(const SceneDev& S, const PassParams
                 const float4 pp = sm.pos[wb + pi], pl = sm.PL[wb + pi], bp = sm.B[wb + pi];
                 const f3 pos = mk(pp.x, pp.y, pp.z);
                 const DiskFrame d{mk(tp.x, tp.y, tp.z), mk(bp.x, bp.y, bp.z), mk(pl.x, pl.y, pl.z)};
-                uint32_t st = lcg_jump(__float_as_uint(pl.w), 2u * k);
+                uint32_t st = lcg_jump_even(__float_as_uint(pl.w), k);
                 const f3 dir = sampleDisk(radius, pos, d, st);
                 trav_init(t, world_set(r, add_rn(pos, scale_rn(dir, offset)), dir), __fadd_rn(pp.w, 1.0f));
                 cur = pi;
