@@ -36,6 +36,28 @@ def test_rnd_golden_and_grid(oracle_lib, kat):
         assert np.all(v * (1 << 24) == np.floor(v * (1 << 24))) and np.all((v >= 0) & (v < 1))
 
 
+def test_lcg_two_step_maps_restated(oracle_lib):
+    """The shadow kernels start sample k of a pixel-light 2k LCG steps after its
+    first state (two draws per sample, random.glsl:21-33) with the map
+    x -> a_k x + c_k (mod 2^32) of 2k steps, read from a table for k < 64.  The
+    table's recurrence, restated here, gives the states of the sequential
+    generator for every k."""
+    M = 1 << 32
+    A, C = 1664525, 1013904223
+    A2, C2 = (A * A) % M, ((A + 1) * C) % M  # two steps: x -> A (A x + C) + C
+    a, c, maps = 1, 0, []
+    for _ in range(64):
+        maps.append((a, c))
+        a, c = (A2 * a) % M, (A2 * c + C2) % M
+    rng = np.random.default_rng(4)
+    for seed in rng.integers(0, M, 8, dtype=np.uint64).tolist():
+        st, _ = po.rnd_seq(int(seed), 2 * 63)
+        for k in range(1, 64):
+            ak, ck = maps[k]
+            assert (ak * seed + ck) % M == int(st[2 * k - 1])
+    assert maps[0] == (1, 0)
+
+
 def test_sample_disk_by_value_seed(oracle_lib):
     """helpers.glsl:82-93 takes the seed by value: the same seed gives the same
     direction however many times it is called (all samples of a pixel agree)."""
