@@ -128,6 +128,54 @@ def test_bvh_bitexact_tiny_and_degenerate(gpu_lib, oracle_lib, n, mode):
     ctx.close()
 
 
+@pytest.mark.parametrize("scale", [1e-6, 1.0, 1e6, 1e12])
+def test_trace_bitexact_coordinate_scales(gpu_lib, oracle_lib, scale):
+    """Scenes from micro to huge coordinates, with axis-aligned rays (a zero
+    direction component: 1/d clamped to 1e20): the node test's plane distances
+    (the node scale times 1/d, taken times 2^24 with the plane bytes as q * 2^-24)
+    span the float range, and hits and counts still equal the oracle's."""
+    from vulkanhybridraytracer_gb300.hybrid import HybridContext
+    rng = np.random.default_rng(31)
+    n = 2000
+    v = np.zeros((3 * n, 11), np.float32)
+    cen = rng.uniform(-1, 1, (n, 3))
+    for t in range(n):
+        for k in range(3):
+            v[3 * t + k, 0:3] = (cen[t] + rng.uniform(-0.1, 0.1, 3)) * scale
+            v[3 * t + k, 4] = 1
+    idx = np.arange(3 * n, dtype=np.uint32)
+    prims = np.array([[0, 3 * n, 0, 0, 0, 0]], np.uint32)
+    xf = np.eye(4, dtype=np.float32).reshape(1, 16)
+    mats = Material().to_shader(0)[None]
+    lights = np.zeros((0, 12), np.float32)
+    ctx = HybridContext(0)
+    ctx.set_scene_arrays(v, idx, prims, xf, mats, lights)
+    orc = po.OracleScene()
+    orc.set_scene_arrays(v, idx, prims, xf, mats, lights)
+    ctx.build_bvh()
+    orc.build_bvh()
+    m = 20000
+    rays = np.zeros((m, 8), np.float32)
+    d = rng.normal(size=(m, 3))
+    d[::5, 0] = 0.0   # axis-parallel to the y-z plane
+    d[::7, 1:] = 0.0  # along x
+    d[::7, 0] = np.where(d[::7, 0] == 0, 1.0, d[::7, 0])
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays[:, 0:3] = rng.uniform(-1.5, 1.5, (m, 3)) * scale
+    rays[:, 3] = 1e-3 * scale
+    rays[:, 4:7] = d
+    rays[:, 7] = 10.0 * scale
+    torch = _torch()
+    for any_hit in (False, True):
+        hg, sg = ctx.trace(torch.from_numpy(rays).cuda(), any_hit, count=True)
+        ho, co = orc.trace(rays, any_hit)
+        assert np.array_equal(hg.cpu().numpy().view(np.uint32), ho.view(np.uint32))
+        assert sg["nodes_visited"] == int(co[:, 0].sum()) and sg["tris_tested"] == int(co[:, 1].sum())
+        assert sg["error_flags"] == 0
+        assert (ho.view(np.uint32)[:, 1] != 0xFFFFFFFF).mean() > 0.05  # the rays do hit
+    ctx.close()
+
+
 def _rays(rng, n, lo=-6, hi=6):
     org = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
     org[:, 1] = rng.uniform(0.1, 4, n)
