@@ -150,3 +150,41 @@ def test_scene_pack_roundtrip():
     assert np.all(idx[prims[0, 0]:prims[0, 0] + prims[0, 1]] < 4)
     assert mats.shape == (17, 12) and lights.shape == (2, 12)
     assert lights[1, 3] == -1  # directional
+
+
+def _bench():
+    import importlib.util
+    root = Path(__file__).resolve().parent.parent
+    spec = importlib.util.spec_from_file_location("bench_under_test", root / "bench.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_bench_source_hash_ignores_comments():
+    """The ncu evidence in profiles/ is tied to a hash of the kernels' code with
+    comments and blank lines stripped: a comment edit keeps it, a code edit does not."""
+    b = _bench()
+    src = {f: (b.ROOT / "vulkanhybridraytracer_gb300" / "csrc" / f).read_text() for f in b.KERNEL_SOURCES}
+    base = b.kernel_source_sha(src.__getitem__)
+    assert base == b.kernel_source_sha()
+    f0 = b.KERNEL_SOURCES[0]
+    commented = dict(src)
+    commented[f0] = "// a new comment\n\n/* and a block\n   comment */\n" + src[f0].replace("\n", "  // note\n", 3)
+    assert b.kernel_source_sha(commented.__getitem__) == base
+    changed = dict(src)
+    changed[f0] = src[f0] + "\nstatic int kUnused = 1;\n"
+    assert b.kernel_source_sha(changed.__getitem__) != base
+    assert b.code_of("a; // x\n\n  /* y */ b;\n") == "a;\n   b;"
+
+
+def test_bench_profile_records():
+    """Every key bench.py reads from the dominant kernel's ncu summaries is there."""
+    b = _bench()
+    rec = b.profile_records("k_shadow_stream<accum>")
+    for k in ("source_sha", "case", "dram_bytes_1920x1080", "dram_gbs", "issue_active_pct", "lanes_per_inst",
+              "alu_pipe_pct", "l2_gbs", "l2_bytes"):
+        assert k in rec, k
+    assert len(rec["source_sha"][0]) == 16
+    assert rec["dram_bytes_1920x1080"][1].startswith("profiles/")
+    assert b.profile_records("no_such_kernel") == {}
